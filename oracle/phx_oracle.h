@@ -1,0 +1,53 @@
+/* FP64 CPU restatement of Photon's gas-phase step (test infrastructure only).
+ *
+ * This is the oracle the CUDA path is checked against. It restates, in plain C
+ * with every real in double precision, the reference's gas-phase step
+ * (src/sim/solver.cpp:226-269 and the stages in src/sim/gasphase.cpp and
+ * src/sim/pressure_mg.cpp). Each function cites the reference lines it follows.
+ * Operation order, reduction order (per-z-slice double partials summed in
+ * order, src/sim/gasphase.cpp:39-49) and branch thresholds follow the
+ * reference, so this oracle agrees with the reference's own source compiled
+ * at FP64 (oracle/make_ref.py) to the last bit on the same inputs; the tests
+ * in tests/test_oracle_pin.py check that.
+ *
+ * It is never linked into the product library.
+ */
+#ifndef PHX_ORACLE_H
+#define PHX_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct Orc Orc;
+
+Orc* orc_new(int nx, int ny, int nz, double dx, double ox, double oy, double oz);
+void orc_free(Orc* o);
+/* profile: cfl, dtMax, maxIters, tol (1/s), relTol (max|r| <= relTol max|b|, 0 = off) */
+void orc_set_profile(Orc* o, double cfl, double dtMax, int maxIters, double tol, double relTol);
+void orc_set_switches(Orc* o, int radiationOn, int adiabatic);
+void orc_set_wind(Orc* o, double speed, double fromDeg, double exponent);
+void orc_mark_geometry_dirty(Orc* o);
+int orc_add_burner(Orc* o, double x0, double y0, double x1, double y1, double z, double peakW, double rampS,
+                   double start, double duration);
+int orc_burner_cells(Orc* o, int b, int* out, int cap);
+void orc_add_ignition(Orc* o, int cell, double power, double duration);
+/* coarsest-level solve: 0 = 20 forward+backward Gauss-Seidel sweeps (the reference), */
+void orc_set_coarse_mode(Orc* o, int mode);
+double orc_step(Orc* o, double dtMax);
+int orc_stage(Orc* o, const char* stage, double dt);
+double orc_stable_dt(Orc* o, double dtMax);
+void orc_precondition(Orc* o, const double* r, double* z);
+long orc_field_len(Orc* o, const char* name);
+int orc_field(Orc* o, const char* name, int dir, void* buf, long n);
+void orc_scalars(Orc* o, double* out);
+void orc_set_scalars(Orc* o, double time, double maxVel, double maxNu, double maxDiv);
+int orc_mg_levels(Orc* o);
+void orc_mg_info(Orc* o, int l, int* info);
+void orc_mg_get(Orc* o, int l, int* agg, int* rowStart, int* col, double* val, double* diag);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
