@@ -1,0 +1,318 @@
+"""Benchmark of the GB300 gas-phase step (one JSON line on stdout).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+
+A step is one gas-phase time step of every scenario of the workload, with the
+pressure solve run to a relative residual of 1e-8 (max|r| <= 1e-8 max|b|).
+value = cell-updates/s (cells x steps / device seconds) with all state resident
+in HBM, timed with CUDA events on the solver's stream, L2 flushed before each
+step when the working set fits in L2. e2e = the same metric through the C ABI
+per step: phx_step from the host, then the temperature field and the stats read
+back into pinned host memory. cpu_baseline = the reference's own FP32 solver
+(oracle/_ref) on the host cores, on a bounded sample of the same workload.
+
+--impl reference times the reference's own CPU step (oracle/_ref) on the same
+workload with all host threads. With --gpus N > 1 (torchrun) the work is
+replicated: every rank steps its own copy, no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-updates/s, mixed+batched vs FP64 GPU @1e-8 resid; p50/p99 scenario latency"
+REL_TOL = 1e-8
+SPINUP_STEPS = 150   # untimed steps that develop the plume before warm-up
+
+
+def rank_info():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def make_workload(name: str):
+    from photon_gb300 import casegen
+    if name == "house_72x52x44":
+        c = casegen.house_small(1)
+    elif name == "single_room_36x24x24":
+        c = casegen.single_room()
+    elif name == "house_144x104x88":
+        c = casegen.house_fine(1)
+    else:
+        raise SystemExit("unknown workload " + name)
+    c.profile.tol = 0.0
+    c.profile.rel_tol = REL_TOL
+    c.profile.maxIters = 400
+    return c
+
+
+# Algorithmic bytes per unit of each kernel's domain (FP64 storage, w = 8 B):
+# each input array read once and each output written once per launch.
+W = 8
+KERNEL_BYTES = {
+    # kernel: (bytes per unit, unit) ; unit 'cell' = N, 'face' = faces of one axis
+    "k_advect": (18 * W + 1 + 10 * W, "cell"),       # 10 scalars + u,v,w,fx,fy,fz + Pb,nu + blocked -> 10 scalars
+    "k_momentum": (8 * W + 1 * W, "face"),             # vel, 2 other comps, fo, Pb, T, nu, p -> vel'
+    "k_gs0": (5 * W, "cell"),                          # half sweep: r,diag,z of its colour, z of the other, 3 coefficient arrays
+    "k_cg_apply": (8 * W, "cell"),                     # z, d, diag, 3 coefficients -> d, q
+    "k_cg_update": (7.5 * W, "cell"),                  # p, d, r, q, diag -> p, r, z(red)
+    "k_res0_restrict": (6 * W + 4, "cell"),            # r, z, diag, 3 coefficients, agg
+    "k_gs0_last_dot": (6 * W, "cell"),
+    "k_rhs": (13 * W + 1, "cell"),
+    "k_heat": (8 * W + 1, "cell"),
+    "k_energy": (6 * W + 1, "cell"),
+    "k_combust": (6 * W + 3, "cell"),
+    "k_turb_filter": (2 * W + 1, "cell"),
+    "k_turb_center": (6 * W + 1, "cell"),
+    "k_turb_nu": (5 * W + 1, "cell"),
+    "k_velcorr": (5 * W, "face"),
+    "k_stats": (4 * W + 1, "cell"),
+}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock and throttle-reason samples during the timed region."""
+
+    def __init__(self, gpu_index: int):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "bench_clocks_%d.csv" % os.getpid())
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu),
+                 "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        try:
+            rows = [l.strip().split(",") for l in open(self.path) if l.strip()]
+        except Exception:
+            return out
+        sm, mxs, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[0]))
+                mxs.append(float(r[1]))
+                for n, v in zip(names, r[2:6]):
+                    if v.strip().lower() in ("active", "1", "yes"):
+                        reasons.add(n)
+            except Exception:
+                continue
+        if sm:
+            out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mxs), "reasons": sorted(reasons),
+                   "samples": len(sm)}
+        return out
+
+
+def cpu_reference_rate(case, steps: int, warm: int, threads: int, bits: int = 32, budget_s: float = 20.0):
+    """cell-updates/s of the reference's own CPU step on this case (oracle/_ref),
+    or of the FP64 oracle port when the reference build is absent."""
+    from oracle import refpy
+    kind = "reference"
+    if refpy.available(bits):
+        s = refpy.RefSolver(case, bits, threads)
+        stepf = lambda: s.step(case.profile.dtMax)
+    else:
+        from oracle.oraclepy import OracleSolver
+        s = OracleSolver(case)
+        kind, threads = "port", 1
+        stepf = lambda: s.step(case.profile.dtMax)
+    for _ in range(warm):
+        stepf()
+    t0 = time.perf_counter()
+    n = 0
+    while n < steps and (n == 0 or time.perf_counter() - t0 < budget_s):
+        stepf()
+        n += 1
+    el = time.perf_counter() - t0
+    return case.N * n / el, kind, threads, n, el
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    case = make_workload(args.workload)
+    # the reference stops on its own absolute test only: 1e-8 1/s is at least as strict
+    case.profile.tol = 1e-8
+    threads = os.cpu_count() or 1
+    from oracle import refpy
+    if not refpy.available(32):
+        print(json.dumps({"impl": "reference", "unavailable": "reference CPU build (oracle/_ref) is not present"}))
+        return 0
+    s = refpy.RefSolver(case, 32, threads)
+    for _ in range(args.warmup):
+        s.step(case.profile.dtMax)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.step(case.profile.dtMax)
+    el = time.perf_counter() - t0
+    v = case.N * args.steps / el
+    line = {"metric": METRIC, "value": v, "unit": "cell-updates/s", "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded house generator)",
+            "config": {"workload": args.workload, "cells": case.N, "pressure_stop": "absolute 1e-8 1/s",
+                       "threads": threads},
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": "reference",
+                             "sample": "%d steps of %s after %d warm-up steps" % (args.steps, args.workload, args.warmup)},
+            "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="house_72x52x44")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = rank_info()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+
+    from photon_gb300 import _lib
+    from photon_gb300.solver import Solver
+    L = _lib.load()
+    if L.phx_select_device(local) != 0:
+        raise SystemExit("cannot select device %d" % local)
+
+    case = make_workload(args.workload)
+    g = Solver(case, _lib.PREC_FP64)
+    dtMax = case.profile.dtMax
+    g.run(SPINUP_STEPS, dtMax)
+    g.run(max(3, args.warmup), dtMax)
+    # the working set of one scenario fits in L2: flush it before every timed step
+    flush = g.device_bytes() < (200 << 20)
+
+    if dist:
+        dist.barrier()
+    g.sync()
+    with ClockSampler(local) as clk:
+        ms, launches = g.time_steps(args.steps, dtMax, flush_l2=flush)
+    g.sync()
+    t_s = ms / 1e3
+    if dist:
+        import torch
+        t = torch.tensor([t_s], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_s = float(t[0])
+    value = case.N * args.steps * world / t_s
+    st = g.stats()
+
+    # e2e through the C ABI: step from the host, read T and the stats back to pinned memory
+    import ctypes
+    nbytesT = case.N * 8
+    hbuf = L.phx_alloc_host(nbytesT)
+    stats = _lib.PhxStats()
+    dt_c = ctypes.c_double()
+    e2e_steps = args.steps
+    for _ in range(2):
+        L.phx_step(g.h, dtMax, ctypes.byref(dt_c))
+    g.sync()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        if L.phx_step(g.h, dtMax, ctypes.byref(dt_c)) != 0:
+            raise SystemExit(L.phx_last_error(g.h).decode())
+        L.phx_get_field(g.h, _lib.FIELD_ID["T"], ctypes.c_void_p(hbuf), nbytesT)
+        L.phx_get_stats(g.h, ctypes.byref(stats))
+    e2e_s = time.perf_counter() - t0
+    L.phx_free_host(ctypes.c_void_p(hbuf))
+    e2e_value = case.N * e2e_steps * world / e2e_s
+
+    # per-kernel device times of one step (outside the timed region) for the roofline
+    prof = g.profile_step(dtMax, flush_l2=flush)
+    tot_prof = sum(p[2] for p in prof)
+    top = max(prof, key=lambda p: p[2])
+    per_unit, unit = KERNEL_BYTES.get(top[0], (None, None))
+    peak, peak_kind = measured_peak()
+    roof = None
+    if per_unit:
+        units = case.N if unit == "cell" else (case.N * 1.0)
+        bytes_per_launch = per_unit * units
+        achieved = bytes_per_launch / (top[2] / top[1] / 1e3) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "kernel": top[0], "kernel_share": top[2] / tot_prof,
+                "algorithmic_bytes_per_launch": bytes_per_launch, "peak_kind": peak_kind}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cref = make_workload(args.workload)
+        cref.profile.tol = 1e-8
+        threads = os.cpu_count() or 1
+        v, kind, thr, n, el = cpu_reference_rate(cref, steps=20, warm=2, threads=threads)
+        cpu = {"value": v, "unit": "cell-updates/s", "cores": thr, "kind": kind,
+               "sample": "%d steps of %s (%.1f s) after 2 warm-up steps, FP32 reference build" % (n, args.workload, el)}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t_s / args.steps * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded house generator; random-free physics, no dataset)",
+                "config": {"workload": args.workload, "cells": case.N, "precision": "fp64",
+                           "pressure_stop": "relative 1e-8 (max|r| <= 1e-8 max|b|)",
+                           "l2": "flushed before each step" if flush else "inputs larger than L2",
+                           "spinup_steps": SPINUP_STEPS, "cg_iters_last_step": st["pressure_iters"],
+                           "parallelism": "replicas" if world > 1 else "single"},
+                "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": 8,
+                        "d2h_bytes_per_step": nbytesT + ctypes.sizeof(_lib.PhxStats)},
+                "gpu_launches": launches,
+                "roofline": roof,
+                "cpu_baseline": cpu,
+                "clocks": clk.summary(),
+                "kernels": [{"name": p[0], "launches": p[1], "ms": round(p[2], 4)} for p in
+                            sorted(prof, key=lambda p: -p[2])[:12]]}
+        print(json.dumps(line))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

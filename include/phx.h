@@ -1,0 +1,180 @@
+/* phx.h -- C ABI of the GB300 gas-phase step for Photon's src/sim solver.
+ *
+ * Drop-in boundary. Photon's callers hold a photon::Solver and call
+ * `float Solver::step(float dtMax)` (src/sim/solver.h:195), then read its public
+ * field vectors (src/sim/solver.h:231-284) and stats (src/sim/solver.h:141-154,
+ * 273-278). The reference has no FFI layer; this header is the C boundary a
+ * host (the C++ adapter in include/photon_gpu/solver.hpp, a ctypes binding, a
+ * cgo/JNI stub) binds instead of linking photon::Solver's gas phase.
+ *
+ * Conventions: every call returns an int status (PHX_OK = 0) and never throws;
+ * the message of the last failure is phx_last_error(ctx) (or
+ * phx_last_global_error() when no context exists). All buffers passed in are
+ * owned by the caller and are copied before the call returns. Grid indexing is
+ * the reference's (src/sim/solver.h:216-220): cell i + nx (j + ny k), x-face
+ * i + (nx+1)(j + ny k), y-face i + nx (j + (ny+1) k), z-face i + nx (j + ny k).
+ * One context is driven by one host thread at a time (as photon::Solver).
+ */
+#ifndef PHX_H
+#define PHX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PHX_ABI_VERSION 1
+
+/* status codes */
+enum {
+    PHX_OK = 0,
+    PHX_ERR_INVALID = 1,      /* bad argument or size */
+    PHX_ERR_UNSUPPORTED = 2,  /* input outside what the GPU step implements */
+    PHX_ERR_OOM = 3,          /* device allocation failed */
+    PHX_ERR_CUDA = 4,         /* CUDA runtime error (message has the detail) */
+    PHX_ERR_TIMEOUT = 5,      /* a bounded device wait gave up */
+    PHX_ERR_BUDGET = 6,       /* admission refused by the memory budget */
+    PHX_ERR_STATE = 7         /* call not valid in the current state */
+};
+
+/* precision of a context */
+enum {
+    PHX_PREC_FP64 = 0,   /* every field and every operation in FP64 */
+    PHX_PREC_MIXED = 1   /* FP32 fields and stencils, FP16 smoother scratch, FP64 dots/refinement/global sums */
+};
+
+/* Grid and settings of one scenario. Mirrors what Solver::build leaves in the
+ * solver (src/sim/discretize.cpp:10-62, FidelityProfile src/sim/solver.h:82-104,
+ * Wind :107-111, switches :187-188). Geometry arrays are host pointers with the
+ * reference's sizes: blocked N, fx/ax/lx (nx+1) ny nz, fy/ay/ly nx (ny+1) nz,
+ * fz/az/lz nx ny (nz+1). lx/ly/lz may be NULL (no crack faces). */
+typedef struct phx_grid {
+    int nx, ny, nz;
+    double dx, ox, oy, oz;
+    double cfl, dt_max;          /* profile.cfl, profile.dtMax */
+    int max_iters;               /* profile.pressureMaxIters */
+    double tol;                  /* profile.pressureTol: largest divergence error, 1/s */
+    double rel_tol;              /* extra stop: max|r| <= rel_tol * max|b| (0 = off) */
+    int radiation_on;            /* Solver::radiationOn */
+    int adiabatic_surfaces;      /* Solver::adiabaticSurfaces */
+    double wind_speed, wind_from_deg, wind_exponent;
+    const uint8_t* blocked;
+    const double *fx, *fy, *fz;  /* face open fractions */
+    const double *ax, *ay, *az;  /* pressure-matrix coefficients (open, not leak) */
+    const uint8_t *lx, *ly, *lz; /* crack faces (orifice flow) */
+} phx_grid;
+
+/* fields readable/writable with phx_get_field / phx_set_field. Real fields
+ * travel as double (converted in the mixed context), flags as uint8, zone as
+ * int32. */
+enum {
+    PHX_FIELD_U = 0, PHX_FIELD_V, PHX_FIELD_W,
+    PHX_FIELD_P, PHX_FIELD_S,
+    PHX_FIELD_T, PHX_FIELD_YO, PHX_FIELD_YF, PHX_FIELD_YS, PHX_FIELD_YA, PHX_FIELD_YP,
+    PHX_FIELD_YC, PHX_FIELD_YW, PHX_FIELD_YCO, PHX_FIELD_YAI,
+    PHX_FIELD_NU, PHX_FIELD_PB, PHX_FIELD_Q, PHX_FIELD_QR, PHX_FIELD_HRR, PHX_FIELD_MASSSRC,
+    PHX_FIELD_LIT,      /* uint8 */
+    PHX_FIELD_ZONE,     /* int32, read only */
+    PHX_FIELD_RHS, PHX_FIELD_CGR, PHX_FIELD_CGZ,
+    PHX_FIELD_COUNT
+};
+
+/* stages for per-stage parity runs (phx_stage); the names follow the
+ * reference's Solver methods. */
+enum {
+    PHX_STAGE_BEGIN = 0,     /* dt = stableDt(dtMax) and burner/ignition injection amounts */
+    PHX_STAGE_COMBUSTION,    /* clears + injectIgnitions + injectBurners + combustion */
+    PHX_STAGE_TURBULENCE,
+    PHX_STAGE_HEAT,
+    PHX_STAGE_ENERGY,
+    PHX_STAGE_MOMENTUM,
+    PHX_STAGE_LEAKAGE,
+    PHX_STAGE_PROJECT,
+    PHX_STAGE_ADVECT,
+    PHX_STAGE_END,           /* zone pressure, Pb, gatherStats, time += dt */
+    PHX_STAGE_COUNT
+};
+
+/* Solver scalars after a step (src/sim/solver.h:141-154, 273-278) */
+typedef struct phx_stats {
+    double time, dt;
+    double max_vel, max_nu, max_div;
+    int pressure_iters;
+    double pressure_residual;    /* 1/s, largest divergence error left */
+    double pressure_rel_residual;/* max|r| / max|b| of the last solve */
+    double hrr, max_gas_t;
+    int burning_cells;
+    double fuel_in, fuel_burned, fuel_in_domain;
+    int zones, leak_faces;
+} phx_stats;
+
+/* Create a context for one scenario and upload its geometry.
+ * Replaces Solver::build (src/sim/discretize.cpp:10) for a discretized grid;
+ * zones (src/sim/gasphase.cpp:111-158) and the multigrid hierarchy
+ * (src/sim/pressure_mg.cpp:28-191) are built on the host here. */
+int phx_create(const phx_grid* grid, int precision, struct phx_ctx** out);
+void phx_destroy(struct phx_ctx* ctx);
+const char* phx_last_error(const struct phx_ctx* ctx);
+const char* phx_last_global_error(void);
+int phx_abi_version(void);
+
+/* Solver::addBurner (src/sim/gasphase.cpp:72-90): index_out gets the burner
+ * index, or -1 with PHX_ERR_INVALID if it covers no gas cell. */
+int phx_add_burner(struct phx_ctx* ctx, double x0, double y0, double x1, double y1, double z, double peak_w,
+                   double ramp_s, double start, double duration, int* index_out);
+/* Solver::addIgnition (src/sim/solver.cpp:122-134) */
+int phx_add_ignition(struct phx_ctx* ctx, int cell, double power, double duration);
+
+/* Solver::step (src/sim/solver.cpp:226-269), gas-only stages. dt_out may be NULL. */
+int phx_step(struct phx_ctx* ctx, double dt_max, double* dt_out);
+/* n steps back to back; dt_out (n entries) may be NULL */
+int phx_run(struct phx_ctx* ctx, int n, double dt_max, double* dt_out);
+
+/* one stage of the step, for per-stage parity runs; dt is used by the stages
+ * that take it (the BEGIN stage ignores it and takes dt_max from the argument) */
+int phx_stage(struct phx_ctx* ctx, int stage, double dt_or_dtmax);
+/* z = M^-1 r with one V-cycle of the pressure multigrid (src/sim/pressure_mg.cpp:270-300) */
+int phx_precondition(struct phx_ctx* ctx, const double* r, double* z);
+
+int phx_get_field(struct phx_ctx* ctx, int field, void* host, size_t bytes);
+int phx_set_field(struct phx_ctx* ctx, int field, const void* host, size_t bytes);
+size_t phx_field_count(const struct phx_ctx* ctx, int field);
+int phx_get_stats(struct phx_ctx* ctx, phx_stats* out);
+/* time, maxVel, maxNu, maxDiv as read by the next stableDt */
+int phx_set_scalars(struct phx_ctx* ctx, double time, double max_vel, double max_nu, double max_div);
+/* device bytes this context holds */
+size_t phx_device_bytes(const struct phx_ctx* ctx);
+/* wait for the context's stream */
+int phx_sync(struct phx_ctx* ctx);
+
+/* --- measurement helpers (the GPU analog of Solver::phaseMs, src/sim/solver.h:280-284)
+ * Run n steps with everything resident in HBM; total_ms is the device time of
+ * the steps measured with CUDA events on the context's stream. flush_l2 != 0
+ * writes a buffer larger than L2 (untimed) before each step. launches gets the
+ * number of kernel launches of the n steps. */
+int phx_time_steps(struct phx_ctx* ctx, int n, double dt_max, int flush_l2, double* total_ms, int* launches);
+
+typedef struct phx_kernel_time {
+    char name[48];
+    int launches;
+    double ms;
+} phx_kernel_time;
+/* one step with CUDA events around every kernel launch; out[0..cap) gets the
+ * per-kernel launch counts and summed times, *count the number of kernels */
+int phx_profile_step(struct phx_ctx* ctx, double dt_max, int flush_l2, phx_kernel_time* out, int cap, int* count);
+/* kernel launches of the last step */
+int phx_last_step_launches(const struct phx_ctx* ctx);
+
+/* --- process-level helpers ------------------------------------------------
+ * select the CUDA device later contexts of this thread are created on */
+int phx_select_device(int device);
+/* page-locked host buffers for callers that stream fields every step */
+void* phx_alloc_host(size_t bytes);
+void phx_free_host(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PHX_H */

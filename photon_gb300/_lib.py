@@ -1,0 +1,108 @@
+"""ctypes binding of libphx.so (include/phx.h).
+
+The library is built in-tree by photon_gb300.build; loading fails loudly when
+it is missing -- there is no CPU fallback for the GPU step.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libphx.so")
+
+PHX_OK, PHX_ERR_INVALID, PHX_ERR_UNSUPPORTED, PHX_ERR_OOM, PHX_ERR_CUDA, PHX_ERR_TIMEOUT, PHX_ERR_BUDGET, PHX_ERR_STATE = range(8)
+PREC_FP64, PREC_MIXED = 0, 1
+
+FIELDS = ["u", "v", "w", "p", "S", "T", "Yo", "Yf", "Ys", "Ya", "Yp", "Yc", "Yw", "Yco", "Yai", "nu", "Pb", "Q", "Qr",
+          "hrr", "massSrc", "lit", "zone", "rhs", "cgR", "cgZ"]
+FIELD_ID = {n: i for i, n in enumerate(FIELDS)}
+STAGES = ["begin", "combustion", "turbulence", "heat", "energy", "momentum", "leakage", "project", "advect", "end"]
+STAGE_ID = {n: i for i, n in enumerate(STAGES)}
+
+# exported symbols, as declared in include/phx.h
+SYMBOLS = ["phx_create", "phx_destroy", "phx_last_error", "phx_last_global_error", "phx_abi_version", "phx_add_burner",
+           "phx_add_ignition", "phx_step", "phx_run", "phx_stage", "phx_precondition", "phx_get_field",
+           "phx_set_field", "phx_field_count", "phx_get_stats", "phx_set_scalars", "phx_device_bytes", "phx_sync",
+           "phx_time_steps", "phx_profile_step", "phx_last_step_launches", "phx_select_device", "phx_alloc_host",
+           "phx_free_host"]
+
+
+class PhxGrid(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+                ("dx", ctypes.c_double), ("ox", ctypes.c_double), ("oy", ctypes.c_double), ("oz", ctypes.c_double),
+                ("cfl", ctypes.c_double), ("dt_max", ctypes.c_double), ("max_iters", ctypes.c_int),
+                ("tol", ctypes.c_double), ("rel_tol", ctypes.c_double),
+                ("radiation_on", ctypes.c_int), ("adiabatic_surfaces", ctypes.c_int),
+                ("wind_speed", ctypes.c_double), ("wind_from_deg", ctypes.c_double), ("wind_exponent", ctypes.c_double),
+                ("blocked", ctypes.c_void_p),
+                ("fx", ctypes.c_void_p), ("fy", ctypes.c_void_p), ("fz", ctypes.c_void_p),
+                ("ax", ctypes.c_void_p), ("ay", ctypes.c_void_p), ("az", ctypes.c_void_p),
+                ("lx", ctypes.c_void_p), ("ly", ctypes.c_void_p), ("lz", ctypes.c_void_p)]
+
+
+class PhxStats(ctypes.Structure):
+    _fields_ = [("time", ctypes.c_double), ("dt", ctypes.c_double),
+                ("max_vel", ctypes.c_double), ("max_nu", ctypes.c_double), ("max_div", ctypes.c_double),
+                ("pressure_iters", ctypes.c_int), ("pressure_residual", ctypes.c_double),
+                ("pressure_rel_residual", ctypes.c_double),
+                ("hrr", ctypes.c_double), ("max_gas_t", ctypes.c_double), ("burning_cells", ctypes.c_int),
+                ("fuel_in", ctypes.c_double), ("fuel_burned", ctypes.c_double), ("fuel_in_domain", ctypes.c_double),
+                ("zones", ctypes.c_int), ("leak_faces", ctypes.c_int)]
+
+
+class PhxKernelTime(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 48), ("launches", ctypes.c_int), ("ms", ctypes.c_double)]
+
+
+_L = None
+
+
+def lib_path() -> str:
+    return LIB_PATH
+
+
+def load():
+    """Load libphx.so; raises if it has not been built."""
+    global _L
+    if _L is not None:
+        return _L
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libphx.so is not built (run python -m photon_gb300.build); the GPU step has no CPU fallback")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, d, i, sz = ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_size_t
+    L.phx_create.argtypes = [ctypes.POINTER(PhxGrid), i, ctypes.POINTER(vp)]
+    L.phx_destroy.argtypes = [vp]
+    L.phx_last_error.restype = ctypes.c_char_p
+    L.phx_last_error.argtypes = [vp]
+    L.phx_last_global_error.restype = ctypes.c_char_p
+    L.phx_add_burner.argtypes = [vp, d, d, d, d, d, d, d, d, d, ctypes.POINTER(i)]
+    L.phx_add_ignition.argtypes = [vp, i, d, d]
+    L.phx_step.argtypes = [vp, d, ctypes.POINTER(d)]
+    L.phx_run.argtypes = [vp, i, d, vp]
+    L.phx_stage.argtypes = [vp, i, d]
+    L.phx_precondition.argtypes = [vp, vp, vp]
+    L.phx_get_field.argtypes = [vp, i, vp, sz]
+    L.phx_set_field.argtypes = [vp, i, vp, sz]
+    L.phx_field_count.restype = sz
+    L.phx_field_count.argtypes = [vp, i]
+    L.phx_get_stats.argtypes = [vp, ctypes.POINTER(PhxStats)]
+    L.phx_set_scalars.argtypes = [vp, d, d, d, d]
+    L.phx_device_bytes.restype = sz
+    L.phx_device_bytes.argtypes = [vp]
+    L.phx_sync.argtypes = [vp]
+    L.phx_time_steps.argtypes = [vp, i, d, i, ctypes.POINTER(d), ctypes.POINTER(i)]
+    L.phx_profile_step.argtypes = [vp, d, i, ctypes.POINTER(PhxKernelTime), i, ctypes.POINTER(i)]
+    L.phx_last_step_launches.argtypes = [vp]
+    L.phx_select_device.argtypes = [i]
+    L.phx_alloc_host.restype = vp
+    L.phx_alloc_host.argtypes = [sz]
+    L.phx_free_host.argtypes = [vp]
+    _L = L
+    return L
+
+
+class PhxError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("phx error %d: %s" % (code, msg))
+        self.code = code

@@ -1,0 +1,741 @@
+// One scenario context: device arena, descriptor, domain tables and the launch
+// sequence of the gas-phase step (src/sim/solver.cpp:226-269). Instantiated
+// per precision by engine_fp64.cu (and the mixed path).
+#pragma once
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "engine.h"
+#include "host_setup.h"
+#include "pressure_kernels.cuh"
+
+namespace phx {
+
+#define PHX_CK(x)                                                                        \
+    do {                                                                                 \
+        cudaError_t e_ = (x);                                                            \
+        if (e_ != cudaSuccess) {                                                         \
+            err = std::string(#x) + ": " + cudaGetErrorString(e_);                      \
+            return PHX_ERR_CUDA;                                                         \
+        }                                                                                \
+    } while (0)
+
+// dense coarse operators up to this many unknowns (n^2 reals)
+constexpr int DENSE_MAX = 4096;
+
+enum DomId {
+    D_ONE = 0, D_CELLS, D_HALF, D_BLK, D_FX, D_FY, D_FZ, D_BX, D_BY, D_BZ, D_CZ, D_CC, D_CO_DENSE, D_CO_SERIAL,
+    D_LV0,                       // D_LV0 + l: rows of level l when l is not the coarsest (1 <= l < 12)
+    D_RS0 = D_LV0 + MAX_LEVELS,  // D_RS0 + l: rows of level l+1 for restriction from level l >= 1
+    D_COUNT = D_RS0 + MAX_LEVELS
+};
+
+struct SourceHost {
+    Src s;
+};
+
+template <class R>
+class Ctx : public CtxBase {
+public:
+    GridGeom geo;
+    double cfl = 0.5, dtMaxP = 0.02, tol = 0.002, relTol = 0;
+    int maxIters = 400, radiationOn = 1;
+    Zones Z;
+    Multigrid MG;
+    std::vector<double> Pb0;
+    std::vector<Src> ignitions, burners;
+    cudaStream_t st = nullptr;
+    char* arena = nullptr;
+    size_t arenaBytes = 0;
+    Scn<R> h{};
+    Scn<R>* dS = nullptr;
+    R** dD = nullptr;
+    R* dbuf[2] = {nullptr, nullptr};
+    double* hPin = nullptr;      // pinned: [0] dtMax, [1..] scalar read-back
+    int* dDomStart = nullptr;    // D_COUNT x 2
+    Dom dom[D_COUNT];
+    int maxLevels = 0;
+    int launches = 0;
+    cudaEvent_t ev[4] = {};
+
+    ~Ctx() override {
+        if (st) cudaStreamSynchronize(st);
+        if (arena) cudaFree(arena);
+        if (hPin) cudaFreeHost(hPin);
+        if (flushBuf) cudaFree(flushBuf);
+        for (auto e : evPool) cudaEventDestroy(e);
+        for (auto& e : ev) if (e) cudaEventDestroy(e);
+        if (st) cudaStreamDestroy(st);
+    }
+
+    int init(const phx_grid* g) {
+        if (!g || g->nx <= 0 || g->ny <= 0 || g->nz <= 0 || !(g->dx > 0)) { err = "invalid grid dimensions"; return PHX_ERR_INVALID; }
+        long long N = (long long)g->nx * g->ny * g->nz;
+        if (N > 20000000LL) { err = "grid size out of range (the reference caps N at 20,000,000)"; return PHX_ERR_INVALID; }
+        if (!g->blocked || !g->fx || !g->fy || !g->fz || !g->ax || !g->ay || !g->az) { err = "missing geometry array"; return PHX_ERR_INVALID; }
+        if (g->radiation_on && !g->adiabatic_surfaces) {
+            err = "radiation with non-adiabatic surfaces (the ray-traced radiation stage) is not part of the GPU step";
+            return PHX_ERR_UNSUPPORTED;
+        }
+        geo.nx = g->nx; geo.ny = g->ny; geo.nz = g->nz;
+        geo.dx = g->dx; geo.ox = g->ox; geo.oy = g->oy; geo.oz = g->oz;
+        geo.windSpeed = g->wind_speed; geo.windFromDeg = g->wind_from_deg; geo.windExp = g->wind_exponent;
+        const int NN = geo.N(), NX = geo.NX(), NY = geo.NY(), NZ = geo.NZ();
+        geo.blocked.assign(g->blocked, g->blocked + NN);
+        geo.fx.assign(g->fx, g->fx + NX); geo.fy.assign(g->fy, g->fy + NY); geo.fz.assign(g->fz, g->fz + NZ);
+        geo.ax.assign(g->ax, g->ax + NX); geo.ay.assign(g->ay, g->ay + NY); geo.az.assign(g->az, g->az + NZ);
+        geo.lx.assign(NX, 0); geo.ly.assign(NY, 0); geo.lz.assign(NZ, 0);
+        if (g->lx) geo.lx.assign(g->lx, g->lx + NX);
+        if (g->ly) geo.ly.assign(g->ly, g->ly + NY);
+        if (g->lz) geo.lz.assign(g->lz, g->lz + NZ);
+        geo.anyLeak = false;
+        for (auto v : geo.lx) geo.anyLeak |= v != 0;
+        for (auto v : geo.ly) geo.anyLeak |= v != 0;
+        for (auto v : geo.lz) geo.anyLeak |= v != 0;
+        if (geo.anyLeak) {
+            err = "crack faces (orifice-flow leakage) are not implemented in the GPU step yet";
+            return PHX_ERR_UNSUPPORTED;
+        }
+        cfl = g->cfl; dtMaxP = g->dt_max; tol = g->tol; relTol = g->rel_tol; maxIters = g->max_iters;
+        radiationOn = g->radiation_on;
+        // set-up on the host: zones, multigrid
+        Pb0.assign(NN, 101325.0);
+        Z = computeZones(geo, Pb0);
+        MG = buildMultigrid(geo, DENSE_MAX);
+        maxLevels = (int)MG.lv.size();
+        return allocate();
+    }
+
+    template <class T>
+    static T* carve(char*& base, size_t& off, size_t n) {
+        off = (off + 255) & ~(size_t)255;
+        T* p = base ? (T*)(base + off) : nullptr;
+        off += n * sizeof(T);
+        return p;
+    }
+
+    int allocate() {
+        const int N = geo.N(), NX = geo.NX(), NY = geo.NY(), NZ = geo.NZ();
+        const int nl = (int)MG.lv.size();
+        const int partStride = (N + TPB - 1) / TPB + 1;
+        for (int pass = 0; pass < 2; ++pass) {
+            char* base = pass == 0 ? nullptr : arena;
+            size_t off = 0;
+            Scn<R>& s = h;
+            s.blocked = carve<uint8_t>(base, off, N);
+            s.fx = carve<R>(base, off, NX); s.fy = carve<R>(base, off, NY); s.fz = carve<R>(base, off, NZ);
+            s.ax = carve<R>(base, off, NX); s.ay = carve<R>(base, off, NY); s.az = carve<R>(base, off, NZ);
+            s.a0x = carve<R>(base, off, NX); s.a0y = carve<R>(base, off, NY); s.a0z = carve<R>(base, off, NZ);
+            s.lx = nullptr; s.ly = nullptr; s.lz = nullptr;
+            s.diag = carve<R>(base, off, N);
+            s.zone = carve<int>(base, off, N);
+            const int nZ = (int)Z.zoneP.size(), nC = (int)Z.closed.size();
+            s.zoneOpen = carve<uint8_t>(base, off, nZ + 1);
+            s.closedZone = carve<int>(base, off, nC + 1);
+            s.closedStart = carve<int>(base, off, nC + 1);
+            s.closedCells = carve<int>(base, off, Z.closedCells.size() + 1);
+            s.zoneP = carve<double>(base, off, nZ + 1);
+            s.zoneVol = carve<double>(base, off, nZ + 1);
+            s.zoneDP = carve<double>(base, off, nZ + 1);
+            s.zoneShift = carve<double>(base, off, nZ + 1);
+            s.zoneMean = carve<double>(base, off, nZ + 1);
+            s.u = carve<R>(base, off, NX); s.v = carve<R>(base, off, NY); s.w = carve<R>(base, off, NZ);
+            s.u2 = carve<R>(base, off, NX); s.v2 = carve<R>(base, off, NY); s.w2 = carve<R>(base, off, NZ);
+            for (int q = 0; q < NSC; ++q) { s.sc[q] = carve<R>(base, off, N); s.sc2[q] = carve<R>(base, off, N); }
+            s.p = carve<R>(base, off, N); s.S = carve<R>(base, off, N); s.nu = carve<R>(base, off, N);
+            s.Pb = carve<R>(base, off, N); s.Q = carve<R>(base, off, N); s.Qr = carve<R>(base, off, N);
+            s.hrr = carve<R>(base, off, N); s.massSrc = carve<R>(base, off, N);
+            s.lit = carve<uint8_t>(base, off, N); s.lit2 = carve<uint8_t>(base, off, N); s.pilot = carve<uint8_t>(base, off, N);
+            for (int q = 0; q < 9; ++q) s.tmp[q] = carve<R>(base, off, N);
+            s.b = carve<R>(base, off, N); s.r = carve<R>(base, off, N); s.z = carve<R>(base, off, N);
+            dbuf[0] = carve<R>(base, off, N); dbuf[1] = carve<R>(base, off, N);
+            s.d = dbuf[0];
+            s.q = carve<R>(base, off, N);
+            s.nLevels = nl;
+            for (int l = 0; l < nl; ++l) {
+                const MgLevel& L = MG.lv[l];
+                Level<R>& D = s.lv[l];
+                D.n = L.n;
+                if (l == 0) {
+                    D.diag = s.diag;
+                    D.x = s.z; D.y = nullptr; D.b = s.r;
+                    D.rowStart = nullptr; D.col = nullptr; D.val = nullptr;
+                } else {
+                    D.rowStart = carve<int>(base, off, L.rowStart.size());
+                    D.col = carve<int>(base, off, L.col.size() + 1);
+                    D.val = carve<R>(base, off, L.val.size() + 1);
+                    D.diag = carve<R>(base, off, L.n + 1);
+                    D.x = carve<R>(base, off, L.n + 1); D.y = carve<R>(base, off, L.n + 1); D.b = carve<R>(base, off, L.n + 1);
+                }
+                D.agg = L.agg.empty() ? nullptr : carve<int>(base, off, L.agg.size());
+                D.childStart = L.childStart.empty() ? nullptr : carve<int>(base, off, L.childStart.size());
+                D.child = L.child.empty() ? nullptr : carve<int>(base, off, L.child.size() + 1);
+                D.dense = L.dense.empty() ? nullptr : carve<R>(base, off, L.dense.size());
+            }
+            s.sv = carve<double>(base, off, SV_COUNT);
+            s.part = carve<double>(base, off, (size_t)PS_COUNT * partStride);
+            s.partStride = partStride;
+            s.cnt = carve<unsigned>(base, off, PS_COUNT + 4);
+            dS = carve<Scn<R>>(base, off, 1);
+            dD = carve<R*>(base, off, 2);
+            dDomStart = carve<int>(base, off, D_COUNT * 2);
+            if (pass == 0) {
+                arenaBytes = off + 256;
+                cudaError_t e = cudaMalloc(&arena, arenaBytes);
+                if (e != cudaSuccess) {
+                    arena = nullptr;
+                    err = std::string("device allocation of ") + std::to_string(arenaBytes) + " bytes failed: " + cudaGetErrorString(e);
+                    return PHX_ERR_OOM;
+                }
+            }
+        }
+        PHX_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        PHX_CK(cudaMallocHost(&hPin, 4096));
+        for (auto& e : ev) PHX_CK(cudaEventCreate(&e));
+        PHX_CK(cudaMemsetAsync(arena, 0, arenaBytes, st));
+        return upload();
+    }
+
+    // host -> device uploads; device pointers of read-only arrays are const in
+    // the descriptor, so they are cast back here
+    template <class T>
+    int put(const T* dstc, const std::vector<double>& src) {
+        using U = typename std::remove_const<T>::type;
+        U* dst = const_cast<U*>(dstc);
+        std::vector<U> tmp(src.begin(), src.end());
+        if (!tmp.empty()) PHX_CK(cudaMemcpyAsync(dst, tmp.data(), tmp.size() * sizeof(U), cudaMemcpyHostToDevice, st));
+        PHX_CK(cudaStreamSynchronize(st));
+        return PHX_OK;
+    }
+    template <class T, class V>
+    int putRaw(const T* dstc, const V* src, size_t n) {
+        static_assert(sizeof(T) == sizeof(V), "element size");
+        void* dst = const_cast<void*>((const void*)dstc);
+        if (n) PHX_CK(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyHostToDevice, st));
+        PHX_CK(cudaStreamSynchronize(st));
+        return PHX_OK;
+    }
+    int fillR(R* dst, size_t n, double v) { return put<R>(dst, std::vector<double>(n, v)); }
+
+#define PHX_TRY(x) do { int r_ = (x); if (r_) return r_; } while (0)
+
+    int upload() {
+        const int N = geo.N();
+        Scn<R>& s = h;
+        s.nx = geo.nx; s.ny = geo.ny; s.nz = geo.nz; s.N = N; s.NX = geo.NX(); s.NY = geo.NY(); s.NZ = geo.NZ();
+        s.dx = geo.dx; s.ox = geo.ox; s.oy = geo.oy; s.oz = geo.oz;
+        s.cfl = cfl; s.dtMaxP = dtMaxP; s.tol = tol; s.relTol = relTol; s.maxIters = maxIters; s.radiationOn = radiationOn;
+        double th = geo.windFromDeg * 3.14159265 / 180.0;
+        s.windSpeed = geo.windSpeed; s.windSin = std::sin(th); s.windCos = std::cos(th); s.windExp = geo.windExp;
+        s.nZones = (int)Z.zoneP.size();
+        s.nClosed = (int)Z.closed.size();
+        PHX_TRY(putRaw(s.blocked, geo.blocked.data(), N));
+        PHX_TRY(put(s.fx, geo.fx)); PHX_TRY(put(s.fy, geo.fy)); PHX_TRY(put(s.fz, geo.fz));
+        PHX_TRY(put(s.ax, geo.ax)); PHX_TRY(put(s.ay, geo.ay)); PHX_TRY(put(s.az, geo.az));
+        PHX_TRY(put(s.a0x, MG.a0x)); PHX_TRY(put(s.a0y, MG.a0y)); PHX_TRY(put(s.a0z, MG.a0z));
+        PHX_TRY(put(s.diag, MG.lv[0].diag));
+        PHX_TRY(putRaw(const_cast<int*>(s.zone), Z.zone.data(), N));
+        PHX_TRY(putRaw(const_cast<uint8_t*>(s.zoneOpen), Z.zoneOpen.data(), Z.zoneOpen.size()));
+        PHX_TRY(putRaw(const_cast<int*>(s.closedZone), Z.closed.data(), Z.closed.size()));
+        PHX_TRY(putRaw(const_cast<int*>(s.closedStart), Z.closedStart.data(), Z.closedStart.size()));
+        PHX_TRY(putRaw(const_cast<int*>(s.closedCells), Z.closedCells.data(), Z.closedCells.size()));
+        PHX_TRY(putRaw(s.zoneP, Z.zoneP.data(), Z.zoneP.size()));
+        PHX_TRY(putRaw(s.zoneVol, Z.zoneVol.data(), Z.zoneVol.size()));
+        // initial state (src/sim/discretize.cpp:28-31)
+        const double amb[NSC] = {K_T0, K_YO2_AMB, 0, 0, 0, 0, K_YCO2_AMB, K_YH2O_AMB, 0, 0};
+        for (int q = 0; q < NSC; ++q) { PHX_TRY(fillR(s.sc[q], N, amb[q])); PHX_TRY(fillR(s.sc2[q], N, amb[q])); }
+        PHX_TRY(put(s.Pb, Pb0));
+        for (int l = 1; l < (int)MG.lv.size(); ++l) {
+            const MgLevel& L = MG.lv[l];
+            Level<R>& D = s.lv[l];
+            PHX_TRY(putRaw(const_cast<int*>(D.rowStart), L.rowStart.data(), L.rowStart.size()));
+            PHX_TRY(putRaw(const_cast<int*>(D.col), L.col.data(), L.col.size()));
+            PHX_TRY(put(const_cast<R*>(D.val), L.val));
+            PHX_TRY(put(const_cast<R*>(D.diag), L.diag));
+        }
+        for (int l = 0; l < (int)MG.lv.size(); ++l) {
+            const MgLevel& L = MG.lv[l];
+            Level<R>& D = s.lv[l];
+            if (D.agg) PHX_TRY(putRaw(const_cast<int*>(D.agg), L.agg.data(), L.agg.size()));
+            if (D.childStart) PHX_TRY(putRaw(const_cast<int*>(D.childStart), L.childStart.data(), L.childStart.size()));
+            if (D.child) PHX_TRY(putRaw(const_cast<int*>(D.child), L.child.data(), L.child.size()));
+            if (D.dense) PHX_TRY(put(const_cast<R*>(D.dense), L.dense));
+        }
+        R* dd[2] = {dbuf[0], dbuf[1]};
+        PHX_TRY(putRaw(dD, dd, 2));
+        PHX_TRY(buildDomains());
+        return pushDescriptor();
+    }
+
+    int pushDescriptor() {
+        h.nsrc = (int)(ignitions.size() + burners.size());
+        int q = 0;
+        for (auto& s : ignitions) h.src[q++] = s;
+        for (auto& s : burners) h.src[q++] = s;
+        PHX_CK(cudaMemcpyAsync(dS, &h, sizeof(Scn<R>), cudaMemcpyHostToDevice, st));
+        PHX_CK(cudaStreamSynchronize(st));
+        return PHX_OK;
+    }
+
+    int buildDomains() {
+        const int N = geo.N(), nx = geo.nx, ny = geo.ny, nz = geo.nz;
+        auto cdiv = [](long long a, long long b) { return (int)((a + b - 1) / b); };
+        int tiles[D_COUNT] = {};
+        tiles[D_ONE] = 1;
+        tiles[D_CELLS] = cdiv(N, TPB);
+        tiles[D_HALF] = cdiv((long long)((nx + 1) / 2) * ny * nz, TPB);
+        tiles[D_BLK] = cdiv((long long)((nx + 1) / 2) * ((ny + 1) / 2) * ((nz + 1) / 2), TPB);
+        tiles[D_FX] = cdiv(geo.NX(), TPB);
+        tiles[D_FY] = cdiv(geo.NY(), TPB);
+        tiles[D_FZ] = cdiv(geo.NZ(), TPB);
+        tiles[D_BX] = cdiv((long long)ny * nz * 2, TPB);
+        tiles[D_BY] = cdiv((long long)nx * nz * 2, TPB);
+        tiles[D_BZ] = cdiv((long long)nx * ny, TPB);
+        tiles[D_CZ] = (int)Z.closed.size();
+        tiles[D_CC] = cdiv((long long)Z.closedCells.size(), TPB);
+        const int nl = (int)MG.lv.size();
+        const MgLevel& Lc = MG.lv[nl - 1];
+        tiles[D_CO_DENSE] = Lc.dense.empty() ? 0 : cdiv(Lc.n, TPB / 32);
+        tiles[D_CO_SERIAL] = Lc.dense.empty() ? 1 : 0;
+        for (int l = 1; l < MAX_LEVELS; ++l) {
+            tiles[D_LV0 + l] = (l < nl - 1) ? cdiv(MG.lv[l].n, TPB) : 0;
+            tiles[D_RS0 + l] = (l + 1 <= nl - 1) ? cdiv(MG.lv[l + 1].n, TPB) : 0;
+        }
+        std::vector<int> starts(D_COUNT * 2);
+        for (int d = 0; d < D_COUNT; ++d) {
+            starts[2 * d] = 0;
+            starts[2 * d + 1] = tiles[d];
+            dom[d].start = dDomStart + 2 * d;
+            dom[d].nscn = 1;
+            dom[d].total = tiles[d];
+        }
+        return putRaw(dDomStart, starts.data(), starts.size());
+    }
+
+    // ---- sources ---------------------------------------------------------------
+    int addBurner(double x0, double y0, double x1, double y1, double z, double peakW, double rampS, double start,
+                  double duration, int* index) override {
+        if (index) *index = -1;
+        std::vector<int> cells = burnerCells(geo, x0, y0, x1, y1, z);
+        if (cells.empty()) { err = "burner covers no gas cell"; return PHX_ERR_INVALID; }
+        if ((int)(ignitions.size() + burners.size()) >= MAX_SRC) { err = "too many burners and ignitions (16)"; return PHX_ERR_INVALID; }
+        Src s{};
+        s.kind = 1;
+        s.i0 = s.j0 = 1 << 30; s.i1 = s.j1 = -1; s.k = -1;
+        for (int c : cells) {
+            int i = c % geo.nx, j = (c / geo.nx) % geo.ny, k = c / (geo.nx * geo.ny);
+            s.i0 = std::min(s.i0, i); s.i1 = std::max(s.i1, i); s.j0 = std::min(s.j0, j); s.j1 = std::max(s.j1, j);
+            if (s.k >= 0 && s.k != k) { err = "burner cells span several layers"; return PHX_ERR_UNSUPPORTED; }
+            s.k = k;
+        }
+        // the device selects the unblocked cells of the box: check that this is the same set
+        size_t inBox = 0;
+        for (int j = s.j0; j <= s.j1; ++j)
+            for (int i = s.i0; i <= s.i1; ++i) inBox += !geo.blocked[geo.cell(i, j, s.k)];
+        if (inBox != cells.size()) { err = "burner cells do not form a box of gas cells"; return PHX_ERR_UNSUPPORTED; }
+        s.ncells = (int)cells.size();
+        s.peakW = peakW; s.rampS = rampS; s.start = start; s.duration = duration;
+        burners.push_back(s);
+        if (index) *index = (int)burners.size() - 1;
+        return pushDescriptor();
+    }
+
+    int addIgnition(int cell, double power, double duration) override {
+        if (cell < 0 || cell >= geo.N()) return PHX_OK;   // the reference ignores it
+        if ((int)(ignitions.size() + burners.size()) >= MAX_SRC) { err = "too many burners and ignitions (16)"; return PHX_ERR_INVALID; }
+        PHX_CK(cudaMemcpyAsync(hPin, h.sv + SV_TIME, sizeof(double), cudaMemcpyDeviceToHost, st));
+        PHX_CK(cudaStreamSynchronize(st));
+        Src s{};
+        s.kind = 0;
+        s.i0 = s.i1 = cell % geo.nx; s.j0 = s.j1 = (cell / geo.nx) % geo.ny; s.k = cell / (geo.nx * geo.ny);
+        s.ncells = 1;
+        s.power = power; s.start = hPin[0]; s.duration = duration;
+        ignitions.push_back(s);
+        return pushDescriptor();
+    }
+
+    // ---- launch helpers -------------------------------------------------------
+    // ---- profiling: CUDA events around every launch, summed per kernel name
+    bool prof = false;
+    std::vector<cudaEvent_t> evPool;
+    std::vector<std::pair<const char*, int>> evUse;   // (kernel name, first event index)
+    int evNext = 0;
+    struct KStat { std::string name; int launches = 0; double ms = 0; };
+    std::vector<KStat> kstats;
+    void* flushBuf = nullptr;
+    size_t flushBytes = 0;
+
+    template <class K, class... A>
+    void launch(const char* name, int d, int threads, K kern, A... args) {
+        if (dom[d].total <= 0) return;
+        if (prof) {
+            if (evNext + 2 > (int)evPool.size()) {
+                for (int i = 0; i < 64; ++i) { cudaEvent_t e; cudaEventCreate(&e); evPool.push_back(e); }
+            }
+            cudaEventRecord(evPool[evNext], st);
+            kern<<<dom[d].total, threads, 0, st>>>(args...);
+            cudaEventRecord(evPool[evNext + 1], st);
+            evUse.push_back({name, evNext});
+            evNext += 2;
+        } else {
+            kern<<<dom[d].total, threads, 0, st>>>(args...);
+        }
+        ++launches;
+    }
+
+    int collectProfile() {
+        PHX_CK(cudaStreamSynchronize(st));
+        for (auto& u : evUse) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, evPool[u.second], evPool[u.second + 1]);
+            KStat* k = nullptr;
+            for (auto& x : kstats) if (x.name == u.first) k = &x;
+            if (!k) { kstats.push_back(KStat{u.first, 0, 0}); k = &kstats.back(); }
+            k->launches++;
+            k->ms += ms;
+        }
+        evUse.clear();
+        evNext = 0;
+        return PHX_OK;
+    }
+
+    void swapHost(int what) {
+        if (what & 1) std::swap(h.lit, h.lit2);
+        if (what & 2) { std::swap(h.u, h.u2); std::swap(h.v, h.v2); std::swap(h.w, h.w2); }
+        if (what & 4) for (int q = 0; q < NSC; ++q) std::swap(h.sc[q], h.sc2[q]);
+    }
+    void swapBoth(int what) {
+        launch("k_swap", D_ONE, 32, k_swap<R>, dS, dom[D_ONE], what);
+        swapHost(what);
+    }
+
+    // stages -----------------------------------------------------------------
+    void stBegin(bool computeDt, double dtMaxOrDt) {
+        // dtMax travels through the scalar block
+        if (computeDt) {
+            hPin[0] = dtMaxOrDt;
+            cudaMemcpyAsync(h.sv + SV_DTMAX_ARG, hPin, sizeof(double), cudaMemcpyHostToDevice, st);
+        }
+        launch("k_begin", D_ONE, 32, k_begin<R>, (const Scn<R>*)dS, dom[D_ONE], computeDt ? 1 : 0, dtMaxOrDt);
+    }
+    void stCombustion() {
+        launch("k_combust", D_CELLS, TPB, k_combust<R>, (const Scn<R>*)dS, dom[D_CELLS]);
+        swapBoth(1);
+    }
+    void stTurbulence() {
+        const Scn<R>* S = dS;
+        launch("k_turb_center", D_CELLS, TPB, k_turb_center<R>, S, dom[D_CELLS]);
+        for (int q = 0; q < 3; ++q)
+            for (int a = 0; a < 3; ++a) launch("k_turb_filter", D_CELLS, TPB, k_turb_filter<R>, S, dom[D_CELLS], q, a);
+        launch("k_turb_nu", D_CELLS, TPB, k_turb_nu<R>, S, dom[D_CELLS]);
+    }
+    void stHeat() { launch("k_heat", D_CELLS, TPB, k_heat<R>, (const Scn<R>*)dS, dom[D_CELLS]); }
+    void stEnergy() { launch("k_energy", D_CELLS, TPB, k_energy<R>, (const Scn<R>*)dS, dom[D_CELLS]); }
+    void stMomentum() {
+        const Scn<R>* S = dS;
+        launch("k_momentum", D_FX, TPB, k_momentum<R>, S, dom[D_FX], 0);
+        launch("k_momentum", D_FY, TPB, k_momentum<R>, S, dom[D_FY], 1);
+        launch("k_momentum", D_FZ, TPB, k_momentum<R>, S, dom[D_FZ], 2);
+        launch("k_mom_bnd", D_BX, TPB, k_mom_bnd<R>, S, dom[D_BX], 0);
+        launch("k_mom_bnd", D_BY, TPB, k_mom_bnd<R>, S, dom[D_BY], 1);
+        launch("k_mom_bnd", D_BZ, TPB, k_mom_bnd<R>, S, dom[D_BZ], 2);
+        swapBoth(2);
+    }
+    void stLeakage() {
+        if (!Z.closed.empty()) launch("k_zone_integral", D_CZ, TPB, k_zone_integral<R>, (const Scn<R>*)dS, dom[D_CZ]);
+    }
+    void vcycleBody() {
+        const Scn<R>* S = dS;
+        launch("k_gs0", D_HALF, TPB, k_gs0<R>, S, dom[D_HALF], 1, 1);
+        launch("k_res0_restrict", D_BLK, TPB, k_res0_restrict<R>, S, dom[D_BLK]);
+        for (int l = 1; l < maxLevels - 1; ++l) {
+            launch("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, dom[D_LV0 + l], l, 0);
+            launch("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, dom[D_LV0 + l], l, 1);
+            launch("k_restrict", D_RS0 + l, TPB, k_restrict<R>, S, dom[D_RS0 + l], l);
+        }
+        launch("k_coarse_dense", D_CO_DENSE, TPB, k_coarse_dense<R>, S, dom[D_CO_DENSE], maxLevels - 1);
+        launch("k_coarse_serial", D_CO_SERIAL, 32, k_coarse_serial<R>, S, dom[D_CO_SERIAL], maxLevels - 1);
+        for (int l = maxLevels - 2; l >= 1; --l) {
+            launch("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, dom[D_LV0 + l], l, 2);
+            launch("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, dom[D_LV0 + l], l, 1);
+        }
+        launch("k_gs0", D_HALF, TPB, k_gs0<R>, S, dom[D_HALF], 1, 2);
+    }
+    int readDone(bool& allDone) {
+        PHX_CK(cudaMemcpyAsync(hPin + 8, h.sv + SV_DONE, sizeof(double), cudaMemcpyDeviceToHost, st));
+        PHX_CK(cudaStreamSynchronize(st));
+        allDone = hPin[8] != 0;
+        return PHX_OK;
+    }
+    int stProject() {
+        const Scn<R>* S = dS;
+        cudaMemsetAsync(h.sv + SV_DONE, 0, sizeof(double), st);
+        cudaMemsetAsync(h.sv + SV_IT, 0, sizeof(double), st);
+        cudaMemsetAsync(h.sv + SV_RMAX, 0, sizeof(double), st);
+        cudaMemsetAsync(h.sv + SV_BMAX, 0, sizeof(double), st);
+        launch("k_rhs", D_CELLS, TPB, k_rhs<R>, S, dom[D_CELLS]);
+        launch("k_gs0", D_HALF, TPB, k_gs0<R>, S, dom[D_HALF], 0, 0);
+        vcycleBody();
+        launch("k_gs0_last_dot", D_CELLS, TPB, k_gs0_last_dot<R>, S, dom[D_CELLS], 0);
+        bool done = false;
+        PHX_TRY(readDone(done));
+        for (int it = 0; !done && it <= maxIters + 1; ++it) {
+            launch("k_cg_apply", D_CELLS, TPB, k_cg_apply<R>, S, dom[D_CELLS], (R* const*)dD);
+            launch("k_cg_update", D_CELLS, TPB, k_cg_update<R>, S, dom[D_CELLS], (R* const*)dD);
+            vcycleBody();
+            launch("k_gs0_last_dot", D_CELLS, TPB, k_gs0_last_dot<R>, S, dom[D_CELLS], 1);
+            PHX_TRY(readDone(done));
+        }
+        if (!Z.closed.empty()) {
+            launch("k_zone_mean", D_CZ, TPB, k_zone_mean<R>, S, dom[D_CZ]);
+            launch("k_zone_mean_sub", D_CC, TPB, k_zone_mean_sub<R>, S, dom[D_CC]);
+        }
+        launch("k_velcorr", D_FX, TPB, k_velcorr<R>, S, dom[D_FX], 0);
+        launch("k_velcorr", D_FY, TPB, k_velcorr<R>, S, dom[D_FY], 1);
+        launch("k_velcorr", D_FZ, TPB, k_velcorr<R>, S, dom[D_FZ], 2);
+        return PHX_OK;
+    }
+    void stAdvect() {
+        launch("k_advect", D_CELLS, TPB, k_advect<R>, (const Scn<R>*)dS, dom[D_CELLS]);
+        swapBoth(4);
+    }
+    void stEnd() {
+        const Scn<R>* S = dS;
+        if (!Z.closed.empty()) {
+            launch("k_zone_pressure", D_ONE, 32, k_zone_pressure<R>, S, dom[D_ONE]);
+            launch("k_zone_pb", D_CC, TPB, k_zone_pb<R>, S, dom[D_CC]);
+        }
+        launch("k_stats", D_CELLS, TPB, k_stats<R>, S, dom[D_CELLS]);
+    }
+
+    int checkLaunch() {
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) { err = std::string("kernel launch: ") + cudaGetErrorString(e); return PHX_ERR_CUDA; }
+        return PHX_OK;
+    }
+
+    int oneStep(double dtMax) {
+        stBegin(true, dtMax);
+        stCombustion();
+        stTurbulence();
+        stHeat();
+        stEnergy();
+        stMomentum();
+        stLeakage();
+        PHX_TRY(stProject());
+        stAdvect();
+        stEnd();
+        return checkLaunch();
+    }
+
+    int step(int n, double dtMax, double* dtOut) override {
+        for (int i = 0; i < n; ++i) {
+            launches = 0;
+            PHX_TRY(oneStep(dtMax));
+            if (dtOut) {
+                PHX_CK(cudaMemcpyAsync(hPin + 16, h.sv + SV_DT, sizeof(double), cudaMemcpyDeviceToHost, st));
+                PHX_CK(cudaStreamSynchronize(st));
+                dtOut[i] = hPin[16];
+            }
+        }
+        return PHX_OK;
+    }
+
+    int stage(int which, double arg) override {
+        switch (which) {
+        case PHX_STAGE_BEGIN: stBegin(true, arg); break;
+        case PHX_STAGE_COMBUSTION: stBegin(false, arg); stCombustion(); break;
+        case PHX_STAGE_TURBULENCE: stTurbulence(); break;
+        case PHX_STAGE_HEAT: stBegin(false, arg); stHeat(); break;
+        case PHX_STAGE_ENERGY: stBegin(false, arg); stEnergy(); break;
+        case PHX_STAGE_MOMENTUM: stBegin(false, arg); stMomentum(); break;
+        case PHX_STAGE_LEAKAGE: stBegin(false, arg); stLeakage(); break;
+        case PHX_STAGE_PROJECT: stBegin(false, arg); PHX_TRY(stProject()); break;
+        case PHX_STAGE_ADVECT: stBegin(false, arg); stAdvect(); break;
+        case PHX_STAGE_END: stBegin(false, arg); stEnd(); break;
+        default: err = "unknown stage"; return PHX_ERR_INVALID;
+        }
+        PHX_TRY(checkLaunch());
+        PHX_CK(cudaStreamSynchronize(st));
+        return PHX_OK;
+    }
+
+    int precondition(const double* r, double* z) override {
+        const int N = geo.N();
+        std::vector<double> rv(r, r + N);
+        PHX_TRY(put(h.r, rv));
+        cudaMemsetAsync(h.sv + SV_DONE, 0, sizeof(double), st);
+        launch("k_gs0", D_HALF, TPB, k_gs0<R>, (const Scn<R>*)dS, dom[D_HALF], 0, 0);
+        vcycleBody();
+        launch("k_gs0_last_dot", D_CELLS, TPB, k_gs0_last_dot<R>, (const Scn<R>*)dS, dom[D_CELLS], 2);
+        PHX_TRY(checkLaunch());
+        return getReal(h.z, N, z);
+    }
+
+    // ---- fields ----------------------------------------------------------------
+    int getReal(const R* src, size_t n, double* out) {
+        if (std::is_same<R, double>::value) {
+            PHX_CK(cudaMemcpyAsync(out, src, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+            PHX_CK(cudaStreamSynchronize(st));
+            return PHX_OK;
+        }
+        std::vector<R> tmp(n);
+        PHX_CK(cudaMemcpyAsync(tmp.data(), src, n * sizeof(R), cudaMemcpyDeviceToHost, st));
+        PHX_CK(cudaStreamSynchronize(st));
+        for (size_t i = 0; i < n; ++i) out[i] = (double)tmp[i];
+        return PHX_OK;
+    }
+
+    bool fieldPtr(int f, void** p, size_t* n, int* type) {
+        const size_t N = geo.N(), NX = geo.NX(), NY = geo.NY(), NZ = geo.NZ();
+        *type = 0;
+        switch (f) {
+        case PHX_FIELD_U: *p = h.u; *n = NX; return true;
+        case PHX_FIELD_V: *p = h.v; *n = NY; return true;
+        case PHX_FIELD_W: *p = h.w; *n = NZ; return true;
+        case PHX_FIELD_P: *p = h.p; *n = N; return true;
+        case PHX_FIELD_S: *p = h.S; *n = N; return true;
+        case PHX_FIELD_NU: *p = h.nu; *n = N; return true;
+        case PHX_FIELD_PB: *p = h.Pb; *n = N; return true;
+        case PHX_FIELD_Q: *p = h.Q; *n = N; return true;
+        case PHX_FIELD_QR: *p = h.Qr; *n = N; return true;
+        case PHX_FIELD_HRR: *p = h.hrr; *n = N; return true;
+        case PHX_FIELD_MASSSRC: *p = h.massSrc; *n = N; return true;
+        case PHX_FIELD_RHS: *p = h.b; *n = N; return true;
+        case PHX_FIELD_CGR: *p = h.r; *n = N; return true;
+        case PHX_FIELD_CGZ: *p = h.z; *n = N; return true;
+        case PHX_FIELD_LIT: *p = h.lit; *n = N; *type = 1; return true;
+        case PHX_FIELD_ZONE: *p = (void*)h.zone; *n = N; *type = 2; return true;
+        default:
+            if (f >= PHX_FIELD_T && f <= PHX_FIELD_YAI) { *p = h.sc[f - PHX_FIELD_T]; *n = N; return true; }
+            return false;
+        }
+    }
+
+    size_t fieldCount(int f) const override {
+        void* p;
+        size_t n;
+        int t;
+        return const_cast<Ctx*>(this)->fieldPtr(f, &p, &n, &t) ? n : 0;
+    }
+
+    int getField(int f, void* host, size_t bytes) override {
+        void* p;
+        size_t n;
+        int t;
+        if (!fieldPtr(f, &p, &n, &t)) { err = "unknown field"; return PHX_ERR_INVALID; }
+        size_t want = n * (t == 0 ? sizeof(double) : t == 1 ? 1 : 4);
+        if (bytes != want) { err = "field size mismatch: expected " + std::to_string(want) + " bytes"; return PHX_ERR_INVALID; }
+        if (t == 0) return getReal((const R*)p, n, (double*)host);
+        PHX_CK(cudaMemcpyAsync(host, p, bytes, cudaMemcpyDeviceToHost, st));
+        PHX_CK(cudaStreamSynchronize(st));
+        return PHX_OK;
+    }
+
+    int setField(int f, const void* host, size_t bytes) override {
+        void* p;
+        size_t n;
+        int t;
+        if (!fieldPtr(f, &p, &n, &t) || f == PHX_FIELD_ZONE) { err = "unknown or read-only field"; return PHX_ERR_INVALID; }
+        size_t want = n * (t == 0 ? sizeof(double) : t == 1 ? 1 : 4);
+        if (bytes != want) { err = "field size mismatch: expected " + std::to_string(want) + " bytes"; return PHX_ERR_INVALID; }
+        if (t == 0) {
+            const double* d = (const double*)host;
+            return put<R>((R*)p, std::vector<double>(d, d + n));
+        }
+        PHX_CK(cudaMemcpyAsync(p, host, bytes, cudaMemcpyHostToDevice, st));
+        PHX_CK(cudaStreamSynchronize(st));
+        return PHX_OK;
+    }
+
+    int getStats(phx_stats* o) override {
+        PHX_CK(cudaMemcpyAsync(hPin + 64, h.sv, SV_COUNT * sizeof(double), cudaMemcpyDeviceToHost, st));
+        PHX_CK(cudaStreamSynchronize(st));
+        const double* sv = hPin + 64;
+        o->time = sv[SV_TIME]; o->dt = sv[SV_DT];
+        o->max_vel = sv[SV_MAXVEL]; o->max_nu = sv[SV_MAXNU]; o->max_div = sv[SV_MAXDIV];
+        o->pressure_iters = (int)sv[SV_IT]; o->pressure_residual = sv[SV_PRES]; o->pressure_rel_residual = sv[SV_PREL];
+        o->hrr = sv[SV_HRR]; o->max_gas_t = sv[SV_MAXGAST]; o->burning_cells = (int)sv[SV_BURNING];
+        o->fuel_in = sv[SV_FUELIN]; o->fuel_burned = sv[SV_FUELBURNED]; o->fuel_in_domain = sv[SV_FUELINDOMAIN];
+        o->zones = (int)Z.zoneP.size(); o->leak_faces = 0;
+        return PHX_OK;
+    }
+
+    int setScalars(double time, double maxVel, double maxNu, double maxDiv) override {
+        double v[4] = {time, maxVel, maxNu, maxDiv};
+        PHX_CK(cudaMemcpyAsync(h.sv + SV_TIME, &v[0], sizeof(double), cudaMemcpyHostToDevice, st));
+        PHX_CK(cudaMemcpyAsync(h.sv + SV_MAXVEL, &v[1], sizeof(double), cudaMemcpyHostToDevice, st));
+        PHX_CK(cudaMemcpyAsync(h.sv + SV_MAXNU, &v[2], sizeof(double), cudaMemcpyHostToDevice, st));
+        PHX_CK(cudaMemcpyAsync(h.sv + SV_MAXDIV, &v[3], sizeof(double), cudaMemcpyHostToDevice, st));
+        PHX_CK(cudaStreamSynchronize(st));
+        return PHX_OK;
+    }
+
+    size_t deviceBytes() const override { return arenaBytes; }
+    int sync() override {
+        PHX_CK(cudaStreamSynchronize(st));
+        return PHX_OK;
+    }
+    int lastLaunches() const override { return launches; }
+
+    // n steps timed with CUDA events on the context's stream; with flushL2 a
+    // buffer larger than L2 is written (untimed) before each step
+    int timeSteps(int n, double dtMax, int flushL2, double* totalMs, int* launchesOut) override {
+        if (flushL2 && !flushBuf) {
+            flushBytes = (size_t)512 << 20;
+            PHX_CK(cudaMalloc(&flushBuf, flushBytes));
+        }
+        PHX_CK(cudaStreamSynchronize(st));
+        double total = 0;
+        int nl = 0;
+        for (int i = 0; i < n; ++i) {
+            if (flushL2) PHX_CK(cudaMemsetAsync(flushBuf, i & 0xff, flushBytes, st));
+            PHX_CK(cudaEventRecord(ev[0], st));
+            launches = 0;
+            PHX_TRY(oneStep(dtMax));
+            nl += launches;
+            PHX_CK(cudaEventRecord(ev[1], st));
+            PHX_CK(cudaEventSynchronize(ev[1]));
+            float ms = 0;
+            PHX_CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+            total += ms;
+        }
+        if (totalMs) *totalMs = total;
+        if (launchesOut) *launchesOut = nl;
+        return PHX_OK;
+    }
+
+    // one step with an event pair around every launch; per-kernel totals
+    int profileStep(double dtMax, int flushL2, phx_kernel_time* out, int cap, int* count) override {
+        if (flushL2) {
+            if (!flushBuf) { flushBytes = (size_t)512 << 20; PHX_CK(cudaMalloc(&flushBuf, flushBytes)); }
+            PHX_CK(cudaMemsetAsync(flushBuf, 0x5a, flushBytes, st));
+        }
+        kstats.clear();
+        prof = true;
+        launches = 0;
+        int r = oneStep(dtMax);
+        prof = false;
+        PHX_TRY(r);
+        PHX_TRY(collectProfile());
+        int n = 0;
+        for (auto& k : kstats) {
+            if (n < cap && out) {
+                std::memset(&out[n], 0, sizeof(phx_kernel_time));
+                std::strncpy(out[n].name, k.name.c_str(), sizeof(out[n].name) - 1);
+                out[n].launches = k.launches;
+                out[n].ms = k.ms;
+            }
+            ++n;
+        }
+        if (count) *count = n;
+        return PHX_OK;
+    }
+};
+
+#undef PHX_TRY
+}  // namespace phx

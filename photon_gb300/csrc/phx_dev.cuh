@@ -1,0 +1,206 @@
+// Device-side data layout and helpers of the GB300 gas-phase step.
+//
+// One scenario's state lives in HBM as structure-of-arrays in the reference's
+// index order (src/sim/solver.h:216-220), so a field downloads into a
+// photon::Solver vector with one copy. A scenario is described to the kernels
+// by a Scn record in device memory; a launch covers one "domain" (cells,
+// faces of one axis, one multigrid level, ...) of every scenario of a batch,
+// with CTA b of the launch mapped to (scenario, tile) by a prefix table.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace phx {
+
+// model constants: src/sim/solver.h:159-181, src/sim/gasphase.cpp:25-32,
+// src/sim/solver.cpp:15-20, all as the FP64 values of the reference's literals
+constexpr double K_T0 = 293.15;
+constexpr double K_P0 = 101325.0;
+constexpr double K_RS = 287.0;
+constexpr double K_CP = 1100.0;
+constexpr double K_G = 9.81;
+constexpr double K_YO2_AMB = 0.232;
+constexpr double K_DHC_FUEL = 25.0e6;
+constexpr double K_S_O2 = 1.95;
+constexpr double K_Y_H2O = 0.761;
+constexpr double K_C_FRAC = 0.597;
+constexpr double K_CO_YIELD = 0.02;
+constexpr double K_YCO2_AMB = 0.0006;
+constexpr double K_YH2O_AMB = 0.0073;
+constexpr double K_CHI_R = 0.35;
+constexpr double K_T_CRIT = 1600.0;
+constexpr double K_T_AUTO = 800.0;
+constexpr double K_TAU_MIX = 0.1;
+constexpr double K_PR_T = 0.5;
+constexpr double K_SC_T = 0.5;
+constexpr double K_C_NU = 0.1;
+constexpr double K_D_MAX = 50.0;
+constexpr double K_VMAX = 40.0;
+constexpr double K_T_MIN = 200.0;
+constexpr double K_T_MAX = 2300.0;
+constexpr double K_BURNER_SOOT = 0.01;
+constexpr double K_GAMMA = K_CP / (K_CP - K_RS);
+
+constexpr int NSC = 10;          // transported scalars: T Yo Yf Ys Ya Yp Yc Yw Yco Yai
+constexpr int MAX_SRC = 16;      // burners + ignitions per scenario
+constexpr int MAX_LEVELS = 12;   // multigrid levels (the reference's cap)
+constexpr int TPB = 256;         // threads per CTA of the cell/face kernels
+
+// scalar slots of a scenario (double each)
+enum Slot {
+    SV_DTMAX_ARG = 0, SV_DT, SV_TIME, SV_MAXVEL, SV_MAXNU, SV_MAXDIV,
+    SV_RZ, SV_ALPHA, SV_BETA, SV_RMAX, SV_BMAX, SV_IT, SV_DONE, SV_DQ,
+    SV_PITERS, SV_PRES, SV_PREL, SV_HRR, SV_MAXGAST, SV_BURNING, SV_FUELIN, SV_FUELBURNED, SV_FUELINDOMAIN,
+    SV_INV, SV_ACTIVE,
+    SV_SRC_MF = 32,              // MAX_SRC injection amounts of this step (-1 = inactive)
+    SV_COUNT = 64
+};
+
+// reduction partial slots (each holds one double per CTA of the cell domain)
+enum PartSlot { PS_DQ = 0, PS_RZ, PS_HRR, PS_FUEL, PS_COUNT };
+
+// a burner or ignition source: the gas cells it feeds are the unblocked cells
+// of the box [i0,i1] x [j0,j1] x {k} (Solver::addBurner, src/sim/gasphase.cpp:72-90)
+struct Src {
+    int kind;                    // 0 ignition, 1 burner
+    int i0, i1, j0, j1, k;
+    int ncells;                  // b.cells.size() at addBurner time
+    double peakW, rampS, start, duration;   // burner
+    double power;                // ignition power (W)
+};
+
+template <class R>
+struct Level {
+    int n;                       // unknowns
+    const int *rowStart, *col;   // couplings (off-diagonal, positive), coarse levels
+    const R* val;
+    const R* diag;
+    const int* agg;              // unknown -> unknown of the next coarser level (nullptr at the coarsest)
+    const int *childStart, *child;   // next coarser unknown -> its unknowns here, ascending
+    R *x, *y, *b;                // iterate, Jacobi scratch, right-hand side
+    const R* dense;              // coarsest only: n x n operator of the reference's coarse solve
+};
+
+template <class R>
+struct Scn {
+    int nx, ny, nz, N, NX, NY, NZ;
+    double dx, ox, oy, oz;
+    double cfl, dtMaxP, tol, relTol;
+    int maxIters;
+    int radiationOn;
+    double windSpeed, windSin, windCos, windExp;   // sin/cos of the wind direction taken on the host
+    int nsrc;
+    Src src[MAX_SRC];
+    // geometry
+    const uint8_t* blocked;
+    const R *fx, *fy, *fz;       // face open fractions
+    const R *ax, *ay, *az;       // pressure-matrix coefficients (ax_, ay_, az_)
+    const R *a0x, *a0y, *a0z;    // the same with wind-inflow boundary faces closed (multigrid level 0)
+    const uint8_t *lx, *ly, *lz; // crack faces (null when there are none)
+    const R* diag;               // level-0 diagonal
+    const int* zone;
+    const uint8_t* zoneOpen;
+    int nZones, nClosed;
+    const int* closedZone;       // closed zone ids
+    const int *closedStart, *closedCells;   // per closed zone: its cells, ascending
+    double* zoneP;               // Pa per zone
+    double* zoneVol;
+    double* zoneDP;
+    double* zoneShift;
+    double* zoneMean;
+    // state
+    R *u, *v, *w, *u2, *v2, *w2;
+    R* sc[NSC];                  // current scalars
+    R* sc2[NSC];                 // next scalars (swapped after transport)
+    R *p, *S, *nu, *Pb, *Q, *Qr, *hrr, *massSrc;
+    uint8_t *lit, *lit2, *pilot;
+    R* tmp[9];                   // turbulence: cell-centre velocities and filter passes
+    // pressure solve
+    R *b, *r, *z, *d, *q;
+    int nLevels;
+    Level<R> lv[MAX_LEVELS];
+    // scalars and reductions
+    double* sv;
+    double* part;                // PS_COUNT x partStride
+    int partStride;
+    unsigned* cnt;               // last-CTA counters, one per reduction kind
+};
+
+// CTA -> (scenario, tile) over a domain
+struct Dom {
+    const int* start;            // [nscn + 1] prefix of CTAs per scenario
+    int nscn;
+    int total;                   // CTAs of the launch
+};
+
+__device__ __forceinline__ void locate(const Dom& d, int b, int& s, int& tile) {
+    int lo = 0, hi = d.nscn - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (__ldg(d.start + mid) <= b) lo = mid; else hi = mid - 1;
+    }
+    s = lo;
+    tile = b - __ldg(d.start + lo);
+}
+
+// libstdc++'s std::min / std::max / std::clamp
+__device__ __forceinline__ double mn(double a, double b) { return (b < a) ? b : a; }
+__device__ __forceinline__ double mx(double a, double b) { return (a < b) ? b : a; }
+__device__ __forceinline__ double clampd(double v, double lo, double hi) { return (v < lo) ? lo : (hi < v) ? hi : v; }
+__device__ __forceinline__ float mn(float a, float b) { return (b < a) ? b : a; }
+__device__ __forceinline__ float mx(float a, float b) { return (a < b) ? b : a; }
+__device__ __forceinline__ float clampd(float v, float lo, float hi) { return (v < lo) ? lo : (hi < v) ? hi : v; }
+
+// max of non-negative doubles through their bit patterns (order independent)
+__device__ __forceinline__ void atomicMaxPos(double* a, double v) {
+    if (!(v > 0)) return;
+    atomicMax(reinterpret_cast<unsigned long long*>(a), (unsigned long long)__double_as_longlong(v));
+}
+
+__device__ __forceinline__ double warpMax(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = mx(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ double warpSum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// CTA-wide max of non-negative values into *dst (one atomic per warp)
+__device__ __forceinline__ void blockMaxTo(double* dst, double v) {
+    v = warpMax(v);
+    if ((threadIdx.x & 31) == 0) atomicMaxPos(dst, v);
+}
+
+// fixed-order CTA sum (the order depends only on the CTA size)
+__device__ __forceinline__ double blockSum(double v, double* sh) {
+    v = warpSum(v);
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    double t = 0;
+    if (w == 0) {
+        t = l < nw ? sh[l] : 0.0;
+        t = warpSum(t);
+    }
+    return t;   // valid in thread 0
+}
+
+// Solver::windAt (src/sim/gasphase.cpp:52-61); NaN = no inflow on this face
+template <class R>
+__device__ __forceinline__ double windAt(const Scn<R>& s, int axis, int side, double z) {
+    if (s.windSpeed <= 0 || axis == 2) return __longlong_as_double(0x7ff8000000000000LL);
+    double U = s.windSpeed * pow(mx(z, 0.05) / 10.0, s.windExp);
+    double comp = axis == 0 ? -s.windSin * U : -s.windCos * U;
+    if (side == 0 && comp > 0) return comp;
+    if (side == 1 && comp < 0) return comp;
+    return __longlong_as_double(0x7ff8000000000000LL);
+}
+
+template <class R>
+__device__ __forceinline__ bool bndOpen(const Scn<R>& s, int axis, int side, double z) {
+    return isnan(windAt(s, axis, side, z));
+}
+
+}  // namespace phx

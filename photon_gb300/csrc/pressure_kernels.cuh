@@ -1,0 +1,346 @@
+// CUDA kernels of the pressure projection: the multigrid V-cycle
+// (src/sim/pressure_mg.cpp:193-300) and the preconditioned CG loop
+// (src/sim/gasphase.cpp:551-626).
+//
+// Level 0 is the structured 7-point grid: red-black Gauss-Seidel half sweeps
+// (gsColor) are order independent, so each colour is one launch. The residual
+// and the restriction to level 1 run in one pass over 2x2x2 blocks: every
+// level-1 aggregate lies inside one block, so a thread sums its aggregates'
+// residuals in ascending cell order -- the order of the reference's scatter.
+// Coarse levels are CSR rows: damped Jacobi (omega 0.7) and a gather of the
+// children's residuals in ascending order. The coarsest level's 20 forward +
+// backward Gauss-Seidel sweeps from x = 0 are a fixed linear map of b; it is
+// applied as a dense operator built on the host from those sweeps.
+//
+// The CG scalars live in device memory per scenario: the last CTA of each
+// reduction computes alpha, beta and the stop test, so no host round trip is
+// needed between iterations, and a converged scenario's CTAs return at once.
+#pragma once
+#include "step_kernels.cuh"
+
+namespace phx {
+
+#define PHX_PROLOGUE_ACTIVE(dom)          \
+    int s_, tile_;                        \
+    locate(dom, blockIdx.x, s_, tile_);   \
+    const Scn<R>& g = S[s_];              \
+    if (g.sv[SV_DONE] != 0) return;
+
+constexpr double OMEGA = 0.7;
+
+// level-0 Gauss-Seidel half sweep of one colour (gsColor, pressure_mg.cpp:195-216)
+// with b = r and x = z. mode 0: the other colour is still zero (x = b / diag);
+// mode 1: plain; mode 2: the other colour is first prolongated from level 1.
+template <class R>
+__global__ void k_gs0(const Scn<R>* __restrict__ S, Dom dom, int color, int mode) {
+    PHX_PROLOGUE_ACTIVE(dom);
+    const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
+    const int hx = (nx + 1) >> 1;
+    int t = tile_ * TPB + threadIdx.x;
+    if (t >= hx * ny * nz) return;
+    const int ii = t % hx, jk = t / hx, j = jk % ny, k = jk / ny;
+    const int i = 2 * ii + ((j + k + color) & 1);
+    if (i >= nx) return;
+    const int c = i + nx * (j + ny * k);
+    const double dg = g.diag[c];
+    R* x = g.z;
+    if (dg <= 0) { x[c] = 0; return; }
+    double s = g.r[c];
+    if (mode != 0) {
+        const int* agg = g.lv[0].agg;
+        const R* xc = g.lv[1].x;
+        auto X = [&](int n) -> double {
+            double v = x[n];
+            if (mode == 2) { int a = agg[n]; if (a >= 0) v = v + (double)xc[a]; }
+            return v;
+        };
+        const int fx0 = i + (nx + 1) * (j + ny * k), fy0 = i + nx * (j + (ny + 1) * k);
+        if (i > 0) s += (double)g.a0x[fx0] * X(c - 1);
+        if (i < nx - 1) s += (double)g.a0x[fx0 + 1] * X(c + 1);
+        if (j > 0) s += (double)g.a0y[fy0] * X(c - nx);
+        if (j < ny - 1) s += (double)g.a0y[fy0 + nx] * X(c + nx);
+        if (k > 0) s += (double)g.a0z[c] * X(c - sxy);
+        if (k < nz - 1) s += (double)g.a0z[c + sxy] * X(c + sxy);
+    }
+    x[c] = (R)(s / dg);
+}
+
+// level-0 residual (residualGrid, pressure_mg.cpp:217-235) and restriction to
+// level 1 (:285-286), one thread per 2x2x2 block
+template <class R>
+__global__ void k_res0_restrict(const Scn<R>* __restrict__ S, Dom dom) {
+    PHX_PROLOGUE_ACTIVE(dom);
+    const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
+    const int bx = (nx + 1) >> 1, by = (ny + 1) >> 1, bz = (nz + 1) >> 1;
+    int t = tile_ * TPB + threadIdx.x;
+    if (t >= bx * by * bz) return;
+    const int bi = t % bx, bj = (t / bx) % by, bk = t / (bx * by);
+    const R* x = g.z;
+    const int* agg = g.lv[0].agg;
+    R* cb = g.lv[1].b;
+    int ids[8];
+    double sums[8];
+    int na = 0;
+    for (int dk = 0; dk < 2; ++dk) {
+        const int k = 2 * bk + dk;
+        if (k >= nz) break;
+        for (int dj = 0; dj < 2; ++dj) {
+            const int j = 2 * bj + dj;
+            if (j >= ny) break;
+            for (int di = 0; di < 2; ++di) {
+                const int i = 2 * bi + di;
+                if (i >= nx) break;
+                const int c = i + nx * (j + ny * k);
+                const int A = agg[c];
+                if (A < 0) continue;
+                const double dg = g.diag[c];
+                const int fx0 = i + (nx + 1) * (j + ny * k), fy0 = i + nx * (j + (ny + 1) * k);
+                double s = (double)g.r[c] - dg * (double)x[c];
+                if (i > 0) s += (double)g.a0x[fx0] * (double)x[c - 1];
+                if (i < nx - 1) s += (double)g.a0x[fx0 + 1] * (double)x[c + 1];
+                if (j > 0) s += (double)g.a0y[fy0] * (double)x[c - nx];
+                if (j < ny - 1) s += (double)g.a0y[fy0 + nx] * (double)x[c + nx];
+                if (k > 0) s += (double)g.a0z[c] * (double)x[c - sxy];
+                if (k < nz - 1) s += (double)g.a0z[c + sxy] * (double)x[c + sxy];
+                s = (double)(R)s;
+                int e = 0;
+                while (e < na && ids[e] != A) ++e;
+                if (e == na) { ids[na] = A; sums[na] = 0.0; ++na; }
+                sums[e] = (double)(R)(sums[e] + s);
+            }
+        }
+    }
+    for (int e = 0; e < na; ++e) cb[ids[e]] = (R)sums[e];
+}
+
+// damped Jacobi sweep on a coarse level (jacobi, pressure_mg.cpp:237-247).
+// mode 0: from x = 0, into y; mode 1: y -> x; mode 2: x plus the coarser
+// level's x prolongated (:290-297), into y.
+template <class R>
+__global__ void k_jacobi(const Scn<R>* __restrict__ S, Dom dom, int l, int mode) {
+    PHX_PROLOGUE_ACTIVE(dom);
+    const Level<R>& L = g.lv[l];
+    const int I = tile_ * TPB + threadIdx.x;
+    if (I >= L.n) return;
+    R* out = mode == 1 ? L.x : L.y;
+    const double dg = L.diag[I];
+    if (dg <= 0) { out[I] = 0; return; }
+    if (mode == 0) {
+        double s = L.b[I];
+        out[I] = (R)((1 - OMEGA) * 0.0 + OMEGA * s / dg);
+        return;
+    }
+    const R* in = mode == 1 ? L.y : L.x;
+    const R* xc = mode == 2 ? g.lv[l + 1].x : nullptr;
+    const int* agg = L.agg;
+    auto X = [&](int n) -> double {
+        double v = in[n];
+        if (mode == 2) v = v + (double)xc[agg[n]];
+        return v;
+    };
+    double s = L.b[I];
+    for (int q = L.rowStart[I]; q < L.rowStart[I + 1]; ++q) s += (double)L.val[q] * X(L.col[q]);
+    out[I] = (R)((1 - OMEGA) * X(I) + OMEGA * s / dg);
+}
+
+// residual of coarse level l (residualSparse, pressure_mg.cpp:248-257) summed
+// into each unknown of level l+1 over its children in ascending order (:285-286)
+template <class R>
+__global__ void k_restrict(const Scn<R>* __restrict__ S, Dom dom, int l) {
+    PHX_PROLOGUE_ACTIVE(dom);
+    const Level<R>& L = g.lv[l];
+    Level<R>& C = const_cast<Level<R>&>(g.lv[l + 1]);
+    const int J = tile_ * TPB + threadIdx.x;
+    if (J >= C.n) return;
+    double acc = 0.0;
+    for (int e = L.childStart[J]; e < L.childStart[J + 1]; ++e) {
+        const int I = L.child[e];
+        const double dg = L.diag[I];
+        double r = 0;
+        if (dg > 0) {
+            double s = (double)L.b[I] - dg * (double)L.x[I];
+            for (int q = L.rowStart[I]; q < L.rowStart[I + 1]; ++q) s += (double)L.val[q] * (double)L.x[L.col[q]];
+            r = (double)(R)s;
+        }
+        acc = (double)(R)(acc + r);
+    }
+    C.b[J] = (R)acc;
+}
+
+// coarsest level: x = M b with the dense operator of the reference's 20
+// forward + backward Gauss-Seidel sweeps (pressure_mg.cpp:258-266, 279).
+// One warp per row.
+template <class R>
+__global__ void k_coarse_dense(const Scn<R>* __restrict__ S, Dom dom, int l) {
+    PHX_PROLOGUE_ACTIVE(dom);
+    const Level<R>& L = g.lv[l];
+    const int row = tile_ * (TPB / 32) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (row >= L.n) return;
+    const R* M = L.dense + (size_t)row * L.n;
+    double acc = 0;
+    for (int j = lane; j < L.n; j += 32) acc += (double)M[j] * (double)L.b[j];
+    acc = warpSum(acc);
+    if (lane == 0) L.x[row] = (R)acc;
+}
+
+// coarsest level solved as the reference does it: 20 forward + backward
+// sweeps, serially in one thread (used when the level is too large for a dense
+// operator)
+template <class R>
+__global__ void k_coarse_serial(const Scn<R>* __restrict__ S, Dom dom, int l) {
+    PHX_PROLOGUE_ACTIVE(dom);
+    if (threadIdx.x != 0) return;
+    const Level<R>& L = g.lv[l];
+    for (int I = 0; I < L.n; ++I) L.x[I] = 0;
+    for (int it = 0; it < 20; ++it)
+        for (int dir = 0; dir < 2; ++dir)
+            for (int t = 0; t < L.n; ++t) {
+                int I = dir == 0 ? t : L.n - 1 - t;
+                double dg = L.diag[I];
+                if (dg <= 0) { L.x[I] = 0; continue; }
+                double s = L.b[I];
+                for (int q = L.rowStart[I]; q < L.rowStart[I + 1]; ++q) s += (double)L.val[q] * (double)L.x[L.col[q]];
+                L.x[I] = (R)(s / dg);
+            }
+}
+
+// CG stop test of the reference (src/sim/gasphase.cpp:605) plus the optional
+// relative test max|r| <= relTol max|b|
+template <class R>
+__device__ __forceinline__ bool cgContinue(const Scn<R>& g, double res, double rmax, int it, double rz) {
+    double relStop = g.relTol > 0 ? g.relTol * g.sv[SV_BMAX] : -1.0;
+    return res > g.tol && it < g.maxIters && rz > 0 && !(rmax <= relStop);
+}
+
+// last level-0 half sweep of the V-cycle (red, after black) fused with the
+// r.z dot product of the CG (dotRZ, src/sim/gasphase.cpp:582-588); the last
+// CTA of the scenario closes the iteration. phase 0: first preconditioning
+// before the loop; 1: inside the loop; 2: a bare V-cycle (no CG bookkeeping).
+template <class R>
+__global__ void k_gs0_last_dot(const Scn<R>* __restrict__ S, Dom dom, int phase) {
+    PHX_PROLOGUE_ACTIVE(dom);
+    const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
+    const int c = tile_ * TPB + threadIdx.x;
+    double dot = 0;
+    if (c < g.N) {
+        const int i = c % nx, j = (c / nx) % ny, k = c / sxy;
+        R* x = g.z;
+        double zc;
+        if (((i + j + k) & 1) == 0) {
+            const double dg = g.diag[c];
+            if (dg <= 0) zc = 0;
+            else {
+                const int fx0 = i + (nx + 1) * (j + ny * k), fy0 = i + nx * (j + (ny + 1) * k);
+                double s = g.r[c];
+                if (i > 0) s += (double)g.a0x[fx0] * (double)x[c - 1];
+                if (i < nx - 1) s += (double)g.a0x[fx0 + 1] * (double)x[c + 1];
+                if (j > 0) s += (double)g.a0y[fy0] * (double)x[c - nx];
+                if (j < ny - 1) s += (double)g.a0y[fy0 + nx] * (double)x[c + nx];
+                if (k > 0) s += (double)g.a0z[c] * (double)x[c - sxy];
+                if (k < nz - 1) s += (double)g.a0z[c + sxy] * (double)x[c + sxy];
+                zc = (double)(R)(s / dg);
+            }
+            x[c] = (R)zc;
+        } else {
+            zc = x[c];
+        }
+        dot = (double)g.r[c] * zc;
+    }
+    if (phase == 2) return;
+    double tot;
+    if (lastCtaSum(g, PS_RZ, tile_, ntilesOf(dom, s_), dot, &tot) && threadIdx.x == 0) {
+        double* sv = g.sv;
+        const double rmax = sv[SV_RMAX];
+        const double res = rmax / sv[SV_INV];
+        int it = (int)sv[SV_IT];
+        if (phase == 0) {
+            sv[SV_RZ] = tot;
+            it = 0;
+        } else {
+            sv[SV_BETA] = tot / sv[SV_RZ];
+            sv[SV_RZ] = tot;
+            it += 1;
+        }
+        sv[SV_IT] = it;
+        sv[SV_PRES] = res;
+        sv[SV_PREL] = sv[SV_BMAX] > 0 ? rmax / sv[SV_BMAX] : 0.0;
+        sv[SV_RMAX] = 0;
+        if (!cgContinue(g, res, rmax, it, sv[SV_RZ])) sv[SV_DONE] = 1;
+    }
+}
+
+// q = A d with the search direction updated on the fly
+// (d = z + beta d, src/sim/gasphase.cpp:620-622, and apply :551-570), and the
+// d.q partial sums; the last CTA computes alpha or stops on d.q <= 0 (:606-608).
+// d is double-buffered by iteration parity.
+template <class R>
+__global__ void k_cg_apply(const Scn<R>* __restrict__ S, Dom dom, R* const* dbuf) {
+    PHX_PROLOGUE_ACTIVE(dom);
+    const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
+    const int c = tile_ * TPB + threadIdx.x;
+    const int it = (int)g.sv[SV_IT];
+    const R* dprev = dbuf[2 * s_ + (it & 1)];
+    R* dnew = dbuf[2 * s_ + ((it + 1) & 1)];
+    const double beta = g.sv[SV_BETA];
+    const R* z = g.z;
+    auto D = [&](int n) -> double {
+        return it == 0 ? (double)z[n] : (double)(R)((double)z[n] + (double)(R)(beta * (double)dprev[n]));
+    };
+    double dot = 0;
+    if (c < g.N) {
+        const double dc = D(c);
+        dnew[c] = (R)dc;
+        const double dg = g.diag[c];
+        if (dg <= 0) g.q[c] = 0;
+        else {
+            const int i = c % nx, j = (c / nx) % ny, k = c / sxy;
+            const int fx0 = i + (nx + 1) * (j + ny * k), fy0 = i + nx * (j + (ny + 1) * k);
+            double s = dg * dc;
+            if (i > 0) s -= (double)g.a0x[fx0] * D(c - 1);
+            if (i < nx - 1) s -= (double)g.a0x[fx0 + 1] * D(c + 1);
+            if (j > 0) s -= (double)g.a0y[fy0] * D(c - nx);
+            if (j < ny - 1) s -= (double)g.a0y[fy0 + nx] * D(c + nx);
+            if (k > 0) s -= (double)g.a0z[c] * D(c - sxy);
+            if (k < nz - 1) s -= (double)g.a0z[c + sxy] * D(c + sxy);
+            g.q[c] = (R)s;
+            dot = (double)(R)s * dc;
+        }
+    }
+    double tot;
+    if (lastCtaSum(g, PS_DQ, tile_, ntilesOf(dom, s_), dot, &tot) && threadIdx.x == 0) {
+        g.sv[SV_DQ] = tot;
+        if (tot <= 0) g.sv[SV_DONE] = 1;
+        else g.sv[SV_ALPHA] = g.sv[SV_RZ] / tot;
+    }
+}
+
+// p += alpha d; r -= alpha q (src/sim/gasphase.cpp:609-615), max|r| for the
+// stop test (:592-602), and the first red half sweep of the next V-cycle
+// (x = r / diag, the black cells being zero)
+template <class R>
+__global__ void k_cg_update(const Scn<R>* __restrict__ S, Dom dom, R* const* dbuf) {
+    PHX_PROLOGUE_ACTIVE(dom);
+    const int c = tile_ * TPB + threadIdx.x;
+    double rm = 0;
+    if (c < g.N) {
+        const int it = (int)g.sv[SV_IT];
+        const R* d = dbuf[2 * s_ + ((it + 1) & 1)];
+        const double alpha = g.sv[SV_ALPHA];
+        const double dg = g.diag[c];
+        double r = g.r[c];
+        if (dg > 0) {
+            g.p[c] = (R)((double)g.p[c] + (double)(R)(alpha * (double)d[c]));
+            r = (double)(R)(r - (double)(R)(alpha * (double)g.q[c]));
+            g.r[c] = (R)r;
+        }
+        rm = fabs(r);
+        const int nx = g.nx, ny = g.ny;
+        const int i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
+        if (((i + j + k) & 1) == 0) g.z[c] = dg > 0 ? (R)(r / dg) : (R)0;
+    }
+    blockMaxTo(g.sv + SV_RMAX, rm);
+}
+
+#undef PHX_PROLOGUE_ACTIVE
+}  // namespace phx

@@ -1,0 +1,830 @@
+// CUDA kernels of the gas-phase step (all stages except the pressure solve).
+//
+// Each kernel is one pass of the reference's step over one domain of every
+// scenario in a launch; the arithmetic of every cell or face restates the
+// reference expression in its own evaluation order (the FP64 build is compiled
+// with --fmad=false so no multiply-add is fused), which keeps the FP64 path
+// within rounding of the reference's own FP64 step. Reductions that the
+// reference sums in a fixed order are summed here in a fixed order as well:
+// per-CTA partials, then the last CTA of a scenario sums the partials in CTA
+// order, so results do not depend on scheduling.
+#pragma once
+#include "phx_dev.cuh"
+
+namespace phx {
+
+#define PHX_PROLOGUE(dom)                 \
+    int s_, tile_;                        \
+    locate(dom, blockIdx.x, s_, tile_);   \
+    const Scn<R>& g = S[s_];
+
+template <class R>
+__device__ __forceinline__ double gasDensity(const Scn<R>& g, int c) {
+    return (double)g.Pb[c] / (K_RS * (double)g.sc[0][c]);
+}
+
+// ---------------------------------------------------------------------------
+// Last-CTA reduction: every CTA of a scenario sums its threads' values (fixed
+// order) and stores the partial; the CTA that finishes last sums the partials
+// in CTA order. Every thread of the CTA must call it. Returns true in every
+// thread of the last CTA, with the total in *total (thread 0).
+template <class R>
+__device__ bool lastCtaSum(const Scn<R>& g, int slot, int tile, int ntiles, double vThread, double* total) {
+    __shared__ double sh[32];
+    __shared__ int amLast;
+    double v = blockSum(vThread, sh);
+    double* part = g.part + (size_t)slot * g.partStride;
+    if (threadIdx.x == 0) {
+        part[tile] = v;
+        __threadfence();
+        unsigned t = atomicAdd(g.cnt + slot, 1u);
+        amLast = (t == (unsigned)ntiles - 1u);
+    }
+    __syncthreads();
+    if (!amLast) return false;
+    __threadfence();
+    double acc = 0;
+    for (int i = threadIdx.x; i < ntiles; i += blockDim.x) acc += __ldcg(part + i);
+    double tot = blockSum(acc, sh);
+    if (threadIdx.x == 0) {
+        *total = tot;
+        g.cnt[slot] = 0;
+    }
+    return true;
+}
+
+__device__ __forceinline__ int ntilesOf(const Dom& d, int s) { return __ldg(d.start + s + 1) - __ldg(d.start + s); }
+
+// ---------------------------------------------------------------------------
+// Solver::stableDt (src/sim/gasphase.cpp:63-70) and the injection amounts of
+// injectIgnitions / injectBurners (src/sim/solver.cpp:271-280,
+// src/sim/gasphase.cpp:92-105, Burner::powerAt src/sim/solver.h:122-126).
+// One thread per scenario.
+template <class R>
+__global__ void k_begin(const Scn<R>* __restrict__ S, Dom dom, int computeDt, double dtGiven) {
+    PHX_PROLOGUE(dom);
+    if (threadIdx.x != 0) return;
+    double* sv = g.sv;
+    double dt;
+    if (computeDt) {
+        double dtMax = sv[SV_DTMAX_ARG];
+        dt = mn(dtMax, g.dtMaxP);
+        dt = mn(dt, g.cfl * g.dx / mx(sv[SV_MAXVEL], 0.1));
+        double alpha = sv[SV_MAXNU] * (1.0 + 1.0 / K_PR_T);
+        if (alpha > 0) dt = mn(dt, 0.9 * g.dx * g.dx / (6.0 * alpha));
+        if (sv[SV_MAXDIV] > 0) dt = mn(dt, 0.25 / sv[SV_MAXDIV]);
+        dt = mx(dt, 1e-3);
+    } else {
+        dt = dtGiven;
+    }
+    sv[SV_DT] = dt;
+    sv[SV_INV] = g.dx * g.dx / dt;
+    double time = sv[SV_TIME];
+    double fuelIn = sv[SV_FUELIN];
+    for (int q = 0; q < g.nsrc; ++q) {
+        const Src& src = g.src[q];
+        double mf = -1.0;
+        if (src.kind == 0) {
+            int c = src.i0 + g.nx * (src.j0 + g.ny * src.k);
+            if (!(time < src.start || time > src.start + src.duration) && !g.blocked[c]) {
+                mf = src.power * dt / K_DHC_FUEL;
+                fuelIn += mf;
+            }
+        } else {
+            double P = 0;
+            if (!(time < src.start || time > src.start + src.duration)) {
+                double r = src.rampS > 0 ? mn(1.0, (time - src.start) / src.rampS) : 1.0;
+                P = src.peakW * r * r;
+            }
+            if (P > 0) {
+                mf = P * dt / K_DHC_FUEL / src.ncells;
+                for (int n = 0; n < src.ncells; ++n) fuelIn += mf;
+            }
+        }
+        sv[SV_SRC_MF + q] = mf;
+    }
+    sv[SV_FUELIN] = fuelIn;
+    // reductions of this step start from their neutral values
+    sv[SV_MAXNU] = 0;
+    sv[SV_MAXDIV] = 0;
+    sv[SV_MAXVEL] = 0;
+    sv[SV_RMAX] = 0;
+    sv[SV_BMAX] = 0;
+    sv[SV_MAXGAST] = K_T0;
+    sv[SV_BURNING] = 0;
+}
+
+// ---------------------------------------------------------------------------
+// Per-step clears (src/sim/solver.cpp:231-233), injectIgnitions + injectBurners
+// through addGasSpecies (src/sim/solver.cpp:212-223), and combustion
+// (src/sim/solver.cpp:284-344). lit is double-buffered: neighbours read the
+// previous step's flags from lit, the new flags go to lit2.
+template <class R>
+__global__ void k_combust(const Scn<R>* __restrict__ S, Dom dom) {
+    PHX_PROLOGUE(dom);
+    int c = tile_ * TPB + threadIdx.x;
+    if (c >= g.N) return;
+    const double* sv = g.sv;
+    const double dt = sv[SV_DT];
+    const int nx = g.nx, ny = g.ny, nz = g.nz, sz = nx * ny;
+    double Qc = 0, Qrc = 0, hrrc = 0, ms = 0;
+    uint8_t pil = 0, litn = 0;
+    if (!g.blocked[c]) {
+        const int i = c % nx, j = (c / nx) % ny, k = c / sz;
+        R* const* Y = g.sc;
+        double Tc = Y[0][c];
+        double yf = Y[2][c];
+        bool member = false;
+        for (int q = 0; q < g.nsrc; ++q) {
+            const Src& sr = g.src[q];
+            if (sv[SV_SRC_MF + q] >= 0 && k == sr.k && i >= sr.i0 && i <= sr.i1 && j >= sr.j0 && j <= sr.j1) member = true;
+        }
+        if (member || yf >= 1e-6) {
+            double Yo = Y[1][c], Ys = Y[3][c], Ya = Y[4][c], Yp = Y[5][c], Yc = Y[6][c], Yw = Y[7][c], Yco = Y[8][c],
+                   Yai = Y[9][c];
+            bool modified = false;
+            if (member) {
+                const double m = gasDensity(g, c) * g.dx * g.dx * g.dx;
+                for (int q = 0; q < g.nsrc; ++q) {
+                    const Src& sr = g.src[q];
+                    double mf = sv[SV_SRC_MF + q];
+                    if (!(mf >= 0 && k == sr.k && i >= sr.i0 && i <= sr.i1 && j >= sr.j0 && j <= sr.j1)) continue;
+                    const double fuelGen = mf, aerosol = 0.0, sootPot = mf * K_BURNER_SOOT;
+                    const double madd = fuelGen + aerosol;
+                    if (madd <= 0) continue;
+                    const double mt = m + madd, scl = m / mt;
+                    Yo *= scl; Ys *= scl; Yc *= scl; Yw *= scl; Yco *= scl;
+                    Yai = Yai * scl + fuelGen * K_T_AUTO / mt;
+                    yf = yf * scl + fuelGen / mt;
+                    Ya = Ya * scl + aerosol / mt;
+                    Yp = Yp * scl + sootPot / mt;
+                    ms += madd;
+                    pil = 1;
+                    modified = true;
+                }
+            }
+            if (yf >= 1e-6) {
+                const double V = g.dx * g.dx * g.dx;
+                const double frac = 1.0 - exp(-dt / K_TAU_MIX);
+                const double chiR = g.radiationOn ? K_CHI_R : 0.0;
+                double ait = yf > 1e-9 ? Yai / yf : K_T_AUTO;
+                bool ign = pil || Tc > ait;
+                if (!ign) {
+                    const uint8_t* lit = g.lit;
+                    ign = (i > 0 && lit[c - 1]) || (i < nx - 1 && lit[c + 1]) || (j > 0 && lit[c - nx]) ||
+                          (j < ny - 1 && lit[c + nx]) || (k > 0 && lit[c - sz]) || (k < nz - 1 && lit[c + sz]);
+                }
+                if (ign) {
+                    double burnable = mn(yf, Yo / K_S_O2);
+                    if (burnable > 1e-7) {
+                        double tAd = Tc + K_DHC_FUEL / (K_CP * (1.0 + K_S_O2 / mx(Yo, 1e-4)));
+                        if (pil || !(tAd < K_T_CRIT)) {
+                            double m = gasDensity(g, c) * V;
+                            double dmf = burnable * m * frac;
+                            double q = dmf * K_DHC_FUEL;
+                            double sootMade = yf > 0 ? Yp * (dmf / m) / yf : 0;
+                            double coMade = K_CO_YIELD * dmf / m;
+                            double co2Made = mx(0.0, (K_C_FRAC * dmf / m - sootMade - (12.0 / 28.0) * coMade) * (44.0 / 12.0));
+                            double o2Used = K_S_O2 * dmf / m - (32.0 / 12.0) * sootMade - (16.0 / 28.0) * coMade;
+                            yf = mx(0.0, yf - dmf / m);
+                            Yai = yf * ait;
+                            Yo = mx(0.0, Yo - o2Used);
+                            Yp = mx(0.0, Yp - sootMade);
+                            Ys += sootMade;
+                            Yco += coMade;
+                            Yc += co2Made;
+                            Yw += K_Y_H2O * dmf / m;
+                            Ya *= (1.0 - frac);
+                            Qc = q * (1.0 - chiR);
+                            Qrc = q * chiR;
+                            hrrc = q / (dt * V);
+                            litn = q > 1e-3 ? 1 : 0;
+                            modified = true;
+                        }
+                    }
+                }
+            }
+            if (modified) {
+                Y[1][c] = (R)Yo; Y[2][c] = (R)yf; Y[3][c] = (R)Ys; Y[4][c] = (R)Ya; Y[5][c] = (R)Yp;
+                Y[6][c] = (R)Yc; Y[7][c] = (R)Yw; Y[8][c] = (R)Yco; Y[9][c] = (R)Yai;
+            }
+        }
+    }
+    g.Q[c] = (R)Qc;
+    g.Qr[c] = (R)Qrc;
+    g.hrr[c] = (R)hrrc;
+    g.massSrc[c] = (R)ms;
+    g.pilot[c] = pil;
+    g.lit2[c] = litn;
+}
+
+// ---------------------------------------------------------------------------
+// Solver::turbulence (src/sim/gasphase.cpp:163-218): cell-centre velocities,
+// the blocked-aware 1-2-1 test filter x -> y -> z per component, and the
+// Deardorff viscosity.
+template <class R>
+__global__ void k_turb_center(const Scn<R>* __restrict__ S, Dom dom) {
+    PHX_PROLOGUE(dom);
+    int c = tile_ * TPB + threadIdx.x;
+    if (c >= g.N) return;
+    R *uc = g.tmp[0], *vc = g.tmp[1], *wc = g.tmp[2];
+    if (g.blocked[c]) { uc[c] = vc[c] = wc[c] = 0; return; }
+    const int nx = g.nx, ny = g.ny;
+    const int i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
+    int fx0 = i + (nx + 1) * (j + ny * k);
+    int fy0 = i + nx * (j + (ny + 1) * k);
+    uc[c] = (R)(0.5 * ((double)g.u[fx0] + (double)g.u[fx0 + 1]));
+    vc[c] = (R)(0.5 * ((double)g.v[fy0] + (double)g.v[fy0 + nx]));
+    wc[c] = (R)(0.5 * ((double)g.w[c] + (double)g.w[c + nx * ny]));
+}
+
+template <class R>
+__global__ void k_turb_filter(const Scn<R>* __restrict__ S, Dom dom, int q, int axis) {
+    PHX_PROLOGUE(dom);
+    int c = tile_ * TPB + threadIdx.x;
+    if (c >= g.N) return;
+    const R* in = axis == 0 ? g.tmp[q] : axis == 1 ? g.tmp[3 + q] : g.tmp[6 + q];
+    R* out = axis == 1 ? g.tmp[6 + q] : g.tmp[3 + q];
+    if (g.blocked[c]) { out[c] = 0; return; }
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const int i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
+    const int id = axis == 0 ? i : axis == 1 ? j : k, n = axis == 0 ? nx : axis == 1 ? ny : nz;
+    const int st = axis == 0 ? 1 : axis == 1 ? nx : nx * ny;
+    double self = in[c];
+    double lo = id > 0 && !g.blocked[c - st] ? (double)in[c - st] : self;
+    double hi = id < n - 1 && !g.blocked[c + st] ? (double)in[c + st] : self;
+    out[c] = (R)(0.25 * lo + 0.5 * self + 0.25 * hi);
+}
+
+template <class R>
+__global__ void k_turb_nu(const Scn<R>* __restrict__ S, Dom dom) {
+    PHX_PROLOGUE(dom);
+    int c = tile_ * TPB + threadIdx.x;
+    double m = 0;
+    if (c < g.N) {
+        if (g.blocked[c]) g.nu[c] = 0;
+        else {
+            double du = (double)g.tmp[0][c] - (double)g.tmp[3][c];
+            double dv = (double)g.tmp[1][c] - (double)g.tmp[4][c];
+            double dw = (double)g.tmp[2][c] - (double)g.tmp[5][c];
+            double ks = 0.5 * (du * du + dv * dv + dw * dw);
+            double nu = mn(1.0, K_C_NU * g.dx * sqrt(ks) + 1.5e-5 * pow((double)g.sc[0][c] / 293.15, 1.7));
+            g.nu[c] = (R)nu;
+            m = (double)(R)nu;
+        }
+    }
+    blockMaxTo(g.sv + SV_MAXNU, m);
+}
+
+// ---------------------------------------------------------------------------
+// Solver::heatDiffusion (src/sim/gasphase.cpp:221-248)
+template <class R>
+__global__ void k_heat(const Scn<R>* __restrict__ S, Dom dom) {
+    PHX_PROLOGUE(dom);
+    int c = tile_ * TPB + threadIdx.x;
+    if (c >= g.N || g.blocked[c]) return;
+    const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
+    const int i = c % nx, j = (c / nx) % ny, k = c / sxy;
+    const int fx0 = i + (nx + 1) * (j + ny * k), fy0 = i + nx * (j + (ny + 1) * k);
+    const double fo[6] = {(double)g.fx[fx0], (double)g.fx[fx0 + 1], (double)g.fy[fy0], (double)g.fy[fy0 + nx],
+                          (double)g.fz[c], (double)g.fz[c + sxy]};
+    const int nb[6] = {i > 0 ? c - 1 : -1, i < nx - 1 ? c + 1 : -1, j > 0 ? c - nx : -1, j < ny - 1 ? c + nx : -1,
+                       k > 0 ? c - sxy : -1, k < nz - 1 ? c + sxy : -1};
+    const R* T = g.sc[0];
+    const double Tc = T[c], nuc = g.nu[c];
+    double rc = gasDensity(g, c), q = 0;
+    for (int d = 0; d < 6; ++d) {
+        if (fo[d] <= 0) continue;
+        int n = nb[d];
+        if (n >= 0 && g.blocked[n]) continue;
+        double Tn = n >= 0 ? (double)T[n] : K_T0;
+        double nun = n >= 0 ? (double)g.nu[n] : nuc;
+        double rn = n >= 0 ? gasDensity(g, n) : K_P0 / (K_RS * K_T0);
+        double Tf = 0.5 * (Tc + Tn);
+        double kf = 0.5 * (rc + rn) * K_CP * 0.5 * (nuc + nun) / K_PR_T + 0.0258 * pow(Tf / 293.15, 0.8);
+        q += fo[d] * kf * g.dx * (Tn - Tc);
+    }
+    g.Q[c] = (R)((double)g.Q[c] + q * g.sv[SV_DT]);
+}
+
+// Solver::energyAndExpansion (src/sim/gasphase.cpp:251-271)
+template <class R>
+__global__ void k_energy(const Scn<R>* __restrict__ S, Dom dom) {
+    PHX_PROLOGUE(dom);
+    int c = tile_ * TPB + threadIdx.x;
+    double md = 0;
+    if (c < g.N) {
+        if (g.blocked[c]) g.S[c] = 0;
+        else {
+            const double dt = g.sv[SV_DT];
+            const double V = g.dx * g.dx * g.dx;
+            const double T = g.sc[0][c], Q = g.Q[c], Pb = g.Pb[c];
+            double rho = Pb / (K_RS * T);
+            double m = rho * V;
+            double Tn = clampd(T + Q / (m * K_CP), K_T_MIN, K_T_MAX);
+            double rhoN = Pb / (K_RS * Tn);
+            double D = Q / (m * K_CP * T * dt) + (double)g.massSrc[c] / (rhoN * V * dt);
+            g.sc[0][c] = (R)Tn;
+            double Sv = clampd(D, -K_D_MAX, K_D_MAX);
+            g.S[c] = (R)Sv;
+            md = fabs((double)(R)Sv);
+        }
+    }
+    blockMaxTo(g.sv + SV_MAXDIV, md);
+}
+
+// ---------------------------------------------------------------------------
+// Solver::momentum (src/sim/gasphase.cpp:275-372): one component on its faces,
+// written to the second velocity buffer.
+__device__ __forceinline__ double vanLeer(double a, double b) { return a * b > 0 ? 2 * a * b / (a + b) : 0.0; }
+
+template <class R>
+__global__ void k_momentum(const Scn<R>* __restrict__ S, Dom dom, int comp) {
+    PHX_PROLOGUE(dom);
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const int dX = nx + (comp == 0), dY = ny + (comp == 1), dZ = nz + (comp == 2);
+    const int nf = dX * dY * dZ;
+    int f = tile_ * TPB + threadIdx.x;
+    if (f >= nf) return;
+    const R* vel = comp == 0 ? g.u : comp == 1 ? g.v : g.w;
+    const R* fo = comp == 0 ? g.fx : comp == 1 ? g.fy : g.fz;
+    const uint8_t* lk = comp == 0 ? g.lx : comp == 1 ? g.ly : g.lz;   // null: no crack faces
+    R* out = comp == 0 ? g.u2 : comp == 1 ? g.v2 : g.w2;
+    if (fo[f] <= 0) { out[f] = 0; return; }
+    if (lk && lk[f]) { out[f] = vel[f]; return; }   // set by leakage()
+    const int i = f % dX, j = (f / dX) % dY, k = f / (dX * dY);
+    const int id[3] = {i, j, k};
+    const int ncell[3] = {nx, ny, nz};
+    const int st[3] = {1, dX, dX * dY};
+    const int dim[3] = {dX, dY, dZ};
+    const int lo = id[comp] - 1;
+    const bool bnd = lo < 0 || id[comp] >= ncell[comp];
+    const double zc = g.oz + (comp == 2 ? (double)k : k + 0.5) * g.dx;
+    if (bnd) {
+        double wv = windAt(g, comp, lo < 0 ? 0 : 1, zc);
+        out[f] = isnan(wv) ? vel[f] : (R)wv;
+        return;
+    }
+    int a3[3] = {i, j, k};
+    a3[comp] -= 1;
+    const int ca = a3[0] + nx * (a3[1] + ny * a3[2]);
+    const int cb = i + nx * (j + ny * k);
+    const double v0 = vel[f];
+    double adv[3];
+    adv[comp] = v0;
+    for (int a = 0; a < 3; ++a) {
+        if (a == comp) continue;
+        const R* va = a == 0 ? g.u : a == 1 ? g.v : g.w;
+        const int aX = nx + (a == 0), aY = ny + (a == 1);
+        double s = 0;
+        for (int q = 0; q < 4; ++q) {
+            int p[3] = {i, j, k};
+            if (q & 1) p[a] += 1;
+            if (q & 2) p[comp] -= 1;
+            p[a] = p[a] < ncell[a] ? p[a] : ncell[a];
+            p[comp] = p[comp] > 0 ? p[comp] : 0;
+            s += (double)va[p[0] + aX * (p[1] + aY * p[2])];
+        }
+        adv[a] = 0.25 * s;
+    }
+    const double idx = 1.0 / g.dx, idx2 = 1.0 / (g.dx * g.dx);
+    double acc = 0, lap = 0;
+    for (int a = 0; a < 3; ++a) {
+        double m1, p1, m2, p2;
+        // free slip across closed faces: neighbour along a, then the second
+        // neighbour only through two open faces
+        {
+            int ni = id[a] - 1, gg = f - st[a];
+            m1 = (ni < 0) ? v0 : (fo[gg] > 0 && !(lk && lk[gg]) ? (double)vel[gg] : v0);
+            ni = id[a] + 1;
+            gg = f + st[a];
+            p1 = (ni >= dim[a]) ? v0 : (fo[gg] > 0 && !(lk && lk[gg]) ? (double)vel[gg] : v0);
+        }
+        {
+            int ni = id[a] - 2;
+            if (ni < 0) m2 = m1;
+            else {
+                int gg = f - 2 * st[a], g1 = f - st[a];
+                m2 = fo[gg] > 0 && fo[g1] > 0 && !(lk && (lk[gg] || lk[g1])) ? (double)vel[gg] : m1;
+            }
+            ni = id[a] + 2;
+            if (ni >= dim[a]) p2 = p1;
+            else {
+                int gg = f + 2 * st[a], g1 = f + st[a];
+                p2 = fo[gg] > 0 && fo[g1] > 0 && !(lk && (lk[gg] || lk[g1])) ? (double)vel[gg] : p1;
+            }
+        }
+        double fp, fm;
+        if (adv[a] >= 0) {
+            fp = v0 + 0.5 * vanLeer(v0 - m1, p1 - v0);
+            fm = m1 + 0.5 * vanLeer(m1 - m2, v0 - m1);
+        } else {
+            fp = p1 - 0.5 * vanLeer(p1 - v0, p2 - p1);
+            fm = v0 - 0.5 * vanLeer(v0 - m1, p1 - v0);
+        }
+        acc -= adv[a] * (fp - fm) * idx;
+        lap += (m1 - 2 * v0 + p1) * idx2;
+    }
+    double ra = gasDensity(g, ca), rb = gasDensity(g, cb);
+    double rf = 0.5 * (ra + rb);
+    double nuf = 0.5 * ((double)g.nu[ca] + (double)g.nu[cb]);
+    acc += nuf * lap;
+    if (comp == 2) {
+        double r0 = 0.5 * ((double)g.Pb[ca] + (double)g.Pb[cb]) / (K_RS * K_T0);
+        acc += K_G * (r0 - rf) / rf;
+    }
+    double pt = rf * 0.5 * ((double)g.p[ca] + (double)g.p[cb]);
+    acc += pt * (1.0 / rb - 1.0 / ra) * idx;
+    out[f] = (R)clampd(v0 + g.sv[SV_DT] * acc, -K_VMAX, K_VMAX);
+}
+
+// open boundary faces without wind inflow take the new value of the face one
+// cell inside (src/sim/gasphase.cpp:374-393). One thread per boundary face.
+template <class R>
+__global__ void k_mom_bnd(const Scn<R>* __restrict__ S, Dom dom, int comp) {
+    PHX_PROLOGUE(dom);
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const int dX = nx + (comp == 0), dY = ny + (comp == 1), dZ = nz + (comp == 2);
+    const int dim[3] = {dX, dY, dZ};
+    const int st[3] = {1, dX, dX * dY};
+    const int nAx = comp == 0 ? nx : comp == 1 ? ny : nz;
+    const int nA = dim[(comp + 1) % 3], nB = dim[(comp + 2) % 3];
+    const int sides = comp == 2 ? 1 : 2;
+    int t = tile_ * TPB + threadIdx.x;
+    if (t >= nA * nB * sides) return;
+    int side = comp == 2 ? 1 : t % 2;
+    int ab = comp == 2 ? t : t / 2;
+    int a2 = ab % nA, b2 = ab / nA;
+    int id[3];
+    id[comp] = side == 0 ? 0 : nAx;
+    id[(comp + 1) % 3] = a2;
+    id[(comp + 2) % 3] = b2;
+    int f = id[0] + dX * (id[1] + dY * id[2]);
+    const R* fo = comp == 0 ? g.fx : comp == 1 ? g.fy : g.fz;
+    const uint8_t* lk = comp == 0 ? g.lx : comp == 1 ? g.ly : g.lz;
+    R* out = comp == 0 ? g.u2 : comp == 1 ? g.v2 : g.w2;
+    if (fo[f] <= 0 || (lk && lk[f])) return;
+    double zc = g.oz + (comp == 2 ? (double)id[2] : id[2] + 0.5) * g.dx;
+    if (!isnan(windAt(g, comp, side, zc))) return;
+    int gg = f + (side == 0 ? 1 : -1) * st[comp];
+    out[f] = fo[gg] > 0 && !(lk && lk[gg]) ? out[gg] : (R)0;
+}
+
+// ---------------------------------------------------------------------------
+// Solver::leakage without crack faces (src/sim/gasphase.cpp:403-409, 486-498):
+// per closed zone the integral of S, the zone's pressure-rise rate and the
+// divergence shift. One CTA per closed zone.
+template <class R>
+__global__ void k_zone_integral(const Scn<R>* __restrict__ S, Dom dom) {
+    PHX_PROLOGUE(dom);
+    __shared__ double sh[32];
+    const int zi = tile_;
+    const int z = g.closedZone[zi];
+    const double V = g.dx * g.dx * g.dx;
+    double acc = 0;
+    for (int e = g.closedStart[zi] + threadIdx.x; e < g.closedStart[zi + 1]; e += blockDim.x) {
+        int c = g.closedCells[e];
+        acc += (double)g.S[c] * V;
+    }
+    double dInt = blockSum(acc, sh);
+    if (threadIdx.x == 0) {
+        double Vz = g.zoneVol[z];
+        double out = 0.0;
+        g.zoneDP[z] = K_GAMMA * g.zoneP[z] * (double)(dInt - out) / Vz;
+        g.zoneShift[z] = (double)(dInt - out) / Vz;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Solver::project, right-hand side and warm-start residual
+// (src/sim/gasphase.cpp:528-549, 576-581), with the closed-zone divergence
+// shift of leakage (:495-498) applied to S first.
+template <class R>
+__global__ void k_rhs(const Scn<R>* __restrict__ S, Dom dom) {
+    PHX_PROLOGUE(dom);
+    int c = tile_ * TPB + threadIdx.x;
+    double bm = 0, rm = 0;
+    if (c < g.N) {
+        if (g.blocked[c]) {
+            g.b[c] = 0;
+            g.p[c] = 0;
+            g.r[c] = 0;
+        } else {
+            const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
+            const int i = c % nx, j = (c / nx) % ny, k = c / sxy;
+            const double dt = g.sv[SV_DT];
+            const double inv = g.dx * g.dx / dt;
+            double Sc = g.S[c];
+            if (g.nClosed > 0) {
+                int z = g.zone[c];
+                if (z >= 0 && !g.zoneOpen[z]) {
+                    Sc -= g.zoneShift[z];
+                    g.S[c] = (R)Sc;
+                }
+            }
+            const int a0 = i + (nx + 1) * (j + ny * k), a1 = a0 + 1;
+            const int b0 = i + nx * (j + (ny + 1) * k), b1 = b0 + nx;
+            const int c0 = c, c1 = c + sxy;
+            const double u0 = g.u[a0], u1 = g.u[a1], v0 = g.v[b0], v1 = g.v[b1], w0 = g.w[c0], w1 = g.w[c1];
+            double div = ((double)g.fx[a1] * u1 - (double)g.fx[a0] * u0 + (double)g.fy[b1] * v1 - (double)g.fy[b0] * v0 +
+                          (double)g.fz[c1] * w1 - (double)g.fz[c0] * w0) / g.dx;
+            double b = (Sc - div) * inv;
+            const double A0 = g.a0x[a0], A1 = g.a0x[a1], A2 = g.a0y[b0], A3 = g.a0y[b1], A4 = g.a0z[c0], A5 = g.a0z[c1];
+            if (i == 0 && A0 > 0) b += A0 * (u0 > 0 ? -0.5 * u0 * u0 : 0.0);
+            if (i == nx - 1 && A1 > 0) b += A1 * (u1 < 0 ? -0.5 * u1 * u1 : 0.0);
+            if (j == 0 && A2 > 0) b += A2 * (v0 > 0 ? -0.5 * v0 * v0 : 0.0);
+            if (j == ny - 1 && A3 > 0) b += A3 * (v1 < 0 ? -0.5 * v1 * v1 : 0.0);
+            if (k == nz - 1 && A5 > 0) b += A5 * (w1 < 0 ? -0.5 * w1 * w1 : 0.0);
+            g.b[c] = (R)b;
+            const double dg = g.diag[c];
+            double r = 0;
+            if (dg > 0) {
+                const R* x = g.p;
+                double s = dg * (double)x[c];
+                if (i > 0) s -= A0 * (double)x[c - 1];
+                if (i < nx - 1) s -= A1 * (double)x[c + 1];
+                if (j > 0) s -= A2 * (double)x[c - nx];
+                if (j < ny - 1) s -= A3 * (double)x[c + nx];
+                if (k > 0) s -= A4 * (double)x[c - sxy];
+                if (k < nz - 1) s -= A5 * (double)x[c + sxy];
+                r = b - (double)(R)s;
+                bm = fabs(b);
+            }
+            g.r[c] = (R)r;
+            rm = fabs((double)(R)r);
+        }
+    }
+    blockMaxTo(g.sv + SV_BMAX, bm);
+    blockMaxTo(g.sv + SV_RMAX, rm);
+}
+
+// closed zones: H is defined up to a constant; its zone mean is removed
+// (src/sim/gasphase.cpp:629-639). One CTA per closed zone, then a pass over
+// the closed cells.
+template <class R>
+__global__ void k_zone_mean(const Scn<R>* __restrict__ S, Dom dom) {
+    PHX_PROLOGUE(dom);
+    __shared__ double sh[32];
+    const int zi = tile_;
+    double acc = 0;
+    for (int e = g.closedStart[zi] + threadIdx.x; e < g.closedStart[zi + 1]; e += blockDim.x) acc += (double)g.p[g.closedCells[e]];
+    double sum = blockSum(acc, sh);
+    if (threadIdx.x == 0) {
+        double cnt = (double)(g.closedStart[zi + 1] - g.closedStart[zi]);
+        g.zoneMean[g.closedZone[zi]] = cnt > 0 ? sum / cnt : 0.0;
+    }
+}
+
+template <class R>
+__global__ void k_zone_mean_sub(const Scn<R>* __restrict__ S, Dom dom) {
+    PHX_PROLOGUE(dom);
+    int e = tile_ * TPB + threadIdx.x;
+    int n = g.closedStart[g.nClosed];
+    if (e >= n) return;
+    int c = g.closedCells[e];
+    g.p[c] = (R)((double)g.p[c] - g.zoneMean[g.zone[c]]);
+}
+
+// velocity correction u -= dt/dx grad H on matrix faces, clamp, maxVel
+// (src/sim/gasphase.cpp:641-676). One thread per face of one axis.
+template <class R>
+__global__ void k_velcorr(const Scn<R>* __restrict__ S, Dom dom, int comp) {
+    PHX_PROLOGUE(dom);
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const int dX = nx + (comp == 0), dY = ny + (comp == 1), dZ = nz + (comp == 2);
+    int f = tile_ * TPB + threadIdx.x;
+    double vm = 0;
+    if (f < dX * dY * dZ) {
+        const int i = f % dX, j = (f / dX) % dY, k = f / (dX * dY);
+        R* vel = comp == 0 ? g.u : comp == 1 ? g.v : g.w;
+        const R* fo = comp == 0 ? g.fx : comp == 1 ? g.fy : g.fz;
+        const R* am = comp == 0 ? g.ax : comp == 1 ? g.ay : g.az;
+        const double s = g.sv[SV_DT] / g.dx;
+        const R* P = g.p;
+        const double fof = fo[f];
+        if (comp == 2 && k == 0) {
+            // the ground faces are not visited by the reference's loop
+            vm = 0;
+        } else if (fof <= 0) {
+            vel[f] = 0;
+        } else {
+            double un = vel[f];
+            if (comp == 0) {
+                double zc = g.oz + (k + 0.5) * g.dx;
+                if (am[f] > 0 && !((i == 0 || i == nx) && !bndOpen(g, 0, i == 0 ? 0 : 1, zc))) {
+                    double hi = i < nx ? (double)P[i + nx * (j + ny * k)] : (un < 0 ? -0.5 * un * un : 0.0);
+                    double lo = i > 0 ? (double)P[i - 1 + nx * (j + ny * k)] : (un > 0 ? -0.5 * un * un : 0.0);
+                    un = clampd(un - s * (hi - lo), -K_VMAX, K_VMAX);
+                    vel[f] = (R)un;
+                    un = (double)(R)un;
+                }
+            } else if (comp == 1) {
+                double zc = g.oz + (k + 0.5) * g.dx;
+                if (am[f] > 0 && !((j == 0 || j == ny) && !bndOpen(g, 1, j == 0 ? 0 : 1, zc))) {
+                    double hi = j < ny ? (double)P[i + nx * (j + ny * k)] : (un < 0 ? -0.5 * un * un : 0.0);
+                    double lo = j > 0 ? (double)P[i + nx * (j - 1 + ny * k)] : (un > 0 ? -0.5 * un * un : 0.0);
+                    un = clampd(un - s * (hi - lo), -K_VMAX, K_VMAX);
+                    vel[f] = (R)un;
+                    un = (double)(R)un;
+                }
+            } else {
+                if (am[f] > 0) {
+                    double hi = k < nz ? (double)P[i + nx * (j + ny * k)] : (un < 0 ? -0.5 * un * un : 0.0);
+                    double lo = (double)P[i + nx * (j + ny * (k - 1))];
+                    un = clampd(un - s * (hi - lo), -K_VMAX, K_VMAX);
+                    vel[f] = (R)un;
+                    un = (double)(R)un;
+                }
+            }
+            vm = fabs(un) * fof;
+        }
+    }
+    blockMaxTo(g.sv + SV_MAXVEL, vm);
+}
+
+// ---------------------------------------------------------------------------
+// Solver::advectScalars (src/sim/gasphase.cpp:685-784): Superbee-limited
+// transport of the ten scalars, written to the second scalar buffers.
+__device__ __forceinline__ double superbee(double r) {
+    double m = 0.0, a = mn(2 * r, 1.0), b = mn(r, 2.0);
+    if (m < a) m = a;
+    if (m < b) m = b;
+    return m;
+}
+
+template <class R>
+__global__ void k_advect(const Scn<R>* __restrict__ S, Dom dom) {
+    PHX_PROLOGUE(dom);
+    int c = tile_ * TPB + threadIdx.x;
+    if (c >= g.N) return;
+    if (g.blocked[c]) {
+        for (int q = 0; q < NSC; ++q) g.sc2[q][c] = g.sc[q][c];
+        return;
+    }
+    const double amb[NSC] = {K_T0, K_YO2_AMB, 0, 0, 0, 0, K_YCO2_AMB, K_YH2O_AMB, 0, 0};
+    const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
+    const int i = c % nx, j = (c / nx) % ny, k = c / sxy;
+    const double dt = g.sv[SV_DT];
+    const double s = dt / g.dx;
+    const int fa0 = i + (nx + 1) * (j + ny * k), fa1 = fa0 + 1;
+    const int fb0 = i + nx * (j + (ny + 1) * k), fb1 = fb0 + nx;
+    const int fc0 = c, fc1 = c + sxy;
+    double fo[6] = {(double)g.fx[fa0], (double)g.fx[fa1], (double)g.fy[fb0], (double)g.fy[fb1], (double)g.fz[fc0],
+                    (double)g.fz[fc1]};
+    double un[6] = {-fo[0] * (double)g.u[fa0], fo[1] * (double)g.u[fa1], -fo[2] * (double)g.v[fb0],
+                    fo[3] * (double)g.v[fb1], -fo[4] * (double)g.w[fc0], fo[5] * (double)g.w[fc1]};
+    const int id[3] = {i, j, k};
+    const int dim[3] = {nx, ny, nz}, st[3] = {1, nx, sxy};
+    int nb[6], nb2[6], opp[6];
+    for (int d = 0; d < 6; ++d) {
+        int a = d >> 1, sg = (d & 1) ? 1 : -1;
+        int n1 = id[a] + sg, n2 = id[a] + 2 * sg, o1 = id[a] - sg;
+        nb[d] = (n1 >= 0 && n1 < dim[a]) ? c + sg * st[a] : -1;
+        nb2[d] = (n2 >= 0 && n2 < dim[a]) ? c + 2 * sg * st[a] : -1;
+        opp[d] = (o1 >= 0 && o1 < dim[a]) ? c - sg * st[a] : -1;
+        if (nb[d] >= 0 && g.blocked[nb[d]]) nb[d] = -2;
+        if (nb2[d] >= 0 && g.blocked[nb2[d]]) nb2[d] = -2;
+        if (opp[d] >= 0 && g.blocked[opp[d]]) opp[d] = -2;
+    }
+    const R* T = g.sc[0];
+    const double nuc = g.nu[c];
+    const double rc = gasDensity(g, c);
+    double rUp[6], Dd[6], rfd[6], mden = rc;
+    for (int d = 0; d < 6; ++d) {
+        rUp[d] = 0;
+        Dd[d] = 0;
+        rfd[d] = 0;
+        if (fo[d] <= 0 || nb[d] == -2) continue;
+        double tn = nb[d] >= 0 ? (double)T[nb[d]] : K_T0, tc = T[c], tf;
+        if (un[d] > 0) {
+            double tu2 = opp[d] >= 0 ? (double)T[opp[d]] : (opp[d] == -1 ? K_T0 : tc);
+            double den = tn - tc;
+            tf = tc + (fabs(den) > 1e-6 ? 0.5 * superbee((tc - tu2) / den) * den : 0.0);
+        } else {
+            double tu2 = nb2[d] >= 0 ? (double)T[nb2[d]] : (nb2[d] == -1 ? K_T0 : tn);
+            double den = tc - tn;
+            tf = tn + (fabs(den) > 1e-6 ? 0.5 * superbee((tn - tu2) / den) * den : 0.0);
+        }
+        double pu = un[d] > 0 ? (double)g.Pb[c] : (nb[d] >= 0 ? (double)g.Pb[nb[d]] : K_P0);
+        rUp[d] = pu / (K_RS * mx(tf, K_T_MIN));
+        mden -= s * rUp[d] * un[d];
+        // species diffusion coefficient and face density: the same for every species
+        double nun = nb[d] >= 0 ? (double)g.nu[nb[d]] : nuc;
+        Dd[d] = 0.5 * (nuc + nun) / K_SC_T + 2.0e-5;
+        rfd[d] = nb[d] >= 0 ? 0.5 * (rc + gasDensity(g, nb[d])) : rc;
+    }
+    const bool conservative = mden > 0.25 * rc;
+    for (int q = 0; q < NSC; ++q) {
+        const R* F = g.sc[q];
+        const double fc = F[c];
+        double lo = fc, hi = fc, acc = 0, macc = 0;
+        for (int d = 0; d < 6; ++d) {
+            if (fo[d] <= 0 || nb[d] == -2) continue;
+            double fn = nb[d] >= 0 ? (double)F[nb[d]] : amb[q];
+            lo = mn(lo, fn);
+            hi = mx(hi, fn);
+            double flux = un[d];
+            double face = fc;
+            if (flux > 0) {
+                double fu2 = opp[d] >= 0 ? (double)F[opp[d]] : (opp[d] == -1 ? amb[q] : fc);
+                double den = fn - fc;
+                if (fabs(den) > 1e-12) face += 0.5 * superbee((fc - fu2) / den) * den;
+            } else if (flux < 0) {
+                double fu2 = nb2[d] >= 0 ? (double)F[nb2[d]] : (nb2[d] == -1 ? amb[q] : fn);
+                double den = fc - fn;
+                face = fn;
+                if (fabs(den) > 1e-12) face += 0.5 * superbee((fn - fu2) / den) * den;
+            }
+            acc -= flux * (face - fc);
+            macc -= rUp[d] * flux * face;
+            if (q > 0) {
+                acc += fo[d] * Dd[d] * (fn - fc) / g.dx;
+                macc += fo[d] * rfd[d] * Dd[d] * (fn - fc) / g.dx;
+            }
+        }
+        double val = conservative ? (rc * fc + s * macc) / mden : fc + s * acc;
+        g.sc2[q][c] = (R)clampd(val, lo, hi);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// End of step (src/sim/solver.cpp:258-268): closed-zone background pressure,
+// Pb of closed-zone cells, gatherStats (:884-915), time += dt.
+template <class R>
+__global__ void k_zone_pressure(const Scn<R>* __restrict__ S, Dom dom) {
+    PHX_PROLOGUE(dom);
+    if (threadIdx.x != 0) return;
+    const double dt = g.sv[SV_DT];
+    for (int zi = 0; zi < g.nClosed; ++zi) {
+        int z = g.closedZone[zi];
+        g.zoneP[z] = clampd(g.zoneP[z] + dt * g.zoneDP[z], K_P0 - 20000.0, K_P0 + 50000.0);
+    }
+}
+
+template <class R>
+__global__ void k_zone_pb(const Scn<R>* __restrict__ S, Dom dom) {
+    PHX_PROLOGUE(dom);
+    int e = tile_ * TPB + threadIdx.x;
+    if (e >= g.closedStart[g.nClosed]) return;
+    int c = g.closedCells[e];
+    g.Pb[c] = (R)g.zoneP[g.zone[c]];
+}
+
+template <class R>
+__global__ void k_stats(const Scn<R>* __restrict__ S, Dom dom) {
+    PHX_PROLOGUE(dom);
+    __shared__ double shA[32];
+    int c = tile_ * TPB + threadIdx.x;
+    const double V = g.dx * g.dx * g.dx;
+    double h = 0, fd = 0, mt = 0, nb = 0;
+    if (c < g.N && !g.blocked[c]) {
+        double hr = g.hrr[c];
+        fd = (double)g.sc[2][c] * gasDensity(g, c) * V;
+        h = hr * V;
+        mt = g.sc[0][c];
+        nb = hr > 0 ? 1.0 : 0.0;
+    }
+    blockMaxTo(g.sv + SV_MAXGAST, mt);
+    double nbs = blockSum(nb, shA);
+    if (threadIdx.x == 0 && nbs > 0) atomicAdd(g.sv + SV_BURNING, nbs);
+    double fs = blockSum(fd, shA);
+    int nt = ntilesOf(dom, s_);
+    double tot;
+    // two partial slots; the last CTA of the first closes both
+    if (threadIdx.x == 0) {
+        g.part[(size_t)PS_FUEL * g.partStride + tile_] = fs;
+    }
+    if (lastCtaSum(g, PS_HRR, tile_, nt, h, &tot)) {
+        double acc = 0;
+        for (int t = threadIdx.x; t < nt; t += blockDim.x) acc += __ldcg(g.part + (size_t)PS_FUEL * g.partStride + t);
+        double fdTot = blockSum(acc, shA);
+        if (threadIdx.x == 0) {
+            const double dt = g.sv[SV_DT];
+            g.sv[SV_HRR] = tot;
+            g.sv[SV_FUELBURNED] += (double)tot * dt / K_DHC_FUEL;
+            g.sv[SV_FUELINDOMAIN] = fdTot;
+            g.sv[SV_TIME] += dt;
+        }
+    }
+}
+
+// pointer swaps of the double-buffered fields, one thread per scenario
+template <class R>
+__global__ void k_swap(Scn<R>* S, Dom dom, int what) {
+    int s_, tile_;
+    locate(dom, blockIdx.x, s_, tile_);
+    if (threadIdx.x != 0) return;
+    Scn<R>& g = S[s_];
+    if (what & 1) { uint8_t* t = g.lit; g.lit = g.lit2; g.lit2 = t; }
+    if (what & 2) {
+        R* t;
+        t = g.u; g.u = g.u2; g.u2 = t;
+        t = g.v; g.v = g.v2; g.v2 = t;
+        t = g.w; g.w = g.w2; g.w2 = t;
+    }
+    if (what & 4)
+        for (int q = 0; q < NSC; ++q) { R* t = g.sc[q]; g.sc[q] = g.sc2[q]; g.sc2[q] = t; }
+}
+
+#undef PHX_PROLOGUE
+}  // namespace phx

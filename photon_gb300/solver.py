@@ -1,0 +1,136 @@
+"""Python mirror of photon::Solver's step API over the GB300 C ABI.
+
+`Solver(case, precision)` creates a device context for a synthetic case
+(photon_gb300.casegen.Case) or any arrays with the reference's layout; the
+methods follow photon::Solver (src/sim/solver.h:156-347): step(dtMax) -> dt,
+add_burner -> index, add_ignition, fields by name, and stats. Everything runs
+in libphx.so on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import FIELD_ID, STAGE_ID, PhxError, PhxGrid, PhxStats
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+class Solver:
+    def __init__(self, case, precision: int = _lib.PREC_FP64, add_burners: bool = True):
+        self.L = _lib.load()
+        self.case = case
+        self.h = ctypes.c_void_p()
+        g = PhxGrid()
+        g.nx, g.ny, g.nz = case.nx, case.ny, case.nz
+        g.dx, g.ox, g.oy, g.oz = case.dx, case.ox, case.oy, case.oz
+        pr = case.profile
+        g.cfl, g.dt_max, g.max_iters, g.tol, g.rel_tol = pr.cfl, pr.dtMax, pr.maxIters, pr.tol, pr.rel_tol
+        g.radiation_on, g.adiabatic_surfaces = int(case.radiationOn), int(case.adiabatic)
+        g.wind_speed, g.wind_from_deg, g.wind_exponent = case.wind
+        keep = {}
+        for n in ("blocked", "lx", "ly", "lz"):
+            keep[n] = np.ascontiguousarray(getattr(case, n), dtype=np.uint8)
+        for n in ("fx", "fy", "fz", "ax", "ay", "az"):
+            keep[n] = np.ascontiguousarray(getattr(case, n), dtype=np.float64)
+        for n, a in keep.items():
+            setattr(g, n, a.ctypes.data)
+        r = self.L.phx_create(ctypes.byref(g), precision, ctypes.byref(self.h))
+        if r != 0:
+            raise PhxError(r, self.L.phx_last_global_error().decode())
+        self.precision = precision
+        self.burner_ids = []
+        if add_burners:
+            for b in case.burners:
+                self.burner_ids.append(self.add_burner(b.x0, b.y0, b.x1, b.y1, b.z, b.peakW, b.rampS, b.start, b.duration))
+
+    def close(self):
+        if self.h:
+            self.L.phx_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, r):
+        if r != 0:
+            raise PhxError(r, self.L.phx_last_error(self.h).decode())
+
+    def add_burner(self, x0, y0, x1, y1, z, peakW, rampS=0.0, start=0.0, duration=1e9) -> int:
+        idx = ctypes.c_int(-1)
+        self._check(self.L.phx_add_burner(self.h, x0, y0, x1, y1, z, peakW, rampS, start, duration, ctypes.byref(idx)))
+        return idx.value
+
+    def add_ignition(self, cell, power, duration):
+        self._check(self.L.phx_add_ignition(self.h, int(cell), float(power), float(duration)))
+
+    def step(self, dtMax: float) -> float:
+        dt = ctypes.c_double()
+        self._check(self.L.phx_step(self.h, dtMax, ctypes.byref(dt)))
+        return dt.value
+
+    def run(self, n: int, dtMax: float) -> np.ndarray:
+        out = np.zeros(n, np.float64)
+        self._check(self.L.phx_run(self.h, n, dtMax, _ptr(out)))
+        return out
+
+    def stage(self, name: str, arg: float = 0.0):
+        self._check(self.L.phx_stage(self.h, STAGE_ID[name], arg))
+
+    def precondition(self, r: np.ndarray) -> np.ndarray:
+        r = np.ascontiguousarray(r, np.float64)
+        z = np.zeros_like(r)
+        self._check(self.L.phx_precondition(self.h, _ptr(r), _ptr(z)))
+        return z
+
+    def _dtype(self, name):
+        return np.uint8 if name == "lit" else np.int32 if name == "zone" else np.float64
+
+    def get(self, name: str) -> np.ndarray:
+        fid = FIELD_ID[name]
+        n = self.L.phx_field_count(self.h, fid)
+        a = np.zeros(n, self._dtype(name))
+        self._check(self.L.phx_get_field(self.h, fid, _ptr(a), a.nbytes))
+        return a
+
+    def set(self, name: str, arr):
+        a = np.ascontiguousarray(arr, dtype=self._dtype(name))
+        self._check(self.L.phx_set_field(self.h, FIELD_ID[name], _ptr(a), a.nbytes))
+
+    def stats(self) -> dict:
+        s = PhxStats()
+        self._check(self.L.phx_get_stats(self.h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in PhxStats._fields_}
+
+    def set_scalars(self, time, maxVel, maxNu, maxDiv):
+        self._check(self.L.phx_set_scalars(self.h, time, maxVel, maxNu, maxDiv))
+
+    def device_bytes(self) -> int:
+        return int(self.L.phx_device_bytes(self.h))
+
+    def sync(self):
+        self._check(self.L.phx_sync(self.h))
+
+    def time_steps(self, n: int, dtMax: float, flush_l2: bool = False):
+        """Device time (ms, CUDA events) of n steps and their kernel launches."""
+        tot, nl = ctypes.c_double(), ctypes.c_int()
+        self._check(self.L.phx_time_steps(self.h, n, dtMax, int(flush_l2), ctypes.byref(tot), ctypes.byref(nl)))
+        return tot.value, nl.value
+
+    def profile_step(self, dtMax: float, flush_l2: bool = True) -> list:
+        """One step with events around every launch: [(kernel, launches, ms)]."""
+        cap = 128
+        arr = (_lib.PhxKernelTime * cap)()
+        n = ctypes.c_int()
+        self._check(self.L.phx_profile_step(self.h, dtMax, int(flush_l2), arr, cap, ctypes.byref(n)))
+        return [(arr[i].name.decode(), arr[i].launches, arr[i].ms) for i in range(min(n.value, cap))]
+
+    def last_launches(self) -> int:
+        return int(self.L.phx_last_step_launches(self.h))

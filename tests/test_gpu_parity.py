@@ -1,0 +1,134 @@
+"""Parity of the FP64 GPU step with the FP64 oracle (oracle/phx_oracle.c,
+itself bit-identical to the reference's own FP64 build).
+
+The bar is the benchmark spec's tolerance: relative L2 difference <= 1e-9 per step
+on pressure, velocity and the scalars, from identical inputs. Stages that do
+not involve the pressure solve are checked tighter (1e-12): they differ from
+the oracle only through the last bits of exp/pow and reduction order."""
+import numpy as np
+import pytest
+
+from oracle.oraclepy import OracleSolver
+from photon_gb300 import casegen
+from photon_gb300.solver import Solver
+
+from gpu_util import STATE, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+STEP_TOL = 1e-9
+STAGE_TOL = 1e-12
+
+
+def warm_pair(case, steps, dtMax=0.02):
+    """Oracle advanced `steps` steps; a GPU context loaded with the same state."""
+    o = OracleSolver(case)
+    for _ in range(steps):
+        o.step(dtMax)
+    g = Solver(case)
+    for f in STATE:
+        g.set(f, o.get(f))
+    g.set("lit", o.get("lit"))
+    sc = o.scalars()
+    g.set_scalars(sc["time"], sc["maxVel"], sc["maxNu"], sc["maxDiv"])
+    return o, g
+
+
+def compare(o, g, fields, tol, what):
+    bad = {}
+    for f in fields:
+        e = rel_l2(g.get(f), o.get(f))
+        if not e <= tol:
+            bad[f] = e
+    assert not bad, "%s: %s" % (what, bad)
+
+
+CASES = {
+    "room": lambda: casegen.tiny_room(12, 10, 9, 0.2, 60e3),
+    "sealed": lambda: casegen.tiny_room(10, 8, 8, 0.2, 40e3, doorway=False),
+    "house": lambda: casegen.house(24, 20, 14, 0.2, 3),
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_zones_and_initial_fields(name):
+    c = CASES[name]()
+    o = OracleSolver(c)
+    o.stage("zones")
+    g = Solver(c)
+    assert np.array_equal(g.get("zone"), o.get("zone"))
+    assert np.array_equal(g.get("Pb"), o.get("Pb"))
+    for f in ("T", "Yo", "Yc", "Yw", "u", "p"):
+        assert np.array_equal(g.get(f), o.get(f)), f
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_precondition_matches_oracle(name):
+    c = CASES[name]()
+    o = OracleSolver(c)
+    o.step(0.02)
+    g = Solver(c)
+    rng = np.random.default_rng(1)
+    r = rng.standard_normal(c.N) * (1 - c.blocked)
+    assert rel_l2(g.precondition(r), o.precondition(r)) <= STAGE_TOL
+
+
+@pytest.mark.parametrize("stage", ["combustion", "turbulence", "heat", "energy", "momentum", "advect"])
+def test_stage_matches_oracle(stage):
+    c = casegen.tiny_room(12, 10, 9, 0.2, 60e3)
+    o, g = warm_pair(c, 8)
+    dt = 0.013
+    if stage == "combustion":
+        o.stage("clear", dt)
+        o.stage("burners", dt)
+        o.stage("combustion", dt)
+        g.stage("combustion", dt)
+        fields = STATE + ("lit",)
+    elif stage == "turbulence":
+        o.stage("turbulence", dt)
+        g.stage("turbulence", dt)
+        fields = ("nu",)
+    else:
+        o.stage(stage, dt)
+        g.stage(stage, dt)
+        fields = STATE
+    compare(o, g, [f for f in fields if f != "lit"], STAGE_TOL, stage)
+    if stage == "combustion":
+        assert np.array_equal(g.get("lit"), o.get("lit"))
+    if stage == "turbulence":
+        assert abs(g.stats()["max_nu"] - o.scalars()["maxNu"]) <= 1e-15 * max(1.0, o.scalars()["maxNu"])
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_project_matches_oracle(name):
+    c = CASES[name]()
+    o, g = warm_pair(c, 6)
+    dt = 0.02
+    for st in ("turbulence", "heat", "energy", "momentum", "leakage"):
+        o.stage(st, dt)
+    for st in ("turbulence", "heat", "energy", "momentum", "leakage"):
+        g.stage(st, dt)
+    o.stage("project", dt)
+    g.stage("project", dt)
+    compare(o, g, ("p", "u", "v", "w", "S"), STEP_TOL, "project")
+    assert g.stats()["pressure_iters"] == o.scalars()["pressureIters"]
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_full_steps_match_oracle(name):
+    c = CASES[name]()
+    o = OracleSolver(c)
+    g = Solver(c)
+    for s in range(12):
+        dto = o.step(0.02)
+        dtg = g.step(0.02)
+        assert abs(dtg - dto) <= 1e-12 * dto, (s, dtg, dto)
+        compare(o, g, STATE, STEP_TOL, "step %d" % s)
+    so, sg = o.scalars(), g.stats()
+    assert sg["pressure_iters"] == so["pressureIters"]
+    assert abs(sg["time"] - so["time"]) <= 1e-12
+    assert abs(sg["fuel_in"] - so["fuelIn"]) <= 1e-12 * so["fuelIn"]
+    assert abs(sg["hrr"] - so["hrr"]) <= 1e-9 * max(1.0, so["hrr"])
+    assert abs(sg["fuel_in_domain"] - so["fuelInDomain"]) <= 1e-9 * max(1e-12, so["fuelInDomain"])
+    assert sg["burning_cells"] == so["burningCells"]
+    assert abs(sg["max_gas_t"] - so["maxGasT"]) <= 1e-12 * so["maxGasT"]
