@@ -206,6 +206,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="house_72x52x44")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--spinup", type=int, default=SPINUP_STEPS, help="untimed steps before warm-up")
     args = ap.parse_args()
     rank, world, local = rank_info()
     if args.impl == "reference":
@@ -225,7 +226,8 @@ def main():
     case = make_workload(args.workload)
     g = Solver(case, _lib.PREC_FP64)
     dtMax = case.profile.dtMax
-    g.run(SPINUP_STEPS, dtMax)
+    if args.spinup > 0:
+        g.run(args.spinup, dtMax)
     g.run(max(3, args.warmup), dtMax)
     # the working set of one scenario fits in L2: flush it before every timed step
     flush = g.device_bytes() < (200 << 20)
@@ -297,7 +299,7 @@ def main():
                 "config": {"workload": args.workload, "cells": case.N, "precision": "fp64",
                            "pressure_stop": "relative 1e-8 (max|r| <= 1e-8 max|b|)",
                            "l2": "flushed before each step" if flush else "inputs larger than L2",
-                           "spinup_steps": SPINUP_STEPS, "cg_iters_last_step": st["pressure_iters"],
+                           "spinup_steps": args.spinup, "cg_iters_last_step": st["pressure_iters"],
                            "parallelism": "replicas" if world > 1 else "single"},
                 "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": 8,
                         "d2h_bytes_per_step": nbytesT + ctypes.sizeof(_lib.PhxStats)},
