@@ -55,28 +55,31 @@ def make_workload(name: str):
     return c
 
 
-# Algorithmic bytes per unit of each kernel's domain (FP64 storage, w = 8 B):
-# each input array read once and each output written once per launch.
-W = 8
-KERNEL_BYTES = {
-    # kernel: (bytes per unit, unit) ; unit 'cell' = N, 'face' = faces of one axis
-    "k_advect": (18 * W + 1 + 10 * W, "cell"),       # 10 scalars + u,v,w,fx,fy,fz + Pb,nu + blocked -> 10 scalars
-    "k_momentum": (8 * W + 1 * W, "face"),             # vel, 2 other comps, fo, Pb, T, nu, p -> vel'
-    "k_gs0": (5 * W, "cell"),                          # half sweep: r,diag,z of its colour, z of the other, 3 coefficient arrays
-    "k_cg_apply": (8 * W, "cell"),                     # z, d, diag, 3 coefficients -> d, q
-    "k_cg_update": (7.5 * W, "cell"),                  # p, d, r, q, diag -> p, r, z(red)
-    "k_res0_restrict": (6 * W + 4, "cell"),            # r, z, diag, 3 coefficients, agg
-    "k_gs0_last_dot": (6 * W, "cell"),
-    "k_rhs": (13 * W + 1, "cell"),
-    "k_heat": (8 * W + 1, "cell"),
-    "k_energy": (6 * W + 1, "cell"),
-    "k_combust": (6 * W + 3, "cell"),
-    "k_turb_filter": (2 * W + 1, "cell"),
-    "k_turb_center": (6 * W + 1, "cell"),
-    "k_turb_nu": (5 * W + 1, "cell"),
-    "k_velcorr": (5 * W, "face"),
-    "k_stats": (4 * W + 1, "cell"),
-}
+# Algorithmic bytes per unit of each kernel's domain for storage width w
+# (8 for FP64 fields, 4 for the mixed path): each input array read once and
+# each output written once per launch; uint8 masks count 1 B, int32 maps 4 B.
+def kernel_bytes(name: str, w: int):
+    table = {
+        "k_advect": 18 * w + 1 + 10 * w,        # 10 scalars + u,v,w + fx,fy,fz + Pb,nu + blocked -> 10 scalars
+        "k_momentum": 9 * w,                    # vel, 2 other components, fo, Pb, T, nu, p -> vel' (per face)
+        "k_gs0": 5 * w,                         # half sweep: r, diag, z of its colour, z of the other, coefficients
+        "k_cg_apply": 8 * w,                    # z, d, diag, 3 coefficients -> d, q
+        "k_cg_update": 7.5 * w,                 # p, d, r, q, diag -> p, r, z(red)
+        "k_res0_restrict": 6 * w + 4,           # r, z, diag, 3 coefficients, agg
+        "k_gs0_last_dot": 6 * w,
+        "k_rhs": 13 * w + 1,
+        "k_heat": 8 * w + 1,
+        "k_energy": 6 * w + 1,
+        "k_combust": 6 * w + 3,
+        "k_turb_filter": 2 * w + 1,
+        "k_turb_center": 6 * w + 1,
+        "k_turb_nu": 5 * w + 1,
+        "k_velcorr": 5 * w,
+        "k_stats": 4 * w + 1,
+        "k_mx_res64": 8 + 5 * w + 4,            # p64, b, diag, coefficients -> r, e
+        "k_mx_update": 8 + 8 + 2 * w,
+    }
+    return table.get(name)
 
 
 def measured_peak():
@@ -142,7 +145,8 @@ class ClockSampler:
         return out
 
 
-def cpu_reference_rate(case, steps: int, warm: int, threads: int, bits: int = 32, budget_s: float = 20.0):
+def cpu_reference_rate(case, steps: int, warm: int, threads: int, bits: int = 32, budget_s: float = 20.0,
+                       spinup: int = 0):
     """cell-updates/s of the reference's own CPU step on this case (oracle/_ref),
     or of the FP64 oracle port when the reference build is absent."""
     from oracle import refpy
@@ -155,7 +159,7 @@ def cpu_reference_rate(case, steps: int, warm: int, threads: int, bits: int = 32
         s = OracleSolver(case)
         kind, threads = "port", 1
         stepf = lambda: s.step(case.profile.dtMax)
-    for _ in range(warm):
+    for _ in range(spinup + warm):
         stepf()
     t0 = time.perf_counter()
     n = 0
@@ -178,7 +182,7 @@ def run_reference(args, rank, world):
         print(json.dumps({"impl": "reference", "unavailable": "reference CPU build (oracle/_ref) is not present"}))
         return 0
     s = refpy.RefSolver(case, 32, threads)
-    for _ in range(args.warmup):
+    for _ in range(args.spinup + args.warmup):   # the same developed flow as the GPU arm
         s.step(case.profile.dtMax)
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -189,13 +193,84 @@ def run_reference(args, rank, world):
             "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded house generator)",
             "config": {"workload": args.workload, "cells": case.N, "pressure_stop": "absolute 1e-8 1/s",
-                       "threads": threads},
+                       "threads": threads, "spinup_steps": args.spinup},
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": "reference",
-                             "sample": "%d steps of %s after %d warm-up steps" % (args.steps, args.workload, args.warmup)},
+                             "sample": "%d steps of %s after %d spin-up and %d warm-up steps" % (
+                                 args.steps, args.workload, args.spinup, args.warmup)},
             "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
+
+
+def measure(args, precision, L, world, clocks: bool):
+    """Timed steps of one precision on the workload: value, launches, per-kernel
+    profile and roofline of the dominant kernel, e2e through the C ABI."""
+    import ctypes
+    from photon_gb300 import _lib
+    from photon_gb300.solver import Solver
+    case = make_workload(args.workload)
+    g = Solver(case, precision)
+    dtMax = case.profile.dtMax
+    if args.spinup > 0:
+        g.run(args.spinup, dtMax)
+    g.run(max(3, args.warmup), dtMax)
+    # a single scenario's working set fits in L2: flush it before every timed step
+    flush = g.device_bytes() < (200 << 20)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    g.sync()
+    clk = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    if clocks:
+        clk.__enter__()
+    ms, launches = g.time_steps(args.steps, dtMax, flush_l2=flush)
+    if clocks:
+        clk.__exit__()
+    g.sync()
+    t_s = ms / 1e3
+    if dist:
+        import torch
+        t = torch.tensor([t_s], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_s = float(t[0])
+    value = case.N * args.steps * world / t_s
+    st = g.stats()
+    # e2e through the C ABI: step from the host, read T and the stats back to pinned memory
+    w = 8 if precision == _lib.PREC_FP64 else 4
+    nbytesT = case.N * 8
+    hbuf = L.phx_alloc_host(nbytesT)
+    stats = _lib.PhxStats()
+    dt_c = ctypes.c_double()
+    for _ in range(2):
+        L.phx_step(g.h, dtMax, ctypes.byref(dt_c))
+    g.sync()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        if L.phx_step(g.h, dtMax, ctypes.byref(dt_c)) != 0:
+            raise SystemExit(L.phx_last_error(g.h).decode())
+        L.phx_get_field(g.h, _lib.FIELD_ID["T"], ctypes.c_void_p(hbuf), nbytesT)
+        L.phx_get_stats(g.h, ctypes.byref(stats))
+    e2e_s = time.perf_counter() - t0
+    L.phx_free_host(ctypes.c_void_p(hbuf))
+    e2e_value = case.N * args.steps * world / e2e_s
+    # per-kernel device times of one step (outside the timed region) for the roofline
+    prof = g.profile_step(dtMax, flush_l2=flush)
+    tot_prof = sum(p[2] for p in prof)
+    top = max(prof, key=lambda p: p[2])
+    per_unit = kernel_bytes(top[0], w)
+    peak, peak_kind = measured_peak()
+    roof = None
+    if per_unit:
+        bytes_per_launch = per_unit * case.N
+        achieved = bytes_per_launch / (top[2] / top[1] / 1e3) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "kernel": top[0], "kernel_share": top[2] / tot_prof,
+                "algorithmic_bytes_per_launch": bytes_per_launch, "peak_kind": peak_kind}
+    g.close()
+    return {"case": case, "value": value, "t_s": t_s, "stats": st, "launches": launches, "roofline": roof,
+            "clk": clk, "prof": prof, "e2e": e2e_value, "d2h": case.N * w, "flush": flush}
 
 
 def main():
@@ -218,91 +293,50 @@ def main():
         dist.init_process_group("gloo")
 
     from photon_gb300 import _lib
-    from photon_gb300.solver import Solver
     L = _lib.load()
     if L.phx_select_device(local) != 0:
         raise SystemExit("cannot select device %d" % local)
 
-    case = make_workload(args.workload)
-    g = Solver(case, _lib.PREC_FP64)
-    dtMax = case.profile.dtMax
-    if args.spinup > 0:
-        g.run(args.spinup, dtMax)
-    g.run(max(3, args.warmup), dtMax)
-    # the working set of one scenario fits in L2: flush it before every timed step
-    flush = g.device_bytes() < (200 << 20)
-
-    if dist:
-        dist.barrier()
-    g.sync()
-    with ClockSampler(local) as clk:
-        ms, launches = g.time_steps(args.steps, dtMax, flush_l2=flush)
-    g.sync()
-    t_s = ms / 1e3
-    if dist:
-        import torch
-        t = torch.tensor([t_s], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_s = float(t[0])
-    value = case.N * args.steps * world / t_s
-    st = g.stats()
-
-    # e2e through the C ABI: step from the host, read T and the stats back to pinned memory
-    import ctypes
-    nbytesT = case.N * 8
-    hbuf = L.phx_alloc_host(nbytesT)
-    stats = _lib.PhxStats()
-    dt_c = ctypes.c_double()
-    e2e_steps = args.steps
-    for _ in range(2):
-        L.phx_step(g.h, dtMax, ctypes.byref(dt_c))
-    g.sync()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        if L.phx_step(g.h, dtMax, ctypes.byref(dt_c)) != 0:
-            raise SystemExit(L.phx_last_error(g.h).decode())
-        L.phx_get_field(g.h, _lib.FIELD_ID["T"], ctypes.c_void_p(hbuf), nbytesT)
-        L.phx_get_stats(g.h, ctypes.byref(stats))
-    e2e_s = time.perf_counter() - t0
-    L.phx_free_host(ctypes.c_void_p(hbuf))
-    e2e_value = case.N * e2e_steps * world / e2e_s
-
-    # per-kernel device times of one step (outside the timed region) for the roofline
-    prof = g.profile_step(dtMax, flush_l2=flush)
-    tot_prof = sum(p[2] for p in prof)
-    top = max(prof, key=lambda p: p[2])
-    per_unit, unit = KERNEL_BYTES.get(top[0], (None, None))
-    peak, peak_kind = measured_peak()
-    roof = None
-    if per_unit:
-        units = case.N if unit == "cell" else (case.N * 1.0)
-        bytes_per_launch = per_unit * units
-        achieved = bytes_per_launch / (top[2] / top[1] / 1e3) / 1e9
-        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "kernel": top[0], "kernel_share": top[2] / tot_prof,
-                "algorithmic_bytes_per_launch": bytes_per_launch, "peak_kind": peak_kind}
+    mixed = measure(args, _lib.PREC_MIXED, L, world, clocks=True)
+    fp64 = measure(args, _lib.PREC_FP64, L, world, clocks=False)
+    case = mixed["case"]
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cref = make_workload(args.workload)
         cref.profile.tol = 1e-8
         threads = os.cpu_count() or 1
-        v, kind, thr, n, el = cpu_reference_rate(cref, steps=20, warm=2, threads=threads)
+        v, kind, thr, n, el = cpu_reference_rate(cref, steps=20, warm=2, threads=threads, spinup=args.spinup)
         cpu = {"value": v, "unit": "cell-updates/s", "cores": thr, "kind": kind,
-               "sample": "%d steps of %s (%.1f s) after 2 warm-up steps, FP32 reference build" % (n, args.workload, el)}
-
+               "sample": "%d steps of %s (%.1f s) after %d spin-up and 2 warm-up steps, FP32 reference build, "
+                         "pressure stop 1e-8 1/s" % (n, args.workload, el, args.spinup)}
+    value = mixed["value"]
+    t_s = mixed["t_s"]
+    st = mixed["stats"]
+    launches = mixed["launches"]
+    roof = mixed["roofline"]
+    clk = mixed["clk"]
+    prof = mixed["prof"]
+    e2e_value, nbytesT = mixed["e2e"], mixed["d2h"]
+    import ctypes
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_s / args.steps * 1e3, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 (mixed)",
                 "data": "synthetic (seeded house generator; random-free physics, no dataset)",
-                "config": {"workload": args.workload, "cells": case.N, "precision": "fp64",
+                "config": {"workload": args.workload, "cells": case.N, "precision": "mixed (FP32 fields/stencils, FP32 MG-CG in FP64 refinement)",
                            "pressure_stop": "relative 1e-8 (max|r| <= 1e-8 max|b|)",
-                           "l2": "flushed before each step" if flush else "inputs larger than L2",
+                           "l2": "flushed before each step" if mixed["flush"] else "inputs larger than L2",
                            "spinup_steps": args.spinup, "cg_iters_last_step": st["pressure_iters"],
+                           "rel_residual_last_step": st["pressure_rel_residual"],
                            "parallelism": "replicas" if world > 1 else "single"},
                 "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": 8,
                         "d2h_bytes_per_step": nbytesT + ctypes.sizeof(_lib.PhxStats)},
+                "fp64": {"value": fp64["value"], "ms_per_step": fp64["t_s"] / args.steps * 1e3,
+                         "cg_iters_last_step": fp64["stats"]["pressure_iters"],
+                         "rel_residual_last_step": fp64["stats"]["pressure_rel_residual"],
+                         "gpu_launches": fp64["launches"], "roofline": fp64["roofline"], "e2e": fp64["e2e"]},
+                "mixed_over_fp64": value / fp64["value"],
                 "gpu_launches": launches,
                 "roofline": roof,
                 "cpu_baseline": cpu,

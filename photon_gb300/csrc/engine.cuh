@@ -11,7 +11,7 @@
 
 #include "engine.h"
 #include "host_setup.h"
-#include "pressure_kernels.cuh"
+#include "mixed_kernels.cuh"
 
 namespace phx {
 
@@ -41,6 +41,12 @@ struct SourceHost {
 template <class R>
 class Ctx : public CtxBase {
 public:
+    // the float instantiation is the mixed path: FP32 fields and stencils, FP64
+    // refinement of the pressure solve, FP64 dots and global sums
+    static constexpr bool kMixed = std::is_same<R, float>::value;
+    static constexpr int INNER_MAX = 10;        // inner FP32 CG iterations per refinement pass
+    static constexpr double INNER_REL = 1e-4;   // inner stop relative to the pass's starting residual
+    static constexpr int OUTER_MAX = 40;
     GridGeom geo;
     double cfl = 0.5, dtMaxP = 0.02, tol = 0.002, relTol = 0;
     int maxIters = 400, radiationOn = 1;
@@ -67,6 +73,8 @@ public:
         if (arena) cudaFree(arena);
         if (hPin) cudaFreeHost(hPin);
         if (flushBuf) cudaFree(flushBuf);
+        destroyGraph();
+        if (dLoop) cudaFree(dLoop);
         for (auto e : evPool) cudaEventDestroy(e);
         for (auto& e : ev) if (e) cudaEventDestroy(e);
         if (st) cudaStreamDestroy(st);
@@ -155,6 +163,11 @@ public:
             dbuf[0] = carve<R>(base, off, N); dbuf[1] = carve<R>(base, off, N);
             s.d = dbuf[0];
             s.q = carve<R>(base, off, N);
+            s.p64 = kMixed ? carve<double>(base, off, N) : nullptr;
+            s.mixed = kMixed ? 1 : 0;
+            s.innerMax = INNER_MAX;
+            s.innerRel = INNER_REL;
+            s.outerMax = OUTER_MAX;
             s.nLevels = nl;
             for (int l = 0; l < nl; ++l) {
                 const MgLevel& L = MG.lv[l];
@@ -471,7 +484,8 @@ public:
         allDone = hPin[8] != 0;
         return PHX_OK;
     }
-    int stProject() {
+    // Solver::project: right-hand side, first V-cycle and CG set-up
+    void projectPrelude() {
         const Scn<R>* S = dS;
         cudaMemsetAsync(h.sv + SV_DONE, 0, sizeof(double), st);
         cudaMemsetAsync(h.sv + SV_IT, 0, sizeof(double), st);
@@ -481,15 +495,18 @@ public:
         launch("k_gs0", D_HALF, TPB, k_gs0<R>, S, dom[D_HALF], 0, 0);
         vcycleBody();
         launch("k_gs0_last_dot", D_CELLS, TPB, k_gs0_last_dot<R>, S, dom[D_CELLS], 0);
-        bool done = false;
-        PHX_TRY(readDone(done));
-        for (int it = 0; !done && it <= maxIters + 1; ++it) {
-            launch("k_cg_apply", D_CELLS, TPB, k_cg_apply<R>, S, dom[D_CELLS], (R* const*)dD);
-            launch("k_cg_update", D_CELLS, TPB, k_cg_update<R>, S, dom[D_CELLS], (R* const*)dD);
-            vcycleBody();
-            launch("k_gs0_last_dot", D_CELLS, TPB, k_gs0_last_dot<R>, S, dom[D_CELLS], 1);
-            PHX_TRY(readDone(done));
-        }
+    }
+    // one CG iteration (src/sim/gasphase.cpp:605-625)
+    void cgIteration() {
+        const Scn<R>* S = dS;
+        launch("k_cg_apply", D_CELLS, TPB, k_cg_apply<R>, S, dom[D_CELLS], (R* const*)dD);
+        launch("k_cg_update", D_CELLS, TPB, k_cg_update<R>, S, dom[D_CELLS], (R* const*)dD);
+        vcycleBody();
+        launch("k_gs0_last_dot", D_CELLS, TPB, k_gs0_last_dot<R>, S, dom[D_CELLS], 1);
+    }
+    // zone mean removal and velocity correction (:629-676)
+    void projectEpilogue() {
+        const Scn<R>* S = dS;
         if (!Z.closed.empty()) {
             launch("k_zone_mean", D_CZ, TPB, k_zone_mean<R>, S, dom[D_CZ]);
             launch("k_zone_mean_sub", D_CC, TPB, k_zone_mean_sub<R>, S, dom[D_CC]);
@@ -497,6 +514,230 @@ public:
         launch("k_velcorr", D_FX, TPB, k_velcorr<R>, S, dom[D_FX], 0);
         launch("k_velcorr", D_FY, TPB, k_velcorr<R>, S, dom[D_FY], 1);
         launch("k_velcorr", D_FZ, TPB, k_velcorr<R>, S, dom[D_FZ], 2);
+    }
+    // ---- mixed path: FP64 refinement around the FP32 inner CG -------------------
+    void mixedBegin() {
+        const Scn<R>* S = dS;
+        cudaMemsetAsync(h.sv + SV_DONE, 0, sizeof(double), st);
+        cudaMemsetAsync(h.sv + SV_IT, 0, sizeof(double), st);
+        cudaMemsetAsync(h.sv + SV_ODONE, 0, sizeof(double), st);
+        cudaMemsetAsync(h.sv + SV_OUTER, 0, sizeof(double), st);
+        cudaMemsetAsync(h.sv + SV_ITTOT, 0, sizeof(double), st);
+        cudaMemsetAsync(h.sv + SV_R64MAX, 0, sizeof(double), st);
+        cudaMemsetAsync(h.sv + SV_RMAX, 0, sizeof(double), st);
+        cudaMemsetAsync(h.sv + SV_BMAX, 0, sizeof(double), st);
+        launch("k_rhs", D_CELLS, TPB, k_rhs<R>, S, dom[D_CELLS]);
+        launch("k_mx_res64", D_CELLS, TPB, k_mx_res64<R>, S, dom[D_CELLS]);
+    }
+    // the inner solve's first V-cycle and CG set-up
+    void mixedInnerPrelude() {
+        const Scn<R>* S = dS;
+        launch("k_gs0", D_HALF, TPB, k_gs0<R>, S, dom[D_HALF], 0, 0);
+        vcycleBody();
+        launch("k_gs0_last_dot", D_CELLS, TPB, k_gs0_last_dot<R>, S, dom[D_CELLS], 0);
+    }
+    // p64 += e, and the FP64 residual of the next pass
+    void mixedRefine() {
+        const Scn<R>* S = dS;
+        launch("k_mx_update", D_CELLS, TPB, k_mx_update<R>, S, dom[D_CELLS]);
+        launch("k_mx_res64", D_CELLS, TPB, k_mx_res64<R>, S, dom[D_CELLS]);
+    }
+    int readOuterDone(bool& allDone) {
+        PHX_CK(cudaMemcpyAsync(hPin + 8, h.sv + SV_ODONE, sizeof(double), cudaMemcpyDeviceToHost, st));
+        PHX_CK(cudaStreamSynchronize(st));
+        allDone = hPin[8] != 0;
+        return PHX_OK;
+    }
+    int stProjectMixed() {
+        mixedBegin();
+        k_mx_outer<R><<<1, 32, 0, st>>>(dS, 1, cudaGraphConditionalHandle{}, nullptr, 0, 0);
+        ++launches;
+        bool odone = false;
+        PHX_TRY(readOuterDone(odone));
+        for (int pass = 0; !odone && pass <= OUTER_MAX + 1; ++pass) {
+            mixedInnerPrelude();
+            bool done = false;
+            PHX_TRY(readDone(done));
+            for (int it = 0; !done && it <= INNER_MAX + 1; ++it) {
+                cgIteration();
+                PHX_TRY(readDone(done));
+            }
+            mixedRefine();
+            k_mx_outer<R><<<1, 32, 0, st>>>(dS, 1, cudaGraphConditionalHandle{}, nullptr, 0, 0);
+            ++launches;
+            PHX_TRY(readOuterDone(odone));
+        }
+        launch("k_mx_final", D_CELLS, TPB, k_mx_final<R>, dS, dom[D_CELLS]);
+        projectEpilogue();
+        return PHX_OK;
+    }
+
+    // host-driven CG loop: the stop test is read back after every iteration
+    int stProject() {
+        if (kMixed) return stProjectMixed();
+        projectPrelude();
+        bool done = false;
+        PHX_TRY(readDone(done));
+        for (int it = 0; !done && it <= maxIters + 1; ++it) {
+            cgIteration();
+            PHX_TRY(readDone(done));
+        }
+        projectEpilogue();
+        return PHX_OK;
+    }
+
+    // ---- captured step graph: the CG loop is a device-side while node ----------
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    cudaGraphConditionalHandle cgHandle{};
+    int* dLoop = nullptr;
+    int outerKernels = 0, bodyKernels = 0;
+    bool useGraph = true;
+
+    void destroyGraph() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (graph) cudaGraphDestroy(graph);
+        gexec = nullptr;
+        graph = nullptr;
+    }
+
+    int buildGraph() {
+        destroyGraph();
+        if (!dLoop) PHX_CK(cudaMalloc(&dLoop, 2 * sizeof(int)));
+        const Scn<R> saved = h;
+        PHX_CK(cudaGraphCreate(&graph, 0));
+        PHX_CK(cudaGraphConditionalHandleCreate(&cgHandle, graph, 0, 0));
+        PHX_CK(cudaStreamBeginCaptureToGraph(st, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        launches = 0;
+        launch("k_begin", D_ONE, 32, k_begin<R>, (const Scn<R>*)dS, dom[D_ONE], 1, 0.0);
+        stCombustion();
+        stTurbulence();
+        stHeat();
+        stEnergy();
+        stMomentum();
+        stLeakage();
+        if (kMixed) {
+            PHX_TRY(captureMixedProject());
+        } else {
+            projectPrelude();
+            cudaMemsetAsync(dLoop, 0, sizeof(int), st);
+            const int cap = maxIters + 2;
+            k_cg_cond<R><<<1, 32, 0, st>>>(dS, 1, cgHandle, dLoop, cap);
+            ++launches;
+            cudaGraph_t body = nullptr;
+            PHX_TRY(addWhile(graph, cgHandle, &body));
+            projectEpilogue();
+            stAdvect();
+            stEnd();
+            cudaGraph_t outGraph = nullptr;
+            PHX_CK(cudaStreamEndCapture(st, &outGraph));
+            outerKernels = launches;
+            PHX_CK(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+            launches = 0;
+            cgIteration();
+            k_cg_cond<R><<<1, 32, 0, st>>>(dS, 1, cgHandle, dLoop, cap);
+            ++launches;
+            PHX_CK(cudaStreamEndCapture(st, &body));
+            bodyKernels = launches;
+        }
+        h = saved;
+        PHX_CK(cudaGraphInstantiate(&gexec, graph, 0));
+        return checkLaunch();
+    }
+
+    // add a while node after the current capture position of st (which captures
+    // into graph g); capture continues after it
+    int addWhile(cudaGraph_t g, cudaGraphConditionalHandle handle, cudaGraph_t* body) {
+        cudaStreamCaptureStatus cs;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t ndeps = 0;
+        PHX_CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, nullptr, &deps, nullptr, &ndeps));
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = handle;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t cond;
+        PHX_CK(cudaGraphAddNode(&cond, g, deps, nullptr, ndeps, &cp));
+        *body = cp.conditional.phGraph_out[0];
+        PHX_CK(cudaStreamUpdateCaptureDependencies(st, &cond, nullptr, 1, cudaStreamSetCaptureDependencies));
+        return PHX_OK;
+    }
+
+    // mixed project in the step graph: while (refining) { inner prelude;
+    // while (inner CG) { iteration }; refine }. dLoop[0] bounds the refinement
+    // passes, dLoop[1] the inner iterations of a pass.
+    cudaGraphConditionalHandle outerHandle{};
+    int outerBodyKernels = 0, innerPreludeKernels = 0;
+    int captureMixedProject() {
+        mixedBegin();
+        cudaMemsetAsync(dLoop, 0, 2 * sizeof(int), st);
+        const int capOuter = OUTER_MAX + 2, capInner = INNER_MAX + 2;
+        PHX_CK(cudaGraphConditionalHandleCreate(&outerHandle, graph, 0, 0));
+        k_mx_outer<R><<<1, 32, 0, st>>>(dS, 1, outerHandle, dLoop, capOuter, 1);
+        ++launches;
+        cudaGraph_t outerBody = nullptr;
+        PHX_TRY(addWhile(graph, outerHandle, &outerBody));
+        launch("k_mx_final", D_CELLS, TPB, k_mx_final<R>, dS, dom[D_CELLS]);
+        projectEpilogue();
+        stAdvect();
+        stEnd();
+        cudaGraph_t outGraph = nullptr;
+        PHX_CK(cudaStreamEndCapture(st, &outGraph));
+        outerKernels = launches;
+        // refinement pass
+        PHX_CK(cudaStreamBeginCaptureToGraph(st, outerBody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        launches = 0;
+        cudaMemsetAsync(dLoop + 1, 0, sizeof(int), st);
+        mixedInnerPrelude();
+        PHX_CK(cudaGraphConditionalHandleCreate(&cgHandle, outerBody, 0, 0));
+        k_cg_cond<R><<<1, 32, 0, st>>>(dS, 1, cgHandle, dLoop + 1, capInner);
+        ++launches;
+        innerPreludeKernels = launches;
+        cudaGraph_t innerBody = nullptr;
+        PHX_TRY(addWhile(outerBody, cgHandle, &innerBody));
+        mixedRefine();
+        k_mx_outer<R><<<1, 32, 0, st>>>(dS, 1, outerHandle, dLoop, capOuter, 1);
+        ++launches;
+        cudaGraph_t ob = nullptr;
+        PHX_CK(cudaStreamEndCapture(st, &ob));
+        outerBodyKernels = launches;
+        // inner CG iteration
+        PHX_CK(cudaStreamBeginCaptureToGraph(st, innerBody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        launches = 0;
+        cgIteration();
+        k_cg_cond<R><<<1, 32, 0, st>>>(dS, 1, cgHandle, dLoop + 1, capInner);
+        ++launches;
+        PHX_CK(cudaStreamEndCapture(st, &innerBody));
+        bodyKernels = launches;
+        return PHX_OK;
+    }
+
+    int graphStep(double dtMax) {
+        if (!gexec) PHX_TRY(buildGraph());
+        double v = dtMax;   // pageable source: staged at the call, safe to reuse at once
+        PHX_CK(cudaMemcpyAsync(h.sv + SV_DTMAX_ARG, &v, sizeof(double), cudaMemcpyHostToDevice, st));
+        PHX_CK(cudaGraphLaunch(gexec, st));
+        swapHost(1 | 2 | 4);
+        return PHX_OK;
+    }
+
+    // kernels the last graph step ran: the outer nodes plus the loop body per iteration
+    int graphLaunchCount(int* out) {
+        if (kMixed) {
+            // passes from the refinement counter, inner iterations from the scalars
+            int lc[2] = {0, 0};
+            PHX_CK(cudaMemcpyAsync(lc, dLoop, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+            PHX_CK(cudaMemcpyAsync(hPin + 32, h.sv + SV_ITTOT, sizeof(double), cudaMemcpyDeviceToHost, st));
+            PHX_CK(cudaStreamSynchronize(st));
+            const int passes = std::max(0, lc[0] - 1);
+            *out = outerKernels + outerBodyKernels * passes + bodyKernels * ((int)hPin[32] + passes);
+            return PHX_OK;
+        }
+        int lc = 0;
+        PHX_CK(cudaMemcpyAsync(&lc, dLoop, sizeof(int), cudaMemcpyDeviceToHost, st));
+        PHX_CK(cudaStreamSynchronize(st));
+        *out = outerKernels + bodyKernels * std::max(0, lc - 1);
         return PHX_OK;
     }
     void stAdvect() {
@@ -519,6 +760,7 @@ public:
     }
 
     int oneStep(double dtMax) {
+        if (useGraph && !prof) return graphStep(dtMax);
         stBegin(true, dtMax);
         stCombustion();
         stTurbulence();
@@ -630,6 +872,11 @@ public:
         if (!fieldPtr(f, &p, &n, &t)) { err = "unknown field"; return PHX_ERR_INVALID; }
         size_t want = n * (t == 0 ? sizeof(double) : t == 1 ? 1 : 4);
         if (bytes != want) { err = "field size mismatch: expected " + std::to_string(want) + " bytes"; return PHX_ERR_INVALID; }
+        if (kMixed && f == PHX_FIELD_P) {   // the FP64 pressure of the refinement loop
+            PHX_CK(cudaMemcpyAsync(host, h.p64, bytes, cudaMemcpyDeviceToHost, st));
+            PHX_CK(cudaStreamSynchronize(st));
+            return PHX_OK;
+        }
         if (t == 0) return getReal((const R*)p, n, (double*)host);
         PHX_CK(cudaMemcpyAsync(host, p, bytes, cudaMemcpyDeviceToHost, st));
         PHX_CK(cudaStreamSynchronize(st));
@@ -645,6 +892,7 @@ public:
         if (bytes != want) { err = "field size mismatch: expected " + std::to_string(want) + " bytes"; return PHX_ERR_INVALID; }
         if (t == 0) {
             const double* d = (const double*)host;
+            if (kMixed && f == PHX_FIELD_P) PHX_TRY(putRaw(h.p64, d, n));
             return put<R>((R*)p, std::vector<double>(d, d + n));
         }
         PHX_CK(cudaMemcpyAsync(p, host, bytes, cudaMemcpyHostToDevice, st));
@@ -658,7 +906,7 @@ public:
         const double* sv = hPin + 64;
         o->time = sv[SV_TIME]; o->dt = sv[SV_DT];
         o->max_vel = sv[SV_MAXVEL]; o->max_nu = sv[SV_MAXNU]; o->max_div = sv[SV_MAXDIV];
-        o->pressure_iters = (int)sv[SV_IT]; o->pressure_residual = sv[SV_PRES]; o->pressure_rel_residual = sv[SV_PREL];
+        o->pressure_iters = kMixed ? (int)sv[SV_ITTOT] : (int)sv[SV_IT]; o->pressure_residual = sv[SV_PRES]; o->pressure_rel_residual = sv[SV_PREL];
         o->hrr = sv[SV_HRR]; o->max_gas_t = sv[SV_MAXGAST]; o->burning_cells = (int)sv[SV_BURNING];
         o->fuel_in = sv[SV_FUELIN]; o->fuel_burned = sv[SV_FUELBURNED]; o->fuel_in_domain = sv[SV_FUELINDOMAIN];
         o->zones = (int)Z.zoneP.size(); o->leak_faces = 0;
@@ -697,12 +945,18 @@ public:
             PHX_CK(cudaEventRecord(ev[0], st));
             launches = 0;
             PHX_TRY(oneStep(dtMax));
-            nl += launches;
             PHX_CK(cudaEventRecord(ev[1], st));
             PHX_CK(cudaEventSynchronize(ev[1]));
             float ms = 0;
             PHX_CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
             total += ms;
+            if (useGraph) {
+                int k = 0;
+                PHX_TRY(graphLaunchCount(&k));
+                nl += k;
+            } else {
+                nl += launches;
+            }
         }
         if (totalMs) *totalMs = total;
         if (launchesOut) *launchesOut = nl;

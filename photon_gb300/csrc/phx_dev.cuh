@@ -52,6 +52,8 @@ enum Slot {
     SV_RZ, SV_ALPHA, SV_BETA, SV_RMAX, SV_BMAX, SV_IT, SV_DONE, SV_DQ,
     SV_PITERS, SV_PRES, SV_PREL, SV_HRR, SV_MAXGAST, SV_BURNING, SV_FUELIN, SV_FUELBURNED, SV_FUELINDOMAIN,
     SV_INV, SV_ACTIVE,
+    // mixed path: FP64 refinement loop around the FP32 inner CG
+    SV_R64MAX, SV_R0MAX, SV_OUTER, SV_ODONE, SV_ITTOT,
     SV_SRC_MF = 32,              // MAX_SRC injection amounts of this step (-1 = inactive)
     SV_COUNT = 64
 };
@@ -117,6 +119,11 @@ struct Scn {
     R* tmp[9];                   // turbulence: cell-centre velocities and filter passes
     // pressure solve
     R *b, *r, *z, *d, *q;
+    double* p64;                 // mixed path: FP64 pressure accumulated by the refinement loop
+    int mixed;                   // mixed path: the CG below is the inner FP32 solve
+    int innerMax;                // inner CG iterations per refinement
+    double innerRel;             // inner stop: max|r| <= innerRel * max|r| at the inner start
+    int outerMax;                // refinement passes per step
     int nLevels;
     Level<R> lv[MAX_LEVELS];
     // scalars and reductions

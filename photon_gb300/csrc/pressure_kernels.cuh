@@ -209,6 +209,7 @@ __global__ void k_coarse_serial(const Scn<R>* __restrict__ S, Dom dom, int l) {
 // relative test max|r| <= relTol max|b|
 template <class R>
 __device__ __forceinline__ bool cgContinue(const Scn<R>& g, double res, double rmax, int it, double rz) {
+    if (g.mixed) return it < g.innerMax && rz > 0 && rmax > g.innerRel * g.sv[SV_R0MAX];
     double relStop = g.relTol > 0 ? g.relTol * g.sv[SV_BMAX] : -1.0;
     return res > g.tol && it < g.maxIters && rz > 0 && !(rmax <= relStop);
 }
@@ -340,6 +341,21 @@ __global__ void k_cg_update(const Scn<R>* __restrict__ S, Dom dom, R* const* dbu
         if (((i + j + k) & 1) == 0) g.z[c] = dg > 0 ? (R)(r / dg) : (R)0;
     }
     blockMaxTo(g.sv + SV_RMAX, rm);
+}
+
+// Condition of the CG while-loop of the captured step graph: continue while
+// any scenario of the launch has not stopped. The loop counter bounds the
+// loop whatever the scenarios' flags say, so the graph always terminates.
+template <class R>
+__global__ void k_cg_cond(const Scn<R>* __restrict__ S, int nscn, cudaGraphConditionalHandle handle, int* loopCount,
+                          int cap) {
+    bool active = false;
+    for (int s = threadIdx.x; s < nscn; s += blockDim.x) active |= S[s].sv[SV_DONE] == 0;
+    int any = __syncthreads_or(active);
+    if (threadIdx.x == 0) {
+        int lc = ++(*loopCount);
+        cudaGraphSetConditional(handle, (any && lc <= cap) ? 1u : 0u);
+    }
 }
 
 #undef PHX_PROLOGUE_ACTIVE

@@ -115,46 +115,59 @@ __global__ void k_begin(const Scn<R>* __restrict__ S, Dom dom, int computeDt, do
 }
 
 // ---------------------------------------------------------------------------
+// The stage kernels below compute in their storage type T = R: double for the
+// FP64 path (the expressions keep the reference's evaluation order), float for
+// the mixed path. Literals are written T(...) so the float path stays in FP32.
+
+// gas density P / (R T) of a cell in the arithmetic type
+template <class R>
+__device__ __forceinline__ R rhoOf(const Scn<R>& g, int c) {
+    return g.Pb[c] / (R(K_RS) * g.sc[0][c]);
+}
+
 // Per-step clears (src/sim/solver.cpp:231-233), injectIgnitions + injectBurners
 // through addGasSpecies (src/sim/solver.cpp:212-223), and combustion
 // (src/sim/solver.cpp:284-344). lit is double-buffered: neighbours read the
 // previous step's flags from lit, the new flags go to lit2.
 template <class R>
 __global__ void k_combust(const Scn<R>* __restrict__ S, Dom dom) {
+    using T = R;
     PHX_PROLOGUE(dom);
     int c = tile_ * TPB + threadIdx.x;
     if (c >= g.N) return;
     const double* sv = g.sv;
-    const double dt = sv[SV_DT];
+    const T dt = (T)sv[SV_DT];
+    const T dx = (T)g.dx;
     const int nx = g.nx, ny = g.ny, nz = g.nz, sz = nx * ny;
-    double Qc = 0, Qrc = 0, hrrc = 0, ms = 0;
+    T Qc = 0, Qrc = 0, hrrc = 0, ms = 0;
     uint8_t pil = 0, litn = 0;
     if (!g.blocked[c]) {
         const int i = c % nx, j = (c / nx) % ny, k = c / sz;
         R* const* Y = g.sc;
-        double Tc = Y[0][c];
-        double yf = Y[2][c];
+        T Tc = Y[0][c];
+        T yf = Y[2][c];
         bool member = false;
         for (int q = 0; q < g.nsrc; ++q) {
             const Src& sr = g.src[q];
             if (sv[SV_SRC_MF + q] >= 0 && k == sr.k && i >= sr.i0 && i <= sr.i1 && j >= sr.j0 && j <= sr.j1) member = true;
         }
-        if (member || yf >= 1e-6) {
-            double Yo = Y[1][c], Ys = Y[3][c], Ya = Y[4][c], Yp = Y[5][c], Yc = Y[6][c], Yw = Y[7][c], Yco = Y[8][c],
-                   Yai = Y[9][c];
+        if (member || yf >= T(1e-6)) {
+            T Yo = Y[1][c], Ys = Y[3][c], Ya = Y[4][c], Yp = Y[5][c], Yc = Y[6][c], Yw = Y[7][c], Yco = Y[8][c],
+              Yai = Y[9][c];
             bool modified = false;
             if (member) {
-                const double m = gasDensity(g, c) * g.dx * g.dx * g.dx;
+                const T m = rhoOf(g, c) * dx * dx * dx;
                 for (int q = 0; q < g.nsrc; ++q) {
                     const Src& sr = g.src[q];
-                    double mf = sv[SV_SRC_MF + q];
-                    if (!(mf >= 0 && k == sr.k && i >= sr.i0 && i <= sr.i1 && j >= sr.j0 && j <= sr.j1)) continue;
-                    const double fuelGen = mf, aerosol = 0.0, sootPot = mf * K_BURNER_SOOT;
-                    const double madd = fuelGen + aerosol;
-                    if (madd <= 0) continue;
-                    const double mt = m + madd, scl = m / mt;
+                    const double mfd = sv[SV_SRC_MF + q];
+                    if (!(mfd >= 0 && k == sr.k && i >= sr.i0 && i <= sr.i1 && j >= sr.j0 && j <= sr.j1)) continue;
+                    const T mf = (T)mfd;
+                    const T fuelGen = mf, aerosol = T(0), sootPot = mf * T(K_BURNER_SOOT);
+                    const T madd = fuelGen + aerosol;
+                    if (madd <= T(0)) continue;
+                    const T mt = m + madd, scl = m / mt;
                     Yo *= scl; Ys *= scl; Yc *= scl; Yw *= scl; Yco *= scl;
-                    Yai = Yai * scl + fuelGen * K_T_AUTO / mt;
+                    Yai = Yai * scl + fuelGen * T(K_T_AUTO) / mt;
                     yf = yf * scl + fuelGen / mt;
                     Ya = Ya * scl + aerosol / mt;
                     Yp = Yp * scl + sootPot / mt;
@@ -163,11 +176,11 @@ __global__ void k_combust(const Scn<R>* __restrict__ S, Dom dom) {
                     modified = true;
                 }
             }
-            if (yf >= 1e-6) {
-                const double V = g.dx * g.dx * g.dx;
-                const double frac = 1.0 - exp(-dt / K_TAU_MIX);
-                const double chiR = g.radiationOn ? K_CHI_R : 0.0;
-                double ait = yf > 1e-9 ? Yai / yf : K_T_AUTO;
+            if (yf >= T(1e-6)) {
+                const T V = dx * dx * dx;
+                const T frac = T(1) - exp(-dt / T(K_TAU_MIX));
+                const T chiR = g.radiationOn ? T(K_CHI_R) : T(0);
+                T ait = yf > T(1e-9) ? Yai / yf : T(K_T_AUTO);
                 bool ign = pil || Tc > ait;
                 if (!ign) {
                     const uint8_t* lit = g.lit;
@@ -175,45 +188,45 @@ __global__ void k_combust(const Scn<R>* __restrict__ S, Dom dom) {
                           (j < ny - 1 && lit[c + nx]) || (k > 0 && lit[c - sz]) || (k < nz - 1 && lit[c + sz]);
                 }
                 if (ign) {
-                    double burnable = mn(yf, Yo / K_S_O2);
-                    if (burnable > 1e-7) {
-                        double tAd = Tc + K_DHC_FUEL / (K_CP * (1.0 + K_S_O2 / mx(Yo, 1e-4)));
-                        if (pil || !(tAd < K_T_CRIT)) {
-                            double m = gasDensity(g, c) * V;
-                            double dmf = burnable * m * frac;
-                            double q = dmf * K_DHC_FUEL;
-                            double sootMade = yf > 0 ? Yp * (dmf / m) / yf : 0;
-                            double coMade = K_CO_YIELD * dmf / m;
-                            double co2Made = mx(0.0, (K_C_FRAC * dmf / m - sootMade - (12.0 / 28.0) * coMade) * (44.0 / 12.0));
-                            double o2Used = K_S_O2 * dmf / m - (32.0 / 12.0) * sootMade - (16.0 / 28.0) * coMade;
-                            yf = mx(0.0, yf - dmf / m);
+                    T burnable = mn(yf, Yo / T(K_S_O2));
+                    if (burnable > T(1e-7)) {
+                        T tAd = Tc + T(K_DHC_FUEL) / (T(K_CP) * (T(1) + T(K_S_O2) / mx(Yo, T(1e-4))));
+                        if (pil || !(tAd < T(K_T_CRIT))) {
+                            T m = rhoOf(g, c) * V;
+                            T dmf = burnable * m * frac;
+                            T q = dmf * T(K_DHC_FUEL);
+                            T sootMade = yf > T(0) ? Yp * (dmf / m) / yf : T(0);
+                            T coMade = T(K_CO_YIELD) * dmf / m;
+                            T co2Made = mx(T(0), (T(K_C_FRAC) * dmf / m - sootMade - T(12.0 / 28.0) * coMade) * T(44.0 / 12.0));
+                            T o2Used = T(K_S_O2) * dmf / m - T(32.0 / 12.0) * sootMade - T(16.0 / 28.0) * coMade;
+                            yf = mx(T(0), yf - dmf / m);
                             Yai = yf * ait;
-                            Yo = mx(0.0, Yo - o2Used);
-                            Yp = mx(0.0, Yp - sootMade);
+                            Yo = mx(T(0), Yo - o2Used);
+                            Yp = mx(T(0), Yp - sootMade);
                             Ys += sootMade;
                             Yco += coMade;
                             Yc += co2Made;
-                            Yw += K_Y_H2O * dmf / m;
-                            Ya *= (1.0 - frac);
-                            Qc = q * (1.0 - chiR);
+                            Yw += T(K_Y_H2O) * dmf / m;
+                            Ya *= (T(1) - frac);
+                            Qc = q * (T(1) - chiR);
                             Qrc = q * chiR;
                             hrrc = q / (dt * V);
-                            litn = q > 1e-3 ? 1 : 0;
+                            litn = q > T(1e-3) ? 1 : 0;
                             modified = true;
                         }
                     }
                 }
             }
             if (modified) {
-                Y[1][c] = (R)Yo; Y[2][c] = (R)yf; Y[3][c] = (R)Ys; Y[4][c] = (R)Ya; Y[5][c] = (R)Yp;
-                Y[6][c] = (R)Yc; Y[7][c] = (R)Yw; Y[8][c] = (R)Yco; Y[9][c] = (R)Yai;
+                Y[1][c] = Yo; Y[2][c] = yf; Y[3][c] = Ys; Y[4][c] = Ya; Y[5][c] = Yp;
+                Y[6][c] = Yc; Y[7][c] = Yw; Y[8][c] = Yco; Y[9][c] = Yai;
             }
         }
     }
-    g.Q[c] = (R)Qc;
-    g.Qr[c] = (R)Qrc;
-    g.hrr[c] = (R)hrrc;
-    g.massSrc[c] = (R)ms;
+    g.Q[c] = Qc;
+    g.Qr[c] = Qrc;
+    g.hrr[c] = hrrc;
+    g.massSrc[c] = ms;
     g.pilot[c] = pil;
     g.lit2[c] = litn;
 }
@@ -224,6 +237,7 @@ __global__ void k_combust(const Scn<R>* __restrict__ S, Dom dom) {
 // Deardorff viscosity.
 template <class R>
 __global__ void k_turb_center(const Scn<R>* __restrict__ S, Dom dom) {
+    using T = R;
     PHX_PROLOGUE(dom);
     int c = tile_ * TPB + threadIdx.x;
     if (c >= g.N) return;
@@ -233,13 +247,14 @@ __global__ void k_turb_center(const Scn<R>* __restrict__ S, Dom dom) {
     const int i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
     int fx0 = i + (nx + 1) * (j + ny * k);
     int fy0 = i + nx * (j + (ny + 1) * k);
-    uc[c] = (R)(0.5 * ((double)g.u[fx0] + (double)g.u[fx0 + 1]));
-    vc[c] = (R)(0.5 * ((double)g.v[fy0] + (double)g.v[fy0 + nx]));
-    wc[c] = (R)(0.5 * ((double)g.w[c] + (double)g.w[c + nx * ny]));
+    uc[c] = T(0.5) * (g.u[fx0] + g.u[fx0 + 1]);
+    vc[c] = T(0.5) * (g.v[fy0] + g.v[fy0 + nx]);
+    wc[c] = T(0.5) * (g.w[c] + g.w[c + nx * ny]);
 }
 
 template <class R>
 __global__ void k_turb_filter(const Scn<R>* __restrict__ S, Dom dom, int q, int axis) {
+    using T = R;
     PHX_PROLOGUE(dom);
     int c = tile_ * TPB + threadIdx.x;
     if (c >= g.N) return;
@@ -250,27 +265,28 @@ __global__ void k_turb_filter(const Scn<R>* __restrict__ S, Dom dom, int q, int 
     const int i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
     const int id = axis == 0 ? i : axis == 1 ? j : k, n = axis == 0 ? nx : axis == 1 ? ny : nz;
     const int st = axis == 0 ? 1 : axis == 1 ? nx : nx * ny;
-    double self = in[c];
-    double lo = id > 0 && !g.blocked[c - st] ? (double)in[c - st] : self;
-    double hi = id < n - 1 && !g.blocked[c + st] ? (double)in[c + st] : self;
-    out[c] = (R)(0.25 * lo + 0.5 * self + 0.25 * hi);
+    T self = in[c];
+    T lo = id > 0 && !g.blocked[c - st] ? in[c - st] : self;
+    T hi = id < n - 1 && !g.blocked[c + st] ? in[c + st] : self;
+    out[c] = T(0.25) * lo + T(0.5) * self + T(0.25) * hi;
 }
 
 template <class R>
 __global__ void k_turb_nu(const Scn<R>* __restrict__ S, Dom dom) {
+    using T = R;
     PHX_PROLOGUE(dom);
     int c = tile_ * TPB + threadIdx.x;
     double m = 0;
     if (c < g.N) {
         if (g.blocked[c]) g.nu[c] = 0;
         else {
-            double du = (double)g.tmp[0][c] - (double)g.tmp[3][c];
-            double dv = (double)g.tmp[1][c] - (double)g.tmp[4][c];
-            double dw = (double)g.tmp[2][c] - (double)g.tmp[5][c];
-            double ks = 0.5 * (du * du + dv * dv + dw * dw);
-            double nu = mn(1.0, K_C_NU * g.dx * sqrt(ks) + 1.5e-5 * pow((double)g.sc[0][c] / 293.15, 1.7));
-            g.nu[c] = (R)nu;
-            m = (double)(R)nu;
+            T du = g.tmp[0][c] - g.tmp[3][c];
+            T dv = g.tmp[1][c] - g.tmp[4][c];
+            T dw = g.tmp[2][c] - g.tmp[5][c];
+            T ks = T(0.5) * (du * du + dv * dv + dw * dw);
+            T nu = mn(T(1), T(K_C_NU) * (T)g.dx * sqrt(ks) + T(1.5e-5) * pow(g.sc[0][c] / T(293.15), T(1.7)));
+            g.nu[c] = nu;
+            m = (double)nu;
         }
     }
     blockMaxTo(g.sv + SV_MAXNU, m);
@@ -280,54 +296,57 @@ __global__ void k_turb_nu(const Scn<R>* __restrict__ S, Dom dom) {
 // Solver::heatDiffusion (src/sim/gasphase.cpp:221-248)
 template <class R>
 __global__ void k_heat(const Scn<R>* __restrict__ S, Dom dom) {
+    using T = R;
     PHX_PROLOGUE(dom);
     int c = tile_ * TPB + threadIdx.x;
     if (c >= g.N || g.blocked[c]) return;
     const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
     const int i = c % nx, j = (c / nx) % ny, k = c / sxy;
     const int fx0 = i + (nx + 1) * (j + ny * k), fy0 = i + nx * (j + (ny + 1) * k);
-    const double fo[6] = {(double)g.fx[fx0], (double)g.fx[fx0 + 1], (double)g.fy[fy0], (double)g.fy[fy0 + nx],
-                          (double)g.fz[c], (double)g.fz[c + sxy]};
+    const T fo[6] = {g.fx[fx0], g.fx[fx0 + 1], g.fy[fy0], g.fy[fy0 + nx], g.fz[c], g.fz[c + sxy]};
     const int nb[6] = {i > 0 ? c - 1 : -1, i < nx - 1 ? c + 1 : -1, j > 0 ? c - nx : -1, j < ny - 1 ? c + nx : -1,
                        k > 0 ? c - sxy : -1, k < nz - 1 ? c + sxy : -1};
-    const R* T = g.sc[0];
-    const double Tc = T[c], nuc = g.nu[c];
-    double rc = gasDensity(g, c), q = 0;
+    const R* Tf = g.sc[0];
+    const T dx = (T)g.dx;
+    const T Tc = Tf[c], nuc = g.nu[c];
+    T rc = rhoOf(g, c), q = 0;
     for (int d = 0; d < 6; ++d) {
-        if (fo[d] <= 0) continue;
+        if (fo[d] <= T(0)) continue;
         int n = nb[d];
         if (n >= 0 && g.blocked[n]) continue;
-        double Tn = n >= 0 ? (double)T[n] : K_T0;
-        double nun = n >= 0 ? (double)g.nu[n] : nuc;
-        double rn = n >= 0 ? gasDensity(g, n) : K_P0 / (K_RS * K_T0);
-        double Tf = 0.5 * (Tc + Tn);
-        double kf = 0.5 * (rc + rn) * K_CP * 0.5 * (nuc + nun) / K_PR_T + 0.0258 * pow(Tf / 293.15, 0.8);
-        q += fo[d] * kf * g.dx * (Tn - Tc);
+        T Tn = n >= 0 ? Tf[n] : T(K_T0);
+        T nun = n >= 0 ? g.nu[n] : nuc;
+        T rn = n >= 0 ? rhoOf(g, n) : T(K_P0) / (T(K_RS) * T(K_T0));
+        T Tface = T(0.5) * (Tc + Tn);
+        T kf = T(0.5) * (rc + rn) * T(K_CP) * T(0.5) * (nuc + nun) / T(K_PR_T) + T(0.0258) * pow(Tface / T(293.15), T(0.8));
+        q += fo[d] * kf * dx * (Tn - Tc);
     }
-    g.Q[c] = (R)((double)g.Q[c] + q * g.sv[SV_DT]);
+    g.Q[c] = g.Q[c] + q * (T)g.sv[SV_DT];
 }
 
 // Solver::energyAndExpansion (src/sim/gasphase.cpp:251-271)
 template <class R>
 __global__ void k_energy(const Scn<R>* __restrict__ S, Dom dom) {
+    using T = R;
     PHX_PROLOGUE(dom);
     int c = tile_ * TPB + threadIdx.x;
     double md = 0;
     if (c < g.N) {
         if (g.blocked[c]) g.S[c] = 0;
         else {
-            const double dt = g.sv[SV_DT];
-            const double V = g.dx * g.dx * g.dx;
-            const double T = g.sc[0][c], Q = g.Q[c], Pb = g.Pb[c];
-            double rho = Pb / (K_RS * T);
-            double m = rho * V;
-            double Tn = clampd(T + Q / (m * K_CP), K_T_MIN, K_T_MAX);
-            double rhoN = Pb / (K_RS * Tn);
-            double D = Q / (m * K_CP * T * dt) + (double)g.massSrc[c] / (rhoN * V * dt);
-            g.sc[0][c] = (R)Tn;
-            double Sv = clampd(D, -K_D_MAX, K_D_MAX);
-            g.S[c] = (R)Sv;
-            md = fabs((double)(R)Sv);
+            const T dt = (T)g.sv[SV_DT];
+            const T dx = (T)g.dx;
+            const T V = dx * dx * dx;
+            const T Tc = g.sc[0][c], Q = g.Q[c], Pb = g.Pb[c];
+            T rho = Pb / (T(K_RS) * Tc);
+            T m = rho * V;
+            T Tn = clampd(Tc + Q / (m * T(K_CP)), T(K_T_MIN), T(K_T_MAX));
+            T rhoN = Pb / (T(K_RS) * Tn);
+            T D = Q / (m * T(K_CP) * Tc * dt) + g.massSrc[c] / (rhoN * V * dt);
+            g.sc[0][c] = Tn;
+            T Sv = clampd(D, -T(K_D_MAX), T(K_D_MAX));
+            g.S[c] = Sv;
+            md = fabs((double)Sv);
         }
     }
     blockMaxTo(g.sv + SV_MAXDIV, md);
@@ -336,10 +355,12 @@ __global__ void k_energy(const Scn<R>* __restrict__ S, Dom dom) {
 // ---------------------------------------------------------------------------
 // Solver::momentum (src/sim/gasphase.cpp:275-372): one component on its faces,
 // written to the second velocity buffer.
-__device__ __forceinline__ double vanLeer(double a, double b) { return a * b > 0 ? 2 * a * b / (a + b) : 0.0; }
+template <class T>
+__device__ __forceinline__ T vanLeer(T a, T b) { return a * b > T(0) ? T(2) * a * b / (a + b) : T(0); }
 
 template <class R>
 __global__ void k_momentum(const Scn<R>* __restrict__ S, Dom dom, int comp) {
+    using T = R;
     PHX_PROLOGUE(dom);
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     const int dX = nx + (comp == 0), dY = ny + (comp == 1), dZ = nz + (comp == 2);
@@ -350,7 +371,7 @@ __global__ void k_momentum(const Scn<R>* __restrict__ S, Dom dom, int comp) {
     const R* fo = comp == 0 ? g.fx : comp == 1 ? g.fy : g.fz;
     const uint8_t* lk = comp == 0 ? g.lx : comp == 1 ? g.ly : g.lz;   // null: no crack faces
     R* out = comp == 0 ? g.u2 : comp == 1 ? g.v2 : g.w2;
-    if (fo[f] <= 0) { out[f] = 0; return; }
+    if (fo[f] <= T(0)) { out[f] = 0; return; }
     if (lk && lk[f]) { out[f] = vel[f]; return; }   // set by leakage()
     const int i = f % dX, j = (f / dX) % dY, k = f / (dX * dY);
     const int id[3] = {i, j, k};
@@ -359,8 +380,8 @@ __global__ void k_momentum(const Scn<R>* __restrict__ S, Dom dom, int comp) {
     const int dim[3] = {dX, dY, dZ};
     const int lo = id[comp] - 1;
     const bool bnd = lo < 0 || id[comp] >= ncell[comp];
-    const double zc = g.oz + (comp == 2 ? (double)k : k + 0.5) * g.dx;
     if (bnd) {
+        const double zc = g.oz + (comp == 2 ? (double)k : k + 0.5) * g.dx;
         double wv = windAt(g, comp, lo < 0 ? 0 : 1, zc);
         out[f] = isnan(wv) ? vel[f] : (R)wv;
         return;
@@ -369,73 +390,74 @@ __global__ void k_momentum(const Scn<R>* __restrict__ S, Dom dom, int comp) {
     a3[comp] -= 1;
     const int ca = a3[0] + nx * (a3[1] + ny * a3[2]);
     const int cb = i + nx * (j + ny * k);
-    const double v0 = vel[f];
-    double adv[3];
+    const T v0 = vel[f];
+    T adv[3];
     adv[comp] = v0;
     for (int a = 0; a < 3; ++a) {
         if (a == comp) continue;
         const R* va = a == 0 ? g.u : a == 1 ? g.v : g.w;
         const int aX = nx + (a == 0), aY = ny + (a == 1);
-        double s = 0;
+        T s = 0;
         for (int q = 0; q < 4; ++q) {
             int p[3] = {i, j, k};
             if (q & 1) p[a] += 1;
             if (q & 2) p[comp] -= 1;
             p[a] = p[a] < ncell[a] ? p[a] : ncell[a];
             p[comp] = p[comp] > 0 ? p[comp] : 0;
-            s += (double)va[p[0] + aX * (p[1] + aY * p[2])];
+            s += va[p[0] + aX * (p[1] + aY * p[2])];
         }
-        adv[a] = 0.25 * s;
+        adv[a] = T(0.25) * s;
     }
-    const double idx = 1.0 / g.dx, idx2 = 1.0 / (g.dx * g.dx);
-    double acc = 0, lap = 0;
+    const T dx = (T)g.dx;
+    const T idx = T(1) / dx, idx2 = T(1) / (dx * dx);
+    T acc = 0, lap = 0;
     for (int a = 0; a < 3; ++a) {
-        double m1, p1, m2, p2;
+        T m1, p1, m2, p2;
         // free slip across closed faces: neighbour along a, then the second
         // neighbour only through two open faces
         {
             int ni = id[a] - 1, gg = f - st[a];
-            m1 = (ni < 0) ? v0 : (fo[gg] > 0 && !(lk && lk[gg]) ? (double)vel[gg] : v0);
+            m1 = (ni < 0) ? v0 : (fo[gg] > T(0) && !(lk && lk[gg]) ? vel[gg] : v0);
             ni = id[a] + 1;
             gg = f + st[a];
-            p1 = (ni >= dim[a]) ? v0 : (fo[gg] > 0 && !(lk && lk[gg]) ? (double)vel[gg] : v0);
+            p1 = (ni >= dim[a]) ? v0 : (fo[gg] > T(0) && !(lk && lk[gg]) ? vel[gg] : v0);
         }
         {
             int ni = id[a] - 2;
             if (ni < 0) m2 = m1;
             else {
                 int gg = f - 2 * st[a], g1 = f - st[a];
-                m2 = fo[gg] > 0 && fo[g1] > 0 && !(lk && (lk[gg] || lk[g1])) ? (double)vel[gg] : m1;
+                m2 = fo[gg] > T(0) && fo[g1] > T(0) && !(lk && (lk[gg] || lk[g1])) ? vel[gg] : m1;
             }
             ni = id[a] + 2;
             if (ni >= dim[a]) p2 = p1;
             else {
                 int gg = f + 2 * st[a], g1 = f + st[a];
-                p2 = fo[gg] > 0 && fo[g1] > 0 && !(lk && (lk[gg] || lk[g1])) ? (double)vel[gg] : p1;
+                p2 = fo[gg] > T(0) && fo[g1] > T(0) && !(lk && (lk[gg] || lk[g1])) ? vel[gg] : p1;
             }
         }
-        double fp, fm;
-        if (adv[a] >= 0) {
-            fp = v0 + 0.5 * vanLeer(v0 - m1, p1 - v0);
-            fm = m1 + 0.5 * vanLeer(m1 - m2, v0 - m1);
+        T fp, fm;
+        if (adv[a] >= T(0)) {
+            fp = v0 + T(0.5) * vanLeer(v0 - m1, p1 - v0);
+            fm = m1 + T(0.5) * vanLeer(m1 - m2, v0 - m1);
         } else {
-            fp = p1 - 0.5 * vanLeer(p1 - v0, p2 - p1);
-            fm = v0 - 0.5 * vanLeer(v0 - m1, p1 - v0);
+            fp = p1 - T(0.5) * vanLeer(p1 - v0, p2 - p1);
+            fm = v0 - T(0.5) * vanLeer(v0 - m1, p1 - v0);
         }
         acc -= adv[a] * (fp - fm) * idx;
-        lap += (m1 - 2 * v0 + p1) * idx2;
+        lap += (m1 - T(2) * v0 + p1) * idx2;
     }
-    double ra = gasDensity(g, ca), rb = gasDensity(g, cb);
-    double rf = 0.5 * (ra + rb);
-    double nuf = 0.5 * ((double)g.nu[ca] + (double)g.nu[cb]);
+    T ra = rhoOf(g, ca), rb = rhoOf(g, cb);
+    T rf = T(0.5) * (ra + rb);
+    T nuf = T(0.5) * (g.nu[ca] + g.nu[cb]);
     acc += nuf * lap;
     if (comp == 2) {
-        double r0 = 0.5 * ((double)g.Pb[ca] + (double)g.Pb[cb]) / (K_RS * K_T0);
-        acc += K_G * (r0 - rf) / rf;
+        T r0 = T(0.5) * (g.Pb[ca] + g.Pb[cb]) / (T(K_RS) * T(K_T0));
+        acc += T(K_G) * (r0 - rf) / rf;
     }
-    double pt = rf * 0.5 * ((double)g.p[ca] + (double)g.p[cb]);
-    acc += pt * (1.0 / rb - 1.0 / ra) * idx;
-    out[f] = (R)clampd(v0 + g.sv[SV_DT] * acc, -K_VMAX, K_VMAX);
+    T pt = rf * T(0.5) * (g.p[ca] + g.p[cb]);
+    acc += pt * (T(1) / rb - T(1) / ra) * idx;
+    out[f] = clampd(v0 + (T)g.sv[SV_DT] * acc, -T(K_VMAX), T(K_VMAX));
 }
 
 // open boundary faces without wind inflow take the new value of the face one
@@ -463,17 +485,17 @@ __global__ void k_mom_bnd(const Scn<R>* __restrict__ S, Dom dom, int comp) {
     const R* fo = comp == 0 ? g.fx : comp == 1 ? g.fy : g.fz;
     const uint8_t* lk = comp == 0 ? g.lx : comp == 1 ? g.ly : g.lz;
     R* out = comp == 0 ? g.u2 : comp == 1 ? g.v2 : g.w2;
-    if (fo[f] <= 0 || (lk && lk[f])) return;
+    if (fo[f] <= R(0) || (lk && lk[f])) return;
     double zc = g.oz + (comp == 2 ? (double)id[2] : id[2] + 0.5) * g.dx;
     if (!isnan(windAt(g, comp, side, zc))) return;
     int gg = f + (side == 0 ? 1 : -1) * st[comp];
-    out[f] = fo[gg] > 0 && !(lk && lk[gg]) ? out[gg] : (R)0;
+    out[f] = fo[gg] > R(0) && !(lk && lk[gg]) ? out[gg] : (R)0;
 }
 
 // ---------------------------------------------------------------------------
 // Solver::leakage without crack faces (src/sim/gasphase.cpp:403-409, 486-498):
 // per closed zone the integral of S, the zone's pressure-rise rate and the
-// divergence shift. One CTA per closed zone.
+// divergence shift. One CTA per closed zone; FP64 sums in either path.
 template <class R>
 __global__ void k_zone_integral(const Scn<R>* __restrict__ S, Dom dom) {
     PHX_PROLOGUE(dom);
@@ -498,9 +520,11 @@ __global__ void k_zone_integral(const Scn<R>* __restrict__ S, Dom dom) {
 // ---------------------------------------------------------------------------
 // Solver::project, right-hand side and warm-start residual
 // (src/sim/gasphase.cpp:528-549, 576-581), with the closed-zone divergence
-// shift of leakage (:495-498) applied to S first.
+// shift of leakage (:495-498) applied to S first. With b64 set (mixed path)
+// the right-hand side is also stored in FP64 for the refinement loop.
 template <class R>
 __global__ void k_rhs(const Scn<R>* __restrict__ S, Dom dom) {
+    using T = R;
     PHX_PROLOGUE(dom);
     int c = tile_ * TPB + threadIdx.x;
     double bm = 0, rm = 0;
@@ -512,46 +536,46 @@ __global__ void k_rhs(const Scn<R>* __restrict__ S, Dom dom) {
         } else {
             const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
             const int i = c % nx, j = (c / nx) % ny, k = c / sxy;
-            const double dt = g.sv[SV_DT];
-            const double inv = g.dx * g.dx / dt;
-            double Sc = g.S[c];
+            const T dt = (T)g.sv[SV_DT];
+            const T dx = (T)g.dx;
+            const T inv = dx * dx / dt;
+            T Sc = g.S[c];
             if (g.nClosed > 0) {
                 int z = g.zone[c];
                 if (z >= 0 && !g.zoneOpen[z]) {
-                    Sc -= g.zoneShift[z];
-                    g.S[c] = (R)Sc;
+                    Sc -= (T)g.zoneShift[z];
+                    g.S[c] = Sc;
                 }
             }
             const int a0 = i + (nx + 1) * (j + ny * k), a1 = a0 + 1;
             const int b0 = i + nx * (j + (ny + 1) * k), b1 = b0 + nx;
             const int c0 = c, c1 = c + sxy;
-            const double u0 = g.u[a0], u1 = g.u[a1], v0 = g.v[b0], v1 = g.v[b1], w0 = g.w[c0], w1 = g.w[c1];
-            double div = ((double)g.fx[a1] * u1 - (double)g.fx[a0] * u0 + (double)g.fy[b1] * v1 - (double)g.fy[b0] * v0 +
-                          (double)g.fz[c1] * w1 - (double)g.fz[c0] * w0) / g.dx;
-            double b = (Sc - div) * inv;
-            const double A0 = g.a0x[a0], A1 = g.a0x[a1], A2 = g.a0y[b0], A3 = g.a0y[b1], A4 = g.a0z[c0], A5 = g.a0z[c1];
-            if (i == 0 && A0 > 0) b += A0 * (u0 > 0 ? -0.5 * u0 * u0 : 0.0);
-            if (i == nx - 1 && A1 > 0) b += A1 * (u1 < 0 ? -0.5 * u1 * u1 : 0.0);
-            if (j == 0 && A2 > 0) b += A2 * (v0 > 0 ? -0.5 * v0 * v0 : 0.0);
-            if (j == ny - 1 && A3 > 0) b += A3 * (v1 < 0 ? -0.5 * v1 * v1 : 0.0);
-            if (k == nz - 1 && A5 > 0) b += A5 * (w1 < 0 ? -0.5 * w1 * w1 : 0.0);
-            g.b[c] = (R)b;
-            const double dg = g.diag[c];
-            double r = 0;
-            if (dg > 0) {
+            const T u0 = g.u[a0], u1 = g.u[a1], v0 = g.v[b0], v1 = g.v[b1], w0 = g.w[c0], w1 = g.w[c1];
+            T div = (g.fx[a1] * u1 - g.fx[a0] * u0 + g.fy[b1] * v1 - g.fy[b0] * v0 + g.fz[c1] * w1 - g.fz[c0] * w0) / dx;
+            T b = (Sc - div) * inv;
+            const T A0 = g.a0x[a0], A1 = g.a0x[a1], A2 = g.a0y[b0], A3 = g.a0y[b1], A4 = g.a0z[c0], A5 = g.a0z[c1];
+            if (i == 0 && A0 > T(0)) b += A0 * (u0 > T(0) ? T(-0.5) * u0 * u0 : T(0));
+            if (i == nx - 1 && A1 > T(0)) b += A1 * (u1 < T(0) ? T(-0.5) * u1 * u1 : T(0));
+            if (j == 0 && A2 > T(0)) b += A2 * (v0 > T(0) ? T(-0.5) * v0 * v0 : T(0));
+            if (j == ny - 1 && A3 > T(0)) b += A3 * (v1 < T(0) ? T(-0.5) * v1 * v1 : T(0));
+            if (k == nz - 1 && A5 > T(0)) b += A5 * (w1 < T(0) ? T(-0.5) * w1 * w1 : T(0));
+            g.b[c] = b;
+            const T dg = g.diag[c];
+            T r = 0;
+            if (dg > T(0)) {
                 const R* x = g.p;
-                double s = dg * (double)x[c];
-                if (i > 0) s -= A0 * (double)x[c - 1];
-                if (i < nx - 1) s -= A1 * (double)x[c + 1];
-                if (j > 0) s -= A2 * (double)x[c - nx];
-                if (j < ny - 1) s -= A3 * (double)x[c + nx];
-                if (k > 0) s -= A4 * (double)x[c - sxy];
-                if (k < nz - 1) s -= A5 * (double)x[c + sxy];
-                r = b - (double)(R)s;
-                bm = fabs(b);
+                T s = dg * x[c];
+                if (i > 0) s -= A0 * x[c - 1];
+                if (i < nx - 1) s -= A1 * x[c + 1];
+                if (j > 0) s -= A2 * x[c - nx];
+                if (j < ny - 1) s -= A3 * x[c + nx];
+                if (k > 0) s -= A4 * x[c - sxy];
+                if (k < nz - 1) s -= A5 * x[c + sxy];
+                r = b - s;
+                bm = fabs((double)b);
             }
-            g.r[c] = (R)r;
-            rm = fabs((double)(R)r);
+            g.r[c] = r;
+            rm = fabs((double)r);
         }
     }
     blockMaxTo(g.sv + SV_BMAX, bm);
@@ -589,6 +613,7 @@ __global__ void k_zone_mean_sub(const Scn<R>* __restrict__ S, Dom dom) {
 // (src/sim/gasphase.cpp:641-676). One thread per face of one axis.
 template <class R>
 __global__ void k_velcorr(const Scn<R>* __restrict__ S, Dom dom, int comp) {
+    using T = R;
     PHX_PROLOGUE(dom);
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     const int dX = nx + (comp == 0), dY = ny + (comp == 1), dZ = nz + (comp == 2);
@@ -599,44 +624,39 @@ __global__ void k_velcorr(const Scn<R>* __restrict__ S, Dom dom, int comp) {
         R* vel = comp == 0 ? g.u : comp == 1 ? g.v : g.w;
         const R* fo = comp == 0 ? g.fx : comp == 1 ? g.fy : g.fz;
         const R* am = comp == 0 ? g.ax : comp == 1 ? g.ay : g.az;
-        const double s = g.sv[SV_DT] / g.dx;
+        const T s = (T)g.sv[SV_DT] / (T)g.dx;
         const R* P = g.p;
-        const double fof = fo[f];
+        const T fof = fo[f];
         if (comp == 2 && k == 0) {
             // the ground faces are not visited by the reference's loop
             vm = 0;
-        } else if (fof <= 0) {
+        } else if (fof <= T(0)) {
             vel[f] = 0;
         } else {
-            double un = vel[f];
+            T un = vel[f];
             if (comp == 0) {
-                double zc = g.oz + (k + 0.5) * g.dx;
-                if (am[f] > 0 && !((i == 0 || i == nx) && !bndOpen(g, 0, i == 0 ? 0 : 1, zc))) {
-                    double hi = i < nx ? (double)P[i + nx * (j + ny * k)] : (un < 0 ? -0.5 * un * un : 0.0);
-                    double lo = i > 0 ? (double)P[i - 1 + nx * (j + ny * k)] : (un > 0 ? -0.5 * un * un : 0.0);
-                    un = clampd(un - s * (hi - lo), -K_VMAX, K_VMAX);
-                    vel[f] = (R)un;
-                    un = (double)(R)un;
+                if (am[f] > T(0) && !((i == 0 || i == nx) && !bndOpen(g, 0, i == 0 ? 0 : 1, g.oz + (k + 0.5) * g.dx))) {
+                    T hi = i < nx ? P[i + nx * (j + ny * k)] : (un < T(0) ? T(-0.5) * un * un : T(0));
+                    T lo = i > 0 ? P[i - 1 + nx * (j + ny * k)] : (un > T(0) ? T(-0.5) * un * un : T(0));
+                    un = clampd(un - s * (hi - lo), -T(K_VMAX), T(K_VMAX));
+                    vel[f] = un;
                 }
             } else if (comp == 1) {
-                double zc = g.oz + (k + 0.5) * g.dx;
-                if (am[f] > 0 && !((j == 0 || j == ny) && !bndOpen(g, 1, j == 0 ? 0 : 1, zc))) {
-                    double hi = j < ny ? (double)P[i + nx * (j + ny * k)] : (un < 0 ? -0.5 * un * un : 0.0);
-                    double lo = j > 0 ? (double)P[i + nx * (j - 1 + ny * k)] : (un > 0 ? -0.5 * un * un : 0.0);
-                    un = clampd(un - s * (hi - lo), -K_VMAX, K_VMAX);
-                    vel[f] = (R)un;
-                    un = (double)(R)un;
+                if (am[f] > T(0) && !((j == 0 || j == ny) && !bndOpen(g, 1, j == 0 ? 0 : 1, g.oz + (k + 0.5) * g.dx))) {
+                    T hi = j < ny ? P[i + nx * (j + ny * k)] : (un < T(0) ? T(-0.5) * un * un : T(0));
+                    T lo = j > 0 ? P[i + nx * (j - 1 + ny * k)] : (un > T(0) ? T(-0.5) * un * un : T(0));
+                    un = clampd(un - s * (hi - lo), -T(K_VMAX), T(K_VMAX));
+                    vel[f] = un;
                 }
             } else {
-                if (am[f] > 0) {
-                    double hi = k < nz ? (double)P[i + nx * (j + ny * k)] : (un < 0 ? -0.5 * un * un : 0.0);
-                    double lo = (double)P[i + nx * (j + ny * (k - 1))];
-                    un = clampd(un - s * (hi - lo), -K_VMAX, K_VMAX);
-                    vel[f] = (R)un;
-                    un = (double)(R)un;
+                if (am[f] > T(0)) {
+                    T hi = k < nz ? P[i + nx * (j + ny * k)] : (un < T(0) ? T(-0.5) * un * un : T(0));
+                    T lo = P[i + nx * (j + ny * (k - 1))];
+                    un = clampd(un - s * (hi - lo), -T(K_VMAX), T(K_VMAX));
+                    vel[f] = un;
                 }
             }
-            vm = fabs(un) * fof;
+            vm = fabs((double)un) * (double)fof;
         }
     }
     blockMaxTo(g.sv + SV_MAXVEL, vm);
@@ -645,8 +665,9 @@ __global__ void k_velcorr(const Scn<R>* __restrict__ S, Dom dom, int comp) {
 // ---------------------------------------------------------------------------
 // Solver::advectScalars (src/sim/gasphase.cpp:685-784): Superbee-limited
 // transport of the ten scalars, written to the second scalar buffers.
-__device__ __forceinline__ double superbee(double r) {
-    double m = 0.0, a = mn(2 * r, 1.0), b = mn(r, 2.0);
+template <class T>
+__device__ __forceinline__ T superbee(T r) {
+    T m = T(0), a = mn(T(2) * r, T(1)), b = mn(r, T(2));
     if (m < a) m = a;
     if (m < b) m = b;
     return m;
@@ -654,6 +675,7 @@ __device__ __forceinline__ double superbee(double r) {
 
 template <class R>
 __global__ void k_advect(const Scn<R>* __restrict__ S, Dom dom) {
+    using T = R;
     PHX_PROLOGUE(dom);
     int c = tile_ * TPB + threadIdx.x;
     if (c >= g.N) return;
@@ -661,18 +683,18 @@ __global__ void k_advect(const Scn<R>* __restrict__ S, Dom dom) {
         for (int q = 0; q < NSC; ++q) g.sc2[q][c] = g.sc[q][c];
         return;
     }
-    const double amb[NSC] = {K_T0, K_YO2_AMB, 0, 0, 0, 0, K_YCO2_AMB, K_YH2O_AMB, 0, 0};
+    const T amb[NSC] = {T(K_T0), T(K_YO2_AMB), T(0), T(0), T(0), T(0), T(K_YCO2_AMB), T(K_YH2O_AMB), T(0), T(0)};
     const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
     const int i = c % nx, j = (c / nx) % ny, k = c / sxy;
-    const double dt = g.sv[SV_DT];
-    const double s = dt / g.dx;
+    const T dx = (T)g.dx;
+    const T dt = (T)g.sv[SV_DT];
+    const T s = dt / dx;
     const int fa0 = i + (nx + 1) * (j + ny * k), fa1 = fa0 + 1;
     const int fb0 = i + nx * (j + (ny + 1) * k), fb1 = fb0 + nx;
     const int fc0 = c, fc1 = c + sxy;
-    double fo[6] = {(double)g.fx[fa0], (double)g.fx[fa1], (double)g.fy[fb0], (double)g.fy[fb1], (double)g.fz[fc0],
-                    (double)g.fz[fc1]};
-    double un[6] = {-fo[0] * (double)g.u[fa0], fo[1] * (double)g.u[fa1], -fo[2] * (double)g.v[fb0],
-                    fo[3] * (double)g.v[fb1], -fo[4] * (double)g.w[fc0], fo[5] * (double)g.w[fc1]};
+    T fo[6] = {g.fx[fa0], g.fx[fa1], g.fy[fb0], g.fy[fb1], g.fz[fc0], g.fz[fc1]};
+    T un[6] = {-fo[0] * g.u[fa0], fo[1] * g.u[fa1], -fo[2] * g.v[fb0], fo[3] * g.v[fb1], -fo[4] * g.w[fc0],
+               fo[5] * g.w[fc1]};
     const int id[3] = {i, j, k};
     const int dim[3] = {nx, ny, nz}, st[3] = {1, nx, sxy};
     int nb[6], nb2[6], opp[6];
@@ -686,64 +708,64 @@ __global__ void k_advect(const Scn<R>* __restrict__ S, Dom dom) {
         if (nb2[d] >= 0 && g.blocked[nb2[d]]) nb2[d] = -2;
         if (opp[d] >= 0 && g.blocked[opp[d]]) opp[d] = -2;
     }
-    const R* T = g.sc[0];
-    const double nuc = g.nu[c];
-    const double rc = gasDensity(g, c);
-    double rUp[6], Dd[6], rfd[6], mden = rc;
+    const R* Tf = g.sc[0];
+    const T nuc = g.nu[c];
+    const T rc = rhoOf(g, c);
+    T rUp[6], Dd[6], rfd[6], mden = rc;
     for (int d = 0; d < 6; ++d) {
         rUp[d] = 0;
         Dd[d] = 0;
         rfd[d] = 0;
-        if (fo[d] <= 0 || nb[d] == -2) continue;
-        double tn = nb[d] >= 0 ? (double)T[nb[d]] : K_T0, tc = T[c], tf;
-        if (un[d] > 0) {
-            double tu2 = opp[d] >= 0 ? (double)T[opp[d]] : (opp[d] == -1 ? K_T0 : tc);
-            double den = tn - tc;
-            tf = tc + (fabs(den) > 1e-6 ? 0.5 * superbee((tc - tu2) / den) * den : 0.0);
+        if (fo[d] <= T(0) || nb[d] == -2) continue;
+        T tn = nb[d] >= 0 ? Tf[nb[d]] : T(K_T0), tc = Tf[c], tface;
+        if (un[d] > T(0)) {
+            T tu2 = opp[d] >= 0 ? Tf[opp[d]] : (opp[d] == -1 ? T(K_T0) : tc);
+            T den = tn - tc;
+            tface = tc + (fabs(den) > T(1e-6) ? T(0.5) * superbee((tc - tu2) / den) * den : T(0));
         } else {
-            double tu2 = nb2[d] >= 0 ? (double)T[nb2[d]] : (nb2[d] == -1 ? K_T0 : tn);
-            double den = tc - tn;
-            tf = tn + (fabs(den) > 1e-6 ? 0.5 * superbee((tn - tu2) / den) * den : 0.0);
+            T tu2 = nb2[d] >= 0 ? Tf[nb2[d]] : (nb2[d] == -1 ? T(K_T0) : tn);
+            T den = tc - tn;
+            tface = tn + (fabs(den) > T(1e-6) ? T(0.5) * superbee((tn - tu2) / den) * den : T(0));
         }
-        double pu = un[d] > 0 ? (double)g.Pb[c] : (nb[d] >= 0 ? (double)g.Pb[nb[d]] : K_P0);
-        rUp[d] = pu / (K_RS * mx(tf, K_T_MIN));
+        T pu = un[d] > T(0) ? g.Pb[c] : (nb[d] >= 0 ? g.Pb[nb[d]] : T(K_P0));
+        rUp[d] = pu / (T(K_RS) * mx(tface, T(K_T_MIN)));
         mden -= s * rUp[d] * un[d];
         // species diffusion coefficient and face density: the same for every species
-        double nun = nb[d] >= 0 ? (double)g.nu[nb[d]] : nuc;
-        Dd[d] = 0.5 * (nuc + nun) / K_SC_T + 2.0e-5;
-        rfd[d] = nb[d] >= 0 ? 0.5 * (rc + gasDensity(g, nb[d])) : rc;
+        T nun = nb[d] >= 0 ? g.nu[nb[d]] : nuc;
+        Dd[d] = T(0.5) * (nuc + nun) / T(K_SC_T) + T(2.0e-5);
+        rfd[d] = nb[d] >= 0 ? T(0.5) * (rc + rhoOf(g, nb[d])) : rc;
     }
-    const bool conservative = mden > 0.25 * rc;
+    const bool conservative = mden > T(0.25) * rc;
     for (int q = 0; q < NSC; ++q) {
         const R* F = g.sc[q];
-        const double fc = F[c];
-        double lo = fc, hi = fc, acc = 0, macc = 0;
+        const T fc = F[c];
+        T lo = fc, hi = fc, acc = 0, macc = 0;
         for (int d = 0; d < 6; ++d) {
-            if (fo[d] <= 0 || nb[d] == -2) continue;
-            double fn = nb[d] >= 0 ? (double)F[nb[d]] : amb[q];
+            if (fo[d] <= T(0) || nb[d] == -2) continue;
+            T fn = nb[d] >= 0 ? F[nb[d]] : amb[q];
             lo = mn(lo, fn);
             hi = mx(hi, fn);
-            double flux = un[d];
-            double face = fc;
-            if (flux > 0) {
-                double fu2 = opp[d] >= 0 ? (double)F[opp[d]] : (opp[d] == -1 ? amb[q] : fc);
-                double den = fn - fc;
-                if (fabs(den) > 1e-12) face += 0.5 * superbee((fc - fu2) / den) * den;
-            } else if (flux < 0) {
-                double fu2 = nb2[d] >= 0 ? (double)F[nb2[d]] : (nb2[d] == -1 ? amb[q] : fn);
-                double den = fc - fn;
+            T flux = un[d];
+            T face = fc;
+            if (flux > T(0)) {
+                T fu2 = opp[d] >= 0 ? F[opp[d]] : (opp[d] == -1 ? amb[q] : fc);
+                T den = fn - fc;
+                if (fabs(den) > T(1e-12)) face += T(0.5) * superbee((fc - fu2) / den) * den;
+            } else if (flux < T(0)) {
+                T fu2 = nb2[d] >= 0 ? F[nb2[d]] : (nb2[d] == -1 ? amb[q] : fn);
+                T den = fc - fn;
                 face = fn;
-                if (fabs(den) > 1e-12) face += 0.5 * superbee((fn - fu2) / den) * den;
+                if (fabs(den) > T(1e-12)) face += T(0.5) * superbee((fn - fu2) / den) * den;
             }
             acc -= flux * (face - fc);
             macc -= rUp[d] * flux * face;
             if (q > 0) {
-                acc += fo[d] * Dd[d] * (fn - fc) / g.dx;
-                macc += fo[d] * rfd[d] * Dd[d] * (fn - fc) / g.dx;
+                acc += fo[d] * Dd[d] * (fn - fc) / dx;
+                macc += fo[d] * rfd[d] * Dd[d] * (fn - fc) / dx;
             }
         }
-        double val = conservative ? (rc * fc + s * macc) / mden : fc + s * acc;
-        g.sc2[q][c] = (R)clampd(val, lo, hi);
+        T val = conservative ? (rc * fc + s * macc) / mden : fc + s * acc;
+        g.sc2[q][c] = clampd(val, lo, hi);
     }
 }
 

@@ -1,0 +1,88 @@
+"""The mixed-precision GPU step (FP32 fields and stencils, FP32 multigrid CG
+inside an FP64 refinement loop) against the FP64 oracle.
+
+Tolerances, from the benchmark spec's target: pressure within 1e-5 relative (L2) of
+the FP64 oracle per step from identical inputs, with the pressure solve at a
+relative residual of at most 1e-8 (max|r| <= 1e-8 max|b|, checked in FP64).
+Velocities and scalars carry FP32 rounding: 1e-5 relative per step."""
+import numpy as np
+import pytest
+
+from oracle.oraclepy import OracleSolver
+from photon_gb300 import _lib, casegen
+from photon_gb300.solver import Solver
+
+from gpu_util import STATE, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+P_TOL = 1e-5
+FIELD_TOL = 1e-5
+
+
+def rel_case(c):
+    c.profile.tol = 0.0
+    c.profile.rel_tol = 1e-8
+    c.profile.maxIters = 400
+    return c
+
+
+CASES = {
+    "room": lambda: rel_case(casegen.tiny_room(12, 10, 9, 0.2, 60e3)),
+    "sealed": lambda: rel_case(casegen.tiny_room(10, 8, 8, 0.2, 40e3, doorway=False)),
+    "house": lambda: rel_case(casegen.house(24, 20, 14, 0.2, 3)),
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_mixed_step_matches_oracle_from_identical_state(name):
+    c = CASES[name]()
+    o = OracleSolver(c)
+    for _ in range(10):
+        o.step(0.02)
+    g = Solver(c, _lib.PREC_MIXED)
+    for f in STATE:
+        g.set(f, o.get(f))
+    g.set("lit", o.get("lit"))
+    sc = o.scalars()
+    g.set_scalars(sc["time"], sc["maxVel"], sc["maxNu"], sc["maxDiv"])
+    for s in range(3):
+        dto, dtg = o.step(0.02), g.step(0.02)
+        assert abs(dto - dtg) <= 1e-5 * dto
+        st = g.stats()
+        assert st["pressure_rel_residual"] <= 1e-8, st
+        e = rel_l2(g.get("p"), o.get("p"))
+        assert e <= P_TOL * (s + 1), ("p", s, e)
+        for f in ("u", "v", "w", "T", "Yo", "Yf"):
+            ef = rel_l2(g.get(f), o.get(f))
+            assert ef <= FIELD_TOL * (s + 1), (f, s, ef)
+        # start the next step from the oracle's state again
+        for f in STATE:
+            g.set(f, o.get(f))
+        g.set("lit", o.get("lit"))
+        sc = o.scalars()
+        g.set_scalars(sc["time"], sc["maxVel"], sc["maxNu"], sc["maxDiv"])
+
+
+def test_mixed_relative_residual_reached_every_step():
+    c = CASES["house"]()
+    g = Solver(c, _lib.PREC_MIXED)
+    for _ in range(25):
+        g.step(0.02)
+        st = g.stats()
+        assert st["pressure_rel_residual"] <= 1e-8, st
+        assert st["pressure_iters"] > 0
+
+
+def test_mixed_trajectory_stays_close_to_fp64():
+    """20 steps from the same start: FP32 rounding grows along the trajectory;
+    the layer-averaged temperature stays within 1e-3 relative."""
+    c = CASES["room"]()
+    o = OracleSolver(c)
+    g = Solver(c, _lib.PREC_MIXED)
+    for _ in range(20):
+        o.step(0.02)
+        g.step(0.02)
+    To = o.get("T").reshape(c.nz, c.ny, c.nx).mean(axis=(1, 2))
+    Tg = g.get("T").reshape(c.nz, c.ny, c.nx).mean(axis=(1, 2))
+    assert np.max(np.abs(Tg - To) / To) <= 1e-3
