@@ -468,6 +468,7 @@ public:
         for (int l = 1; l < maxLevels - 1; ++l) {
             launch("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, dom[D_LV0 + l], l, 0);
             launch("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, dom[D_LV0 + l], l, 1);
+            launch("k_residual", D_LV0 + l, TPB, k_residual<R>, S, dom[D_LV0 + l], l);
             launch("k_restrict", D_RS0 + l, TPB, k_restrict<R>, S, dom[D_RS0 + l], l);
         }
         launch("k_coarse_dense", D_CO_DENSE, TPB, k_coarse_dense<R>, S, dom[D_CO_DENSE], maxLevels - 1);
@@ -528,6 +529,7 @@ public:
         cudaMemsetAsync(h.sv + SV_BMAX, 0, sizeof(double), st);
         launch("k_rhs", D_CELLS, TPB, k_rhs<R>, S, dom[D_CELLS]);
         launch("k_mx_res64", D_CELLS, TPB, k_mx_res64<R>, S, dom[D_CELLS]);
+        launch("k_mx_zone_proj", D_CZ, TPB, k_mx_zone_proj<R>, S, dom[D_CZ]);
     }
     // the inner solve's first V-cycle and CG set-up
     void mixedInnerPrelude() {
@@ -541,6 +543,7 @@ public:
         const Scn<R>* S = dS;
         launch("k_mx_update", D_CELLS, TPB, k_mx_update<R>, S, dom[D_CELLS]);
         launch("k_mx_res64", D_CELLS, TPB, k_mx_res64<R>, S, dom[D_CELLS]);
+        launch("k_mx_zone_proj", D_CZ, TPB, k_mx_zone_proj<R>, S, dom[D_CZ]);
     }
     int readOuterDone(bool& allDone) {
         PHX_CK(cudaMemcpyAsync(hPin + 8, h.sv + SV_ODONE, sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -606,7 +609,9 @@ public:
         if (!dLoop) PHX_CK(cudaMalloc(&dLoop, 2 * sizeof(int)));
         const Scn<R> saved = h;
         PHX_CK(cudaGraphCreate(&graph, 0));
-        PHX_CK(cudaGraphConditionalHandleCreate(&cgHandle, graph, 0, 0));
+        // conditional handles are created before the capture of the graph that holds their node
+        if (kMixed) PHX_CK(cudaGraphConditionalHandleCreate(&outerHandle, graph, 0, 0));
+        else PHX_CK(cudaGraphConditionalHandleCreate(&cgHandle, graph, 0, 0));
         PHX_CK(cudaStreamBeginCaptureToGraph(st, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
         launches = 0;
         launch("k_begin", D_ONE, 32, k_begin<R>, (const Scn<R>*)dS, dom[D_ONE], 1, 0.0);
@@ -673,7 +678,6 @@ public:
         mixedBegin();
         cudaMemsetAsync(dLoop, 0, 2 * sizeof(int), st);
         const int capOuter = OUTER_MAX + 2, capInner = INNER_MAX + 2;
-        PHX_CK(cudaGraphConditionalHandleCreate(&outerHandle, graph, 0, 0));
         k_mx_outer<R><<<1, 32, 0, st>>>(dS, 1, outerHandle, dLoop, capOuter, 1);
         ++launches;
         cudaGraph_t outerBody = nullptr;
@@ -686,11 +690,11 @@ public:
         PHX_CK(cudaStreamEndCapture(st, &outGraph));
         outerKernels = launches;
         // refinement pass
+        PHX_CK(cudaGraphConditionalHandleCreate(&cgHandle, outerBody, 0, 0));
         PHX_CK(cudaStreamBeginCaptureToGraph(st, outerBody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
         launches = 0;
         cudaMemsetAsync(dLoop + 1, 0, sizeof(int), st);
         mixedInnerPrelude();
-        PHX_CK(cudaGraphConditionalHandleCreate(&cgHandle, outerBody, 0, 0));
         k_cg_cond<R><<<1, 32, 0, st>>>(dS, 1, cgHandle, dLoop + 1, capInner);
         ++launches;
         innerPreludeKernels = launches;
@@ -928,7 +932,13 @@ public:
         PHX_CK(cudaStreamSynchronize(st));
         return PHX_OK;
     }
-    int lastLaunches() const override { return launches; }
+    int lastLaunches() const override {
+        if (useGraph && gexec) {
+            int k = 0;
+            if (const_cast<Ctx*>(this)->graphLaunchCount(&k) == PHX_OK) return k;
+        }
+        return launches;
+    }
 
     // n steps timed with CUDA events on the context's stream; with flushL2 a
     // buffer larger than L2 is written (untimed) before each step

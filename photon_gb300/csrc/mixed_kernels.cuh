@@ -40,7 +40,42 @@ __global__ void k_mx_res64(const Scn<R>* __restrict__ S, Dom dom) {
         }
         g.r[c] = (R)r;
         g.p[c] = 0;
-        rm = fabs(r);
+        // cells of closed zones get their max after the zone-mean projection
+        const int z = g.nClosed > 0 ? g.zone[c] : -1;
+        if (!(z >= 0 && !g.zoneOpen[z])) rm = fabs(r);
+    }
+    blockMaxTo(g.sv + SV_R64MAX, rm);
+}
+
+// Closed zones make A singular (constants are its null space): the right-hand
+// side of the inner solve must have zero mean over each closed zone. In FP64
+// the step's b is consistent to rounding; its FP32 copy is not, so the mean of
+// the residual over each closed zone is removed before the inner solve (one
+// CTA per closed zone; FP64 sums).
+template <class R>
+__global__ void k_mx_zone_proj(const Scn<R>* __restrict__ S, Dom dom) {
+    int s_, tile_;
+    locate(dom, blockIdx.x, s_, tile_);
+    const Scn<R>& g = S[s_];
+    if (g.sv[SV_ODONE] != 0) return;
+    __shared__ double sh[32];
+    __shared__ double meanSh;
+    const int zi = tile_;
+    const int e0 = g.closedStart[zi], e1 = g.closedStart[zi + 1];
+    double acc = 0;
+    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) acc += (double)g.r[g.closedCells[e]];
+    double sum = blockSum(acc, sh);
+    if (threadIdx.x == 0) meanSh = e1 > e0 ? sum / (double)(e1 - e0) : 0.0;
+    __syncthreads();
+    const double mean = meanSh;
+    double rm = 0;
+    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        const int c = g.closedCells[e];
+        if (g.diag[c] > 0) {
+            const R v = (R)((double)g.r[c] - mean);
+            g.r[c] = v;
+            rm = fmax(rm, fabs((double)v));
+        }
     }
     blockMaxTo(g.sv + SV_R64MAX, rm);
 }

@@ -143,27 +143,35 @@ __global__ void k_jacobi(const Scn<R>* __restrict__ S, Dom dom, int l, int mode)
     out[I] = (R)((1 - OMEGA) * X(I) + OMEGA * s / dg);
 }
 
-// residual of coarse level l (residualSparse, pressure_mg.cpp:248-257) summed
-// into each unknown of level l+1 over its children in ascending order (:285-286)
+// residual of coarse level l (residualSparse, pressure_mg.cpp:248-257), one
+// thread per row, into the level's y buffer (free between the sweeps)
+template <class R>
+__global__ void k_residual(const Scn<R>* __restrict__ S, Dom dom, int l) {
+    PHX_PROLOGUE_ACTIVE(dom);
+    const Level<R>& L = g.lv[l];
+    const int I = tile_ * TPB + threadIdx.x;
+    if (I >= L.n) return;
+    const double dg = L.diag[I];
+    double r = 0;
+    if (dg > 0) {
+        double s = (double)L.b[I] - dg * (double)L.x[I];
+        for (int q = L.rowStart[I]; q < L.rowStart[I + 1]; ++q) s += (double)L.val[q] * (double)L.x[L.col[q]];
+        r = s;
+    }
+    L.y[I] = (R)r;
+}
+
+// restriction (pressure_mg.cpp:285-286): each unknown of level l+1 sums its
+// children's residuals in ascending order, the order of the reference's scatter
 template <class R>
 __global__ void k_restrict(const Scn<R>* __restrict__ S, Dom dom, int l) {
     PHX_PROLOGUE_ACTIVE(dom);
     const Level<R>& L = g.lv[l];
-    Level<R>& C = const_cast<Level<R>&>(g.lv[l + 1]);
+    const Level<R>& C = g.lv[l + 1];
     const int J = tile_ * TPB + threadIdx.x;
     if (J >= C.n) return;
     double acc = 0.0;
-    for (int e = L.childStart[J]; e < L.childStart[J + 1]; ++e) {
-        const int I = L.child[e];
-        const double dg = L.diag[I];
-        double r = 0;
-        if (dg > 0) {
-            double s = (double)L.b[I] - dg * (double)L.x[I];
-            for (int q = L.rowStart[I]; q < L.rowStart[I + 1]; ++q) s += (double)L.val[q] * (double)L.x[L.col[q]];
-            r = (double)(R)s;
-        }
-        acc = (double)(R)(acc + r);
-    }
+    for (int e = L.childStart[J]; e < L.childStart[J + 1]; ++e) acc = (double)(R)(acc + (double)L.y[L.child[e]]);
     C.b[J] = (R)acc;
 }
 
