@@ -32,11 +32,24 @@ sys.path.insert(0, ROOT)
 
 METRIC = "cell-updates/s, mixed+batched vs FP64 GPU @1e-8 resid; p50/p99 scenario latency"
 REL_TOL = 1e-8
-SPINUP_STEPS = 150   # untimed steps that develop the plume before warm-up
+SPINUP_STEPS = 100   # untimed steps that develop the plume before warm-up
 
 
 def rank_info():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def make_workloads(name: str):
+    """list of cases of a workload"""
+    from photon_gb300 import casegen
+    if name == "batch64":
+        cs = casegen.batch_scenarios(64)
+        for c in cs:
+            c.profile.tol = 0.0
+            c.profile.rel_tol = REL_TOL
+            c.profile.maxIters = 400
+        return cs
+    return [make_workload(name)]
 
 
 def make_workload(name: str):
@@ -171,33 +184,41 @@ def cpu_reference_rate(case, steps: int, warm: int, threads: int, bits: int = 32
 
 
 def run_reference(args, rank, world):
+    """The reference's own FP32 CPU step on the workload (a sample of every
+    eighth scenario for the batch), all host threads, spun up like our arm."""
     if rank != 0:
         return 0
-    case = make_workload(args.workload)
-    # the reference stops on its own absolute test only: 1e-8 1/s is at least as strict
-    case.profile.tol = 1e-8
+    cases = make_workloads(args.workload)
+    sample = cases[::8] if len(cases) > 8 else cases
     threads = os.cpu_count() or 1
     from oracle import refpy
     if not refpy.available(32):
         print(json.dumps({"impl": "reference", "unavailable": "reference CPU build (oracle/_ref) is not present"}))
         return 0
-    s = refpy.RefSolver(case, 32, threads)
-    for _ in range(args.spinup + args.warmup):   # the same developed flow as the GPU arm
-        s.step(case.profile.dtMax)
+    solvers = []
+    for c in sample:
+        c.profile.tol = 1e-8   # the reference stops on its own absolute test only: 1e-8 1/s is at least as strict
+        solvers.append((c, refpy.RefSolver(c, 32, threads)))
+    for _ in range(args.spinup + args.warmup):
+        for c, s in solvers:
+            s.step(c.profile.dtMax)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        s.step(case.profile.dtMax)
+        for c, s in solvers:
+            s.step(c.profile.dtMax)
     el = time.perf_counter() - t0
-    v = case.N * args.steps / el
+    cells = sum(c.N for c in sample)
+    v = cells * args.steps / el
+    desc = "%d steps of %d of the %d scenarios (%d cells) after %d spin-up and %d warm-up steps" % (
+        args.steps, len(sample), len(cases), cells, args.spinup, args.warmup)
     line = {"metric": METRIC, "value": v, "unit": "cell-updates/s", "n_gpus": 0, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded house generator)",
-            "config": {"workload": args.workload, "cells": case.N, "pressure_stop": "absolute 1e-8 1/s",
-                       "threads": threads, "spinup_steps": args.spinup},
+            "config": {"workload": args.workload, "scenarios_sampled": len(sample), "cells": cells,
+                       "pressure_stop": "absolute 1e-8 1/s", "threads": threads, "spinup_steps": args.spinup},
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": "reference",
-                             "sample": "%d steps of %s after %d spin-up and %d warm-up steps" % (
-                                 args.steps, args.workload, args.spinup, args.warmup)},
+                             "sample": desc},
             "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -208,14 +229,15 @@ def measure(args, precision, L, world, clocks: bool):
     profile and roofline of the dominant kernel, e2e through the C ABI."""
     import ctypes
     from photon_gb300 import _lib
-    from photon_gb300.solver import Solver
-    case = make_workload(args.workload)
-    g = Solver(case, precision)
-    dtMax = case.profile.dtMax
+    from photon_gb300.solver import Batch
+    cases = make_workloads(args.workload)
+    cells = sum(c.N for c in cases)
+    g = Batch(cases, precision)
+    dtMax = cases[0].profile.dtMax
     if args.spinup > 0:
         g.run(args.spinup, dtMax)
     g.run(max(3, args.warmup), dtMax)
-    # a single scenario's working set fits in L2: flush it before every timed step
+    # a working set that fits in L2 is flushed before every timed step
     flush = g.device_bytes() < (200 << 20)
     dist = None
     if world > 1:
@@ -225,52 +247,66 @@ def measure(args, precision, L, world, clocks: bool):
     clk = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     if clocks:
         clk.__enter__()
-    ms, launches = g.time_steps(args.steps, dtMax, flush_l2=flush)
+    step_ms = []
+    launches = 0
+    for _ in range(args.steps):
+        ms, nl = g.time_steps(1, dtMax, flush_l2=flush)
+        step_ms.append(ms)
+        launches += nl
     if clocks:
         clk.__exit__()
     g.sync()
-    t_s = ms / 1e3
+    t_s = sum(step_ms) / 1e3
     if dist:
         import torch
         t = torch.tensor([t_s], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         t_s = float(t[0])
-    value = case.N * args.steps * world / t_s
-    st = g.stats()
-    # e2e through the C ABI: step from the host, read T and the stats back to pinned memory
-    w = 8 if precision == _lib.PREC_FP64 else 4
-    nbytesT = case.N * 8
-    hbuf = L.phx_alloc_host(nbytesT)
-    stats = _lib.PhxStats()
-    dt_c = ctypes.c_double()
+    value = cells * args.steps * world / t_s
+    iters = [g.stats(s)["pressure_iters"] for s in range(len(cases))]
+    rels = [g.stats(s)["pressure_rel_residual"] for s in range(len(cases))]
+    # e2e through the C ABI: per step, the dtMax of every scenario goes down
+    # from pinned memory and every scenario's stats come back
+    n = len(cases)
+    h2d = L.phx_alloc_host(8 * n)
+    dtm = (ctypes.c_double * n).from_address(h2d)
+    for i in range(n):
+        dtm[i] = dtMax
+    dts = (ctypes.c_double * n)()
+    st = _lib.PhxStats()
     for _ in range(2):
-        L.phx_step(g.h, dtMax, ctypes.byref(dt_c))
+        L.phx_batch_step(g.h, ctypes.c_void_p(h2d), 0.0, dts)
     g.sync()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        if L.phx_step(g.h, dtMax, ctypes.byref(dt_c)) != 0:
+        if L.phx_batch_step(g.h, ctypes.c_void_p(h2d), 0.0, dts) != 0:
             raise SystemExit(L.phx_last_error(g.h).decode())
-        L.phx_get_field(g.h, _lib.FIELD_ID["T"], ctypes.c_void_p(hbuf), nbytesT)
-        L.phx_get_stats(g.h, ctypes.byref(stats))
+        for s in range(n):
+            L.phx_batch_get_stats(g.h, s, ctypes.byref(st))
     e2e_s = time.perf_counter() - t0
-    L.phx_free_host(ctypes.c_void_p(hbuf))
-    e2e_value = case.N * args.steps * world / e2e_s
+    L.phx_free_host(ctypes.c_void_p(h2d))
+    e2e_value = cells * args.steps * world / e2e_s
     # per-kernel device times of one step (outside the timed region) for the roofline
     prof = g.profile_step(dtMax, flush_l2=flush)
     tot_prof = sum(p[2] for p in prof)
     top = max(prof, key=lambda p: p[2])
+    w = 8 if precision == _lib.PREC_FP64 else 4
     per_unit = kernel_bytes(top[0], w)
     peak, peak_kind = measured_peak()
     roof = None
     if per_unit:
-        bytes_per_launch = per_unit * case.N
+        bytes_per_launch = per_unit * cells
         achieved = bytes_per_launch / (top[2] / top[1] / 1e3) / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": None, "kernel": top[0], "kernel_share": top[2] / tot_prof,
                 "algorithmic_bytes_per_launch": bytes_per_launch, "peak_kind": peak_kind}
     g.close()
-    return {"case": case, "value": value, "t_s": t_s, "stats": st, "launches": launches, "roofline": roof,
-            "clk": clk, "prof": prof, "e2e": e2e_value, "d2h": case.N * w, "flush": flush}
+    sm = sorted(step_ms)
+    pct = lambda q: sm[min(len(sm) - 1, int(round(q * (len(sm) - 1))))]
+    return {"cases": cases, "cells": cells, "value": value, "t_s": t_s, "iters": iters, "rels": rels,
+            "launches": launches, "roofline": roof, "clk": clk, "prof": prof, "e2e": e2e_value,
+            "h2d": 8 * n, "d2h": n * ctypes.sizeof(_lib.PhxStats) + 8 * n, "flush": flush,
+            "p50_ms": pct(0.5), "p99_ms": pct(0.99)}
 
 
 def main():
@@ -279,7 +315,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="house_72x52x44")
+    ap.add_argument("--workload", default="batch64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--spinup", type=int, default=SPINUP_STEPS, help="untimed steps before warm-up")
     args = ap.parse_args()
@@ -299,50 +335,48 @@ def main():
 
     mixed = measure(args, _lib.PREC_MIXED, L, world, clocks=True)
     fp64 = measure(args, _lib.PREC_FP64, L, world, clocks=False)
-    case = mixed["case"]
+    cases = mixed["cases"]
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cref = make_workload(args.workload)
-        cref.profile.tol = 1e-8
+        # the reference's FP32 CPU step on a sample of the workload: its
+        # median-size scenario, spun up like the GPU arm
+        sample = sorted(make_workloads(args.workload), key=lambda c: c.N)[len(cases) // 2]
+        sample.profile.tol = 1e-8
         threads = os.cpu_count() or 1
-        v, kind, thr, n, el = cpu_reference_rate(cref, steps=20, warm=2, threads=threads, spinup=args.spinup)
+        v, kind, thr, nst, el = cpu_reference_rate(sample, steps=20, warm=2, threads=threads, spinup=args.spinup)
         cpu = {"value": v, "unit": "cell-updates/s", "cores": thr, "kind": kind,
-               "sample": "%d steps of %s (%.1f s) after %d spin-up and 2 warm-up steps, FP32 reference build, "
-                         "pressure stop 1e-8 1/s" % (n, args.workload, el, args.spinup)}
-    value = mixed["value"]
-    t_s = mixed["t_s"]
-    st = mixed["stats"]
-    launches = mixed["launches"]
-    roof = mixed["roofline"]
-    clk = mixed["clk"]
-    prof = mixed["prof"]
-    e2e_value, nbytesT = mixed["e2e"], mixed["d2h"]
-    import ctypes
+               "sample": "%d steps of scenario %s (%d cells, %.1f s) after %d spin-up and 2 warm-up steps, FP32 "
+                         "reference build, pressure stop 1e-8 1/s" % (nst, sample.name, sample.N, el, args.spinup)}
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": t_s / args.steps * 1e3, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 (mixed)",
-                "data": "synthetic (seeded house generator; random-free physics, no dataset)",
-                "config": {"workload": args.workload, "cells": case.N, "precision": "mixed (FP32 fields/stencils, FP32 MG-CG in FP64 refinement)",
-                           "pressure_stop": "relative 1e-8 (max|r| <= 1e-8 max|b|)",
+        import ctypes
+        line = {"metric": METRIC, "value": mixed["value"], "unit": "cell-updates/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": mixed["t_s"] / args.steps * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 (mixed)",
+                "data": "synthetic (seeded house generator; no dataset)",
+                "config": {"workload": args.workload, "scenarios": len(cases), "cells": mixed["cells"],
+                           "precision": "mixed: FP32 fields and stencils, FP32 MG-CG inside FP64 refinement",
+                           "pressure_stop": "relative 1e-8 (max|r| <= 1e-8 max|b|, FP64)",
                            "l2": "flushed before each step" if mixed["flush"] else "inputs larger than L2",
-                           "spinup_steps": args.spinup, "cg_iters_last_step": st["pressure_iters"],
-                           "rel_residual_last_step": st["pressure_rel_residual"],
-                           "parallelism": "replicas" if world > 1 else "single"},
-                "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": 8,
-                        "d2h_bytes_per_step": nbytesT + ctypes.sizeof(_lib.PhxStats)},
+                           "spinup_steps": args.spinup,
+                           "cg_iters_last_step": {"min": min(mixed["iters"]), "max": max(mixed["iters"])},
+                           "max_rel_residual_last_step": max(mixed["rels"]),
+                           "parallelism": "replicas" if world > 1 else "single GPU, batched"},
+                "latency": {"step_p50_ms": mixed["p50_ms"], "step_p99_ms": mixed["p99_ms"]},
+                "e2e": {"value": mixed["e2e"], "unit": "cell-updates/s", "h2d_bytes_per_step": mixed["h2d"],
+                        "d2h_bytes_per_step": mixed["d2h"]},
                 "fp64": {"value": fp64["value"], "ms_per_step": fp64["t_s"] / args.steps * 1e3,
-                         "cg_iters_last_step": fp64["stats"]["pressure_iters"],
-                         "rel_residual_last_step": fp64["stats"]["pressure_rel_residual"],
-                         "gpu_launches": fp64["launches"], "roofline": fp64["roofline"], "e2e": fp64["e2e"]},
-                "mixed_over_fp64": value / fp64["value"],
-                "gpu_launches": launches,
-                "roofline": roof,
+                         "cg_iters_last_step": {"min": min(fp64["iters"]), "max": max(fp64["iters"])},
+                         "max_rel_residual_last_step": max(fp64["rels"]),
+                         "gpu_launches": fp64["launches"], "roofline": fp64["roofline"], "e2e": fp64["e2e"],
+                         "latency": {"step_p50_ms": fp64["p50_ms"], "step_p99_ms": fp64["p99_ms"]}},
+                "mixed_over_fp64": mixed["value"] / fp64["value"],
+                "gpu_launches": mixed["launches"],
+                "roofline": mixed["roofline"],
                 "cpu_baseline": cpu,
-                "clocks": clk.summary(),
+                "clocks": mixed["clk"].summary(),
                 "kernels": [{"name": p[0], "launches": p[1], "ms": round(p[2], 4)} for p in
-                            sorted(prof, key=lambda p: -p[2])[:12]]}
+                            sorted(mixed["prof"], key=lambda p: -p[2])[:14]]}
         print(json.dumps(line))
     if dist:
         dist.barrier()

@@ -167,6 +167,26 @@ int phx_profile_step(struct phx_ctx* ctx, double dt_max, int flush_l2, phx_kerne
 /* kernel launches of the last step */
 int phx_last_step_launches(const struct phx_ctx* ctx);
 
+/* --- batches ---------------------------------------------------------------
+ * A context can hold several scenarios of different grids; every kernel of a
+ * step covers all of them (one launch per pass, one CUDA graph per step). The
+ * single-scenario calls above act on scenario 0. Scenario indices are
+ * positions in the batch: removing a scenario moves the later ones down. */
+int phx_create_batch(const phx_grid* grids, int n, int precision, struct phx_ctx** out);
+int phx_batch_add(struct phx_ctx* ctx, const phx_grid* grid, int* scenario_out);
+int phx_batch_remove(struct phx_ctx* ctx, int scenario);
+int phx_batch_size(const struct phx_ctx* ctx);
+size_t phx_batch_scenario_bytes(const struct phx_ctx* ctx, int scenario);
+int phx_batch_add_burner(struct phx_ctx* ctx, int scenario, double x0, double y0, double x1, double y1, double z,
+                         double peak_w, double ramp_s, double start, double duration, int* index_out);
+/* one step of every scenario: dt_max per scenario (or NULL: dt_max_all for all);
+ * dt_out (may be NULL) gets each scenario's dt */
+int phx_batch_step(struct phx_ctx* ctx, const double* dt_max, double dt_max_all, double* dt_out);
+int phx_batch_get_field(struct phx_ctx* ctx, int scenario, int field, void* host, size_t bytes);
+int phx_batch_set_field(struct phx_ctx* ctx, int scenario, int field, const void* host, size_t bytes);
+size_t phx_batch_field_count(const struct phx_ctx* ctx, int scenario, int field);
+int phx_batch_get_stats(struct phx_ctx* ctx, int scenario, phx_stats* out);
+
 /* --- process-level helpers ------------------------------------------------
  * select the CUDA device later contexts of this thread are created on */
 int phx_select_device(int device);

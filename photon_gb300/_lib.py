@@ -25,7 +25,9 @@ SYMBOLS = ["phx_create", "phx_destroy", "phx_last_error", "phx_last_global_error
            "phx_add_ignition", "phx_step", "phx_run", "phx_stage", "phx_precondition", "phx_get_field",
            "phx_set_field", "phx_field_count", "phx_get_stats", "phx_set_scalars", "phx_device_bytes", "phx_sync",
            "phx_time_steps", "phx_profile_step", "phx_last_step_launches", "phx_select_device", "phx_alloc_host",
-           "phx_free_host"]
+           "phx_free_host", "phx_create_batch", "phx_batch_add", "phx_batch_remove", "phx_batch_size",
+           "phx_batch_scenario_bytes", "phx_batch_add_burner", "phx_batch_step", "phx_batch_get_field",
+           "phx_batch_set_field", "phx_batch_field_count", "phx_batch_get_stats"]
 
 
 class PhxGrid(ctypes.Structure):
@@ -95,6 +97,19 @@ def load():
     L.phx_profile_step.argtypes = [vp, d, i, ctypes.POINTER(PhxKernelTime), i, ctypes.POINTER(i)]
     L.phx_last_step_launches.argtypes = [vp]
     L.phx_select_device.argtypes = [i]
+    L.phx_create_batch.argtypes = [ctypes.POINTER(PhxGrid), i, i, ctypes.POINTER(vp)]
+    L.phx_batch_add.argtypes = [vp, ctypes.POINTER(PhxGrid), ctypes.POINTER(i)]
+    L.phx_batch_remove.argtypes = [vp, i]
+    L.phx_batch_size.argtypes = [vp]
+    L.phx_batch_scenario_bytes.restype = sz
+    L.phx_batch_scenario_bytes.argtypes = [vp, i]
+    L.phx_batch_add_burner.argtypes = [vp, i, d, d, d, d, d, d, d, d, d, ctypes.POINTER(i)]
+    L.phx_batch_step.argtypes = [vp, vp, d, vp]
+    L.phx_batch_get_field.argtypes = [vp, i, i, vp, sz]
+    L.phx_batch_set_field.argtypes = [vp, i, i, vp, sz]
+    L.phx_batch_field_count.restype = sz
+    L.phx_batch_field_count.argtypes = [vp, i, i]
+    L.phx_batch_get_stats.argtypes = [vp, i, ctypes.POINTER(PhxStats)]
     L.phx_alloc_host.restype = vp
     L.phx_alloc_host.argtypes = [sz]
     L.phx_free_host.argtypes = [vp]

@@ -64,7 +64,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         objs = list(ex.map(one, list(UNITS)))
     if force or _newer(LIB, objs):
         tmp = LIB + ".tmp%d" % os.getpid()
-        cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"]
+        cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-Xcompiler", "-pthread", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr[-4000:]))

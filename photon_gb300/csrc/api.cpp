@@ -1,10 +1,11 @@
 // C ABI of the GB300 gas-phase step (include/phx.h). No exception crosses it;
 // every entry point returns a status and keeps the message for phx_last_error.
 #include <cstring>
-
-#include <cuda_runtime.h>
+#include <memory>
 #include <new>
 #include <string>
+
+#include <cuda_runtime.h>
 
 #include "engine.h"
 
@@ -37,6 +38,10 @@ int guarded(phx_ctx* c, F f) {
         return fail(c, PHX_ERR_CUDA, "unknown error");
     }
 }
+
+phx::CtxBase* makeEngine(int precision) {
+    return precision == PHX_PREC_FP64 ? phx::makeCtxFp64() : phx::makeCtxMixed();
+}
 }  // namespace
 
 extern "C" {
@@ -45,24 +50,19 @@ int phx_abi_version(void) { return PHX_ABI_VERSION; }
 const char* phx_last_global_error(void) { return g_err.c_str(); }
 const char* phx_last_error(const phx_ctx* c) { return c ? c->err.c_str() : g_err.c_str(); }
 
-int phx_create(const phx_grid* grid, int precision, phx_ctx** out) {
+int phx_create_batch(const phx_grid* grids, int n, int precision, phx_ctx** out) {
     if (!out) return fail(nullptr, PHX_ERR_INVALID, "out is null");
     *out = nullptr;
-    if (!grid) return fail(nullptr, PHX_ERR_INVALID, "grid is null");
+    if (n < 0 || (n > 0 && !grids)) return fail(nullptr, PHX_ERR_INVALID, "grids is null");
     if (precision != PHX_PREC_FP64 && precision != PHX_PREC_MIXED) return fail(nullptr, PHX_ERR_INVALID, "unknown precision");
     try {
-        std::string err;
-        phx::CtxBase* impl = precision == PHX_PREC_FP64 ? phx::makeCtxFp64(grid, err) : phx::makeCtxMixed(grid, err);
-        if (!impl) {
-            int code = err.find("not implemented") != std::string::npos || err.find("not part of") != std::string::npos
-                           ? PHX_ERR_UNSUPPORTED
-                       : err.find("allocation") != std::string::npos ? PHX_ERR_OOM
-                       : err.find("cuda") != std::string::npos || err.find("CUDA") != std::string::npos ? PHX_ERR_CUDA
-                                                                                                          : PHX_ERR_INVALID;
-            return fail(nullptr, code, err);
+        std::unique_ptr<phx::CtxBase> impl(makeEngine(precision));
+        for (int i = 0; i < n; ++i) {
+            int r = impl->addScenario(&grids[i], nullptr);
+            if (r != PHX_OK) return fail(nullptr, r, "scenario " + std::to_string(i) + ": " + impl->err);
         }
         phx_ctx* c = new phx_ctx;
-        c->impl = impl;
+        c->impl = impl.release();
         c->precision = precision;
         *out = c;
         return PHX_OK;
@@ -73,28 +73,76 @@ int phx_create(const phx_grid* grid, int precision, phx_ctx** out) {
     }
 }
 
+int phx_create(const phx_grid* grid, int precision, phx_ctx** out) {
+    if (!grid) {
+        if (out) *out = nullptr;
+        return fail(nullptr, PHX_ERR_INVALID, "grid is null");
+    }
+    return phx_create_batch(grid, 1, precision, out);
+}
+
 void phx_destroy(phx_ctx* c) {
     if (!c) return;
     delete c->impl;
     delete c;
 }
 
+int phx_batch_add(phx_ctx* c, const phx_grid* grid, int* scenario_out) {
+    if (!grid) return fail(c, PHX_ERR_INVALID, "grid is null");
+    return guarded(c, [&](phx::CtxBase* x) { return x->addScenario(grid, scenario_out); });
+}
+
+int phx_batch_remove(phx_ctx* c, int scenario) {
+    return guarded(c, [&](phx::CtxBase* x) { return x->removeScenario(scenario); });
+}
+
+int phx_batch_size(const phx_ctx* c) { return c && c->impl ? c->impl->scenarioCount() : 0; }
+
+size_t phx_batch_scenario_bytes(const phx_ctx* c, int scenario) {
+    return c && c->impl ? c->impl->scenarioBytes(scenario) : 0;
+}
+
+int phx_batch_add_burner(phx_ctx* c, int s, double x0, double y0, double x1, double y1, double z, double peak_w,
+                         double ramp_s, double start, double duration, int* index_out) {
+    return guarded(c, [&](phx::CtxBase* x) {
+        return x->addBurner(s, x0, y0, x1, y1, z, peak_w, ramp_s, start, duration, index_out);
+    });
+}
+
 int phx_add_burner(phx_ctx* c, double x0, double y0, double x1, double y1, double z, double peak_w, double ramp_s,
                    double start, double duration, int* index_out) {
-    return guarded(c, [&](phx::CtxBase* x) { return x->addBurner(x0, y0, x1, y1, z, peak_w, ramp_s, start, duration, index_out); });
+    return phx_batch_add_burner(c, 0, x0, y0, x1, y1, z, peak_w, ramp_s, start, duration, index_out);
 }
 
 int phx_add_ignition(phx_ctx* c, int cell, double power, double duration) {
-    return guarded(c, [&](phx::CtxBase* x) { return x->addIgnition(cell, power, duration); });
+    return guarded(c, [&](phx::CtxBase* x) { return x->addIgnition(0, cell, power, duration); });
 }
 
 int phx_step(phx_ctx* c, double dt_max, double* dt_out) {
-    return guarded(c, [&](phx::CtxBase* x) { return x->step(1, dt_max, dt_out); });
+    return guarded(c, [&](phx::CtxBase* x) { return x->step(1, dt_max, nullptr, dt_out); });
 }
 
 int phx_run(phx_ctx* c, int n, double dt_max, double* dt_out) {
     if (n < 0) return fail(c, PHX_ERR_INVALID, "negative step count");
-    return guarded(c, [&](phx::CtxBase* x) { return x->step(n, dt_max, dt_out); });
+    return guarded(c, [&](phx::CtxBase* x) { return x->step(n, dt_max, nullptr, dt_out); });
+}
+
+int phx_batch_step(phx_ctx* c, const double* dt_max, double dt_max_all, double* dt_out) {
+    return guarded(c, [&](phx::CtxBase* x) {
+        if (dt_max || dt_out) {
+            // per-scenario dtMax and/or dt read-back
+            const int n = x->scenarioCount();
+            std::unique_ptr<double[]> tmp;
+            const double* per = dt_max;
+            if (!per) {
+                tmp.reset(new double[n > 0 ? n : 1]);
+                for (int i = 0; i < n; ++i) tmp[i] = dt_max_all;
+                per = tmp.get();
+            }
+            return x->step(1, dt_max_all, per, dt_out);
+        }
+        return x->step(1, dt_max_all, nullptr, nullptr);
+    });
 }
 
 int phx_stage(phx_ctx* c, int stage, double arg) {
@@ -106,25 +154,32 @@ int phx_precondition(phx_ctx* c, const double* r, double* z) {
     return guarded(c, [&](phx::CtxBase* x) { return x->precondition(r, z); });
 }
 
-int phx_get_field(phx_ctx* c, int field, void* host, size_t bytes) {
+int phx_batch_get_field(phx_ctx* c, int s, int field, void* host, size_t bytes) {
     if (!host) return fail(c, PHX_ERR_INVALID, "null buffer");
-    return guarded(c, [&](phx::CtxBase* x) { return x->getField(field, host, bytes); });
+    return guarded(c, [&](phx::CtxBase* x) { return x->getField(s, field, host, bytes); });
 }
 
-int phx_set_field(phx_ctx* c, int field, const void* host, size_t bytes) {
+int phx_batch_set_field(phx_ctx* c, int s, int field, const void* host, size_t bytes) {
     if (!host) return fail(c, PHX_ERR_INVALID, "null buffer");
-    return guarded(c, [&](phx::CtxBase* x) { return x->setField(field, host, bytes); });
+    return guarded(c, [&](phx::CtxBase* x) { return x->setField(s, field, host, bytes); });
 }
 
-size_t phx_field_count(const phx_ctx* c, int field) { return c && c->impl ? c->impl->fieldCount(field) : 0; }
+size_t phx_batch_field_count(const phx_ctx* c, int s, int field) {
+    return c && c->impl ? c->impl->fieldCount(s, field) : 0;
+}
 
-int phx_get_stats(phx_ctx* c, phx_stats* out) {
+int phx_batch_get_stats(phx_ctx* c, int s, phx_stats* out) {
     if (!out) return fail(c, PHX_ERR_INVALID, "null stats");
-    return guarded(c, [&](phx::CtxBase* x) { return x->getStats(out); });
+    return guarded(c, [&](phx::CtxBase* x) { return x->getStats(s, out); });
 }
+
+int phx_get_field(phx_ctx* c, int field, void* host, size_t bytes) { return phx_batch_get_field(c, 0, field, host, bytes); }
+int phx_set_field(phx_ctx* c, int field, const void* host, size_t bytes) { return phx_batch_set_field(c, 0, field, host, bytes); }
+size_t phx_field_count(const phx_ctx* c, int field) { return phx_batch_field_count(c, 0, field); }
+int phx_get_stats(phx_ctx* c, phx_stats* out) { return phx_batch_get_stats(c, 0, out); }
 
 int phx_set_scalars(phx_ctx* c, double time, double max_vel, double max_nu, double max_div) {
-    return guarded(c, [&](phx::CtxBase* x) { return x->setScalars(time, max_vel, max_nu, max_div); });
+    return guarded(c, [&](phx::CtxBase* x) { return x->setScalars(0, time, max_vel, max_nu, max_div); });
 }
 
 size_t phx_device_bytes(const phx_ctx* c) { return c && c->impl ? c->impl->deviceBytes() : 0; }

@@ -1,10 +1,15 @@
-// One scenario context: device arena, descriptor, domain tables and the launch
-// sequence of the gas-phase step (src/sim/solver.cpp:226-269). Instantiated
-// per precision by engine_fp64.cu (and the mixed path).
+// The GPU engine: a batch of scenarios stepped together, their device state,
+// the domain tables of the launches and the launch sequence of the gas-phase
+// step (src/sim/solver.cpp:226-269). A single-scenario context is a batch of
+// one. Every kernel launch covers one domain (cells, faces of one axis, one
+// multigrid level, ...) of every scenario; the whole step is captured once as
+// a CUDA graph whose pressure-solve loops are device-side while nodes.
+// Instantiated per precision by engine_fp64.cu and engine_mixed.cu.
 #pragma once
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -23,6 +28,7 @@ namespace phx {
             return PHX_ERR_CUDA;                                                         \
         }                                                                                \
     } while (0)
+#define PHX_TRY(x) do { int r_ = (x); if (r_) return r_; } while (0)
 
 // dense coarse operators up to this many unknowns (n^2 reals)
 constexpr int DENSE_MAX = 4096;
@@ -34,19 +40,18 @@ enum DomId {
     D_COUNT = D_RS0 + MAX_LEVELS
 };
 
-struct SourceHost {
-    Src s;
-};
+template <class T>
+static T* carve(char*& base, size_t& off, size_t n) {
+    off = (off + 255) & ~(size_t)255;
+    T* p = base ? (T*)(base + off) : nullptr;
+    off += n * sizeof(T);
+    return p;
+}
 
+// One scenario: host set-up results, its device arena and its descriptor.
 template <class R>
-class Ctx : public CtxBase {
-public:
-    // the float instantiation is the mixed path: FP32 fields and stencils, FP64
-    // refinement of the pressure solve, FP64 dots and global sums
+struct Scenario {
     static constexpr bool kMixed = std::is_same<R, float>::value;
-    static constexpr int INNER_MAX = 10;        // inner FP32 CG iterations per refinement pass
-    static constexpr double INNER_REL = 1e-4;   // inner stop relative to the pass's starting residual
-    static constexpr int OUTER_MAX = 40;
     GridGeom geo;
     double cfl = 0.5, dtMaxP = 0.02, tol = 0.002, relTol = 0;
     int maxIters = 400, radiationOn = 1;
@@ -54,33 +59,17 @@ public:
     Multigrid MG;
     std::vector<double> Pb0;
     std::vector<Src> ignitions, burners;
-    cudaStream_t st = nullptr;
     char* arena = nullptr;
     size_t arenaBytes = 0;
-    Scn<R> h{};
-    Scn<R>* dS = nullptr;
-    R** dD = nullptr;
+    Scn<R> h{};                  // host copy of the device descriptor
     R* dbuf[2] = {nullptr, nullptr};
-    double* hPin = nullptr;      // pinned: [0] dtMax, [1..] scalar read-back
-    int* dDomStart = nullptr;    // D_COUNT x 2
-    Dom dom[D_COUNT];
-    int maxLevels = 0;
-    int launches = 0;
-    cudaEvent_t ev[4] = {};
+    std::string err;
 
-    ~Ctx() override {
-        if (st) cudaStreamSynchronize(st);
+    ~Scenario() {
         if (arena) cudaFree(arena);
-        if (hPin) cudaFreeHost(hPin);
-        if (flushBuf) cudaFree(flushBuf);
-        destroyGraph();
-        if (dLoop) cudaFree(dLoop);
-        for (auto e : evPool) cudaEventDestroy(e);
-        for (auto& e : ev) if (e) cudaEventDestroy(e);
-        if (st) cudaStreamDestroy(st);
     }
 
-    int init(const phx_grid* g) {
+    int setup(const phx_grid* g) {
         if (!g || g->nx <= 0 || g->ny <= 0 || g->nz <= 0 || !(g->dx > 0)) { err = "invalid grid dimensions"; return PHX_ERR_INVALID; }
         long long N = (long long)g->nx * g->ny * g->nz;
         if (N > 20000000LL) { err = "grid size out of range (the reference caps N at 20,000,000)"; return PHX_ERR_INVALID; }
@@ -114,109 +103,88 @@ public:
         Pb0.assign(NN, 101325.0);
         Z = computeZones(geo, Pb0);
         MG = buildMultigrid(geo, DENSE_MAX);
-        maxLevels = (int)MG.lv.size();
-        return allocate();
+        return PHX_OK;
     }
 
-    template <class T>
-    static T* carve(char*& base, size_t& off, size_t n) {
-        off = (off + 255) & ~(size_t)255;
-        T* p = base ? (T*)(base + off) : nullptr;
-        off += n * sizeof(T);
-        return p;
-    }
-
-    int allocate() {
+    // device bytes the scenario will take (the arena layout without memory)
+    size_t layout(char* base) {
         const int N = geo.N(), NX = geo.NX(), NY = geo.NY(), NZ = geo.NZ();
         const int nl = (int)MG.lv.size();
         const int partStride = (N + TPB - 1) / TPB + 1;
-        for (int pass = 0; pass < 2; ++pass) {
-            char* base = pass == 0 ? nullptr : arena;
-            size_t off = 0;
-            Scn<R>& s = h;
-            s.blocked = carve<uint8_t>(base, off, N);
-            s.fx = carve<R>(base, off, NX); s.fy = carve<R>(base, off, NY); s.fz = carve<R>(base, off, NZ);
-            s.ax = carve<R>(base, off, NX); s.ay = carve<R>(base, off, NY); s.az = carve<R>(base, off, NZ);
-            s.a0x = carve<R>(base, off, NX); s.a0y = carve<R>(base, off, NY); s.a0z = carve<R>(base, off, NZ);
-            s.lx = nullptr; s.ly = nullptr; s.lz = nullptr;
-            s.diag = carve<R>(base, off, N);
-            s.zone = carve<int>(base, off, N);
-            const int nZ = (int)Z.zoneP.size(), nC = (int)Z.closed.size();
-            s.zoneOpen = carve<uint8_t>(base, off, nZ + 1);
-            s.closedZone = carve<int>(base, off, nC + 1);
-            s.closedStart = carve<int>(base, off, nC + 1);
-            s.closedCells = carve<int>(base, off, Z.closedCells.size() + 1);
-            s.zoneP = carve<double>(base, off, nZ + 1);
-            s.zoneVol = carve<double>(base, off, nZ + 1);
-            s.zoneDP = carve<double>(base, off, nZ + 1);
-            s.zoneShift = carve<double>(base, off, nZ + 1);
-            s.zoneMean = carve<double>(base, off, nZ + 1);
-            s.u = carve<R>(base, off, NX); s.v = carve<R>(base, off, NY); s.w = carve<R>(base, off, NZ);
-            s.u2 = carve<R>(base, off, NX); s.v2 = carve<R>(base, off, NY); s.w2 = carve<R>(base, off, NZ);
-            for (int q = 0; q < NSC; ++q) { s.sc[q] = carve<R>(base, off, N); s.sc2[q] = carve<R>(base, off, N); }
-            s.p = carve<R>(base, off, N); s.S = carve<R>(base, off, N); s.nu = carve<R>(base, off, N);
-            s.Pb = carve<R>(base, off, N); s.Q = carve<R>(base, off, N); s.Qr = carve<R>(base, off, N);
-            s.hrr = carve<R>(base, off, N); s.massSrc = carve<R>(base, off, N);
-            s.lit = carve<uint8_t>(base, off, N); s.lit2 = carve<uint8_t>(base, off, N); s.pilot = carve<uint8_t>(base, off, N);
-            for (int q = 0; q < 9; ++q) s.tmp[q] = carve<R>(base, off, N);
-            s.b = carve<R>(base, off, N); s.r = carve<R>(base, off, N); s.z = carve<R>(base, off, N);
-            dbuf[0] = carve<R>(base, off, N); dbuf[1] = carve<R>(base, off, N);
-            s.d = dbuf[0];
-            s.q = carve<R>(base, off, N);
-            s.p64 = kMixed ? carve<double>(base, off, N) : nullptr;
-            s.mixed = kMixed ? 1 : 0;
-            s.innerMax = INNER_MAX;
-            s.innerRel = INNER_REL;
-            s.outerMax = OUTER_MAX;
-            s.nLevels = nl;
-            for (int l = 0; l < nl; ++l) {
-                const MgLevel& L = MG.lv[l];
-                Level<R>& D = s.lv[l];
-                D.n = L.n;
-                if (l == 0) {
-                    D.diag = s.diag;
-                    D.x = s.z; D.y = nullptr; D.b = s.r;
-                    D.rowStart = nullptr; D.col = nullptr; D.val = nullptr;
-                } else {
-                    D.rowStart = carve<int>(base, off, L.rowStart.size());
-                    D.col = carve<int>(base, off, L.col.size() + 1);
-                    D.val = carve<R>(base, off, L.val.size() + 1);
-                    D.diag = carve<R>(base, off, L.n + 1);
-                    D.x = carve<R>(base, off, L.n + 1); D.y = carve<R>(base, off, L.n + 1); D.b = carve<R>(base, off, L.n + 1);
-                }
-                D.agg = L.agg.empty() ? nullptr : carve<int>(base, off, L.agg.size());
-                D.childStart = L.childStart.empty() ? nullptr : carve<int>(base, off, L.childStart.size());
-                D.child = L.child.empty() ? nullptr : carve<int>(base, off, L.child.size() + 1);
-                D.dense = L.dense.empty() ? nullptr : carve<R>(base, off, L.dense.size());
+        size_t off = 0;
+        Scn<R>& s = h;
+        s.blocked = carve<uint8_t>(base, off, N);
+        s.fx = carve<R>(base, off, NX); s.fy = carve<R>(base, off, NY); s.fz = carve<R>(base, off, NZ);
+        s.ax = carve<R>(base, off, NX); s.ay = carve<R>(base, off, NY); s.az = carve<R>(base, off, NZ);
+        s.a0x = carve<R>(base, off, NX); s.a0y = carve<R>(base, off, NY); s.a0z = carve<R>(base, off, NZ);
+        s.lx = nullptr; s.ly = nullptr; s.lz = nullptr;
+        s.diag = carve<R>(base, off, N);
+        s.zone = carve<int>(base, off, N);
+        const int nZ = (int)Z.zoneP.size(), nC = (int)Z.closed.size();
+        s.zoneOpen = carve<uint8_t>(base, off, nZ + 1);
+        s.closedZone = carve<int>(base, off, nC + 1);
+        s.closedStart = carve<int>(base, off, nC + 1);
+        s.closedCells = carve<int>(base, off, Z.closedCells.size() + 1);
+        s.zoneP = carve<double>(base, off, nZ + 1);
+        s.zoneVol = carve<double>(base, off, nZ + 1);
+        s.zoneDP = carve<double>(base, off, nZ + 1);
+        s.zoneShift = carve<double>(base, off, nZ + 1);
+        s.zoneMean = carve<double>(base, off, nZ + 1);
+        s.u = carve<R>(base, off, NX); s.v = carve<R>(base, off, NY); s.w = carve<R>(base, off, NZ);
+        s.u2 = carve<R>(base, off, NX); s.v2 = carve<R>(base, off, NY); s.w2 = carve<R>(base, off, NZ);
+        for (int q = 0; q < NSC; ++q) { s.sc[q] = carve<R>(base, off, N); s.sc2[q] = carve<R>(base, off, N); }
+        s.p = carve<R>(base, off, N); s.S = carve<R>(base, off, N); s.nu = carve<R>(base, off, N);
+        s.Pb = carve<R>(base, off, N); s.Q = carve<R>(base, off, N); s.Qr = carve<R>(base, off, N);
+        s.hrr = carve<R>(base, off, N); s.massSrc = carve<R>(base, off, N);
+        s.lit = carve<uint8_t>(base, off, N); s.lit2 = carve<uint8_t>(base, off, N); s.pilot = carve<uint8_t>(base, off, N);
+        for (int q = 0; q < 9; ++q) s.tmp[q] = carve<R>(base, off, N);
+        s.b = carve<R>(base, off, N); s.r = carve<R>(base, off, N); s.z = carve<R>(base, off, N);
+        dbuf[0] = carve<R>(base, off, N); dbuf[1] = carve<R>(base, off, N);
+        s.d = dbuf[0];
+        s.q = carve<R>(base, off, N);
+        s.p64 = kMixed ? carve<double>(base, off, N) : nullptr;
+        s.nLevels = nl;
+        for (int l = 0; l < nl; ++l) {
+            const MgLevel& L = MG.lv[l];
+            Level<R>& D = s.lv[l];
+            D.n = L.n;
+            if (l == 0) {
+                D.diag = s.diag;
+                D.x = s.z; D.y = nullptr; D.b = s.r;
+                D.rowStart = nullptr; D.col = nullptr; D.val = nullptr;
+            } else {
+                D.rowStart = carve<int>(base, off, L.rowStart.size());
+                D.col = carve<int>(base, off, L.col.size() + 1);
+                D.val = carve<R>(base, off, L.val.size() + 1);
+                D.diag = carve<R>(base, off, L.n + 1);
+                D.x = carve<R>(base, off, L.n + 1); D.y = carve<R>(base, off, L.n + 1); D.b = carve<R>(base, off, L.n + 1);
             }
-            s.sv = carve<double>(base, off, SV_COUNT);
-            s.part = carve<double>(base, off, (size_t)PS_COUNT * partStride);
-            s.partStride = partStride;
-            s.cnt = carve<unsigned>(base, off, PS_COUNT + 4);
-            dS = carve<Scn<R>>(base, off, 1);
-            dD = carve<R*>(base, off, 2);
-            dDomStart = carve<int>(base, off, D_COUNT * 2);
-            if (pass == 0) {
-                arenaBytes = off + 256;
-                cudaError_t e = cudaMalloc(&arena, arenaBytes);
-                if (e != cudaSuccess) {
-                    arena = nullptr;
-                    err = std::string("device allocation of ") + std::to_string(arenaBytes) + " bytes failed: " + cudaGetErrorString(e);
-                    return PHX_ERR_OOM;
-                }
-            }
+            D.agg = L.agg.empty() ? nullptr : carve<int>(base, off, L.agg.size());
+            D.childStart = (l == 0 || L.childStart.empty()) ? nullptr : carve<int>(base, off, L.childStart.size());
+            D.child = (l == 0 || L.child.empty()) ? nullptr : carve<int>(base, off, L.child.size() + 1);
+            D.dense = L.dense.empty() ? nullptr : carve<R>(base, off, L.dense.size());
         }
-        PHX_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-        PHX_CK(cudaMallocHost(&hPin, 4096));
-        for (auto& e : ev) PHX_CK(cudaEventCreate(&e));
-        PHX_CK(cudaMemsetAsync(arena, 0, arenaBytes, st));
-        return upload();
+        s.sv = carve<double>(base, off, SV_COUNT);
+        s.part = carve<double>(base, off, (size_t)PS_COUNT * partStride);
+        s.partStride = partStride;
+        s.cnt = carve<unsigned>(base, off, PS_COUNT + 4);
+        return off + 256;
     }
 
-    // host -> device uploads; device pointers of read-only arrays are const in
-    // the descriptor, so they are cast back here
+    int allocate() {
+        arenaBytes = layout(nullptr);
+        cudaError_t e = cudaMalloc(&arena, arenaBytes);
+        if (e != cudaSuccess) {
+            arena = nullptr;
+            err = std::string("device allocation of ") + std::to_string(arenaBytes) + " bytes failed: " + cudaGetErrorString(e);
+            return PHX_ERR_OOM;
+        }
+        layout(arena);
+        return PHX_OK;
+    }
+
     template <class T>
-    int put(const T* dstc, const std::vector<double>& src) {
+    int put(cudaStream_t st, const T* dstc, const std::vector<double>& src) {
         using U = typename std::remove_const<T>::type;
         U* dst = const_cast<U*>(dstc);
         std::vector<U> tmp(src.begin(), src.end());
@@ -225,20 +193,18 @@ public:
         return PHX_OK;
     }
     template <class T, class V>
-    int putRaw(const T* dstc, const V* src, size_t n) {
+    int putRaw(cudaStream_t st, const T* dstc, const V* src, size_t n) {
         static_assert(sizeof(T) == sizeof(V), "element size");
         void* dst = const_cast<void*>((const void*)dstc);
         if (n) PHX_CK(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyHostToDevice, st));
         PHX_CK(cudaStreamSynchronize(st));
         return PHX_OK;
     }
-    int fillR(R* dst, size_t n, double v) { return put<R>(dst, std::vector<double>(n, v)); }
 
-#define PHX_TRY(x) do { int r_ = (x); if (r_) return r_; } while (0)
-
-    int upload() {
+    int upload(cudaStream_t st) {
         const int N = geo.N();
         Scn<R>& s = h;
+        PHX_CK(cudaMemsetAsync(arena, 0, arenaBytes, st));
         s.nx = geo.nx; s.ny = geo.ny; s.nz = geo.nz; s.N = N; s.NX = geo.NX(); s.NY = geo.NY(); s.NZ = geo.NZ();
         s.dx = geo.dx; s.ox = geo.ox; s.oy = geo.oy; s.oz = geo.oz;
         s.cfl = cfl; s.dtMaxP = dtMaxP; s.tol = tol; s.relTol = relTol; s.maxIters = maxIters; s.radiationOn = radiationOn;
@@ -246,133 +212,267 @@ public:
         s.windSpeed = geo.windSpeed; s.windSin = std::sin(th); s.windCos = std::cos(th); s.windExp = geo.windExp;
         s.nZones = (int)Z.zoneP.size();
         s.nClosed = (int)Z.closed.size();
-        PHX_TRY(putRaw(s.blocked, geo.blocked.data(), N));
-        PHX_TRY(put(s.fx, geo.fx)); PHX_TRY(put(s.fy, geo.fy)); PHX_TRY(put(s.fz, geo.fz));
-        PHX_TRY(put(s.ax, geo.ax)); PHX_TRY(put(s.ay, geo.ay)); PHX_TRY(put(s.az, geo.az));
-        PHX_TRY(put(s.a0x, MG.a0x)); PHX_TRY(put(s.a0y, MG.a0y)); PHX_TRY(put(s.a0z, MG.a0z));
-        PHX_TRY(put(s.diag, MG.lv[0].diag));
-        PHX_TRY(putRaw(const_cast<int*>(s.zone), Z.zone.data(), N));
-        PHX_TRY(putRaw(const_cast<uint8_t*>(s.zoneOpen), Z.zoneOpen.data(), Z.zoneOpen.size()));
-        PHX_TRY(putRaw(const_cast<int*>(s.closedZone), Z.closed.data(), Z.closed.size()));
-        PHX_TRY(putRaw(const_cast<int*>(s.closedStart), Z.closedStart.data(), Z.closedStart.size()));
-        PHX_TRY(putRaw(const_cast<int*>(s.closedCells), Z.closedCells.data(), Z.closedCells.size()));
-        PHX_TRY(putRaw(s.zoneP, Z.zoneP.data(), Z.zoneP.size()));
-        PHX_TRY(putRaw(s.zoneVol, Z.zoneVol.data(), Z.zoneVol.size()));
+        s.mixed = kMixed ? 1 : 0;
+        PHX_TRY(putRaw(st, s.blocked, geo.blocked.data(), N));
+        PHX_TRY(put(st, s.fx, geo.fx)); PHX_TRY(put(st, s.fy, geo.fy)); PHX_TRY(put(st, s.fz, geo.fz));
+        PHX_TRY(put(st, s.ax, geo.ax)); PHX_TRY(put(st, s.ay, geo.ay)); PHX_TRY(put(st, s.az, geo.az));
+        PHX_TRY(put(st, s.a0x, MG.a0x)); PHX_TRY(put(st, s.a0y, MG.a0y)); PHX_TRY(put(st, s.a0z, MG.a0z));
+        PHX_TRY(put(st, s.diag, MG.lv[0].diag));
+        PHX_TRY(putRaw(st, s.zone, Z.zone.data(), N));
+        PHX_TRY(putRaw(st, s.zoneOpen, Z.zoneOpen.data(), Z.zoneOpen.size()));
+        PHX_TRY(putRaw(st, s.closedZone, Z.closed.data(), Z.closed.size()));
+        PHX_TRY(putRaw(st, s.closedStart, Z.closedStart.data(), Z.closedStart.size()));
+        PHX_TRY(putRaw(st, s.closedCells, Z.closedCells.data(), Z.closedCells.size()));
+        PHX_TRY(putRaw(st, s.zoneP, Z.zoneP.data(), Z.zoneP.size()));
+        PHX_TRY(putRaw(st, s.zoneVol, Z.zoneVol.data(), Z.zoneVol.size()));
         // initial state (src/sim/discretize.cpp:28-31)
         const double amb[NSC] = {K_T0, K_YO2_AMB, 0, 0, 0, 0, K_YCO2_AMB, K_YH2O_AMB, 0, 0};
-        for (int q = 0; q < NSC; ++q) { PHX_TRY(fillR(s.sc[q], N, amb[q])); PHX_TRY(fillR(s.sc2[q], N, amb[q])); }
-        PHX_TRY(put(s.Pb, Pb0));
+        for (int q = 0; q < NSC; ++q) {
+            PHX_TRY(put(st, s.sc[q], std::vector<double>(N, amb[q])));
+            PHX_TRY(put(st, s.sc2[q], std::vector<double>(N, amb[q])));
+        }
+        PHX_TRY(put(st, s.Pb, Pb0));
         for (int l = 1; l < (int)MG.lv.size(); ++l) {
             const MgLevel& L = MG.lv[l];
             Level<R>& D = s.lv[l];
-            PHX_TRY(putRaw(const_cast<int*>(D.rowStart), L.rowStart.data(), L.rowStart.size()));
-            PHX_TRY(putRaw(const_cast<int*>(D.col), L.col.data(), L.col.size()));
-            PHX_TRY(put(const_cast<R*>(D.val), L.val));
-            PHX_TRY(put(const_cast<R*>(D.diag), L.diag));
+            PHX_TRY(putRaw(st, D.rowStart, L.rowStart.data(), L.rowStart.size()));
+            PHX_TRY(putRaw(st, D.col, L.col.data(), L.col.size()));
+            PHX_TRY(put(st, D.val, L.val));
+            PHX_TRY(put(st, D.diag, L.diag));
         }
         for (int l = 0; l < (int)MG.lv.size(); ++l) {
             const MgLevel& L = MG.lv[l];
             Level<R>& D = s.lv[l];
-            if (D.agg) PHX_TRY(putRaw(const_cast<int*>(D.agg), L.agg.data(), L.agg.size()));
-            if (D.childStart) PHX_TRY(putRaw(const_cast<int*>(D.childStart), L.childStart.data(), L.childStart.size()));
-            if (D.child) PHX_TRY(putRaw(const_cast<int*>(D.child), L.child.data(), L.child.size()));
-            if (D.dense) PHX_TRY(put(const_cast<R*>(D.dense), L.dense));
+            if (D.agg) PHX_TRY(putRaw(st, D.agg, L.agg.data(), L.agg.size()));
+            if (D.childStart) PHX_TRY(putRaw(st, D.childStart, L.childStart.data(), L.childStart.size()));
+            if (D.child) PHX_TRY(putRaw(st, D.child, L.child.data(), L.child.size()));
+            if (D.dense) PHX_TRY(put(st, D.dense, L.dense));
         }
-        R* dd[2] = {dbuf[0], dbuf[1]};
-        PHX_TRY(putRaw(dD, dd, 2));
-        PHX_TRY(buildDomains());
-        return pushDescriptor();
+        return PHX_OK;
     }
 
-    int pushDescriptor() {
-        h.nsrc = (int)(ignitions.size() + burners.size());
-        int q = 0;
-        for (auto& s : ignitions) h.src[q++] = s;
-        for (auto& s : burners) h.src[q++] = s;
-        PHX_CK(cudaMemcpyAsync(dS, &h, sizeof(Scn<R>), cudaMemcpyHostToDevice, st));
+    // CTAs of each domain of this scenario
+    void tiles(int* t) const {
+        const int N = geo.N(), nx = geo.nx, ny = geo.ny, nz = geo.nz;
+        auto cdiv = [](long long a, long long b) { return (int)((a + b - 1) / b); };
+        for (int d = 0; d < D_COUNT; ++d) t[d] = 0;
+        t[D_ONE] = 1;
+        t[D_CELLS] = cdiv(N, TPB);
+        t[D_HALF] = cdiv((long long)((nx + 1) / 2) * ny * nz, TPB);
+        t[D_BLK] = cdiv((long long)((nx + 1) / 2) * ((ny + 1) / 2) * ((nz + 1) / 2), TPB);
+        t[D_FX] = cdiv(geo.NX(), TPB);
+        t[D_FY] = cdiv(geo.NY(), TPB);
+        t[D_FZ] = cdiv(geo.NZ(), TPB);
+        t[D_BX] = cdiv((long long)ny * nz * 2, TPB);
+        t[D_BY] = cdiv((long long)nx * nz * 2, TPB);
+        t[D_BZ] = cdiv((long long)nx * ny, TPB);
+        t[D_CZ] = (int)Z.closed.size();
+        t[D_CC] = cdiv((long long)Z.closedCells.size(), TPB);
+        const int nl = (int)MG.lv.size();
+        const MgLevel& Lc = MG.lv[nl - 1];
+        t[D_CO_DENSE] = Lc.dense.empty() ? 0 : cdiv(Lc.n, TPB / 32);
+        t[D_CO_SERIAL] = Lc.dense.empty() ? 1 : 0;
+        for (int l = 1; l < MAX_LEVELS; ++l) {
+            t[D_LV0 + l] = (l < nl - 1) ? cdiv(MG.lv[l].n, TPB) : 0;
+            t[D_RS0 + l] = (l + 1 <= nl - 1) ? cdiv(MG.lv[l + 1].n, TPB) : 0;
+        }
+    }
+};
+
+template <class R>
+class Ctx : public CtxBase {
+public:
+    // the float instantiation is the mixed path: FP32 fields and stencils, FP64
+    // refinement of the pressure solve, FP64 dots and global sums
+    static constexpr bool kMixed = std::is_same<R, float>::value;
+    static constexpr int INNER_MAX = 10;        // inner FP32 CG iterations per refinement pass
+    static constexpr double INNER_REL = 1e-4;   // inner stop relative to the pass's starting residual
+    static constexpr int OUTER_MAX = 40;
+
+    std::vector<std::unique_ptr<Scenario<R>>> sc;
+    cudaStream_t st = nullptr;
+    // batch-wide device tables
+    int cap = 0;                 // scenario capacity of the tables
+    char* tab = nullptr;
+    Scn<R>* dS = nullptr;        // descriptors
+    R** dD = nullptr;            // CG direction buffers, 2 per scenario
+    int* dDomStart = nullptr;    // D_COUNT x (cap + 1)
+    double* dDtMax = nullptr;    // per-scenario dtMax of the step
+    int* dLoop = nullptr;        // loop counters of the graph's while nodes
+    double* hPin = nullptr;      // pinned scratch for read-backs
+    Dom dom[D_COUNT];
+    int maxLevels = 0;
+    bool anyClosed = false;
+    bool tablesDirty = true;
+    int launches = 0;
+    cudaEvent_t ev[4] = {};
+
+    ~Ctx() override {
+        if (st) cudaStreamSynchronize(st);
+        destroyGraph();
+        sc.clear();
+        if (tab) cudaFree(tab);
+        if (hPin) cudaFreeHost(hPin);
+        if (flushBuf) cudaFree(flushBuf);
+        for (auto e : evPool) cudaEventDestroy(e);
+        for (auto& e : ev) if (e) cudaEventDestroy(e);
+        if (st) cudaStreamDestroy(st);
+    }
+
+    int nscn() const { return (int)sc.size(); }
+
+    int initStream() {
+        if (st) return PHX_OK;
+        PHX_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        PHX_CK(cudaMallocHost(&hPin, 8192 * sizeof(double)));
+        for (auto& e : ev) PHX_CK(cudaEventCreate(&e));
+        return PHX_OK;
+    }
+
+    // ---- membership ---------------------------------------------------------------
+    int addScenario(const phx_grid* g, int* id) override {
+        auto s = std::make_unique<Scenario<R>>();
+        int r = s->setup(g);   // validation and host set-up first: no device needed to reject bad input
+        if (r == PHX_OK) {
+            r = initStream();
+            if (r != PHX_OK) return r;
+        }
+        if (r == PHX_OK) r = s->allocate();
+        if (r == PHX_OK) r = s->upload(st);
+        if (r != PHX_OK) { err = s->err.empty() ? err : s->err; return r; }
+        sc.push_back(std::move(s));
+        if (id) *id = nscn() - 1;
+        tablesDirty = true;
+        return PHX_OK;
+    }
+
+    int removeScenario(int s) override {
+        if (s < 0 || s >= nscn()) { err = "no such scenario"; return PHX_ERR_INVALID; }
+        PHX_CK(cudaStreamSynchronize(st));
+        sc.erase(sc.begin() + s);
+        tablesDirty = true;
+        return PHX_OK;
+    }
+
+    int scenarioCount() const override { return nscn(); }
+    size_t scenarioBytes(int s) const override { return s >= 0 && s < nscn() ? sc[s]->arenaBytes : 0; }
+
+    // batch tables: descriptors, domain prefixes, CG buffers; invalidates the graph
+    int rebuildTables() {
+        destroyGraph();
+        const int n = nscn();
+        if (n > cap || !tab) {
+            if (tab) { PHX_CK(cudaStreamSynchronize(st)); cudaFree(tab); tab = nullptr; }
+            cap = std::max(n, std::max(1, cap * 2));
+            char* base = nullptr;
+            for (int pass = 0; pass < 2; ++pass) {
+                size_t off = 0;
+                dS = carve<Scn<R>>(base, off, cap);
+                dD = carve<R*>(base, off, 2 * cap);
+                dDomStart = carve<int>(base, off, (size_t)D_COUNT * (cap + 1));
+                dDtMax = carve<double>(base, off, cap);
+                dLoop = carve<int>(base, off, 4);
+                if (pass == 0) {
+                    cudaError_t e = cudaMalloc(&tab, off + 256);
+                    if (e != cudaSuccess) { tab = nullptr; err = "device allocation of the batch tables failed"; return PHX_ERR_OOM; }
+                    base = tab;
+                }
+            }
+        }
+        std::vector<int> starts((size_t)D_COUNT * (n + 1), 0);
+        std::vector<R*> dd(2 * std::max(n, 1), nullptr);
+        maxLevels = 0;
+        anyClosed = false;
+        int t[D_COUNT];
+        for (int s = 0; s < n; ++s) {
+            Scenario<R>& S = *sc[s];
+            S.tiles(t);
+            for (int d = 0; d < D_COUNT; ++d) starts[(size_t)d * (n + 1) + s + 1] = starts[(size_t)d * (n + 1) + s] + t[d];
+            dd[2 * s] = S.dbuf[0];
+            dd[2 * s + 1] = S.dbuf[1];
+            maxLevels = std::max(maxLevels, (int)S.MG.lv.size());
+            anyClosed |= !S.Z.closed.empty();
+            S.h.dtMaxArg = dDtMax + s;
+        }
+        for (int d = 0; d < D_COUNT; ++d) {
+            dom[d].start = dDomStart + (size_t)d * (n + 1);
+            dom[d].nscn = n;
+            dom[d].total = starts[(size_t)d * (n + 1) + n];
+        }
+        PHX_CK(cudaMemcpyAsync(dDomStart, starts.data(), starts.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        if (n > 0) PHX_CK(cudaMemcpyAsync(dD, dd.data(), 2 * n * sizeof(R*), cudaMemcpyHostToDevice, st));
+        tablesDirty = false;
+        for (int s = 0; s < n; ++s) PHX_TRY(pushDescriptor(s, false));
         PHX_CK(cudaStreamSynchronize(st));
         return PHX_OK;
     }
 
-    int buildDomains() {
-        const int N = geo.N(), nx = geo.nx, ny = geo.ny, nz = geo.nz;
-        auto cdiv = [](long long a, long long b) { return (int)((a + b - 1) / b); };
-        int tiles[D_COUNT] = {};
-        tiles[D_ONE] = 1;
-        tiles[D_CELLS] = cdiv(N, TPB);
-        tiles[D_HALF] = cdiv((long long)((nx + 1) / 2) * ny * nz, TPB);
-        tiles[D_BLK] = cdiv((long long)((nx + 1) / 2) * ((ny + 1) / 2) * ((nz + 1) / 2), TPB);
-        tiles[D_FX] = cdiv(geo.NX(), TPB);
-        tiles[D_FY] = cdiv(geo.NY(), TPB);
-        tiles[D_FZ] = cdiv(geo.NZ(), TPB);
-        tiles[D_BX] = cdiv((long long)ny * nz * 2, TPB);
-        tiles[D_BY] = cdiv((long long)nx * nz * 2, TPB);
-        tiles[D_BZ] = cdiv((long long)nx * ny, TPB);
-        tiles[D_CZ] = (int)Z.closed.size();
-        tiles[D_CC] = cdiv((long long)Z.closedCells.size(), TPB);
-        const int nl = (int)MG.lv.size();
-        const MgLevel& Lc = MG.lv[nl - 1];
-        tiles[D_CO_DENSE] = Lc.dense.empty() ? 0 : cdiv(Lc.n, TPB / 32);
-        tiles[D_CO_SERIAL] = Lc.dense.empty() ? 1 : 0;
-        for (int l = 1; l < MAX_LEVELS; ++l) {
-            tiles[D_LV0 + l] = (l < nl - 1) ? cdiv(MG.lv[l].n, TPB) : 0;
-            tiles[D_RS0 + l] = (l + 1 <= nl - 1) ? cdiv(MG.lv[l + 1].n, TPB) : 0;
-        }
-        std::vector<int> starts(D_COUNT * 2);
-        for (int d = 0; d < D_COUNT; ++d) {
-            starts[2 * d] = 0;
-            starts[2 * d + 1] = tiles[d];
-            dom[d].start = dDomStart + 2 * d;
-            dom[d].nscn = 1;
-            dom[d].total = tiles[d];
-        }
-        return putRaw(dDomStart, starts.data(), starts.size());
+    int ensureTables() { return tablesDirty ? rebuildTables() : PHX_OK; }
+
+    int pushDescriptor(int s, bool sync = true) {
+        Scenario<R>& S = *sc[s];
+        S.h.nsrc = (int)(S.ignitions.size() + S.burners.size());
+        int q = 0;
+        for (auto& x : S.ignitions) S.h.src[q++] = x;
+        for (auto& x : S.burners) S.h.src[q++] = x;
+        if (tablesDirty) return PHX_OK;   // uploaded with the tables
+        PHX_CK(cudaMemcpyAsync(dS + s, &S.h, sizeof(Scn<R>), cudaMemcpyHostToDevice, st));
+        if (sync) PHX_CK(cudaStreamSynchronize(st));
+        return PHX_OK;
     }
 
-    // ---- sources ---------------------------------------------------------------
-    int addBurner(double x0, double y0, double x1, double y1, double z, double peakW, double rampS, double start,
-                  double duration, int* index) override {
+    int checkScn(int s) {
+        if (s < 0 || s >= nscn()) { err = "no such scenario"; return PHX_ERR_INVALID; }
+        return PHX_OK;
+    }
+
+    // ---- sources ------------------------------------------------------------------
+    int addBurner(int s, double x0, double y0, double x1, double y1, double z, double peakW, double rampS,
+                  double start, double duration, int* index) override {
         if (index) *index = -1;
-        std::vector<int> cells = burnerCells(geo, x0, y0, x1, y1, z);
+        PHX_TRY(checkScn(s));
+        Scenario<R>& S = *sc[s];
+        std::vector<int> cells = burnerCells(S.geo, x0, y0, x1, y1, z);
         if (cells.empty()) { err = "burner covers no gas cell"; return PHX_ERR_INVALID; }
-        if ((int)(ignitions.size() + burners.size()) >= MAX_SRC) { err = "too many burners and ignitions (16)"; return PHX_ERR_INVALID; }
-        Src s{};
-        s.kind = 1;
-        s.i0 = s.j0 = 1 << 30; s.i1 = s.j1 = -1; s.k = -1;
+        if ((int)(S.ignitions.size() + S.burners.size()) >= MAX_SRC) { err = "too many burners and ignitions (16)"; return PHX_ERR_INVALID; }
+        Src b{};
+        b.kind = 1;
+        b.i0 = b.j0 = 1 << 30; b.i1 = b.j1 = -1; b.k = -1;
         for (int c : cells) {
-            int i = c % geo.nx, j = (c / geo.nx) % geo.ny, k = c / (geo.nx * geo.ny);
-            s.i0 = std::min(s.i0, i); s.i1 = std::max(s.i1, i); s.j0 = std::min(s.j0, j); s.j1 = std::max(s.j1, j);
-            if (s.k >= 0 && s.k != k) { err = "burner cells span several layers"; return PHX_ERR_UNSUPPORTED; }
-            s.k = k;
+            int i = c % S.geo.nx, j = (c / S.geo.nx) % S.geo.ny, k = c / (S.geo.nx * S.geo.ny);
+            b.i0 = std::min(b.i0, i); b.i1 = std::max(b.i1, i); b.j0 = std::min(b.j0, j); b.j1 = std::max(b.j1, j);
+            if (b.k >= 0 && b.k != k) { err = "burner cells span several layers"; return PHX_ERR_UNSUPPORTED; }
+            b.k = k;
         }
         // the device selects the unblocked cells of the box: check that this is the same set
         size_t inBox = 0;
-        for (int j = s.j0; j <= s.j1; ++j)
-            for (int i = s.i0; i <= s.i1; ++i) inBox += !geo.blocked[geo.cell(i, j, s.k)];
+        for (int j = b.j0; j <= b.j1; ++j)
+            for (int i = b.i0; i <= b.i1; ++i) inBox += !S.geo.blocked[S.geo.cell(i, j, b.k)];
         if (inBox != cells.size()) { err = "burner cells do not form a box of gas cells"; return PHX_ERR_UNSUPPORTED; }
-        s.ncells = (int)cells.size();
-        s.peakW = peakW; s.rampS = rampS; s.start = start; s.duration = duration;
-        burners.push_back(s);
-        if (index) *index = (int)burners.size() - 1;
-        return pushDescriptor();
+        b.ncells = (int)cells.size();
+        b.peakW = peakW; b.rampS = rampS; b.start = start; b.duration = duration;
+        S.burners.push_back(b);
+        if (index) *index = (int)S.burners.size() - 1;
+        return pushDescriptor(s);
     }
 
-    int addIgnition(int cell, double power, double duration) override {
-        if (cell < 0 || cell >= geo.N()) return PHX_OK;   // the reference ignores it
-        if ((int)(ignitions.size() + burners.size()) >= MAX_SRC) { err = "too many burners and ignitions (16)"; return PHX_ERR_INVALID; }
-        PHX_CK(cudaMemcpyAsync(hPin, h.sv + SV_TIME, sizeof(double), cudaMemcpyDeviceToHost, st));
+    int addIgnition(int s, int cell, double power, double duration) override {
+        PHX_TRY(checkScn(s));
+        Scenario<R>& S = *sc[s];
+        if (cell < 0 || cell >= S.geo.N()) return PHX_OK;   // the reference ignores it
+        if ((int)(S.ignitions.size() + S.burners.size()) >= MAX_SRC) { err = "too many burners and ignitions (16)"; return PHX_ERR_INVALID; }
+        PHX_CK(cudaMemcpyAsync(hPin, S.h.sv + SV_TIME, sizeof(double), cudaMemcpyDeviceToHost, st));
         PHX_CK(cudaStreamSynchronize(st));
-        Src s{};
-        s.kind = 0;
-        s.i0 = s.i1 = cell % geo.nx; s.j0 = s.j1 = (cell / geo.nx) % geo.ny; s.k = cell / (geo.nx * geo.ny);
-        s.ncells = 1;
-        s.power = power; s.start = hPin[0]; s.duration = duration;
-        ignitions.push_back(s);
-        return pushDescriptor();
+        Src x{};
+        x.kind = 0;
+        x.i0 = x.i1 = cell % S.geo.nx; x.j0 = x.j1 = (cell / S.geo.nx) % S.geo.ny; x.k = cell / (S.geo.nx * S.geo.ny);
+        x.ncells = 1;
+        x.power = power; x.start = hPin[0]; x.duration = duration;
+        S.ignitions.push_back(x);
+        return pushDescriptor(s);
     }
 
-    // ---- launch helpers -------------------------------------------------------
-    // ---- profiling: CUDA events around every launch, summed per kernel name
+    // ---- launch helpers -------------------------------------------------------------
     bool prof = false;
     std::vector<cudaEvent_t> evPool;
     std::vector<std::pair<const char*, int>> evUse;   // (kernel name, first event index)
@@ -417,23 +517,29 @@ public:
     }
 
     void swapHost(int what) {
-        if (what & 1) std::swap(h.lit, h.lit2);
-        if (what & 2) { std::swap(h.u, h.u2); std::swap(h.v, h.v2); std::swap(h.w, h.w2); }
-        if (what & 4) for (int q = 0; q < NSC; ++q) std::swap(h.sc[q], h.sc2[q]);
+        for (auto& S : sc) {
+            Scn<R>& h = S->h;
+            if (what & 1) std::swap(h.lit, h.lit2);
+            if (what & 2) { std::swap(h.u, h.u2); std::swap(h.v, h.v2); std::swap(h.w, h.w2); }
+            if (what & 4) for (int q = 0; q < NSC; ++q) std::swap(h.sc[q], h.sc2[q]);
+        }
     }
     void swapBoth(int what) {
         launch("k_swap", D_ONE, 32, k_swap<R>, dS, dom[D_ONE], what);
         swapHost(what);
     }
 
-    // stages -----------------------------------------------------------------
-    void stBegin(bool computeDt, double dtMaxOrDt) {
-        // dtMax travels through the scalar block
-        if (computeDt) {
-            hPin[0] = dtMaxOrDt;
-            cudaMemcpyAsync(h.sv + SV_DTMAX_ARG, hPin, sizeof(double), cudaMemcpyHostToDevice, st);
-        }
-        launch("k_begin", D_ONE, 32, k_begin<R>, (const Scn<R>*)dS, dom[D_ONE], computeDt ? 1 : 0, dtMaxOrDt);
+    int setDtMax(double dtMax, const double* per) {
+        std::vector<double> v(nscn(), dtMax);
+        if (per) for (int s = 0; s < nscn(); ++s) v[s] = per[s];
+        // pageable source: staged at the call, safe to reuse at once
+        if (!v.empty()) PHX_CK(cudaMemcpyAsync(dDtMax, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+        return PHX_OK;
+    }
+
+    // ---- stages ---------------------------------------------------------------------
+    void stBegin(bool computeDt, double dt) {
+        launch("k_begin", D_ONE, 32, k_begin<R>, (const Scn<R>*)dS, dom[D_ONE], computeDt ? 1 : 0, dt);
     }
     void stCombustion() {
         launch("k_combust", D_CELLS, TPB, k_combust<R>, (const Scn<R>*)dS, dom[D_CELLS]);
@@ -459,7 +565,7 @@ public:
         swapBoth(2);
     }
     void stLeakage() {
-        if (!Z.closed.empty()) launch("k_zone_integral", D_CZ, TPB, k_zone_integral<R>, (const Scn<R>*)dS, dom[D_CZ]);
+        launch("k_zone_integral", D_CZ, TPB, k_zone_integral<R>, (const Scn<R>*)dS, dom[D_CZ]);
     }
     void vcycleBody() {
         const Scn<R>* S = dS;
@@ -471,27 +577,28 @@ public:
             launch("k_residual", D_LV0 + l, TPB, k_residual<R>, S, dom[D_LV0 + l], l);
             launch("k_restrict", D_RS0 + l, TPB, k_restrict<R>, S, dom[D_RS0 + l], l);
         }
-        launch("k_coarse_dense", D_CO_DENSE, TPB, k_coarse_dense<R>, S, dom[D_CO_DENSE], maxLevels - 1);
-        launch("k_coarse_serial", D_CO_SERIAL, 32, k_coarse_serial<R>, S, dom[D_CO_SERIAL], maxLevels - 1);
+        launch("k_coarse_dense", D_CO_DENSE, TPB, k_coarse_dense<R>, S, dom[D_CO_DENSE]);
+        launch("k_coarse_serial", D_CO_SERIAL, 32, k_coarse_serial<R>, S, dom[D_CO_SERIAL]);
         for (int l = maxLevels - 2; l >= 1; --l) {
             launch("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, dom[D_LV0 + l], l, 2);
             launch("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, dom[D_LV0 + l], l, 1);
         }
         launch("k_gs0", D_HALF, TPB, k_gs0<R>, S, dom[D_HALF], 1, 2);
     }
-    int readDone(bool& allDone) {
-        PHX_CK(cudaMemcpyAsync(hPin + 8, h.sv + SV_DONE, sizeof(double), cudaMemcpyDeviceToHost, st));
+    // all scenarios' flag in slot `slot` set?
+    int readAll(int slot, bool& all) {
+        const int n = nscn();
+        for (int s = 0; s < n; ++s)
+            PHX_CK(cudaMemcpyAsync(hPin + 16 + s % 4000, sc[s]->h.sv + slot, sizeof(double), cudaMemcpyDeviceToHost, st));
         PHX_CK(cudaStreamSynchronize(st));
-        allDone = hPin[8] != 0;
+        all = true;
+        for (int s = 0; s < n; ++s) all &= hPin[16 + s % 4000] != 0;
         return PHX_OK;
     }
     // Solver::project: right-hand side, first V-cycle and CG set-up
     void projectPrelude() {
         const Scn<R>* S = dS;
-        cudaMemsetAsync(h.sv + SV_DONE, 0, sizeof(double), st);
-        cudaMemsetAsync(h.sv + SV_IT, 0, sizeof(double), st);
-        cudaMemsetAsync(h.sv + SV_RMAX, 0, sizeof(double), st);
-        cudaMemsetAsync(h.sv + SV_BMAX, 0, sizeof(double), st);
+        launch("k_reset", D_ONE, 32, k_reset<R>, S, dom[D_ONE], 0);
         launch("k_rhs", D_CELLS, TPB, k_rhs<R>, S, dom[D_CELLS]);
         launch("k_gs0", D_HALF, TPB, k_gs0<R>, S, dom[D_HALF], 0, 0);
         vcycleBody();
@@ -508,25 +615,16 @@ public:
     // zone mean removal and velocity correction (:629-676)
     void projectEpilogue() {
         const Scn<R>* S = dS;
-        if (!Z.closed.empty()) {
-            launch("k_zone_mean", D_CZ, TPB, k_zone_mean<R>, S, dom[D_CZ]);
-            launch("k_zone_mean_sub", D_CC, TPB, k_zone_mean_sub<R>, S, dom[D_CC]);
-        }
+        launch("k_zone_mean", D_CZ, TPB, k_zone_mean<R>, S, dom[D_CZ]);
+        launch("k_zone_mean_sub", D_CC, TPB, k_zone_mean_sub<R>, S, dom[D_CC]);
         launch("k_velcorr", D_FX, TPB, k_velcorr<R>, S, dom[D_FX], 0);
         launch("k_velcorr", D_FY, TPB, k_velcorr<R>, S, dom[D_FY], 1);
         launch("k_velcorr", D_FZ, TPB, k_velcorr<R>, S, dom[D_FZ], 2);
     }
-    // ---- mixed path: FP64 refinement around the FP32 inner CG -------------------
+    // ---- mixed path: FP64 refinement around the FP32 inner CG -------------------------
     void mixedBegin() {
         const Scn<R>* S = dS;
-        cudaMemsetAsync(h.sv + SV_DONE, 0, sizeof(double), st);
-        cudaMemsetAsync(h.sv + SV_IT, 0, sizeof(double), st);
-        cudaMemsetAsync(h.sv + SV_ODONE, 0, sizeof(double), st);
-        cudaMemsetAsync(h.sv + SV_OUTER, 0, sizeof(double), st);
-        cudaMemsetAsync(h.sv + SV_ITTOT, 0, sizeof(double), st);
-        cudaMemsetAsync(h.sv + SV_R64MAX, 0, sizeof(double), st);
-        cudaMemsetAsync(h.sv + SV_RMAX, 0, sizeof(double), st);
-        cudaMemsetAsync(h.sv + SV_BMAX, 0, sizeof(double), st);
+        launch("k_reset", D_ONE, 32, k_reset<R>, S, dom[D_ONE], 1);
         launch("k_rhs", D_CELLS, TPB, k_rhs<R>, S, dom[D_CELLS]);
         launch("k_mx_res64", D_CELLS, TPB, k_mx_res64<R>, S, dom[D_CELLS]);
         launch("k_mx_zone_proj", D_CZ, TPB, k_mx_zone_proj<R>, S, dom[D_CZ]);
@@ -545,56 +643,74 @@ public:
         launch("k_mx_res64", D_CELLS, TPB, k_mx_res64<R>, S, dom[D_CELLS]);
         launch("k_mx_zone_proj", D_CZ, TPB, k_mx_zone_proj<R>, S, dom[D_CZ]);
     }
-    int readOuterDone(bool& allDone) {
-        PHX_CK(cudaMemcpyAsync(hPin + 8, h.sv + SV_ODONE, sizeof(double), cudaMemcpyDeviceToHost, st));
-        PHX_CK(cudaStreamSynchronize(st));
-        allDone = hPin[8] != 0;
-        return PHX_OK;
+    void mixedOuterHost() {
+        k_mx_outer<R><<<1, 128, 0, st>>>(dS, nscn(), cudaGraphConditionalHandle{}, nullptr, 0, 0);
+        ++launches;
     }
     int stProjectMixed() {
         mixedBegin();
-        k_mx_outer<R><<<1, 32, 0, st>>>(dS, 1, cudaGraphConditionalHandle{}, nullptr, 0, 0);
-        ++launches;
+        mixedOuterHost();
         bool odone = false;
-        PHX_TRY(readOuterDone(odone));
+        PHX_TRY(readAll(SV_ODONE, odone));
         for (int pass = 0; !odone && pass <= OUTER_MAX + 1; ++pass) {
             mixedInnerPrelude();
             bool done = false;
-            PHX_TRY(readDone(done));
+            PHX_TRY(readAll(SV_DONE, done));
             for (int it = 0; !done && it <= INNER_MAX + 1; ++it) {
                 cgIteration();
-                PHX_TRY(readDone(done));
+                PHX_TRY(readAll(SV_DONE, done));
             }
             mixedRefine();
-            k_mx_outer<R><<<1, 32, 0, st>>>(dS, 1, cudaGraphConditionalHandle{}, nullptr, 0, 0);
-            ++launches;
-            PHX_TRY(readOuterDone(odone));
+            mixedOuterHost();
+            PHX_TRY(readAll(SV_ODONE, odone));
         }
         launch("k_mx_final", D_CELLS, TPB, k_mx_final<R>, dS, dom[D_CELLS]);
         projectEpilogue();
         return PHX_OK;
     }
 
+    int maxItersAll() const {
+        int m = 0;
+        for (auto& S : sc) m = std::max(m, S->maxIters);
+        return m;
+    }
+
     // host-driven CG loop: the stop test is read back after every iteration
     int stProject() {
         if (kMixed) return stProjectMixed();
         projectPrelude();
+        const int maxIt = maxItersAll();
         bool done = false;
-        PHX_TRY(readDone(done));
-        for (int it = 0; !done && it <= maxIters + 1; ++it) {
+        PHX_TRY(readAll(SV_DONE, done));
+        for (int it = 0; !done && it <= maxIt + 1; ++it) {
             cgIteration();
-            PHX_TRY(readDone(done));
+            PHX_TRY(readAll(SV_DONE, done));
         }
         projectEpilogue();
         return PHX_OK;
     }
+    void stAdvect() {
+        launch("k_advect", D_CELLS, TPB, k_advect<R>, (const Scn<R>*)dS, dom[D_CELLS]);
+        swapBoth(4);
+    }
+    void stEnd() {
+        const Scn<R>* S = dS;
+        launch("k_zone_pressure", D_ONE, 32, k_zone_pressure<R>, S, dom[D_ONE]);
+        launch("k_zone_pb", D_CC, TPB, k_zone_pb<R>, S, dom[D_CC]);
+        launch("k_stats", D_CELLS, TPB, k_stats<R>, S, dom[D_CELLS]);
+    }
 
-    // ---- captured step graph: the CG loop is a device-side while node ----------
+    int checkLaunch() {
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) { err = std::string("kernel launch: ") + cudaGetErrorString(e); return PHX_ERR_CUDA; }
+        return PHX_OK;
+    }
+
+    // ---- captured step graph: the CG loops are device-side while nodes ---------------
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
-    cudaGraphConditionalHandle cgHandle{};
-    int* dLoop = nullptr;
-    int outerKernels = 0, bodyKernels = 0;
+    cudaGraphConditionalHandle cgHandle{}, outerHandle{};
+    int outerKernels = 0, bodyKernels = 0, outerBodyKernels = 0;
     bool useGraph = true;
 
     void destroyGraph() {
@@ -602,52 +718,6 @@ public:
         if (graph) cudaGraphDestroy(graph);
         gexec = nullptr;
         graph = nullptr;
-    }
-
-    int buildGraph() {
-        destroyGraph();
-        if (!dLoop) PHX_CK(cudaMalloc(&dLoop, 2 * sizeof(int)));
-        const Scn<R> saved = h;
-        PHX_CK(cudaGraphCreate(&graph, 0));
-        // conditional handles are created before the capture of the graph that holds their node
-        if (kMixed) PHX_CK(cudaGraphConditionalHandleCreate(&outerHandle, graph, 0, 0));
-        else PHX_CK(cudaGraphConditionalHandleCreate(&cgHandle, graph, 0, 0));
-        PHX_CK(cudaStreamBeginCaptureToGraph(st, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-        launches = 0;
-        launch("k_begin", D_ONE, 32, k_begin<R>, (const Scn<R>*)dS, dom[D_ONE], 1, 0.0);
-        stCombustion();
-        stTurbulence();
-        stHeat();
-        stEnergy();
-        stMomentum();
-        stLeakage();
-        if (kMixed) {
-            PHX_TRY(captureMixedProject());
-        } else {
-            projectPrelude();
-            cudaMemsetAsync(dLoop, 0, sizeof(int), st);
-            const int cap = maxIters + 2;
-            k_cg_cond<R><<<1, 32, 0, st>>>(dS, 1, cgHandle, dLoop, cap);
-            ++launches;
-            cudaGraph_t body = nullptr;
-            PHX_TRY(addWhile(graph, cgHandle, &body));
-            projectEpilogue();
-            stAdvect();
-            stEnd();
-            cudaGraph_t outGraph = nullptr;
-            PHX_CK(cudaStreamEndCapture(st, &outGraph));
-            outerKernels = launches;
-            PHX_CK(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-            launches = 0;
-            cgIteration();
-            k_cg_cond<R><<<1, 32, 0, st>>>(dS, 1, cgHandle, dLoop, cap);
-            ++launches;
-            PHX_CK(cudaStreamEndCapture(st, &body));
-            bodyKernels = launches;
-        }
-        h = saved;
-        PHX_CK(cudaGraphInstantiate(&gexec, graph, 0));
-        return checkLaunch();
     }
 
     // add a while node after the current capture position of st (which captures
@@ -669,16 +739,62 @@ public:
         return PHX_OK;
     }
 
+    int buildGraph() {
+        destroyGraph();
+        std::vector<Scn<R>> saved;
+        for (auto& S : sc) saved.push_back(S->h);
+        const int n = nscn();
+        PHX_CK(cudaGraphCreate(&graph, 0));
+        // conditional handles are created before the capture of the graph that holds their node
+        if (kMixed) PHX_CK(cudaGraphConditionalHandleCreate(&outerHandle, graph, 0, 0));
+        else PHX_CK(cudaGraphConditionalHandleCreate(&cgHandle, graph, 0, 0));
+        PHX_CK(cudaStreamBeginCaptureToGraph(st, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        launches = 0;
+        stBegin(true, 0.0);
+        stCombustion();
+        stTurbulence();
+        stHeat();
+        stEnergy();
+        stMomentum();
+        stLeakage();
+        if (kMixed) {
+            PHX_TRY(captureMixedProject());
+        } else {
+            projectPrelude();
+            cudaMemsetAsync(dLoop, 0, sizeof(int), st);
+            const int capIt = maxItersAll() + 2;
+            k_cg_cond<R><<<1, 128, 0, st>>>(dS, n, cgHandle, dLoop, capIt);
+            ++launches;
+            cudaGraph_t body = nullptr;
+            PHX_TRY(addWhile(graph, cgHandle, &body));
+            projectEpilogue();
+            stAdvect();
+            stEnd();
+            cudaGraph_t outGraph = nullptr;
+            PHX_CK(cudaStreamEndCapture(st, &outGraph));
+            outerKernels = launches;
+            PHX_CK(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+            launches = 0;
+            cgIteration();
+            k_cg_cond<R><<<1, 128, 0, st>>>(dS, n, cgHandle, dLoop, capIt);
+            ++launches;
+            PHX_CK(cudaStreamEndCapture(st, &body));
+            bodyKernels = launches;
+        }
+        for (int s = 0; s < n; ++s) sc[s]->h = saved[s];
+        PHX_CK(cudaGraphInstantiate(&gexec, graph, 0));
+        return checkLaunch();
+    }
+
     // mixed project in the step graph: while (refining) { inner prelude;
     // while (inner CG) { iteration }; refine }. dLoop[0] bounds the refinement
     // passes, dLoop[1] the inner iterations of a pass.
-    cudaGraphConditionalHandle outerHandle{};
-    int outerBodyKernels = 0, innerPreludeKernels = 0;
     int captureMixedProject() {
+        const int n = nscn();
         mixedBegin();
         cudaMemsetAsync(dLoop, 0, 2 * sizeof(int), st);
         const int capOuter = OUTER_MAX + 2, capInner = INNER_MAX + 2;
-        k_mx_outer<R><<<1, 32, 0, st>>>(dS, 1, outerHandle, dLoop, capOuter, 1);
+        k_mx_outer<R><<<1, 128, 0, st>>>(dS, n, outerHandle, dLoop, capOuter, 1);
         ++launches;
         cudaGraph_t outerBody = nullptr;
         PHX_TRY(addWhile(graph, outerHandle, &outerBody));
@@ -695,13 +811,12 @@ public:
         launches = 0;
         cudaMemsetAsync(dLoop + 1, 0, sizeof(int), st);
         mixedInnerPrelude();
-        k_cg_cond<R><<<1, 32, 0, st>>>(dS, 1, cgHandle, dLoop + 1, capInner);
+        k_cg_cond<R><<<1, 128, 0, st>>>(dS, n, cgHandle, dLoop + 1, capInner);
         ++launches;
-        innerPreludeKernels = launches;
         cudaGraph_t innerBody = nullptr;
         PHX_TRY(addWhile(outerBody, cgHandle, &innerBody));
         mixedRefine();
-        k_mx_outer<R><<<1, 32, 0, st>>>(dS, 1, outerHandle, dLoop, capOuter, 1);
+        k_mx_outer<R><<<1, 128, 0, st>>>(dS, n, outerHandle, dLoop, capOuter, 1);
         ++launches;
         cudaGraph_t ob = nullptr;
         PHX_CK(cudaStreamEndCapture(st, &ob));
@@ -710,32 +825,35 @@ public:
         PHX_CK(cudaStreamBeginCaptureToGraph(st, innerBody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
         launches = 0;
         cgIteration();
-        k_cg_cond<R><<<1, 32, 0, st>>>(dS, 1, cgHandle, dLoop + 1, capInner);
+        k_cg_cond<R><<<1, 128, 0, st>>>(dS, n, cgHandle, dLoop + 1, capInner);
         ++launches;
         PHX_CK(cudaStreamEndCapture(st, &innerBody));
         bodyKernels = launches;
         return PHX_OK;
     }
 
-    int graphStep(double dtMax) {
+    int graphStep(double dtMax, const double* per) {
         if (!gexec) PHX_TRY(buildGraph());
-        double v = dtMax;   // pageable source: staged at the call, safe to reuse at once
-        PHX_CK(cudaMemcpyAsync(h.sv + SV_DTMAX_ARG, &v, sizeof(double), cudaMemcpyHostToDevice, st));
+        PHX_TRY(setDtMax(dtMax, per));
         PHX_CK(cudaGraphLaunch(gexec, st));
         swapHost(1 | 2 | 4);
         return PHX_OK;
     }
 
-    // kernels the last graph step ran: the outer nodes plus the loop body per iteration
+    // kernels the last graph step ran: the outer nodes plus the loop bodies per pass
     int graphLaunchCount(int* out) {
         if (kMixed) {
-            // passes from the refinement counter, inner iterations from the scalars
             int lc[2] = {0, 0};
             PHX_CK(cudaMemcpyAsync(lc, dLoop, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
-            PHX_CK(cudaMemcpyAsync(hPin + 32, h.sv + SV_ITTOT, sizeof(double), cudaMemcpyDeviceToHost, st));
+            double itTot = 0;
+            for (auto& S : sc) {
+                PHX_CK(cudaMemcpyAsync(hPin + 32, S->h.sv + SV_ITTOT, sizeof(double), cudaMemcpyDeviceToHost, st));
+                PHX_CK(cudaStreamSynchronize(st));
+                itTot = std::max(itTot, hPin[32]);
+            }
             PHX_CK(cudaStreamSynchronize(st));
             const int passes = std::max(0, lc[0] - 1);
-            *out = outerKernels + outerBodyKernels * passes + bodyKernels * ((int)hPin[32] + passes);
+            *out = outerKernels + outerBodyKernels * passes + bodyKernels * ((int)itTot + passes);
             return PHX_OK;
         }
         int lc = 0;
@@ -744,28 +862,13 @@ public:
         *out = outerKernels + bodyKernels * std::max(0, lc - 1);
         return PHX_OK;
     }
-    void stAdvect() {
-        launch("k_advect", D_CELLS, TPB, k_advect<R>, (const Scn<R>*)dS, dom[D_CELLS]);
-        swapBoth(4);
-    }
-    void stEnd() {
-        const Scn<R>* S = dS;
-        if (!Z.closed.empty()) {
-            launch("k_zone_pressure", D_ONE, 32, k_zone_pressure<R>, S, dom[D_ONE]);
-            launch("k_zone_pb", D_CC, TPB, k_zone_pb<R>, S, dom[D_CC]);
-        }
-        launch("k_stats", D_CELLS, TPB, k_stats<R>, S, dom[D_CELLS]);
-    }
 
-    int checkLaunch() {
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) { err = std::string("kernel launch: ") + cudaGetErrorString(e); return PHX_ERR_CUDA; }
-        return PHX_OK;
-    }
-
-    int oneStep(double dtMax) {
-        if (useGraph && !prof) return graphStep(dtMax);
-        stBegin(true, dtMax);
+    int oneStep(double dtMax, const double* per = nullptr) {
+        PHX_TRY(ensureTables());
+        if (nscn() == 0) return PHX_OK;
+        if (useGraph && !prof) return graphStep(dtMax, per);
+        PHX_TRY(setDtMax(dtMax, per));
+        stBegin(true, 0.0);
         stCombustion();
         stTurbulence();
         stHeat();
@@ -778,22 +881,26 @@ public:
         return checkLaunch();
     }
 
-    int step(int n, double dtMax, double* dtOut) override {
+    int step(int n, double dtMax, const double* per, double* dtOut) override {
         for (int i = 0; i < n; ++i) {
             launches = 0;
-            PHX_TRY(oneStep(dtMax));
+            PHX_TRY(oneStep(dtMax, per));
             if (dtOut) {
-                PHX_CK(cudaMemcpyAsync(hPin + 16, h.sv + SV_DT, sizeof(double), cudaMemcpyDeviceToHost, st));
+                const int m = nscn();
+                for (int s = 0; s < m; ++s)
+                    PHX_CK(cudaMemcpyAsync(hPin + 16 + s % 4000, sc[s]->h.sv + SV_DT, sizeof(double), cudaMemcpyDeviceToHost, st));
                 PHX_CK(cudaStreamSynchronize(st));
-                dtOut[i] = hPin[16];
+                if (per) for (int s = 0; s < m; ++s) dtOut[(size_t)i * m + s] = hPin[16 + s % 4000];
+                else dtOut[i] = hPin[16];
             }
         }
         return PHX_OK;
     }
 
     int stage(int which, double arg) override {
+        PHX_TRY(ensureTables());
         switch (which) {
-        case PHX_STAGE_BEGIN: stBegin(true, arg); break;
+        case PHX_STAGE_BEGIN: PHX_TRY(setDtMax(arg, nullptr)); stBegin(true, 0.0); break;
         case PHX_STAGE_COMBUSTION: stBegin(false, arg); stCombustion(); break;
         case PHX_STAGE_TURBULENCE: stTurbulence(); break;
         case PHX_STAGE_HEAT: stBegin(false, arg); stHeat(); break;
@@ -810,19 +917,22 @@ public:
         return PHX_OK;
     }
 
+    // z = M^-1 r with one V-cycle of the multigrid (single-scenario contexts)
     int precondition(const double* r, double* z) override {
-        const int N = geo.N();
-        std::vector<double> rv(r, r + N);
-        PHX_TRY(put(h.r, rv));
-        cudaMemsetAsync(h.sv + SV_DONE, 0, sizeof(double), st);
+        PHX_TRY(ensureTables());
+        if (nscn() != 1) { err = "precondition needs a single-scenario context"; return PHX_ERR_STATE; }
+        Scenario<R>& S = *sc[0];
+        const int N = S.geo.N();
+        PHX_TRY(S.put(st, S.h.r, std::vector<double>(r, r + N)));
+        launch("k_reset", D_ONE, 32, k_reset<R>, (const Scn<R>*)dS, dom[D_ONE], 2);
         launch("k_gs0", D_HALF, TPB, k_gs0<R>, (const Scn<R>*)dS, dom[D_HALF], 0, 0);
         vcycleBody();
         launch("k_gs0_last_dot", D_CELLS, TPB, k_gs0_last_dot<R>, (const Scn<R>*)dS, dom[D_CELLS], 2);
         PHX_TRY(checkLaunch());
-        return getReal(h.z, N, z);
+        return getReal(S.h.z, N, z);
     }
 
-    // ---- fields ----------------------------------------------------------------
+    // ---- fields -----------------------------------------------------------------------
     int getReal(const R* src, size_t n, double* out) {
         if (std::is_same<R, double>::value) {
             PHX_CK(cudaMemcpyAsync(out, src, n * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -836,8 +946,11 @@ public:
         return PHX_OK;
     }
 
-    bool fieldPtr(int f, void** p, size_t* n, int* type) {
-        const size_t N = geo.N(), NX = geo.NX(), NY = geo.NY(), NZ = geo.NZ();
+    bool fieldPtr(int s, int f, void** p, size_t* n, int* type) const {
+        if (s < 0 || s >= nscn()) return false;
+        const Scenario<R>& S = *sc[s];
+        const Scn<R>& h = S.h;
+        const size_t N = S.geo.N(), NX = S.geo.NX(), NY = S.geo.NY(), NZ = S.geo.NZ();
         *type = 0;
         switch (f) {
         case PHX_FIELD_U: *p = h.u; *n = NX; return true;
@@ -862,22 +975,22 @@ public:
         }
     }
 
-    size_t fieldCount(int f) const override {
+    size_t fieldCount(int s, int f) const override {
         void* p;
         size_t n;
         int t;
-        return const_cast<Ctx*>(this)->fieldPtr(f, &p, &n, &t) ? n : 0;
+        return fieldPtr(s, f, &p, &n, &t) ? n : 0;
     }
 
-    int getField(int f, void* host, size_t bytes) override {
+    int getField(int s, int f, void* host, size_t bytes) override {
         void* p;
         size_t n;
         int t;
-        if (!fieldPtr(f, &p, &n, &t)) { err = "unknown field"; return PHX_ERR_INVALID; }
+        if (!fieldPtr(s, f, &p, &n, &t)) { err = "unknown field or scenario"; return PHX_ERR_INVALID; }
         size_t want = n * (t == 0 ? sizeof(double) : t == 1 ? 1 : 4);
         if (bytes != want) { err = "field size mismatch: expected " + std::to_string(want) + " bytes"; return PHX_ERR_INVALID; }
         if (kMixed && f == PHX_FIELD_P) {   // the FP64 pressure of the refinement loop
-            PHX_CK(cudaMemcpyAsync(host, h.p64, bytes, cudaMemcpyDeviceToHost, st));
+            PHX_CK(cudaMemcpyAsync(host, sc[s]->h.p64, bytes, cudaMemcpyDeviceToHost, st));
             PHX_CK(cudaStreamSynchronize(st));
             return PHX_OK;
         }
@@ -887,49 +1000,58 @@ public:
         return PHX_OK;
     }
 
-    int setField(int f, const void* host, size_t bytes) override {
+    int setField(int s, int f, const void* host, size_t bytes) override {
         void* p;
         size_t n;
         int t;
-        if (!fieldPtr(f, &p, &n, &t) || f == PHX_FIELD_ZONE) { err = "unknown or read-only field"; return PHX_ERR_INVALID; }
+        if (!fieldPtr(s, f, &p, &n, &t) || f == PHX_FIELD_ZONE) { err = "unknown or read-only field"; return PHX_ERR_INVALID; }
         size_t want = n * (t == 0 ? sizeof(double) : t == 1 ? 1 : 4);
         if (bytes != want) { err = "field size mismatch: expected " + std::to_string(want) + " bytes"; return PHX_ERR_INVALID; }
+        Scenario<R>& S = *sc[s];
         if (t == 0) {
             const double* d = (const double*)host;
-            if (kMixed && f == PHX_FIELD_P) PHX_TRY(putRaw(h.p64, d, n));
-            return put<R>((R*)p, std::vector<double>(d, d + n));
+            if (kMixed && f == PHX_FIELD_P) PHX_TRY(S.putRaw(st, S.h.p64, d, n));
+            return S.put(st, (R*)p, std::vector<double>(d, d + n));
         }
         PHX_CK(cudaMemcpyAsync(p, host, bytes, cudaMemcpyHostToDevice, st));
         PHX_CK(cudaStreamSynchronize(st));
         return PHX_OK;
     }
 
-    int getStats(phx_stats* o) override {
-        PHX_CK(cudaMemcpyAsync(hPin + 64, h.sv, SV_COUNT * sizeof(double), cudaMemcpyDeviceToHost, st));
+    int getStats(int s, phx_stats* o) override {
+        PHX_TRY(checkScn(s));
+        PHX_CK(cudaMemcpyAsync(hPin + 4096, sc[s]->h.sv, SV_COUNT * sizeof(double), cudaMemcpyDeviceToHost, st));
         PHX_CK(cudaStreamSynchronize(st));
-        const double* sv = hPin + 64;
+        const double* sv = hPin + 4096;
         o->time = sv[SV_TIME]; o->dt = sv[SV_DT];
         o->max_vel = sv[SV_MAXVEL]; o->max_nu = sv[SV_MAXNU]; o->max_div = sv[SV_MAXDIV];
-        o->pressure_iters = kMixed ? (int)sv[SV_ITTOT] : (int)sv[SV_IT]; o->pressure_residual = sv[SV_PRES]; o->pressure_rel_residual = sv[SV_PREL];
+        o->pressure_iters = kMixed ? (int)sv[SV_ITTOT] : (int)sv[SV_IT];
+        o->pressure_residual = sv[SV_PRES]; o->pressure_rel_residual = sv[SV_PREL];
         o->hrr = sv[SV_HRR]; o->max_gas_t = sv[SV_MAXGAST]; o->burning_cells = (int)sv[SV_BURNING];
         o->fuel_in = sv[SV_FUELIN]; o->fuel_burned = sv[SV_FUELBURNED]; o->fuel_in_domain = sv[SV_FUELINDOMAIN];
-        o->zones = (int)Z.zoneP.size(); o->leak_faces = 0;
+        o->zones = (int)sc[s]->Z.zoneP.size(); o->leak_faces = 0;
         return PHX_OK;
     }
 
-    int setScalars(double time, double maxVel, double maxNu, double maxDiv) override {
+    int setScalars(int s, double time, double maxVel, double maxNu, double maxDiv) override {
+        PHX_TRY(checkScn(s));
         double v[4] = {time, maxVel, maxNu, maxDiv};
-        PHX_CK(cudaMemcpyAsync(h.sv + SV_TIME, &v[0], sizeof(double), cudaMemcpyHostToDevice, st));
-        PHX_CK(cudaMemcpyAsync(h.sv + SV_MAXVEL, &v[1], sizeof(double), cudaMemcpyHostToDevice, st));
-        PHX_CK(cudaMemcpyAsync(h.sv + SV_MAXNU, &v[2], sizeof(double), cudaMemcpyHostToDevice, st));
-        PHX_CK(cudaMemcpyAsync(h.sv + SV_MAXDIV, &v[3], sizeof(double), cudaMemcpyHostToDevice, st));
+        double* sv = sc[s]->h.sv;
+        PHX_CK(cudaMemcpyAsync(sv + SV_TIME, &v[0], sizeof(double), cudaMemcpyHostToDevice, st));
+        PHX_CK(cudaMemcpyAsync(sv + SV_MAXVEL, &v[1], sizeof(double), cudaMemcpyHostToDevice, st));
+        PHX_CK(cudaMemcpyAsync(sv + SV_MAXNU, &v[2], sizeof(double), cudaMemcpyHostToDevice, st));
+        PHX_CK(cudaMemcpyAsync(sv + SV_MAXDIV, &v[3], sizeof(double), cudaMemcpyHostToDevice, st));
         PHX_CK(cudaStreamSynchronize(st));
         return PHX_OK;
     }
 
-    size_t deviceBytes() const override { return arenaBytes; }
+    size_t deviceBytes() const override {
+        size_t b = 0;
+        for (auto& S : sc) b += S->arenaBytes;
+        return b;
+    }
     int sync() override {
-        PHX_CK(cudaStreamSynchronize(st));
+        if (st) PHX_CK(cudaStreamSynchronize(st));
         return PHX_OK;
     }
     int lastLaunches() const override {
@@ -943,6 +1065,7 @@ public:
     // n steps timed with CUDA events on the context's stream; with flushL2 a
     // buffer larger than L2 is written (untimed) before each step
     int timeSteps(int n, double dtMax, int flushL2, double* totalMs, int* launchesOut) override {
+        PHX_TRY(ensureTables());
         if (flushL2 && !flushBuf) {
             flushBytes = (size_t)512 << 20;
             PHX_CK(cudaMalloc(&flushBuf, flushBytes));
@@ -974,7 +1097,8 @@ public:
     }
 
     // one step with an event pair around every launch; per-kernel totals
-    int profileStep(double dtMax, int flushL2, phx_kernel_time* out, int cap, int* count) override {
+    int profileStep(double dtMax, int flushL2, phx_kernel_time* out, int cap_, int* count) override {
+        PHX_TRY(ensureTables());
         if (flushL2) {
             if (!flushBuf) { flushBytes = (size_t)512 << 20; PHX_CK(cudaMalloc(&flushBuf, flushBytes)); }
             PHX_CK(cudaMemsetAsync(flushBuf, 0x5a, flushBytes, st));
@@ -988,7 +1112,7 @@ public:
         PHX_TRY(collectProfile());
         int n = 0;
         for (auto& k : kstats) {
-            if (n < cap && out) {
+            if (n < cap_ && out) {
                 std::memset(&out[n], 0, sizeof(phx_kernel_time));
                 std::strncpy(out[n].name, k.name.c_str(), sizeof(out[n].name) - 1);
                 out[n].launches = k.launches;

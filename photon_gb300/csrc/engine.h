@@ -1,4 +1,5 @@
-// Host-facing interface of a scenario context, independent of its precision.
+// Host-facing interface of an engine (a batch of scenarios), independent of
+// its precision. A single-scenario context is a batch of one.
 #pragma once
 #include <cstddef>
 #include <string>
@@ -11,17 +12,23 @@ namespace phx {
 class CtxBase {
 public:
     virtual ~CtxBase() = default;
-    virtual int addBurner(double x0, double y0, double x1, double y1, double z, double peakW, double rampS, double start,
-                          double duration, int* index) = 0;
-    virtual int addIgnition(int cell, double power, double duration) = 0;
-    virtual int step(int n, double dtMax, double* dtOut) = 0;
+    virtual int addScenario(const phx_grid* g, int* id) = 0;
+    virtual int removeScenario(int s) = 0;
+    virtual int scenarioCount() const = 0;
+    virtual size_t scenarioBytes(int s) const = 0;
+    virtual int addBurner(int s, double x0, double y0, double x1, double y1, double z, double peakW, double rampS,
+                          double start, double duration, int* index) = 0;
+    virtual int addIgnition(int s, int cell, double power, double duration) = 0;
+    // n steps of every scenario; per (optional) holds one dtMax per scenario;
+    // dtOut gets one dt per step (per == null) or per step and scenario
+    virtual int step(int n, double dtMax, const double* per, double* dtOut) = 0;
     virtual int stage(int stage, double arg) = 0;
     virtual int precondition(const double* r, double* z) = 0;
-    virtual int getField(int field, void* host, size_t bytes) = 0;
-    virtual int setField(int field, const void* host, size_t bytes) = 0;
-    virtual size_t fieldCount(int field) const = 0;
-    virtual int getStats(phx_stats* out) = 0;
-    virtual int setScalars(double time, double maxVel, double maxNu, double maxDiv) = 0;
+    virtual int getField(int s, int field, void* host, size_t bytes) = 0;
+    virtual int setField(int s, int field, const void* host, size_t bytes) = 0;
+    virtual size_t fieldCount(int s, int field) const = 0;
+    virtual int getStats(int s, phx_stats* out) = 0;
+    virtual int setScalars(int s, double time, double maxVel, double maxNu, double maxDiv) = 0;
     virtual size_t deviceBytes() const = 0;
     virtual int sync() = 0;
     virtual int timeSteps(int n, double dtMax, int flushL2, double* totalMs, int* launches) = 0;
@@ -30,8 +37,8 @@ public:
     std::string err;
 };
 
-// factories (one translation unit per precision)
-CtxBase* makeCtxFp64(const phx_grid* g, std::string& err);
-CtxBase* makeCtxMixed(const phx_grid* g, std::string& err);
+// empty engines (one translation unit per precision)
+CtxBase* makeCtxFp64();
+CtxBase* makeCtxMixed();
 
 }  // namespace phx

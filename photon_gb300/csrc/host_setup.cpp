@@ -5,6 +5,7 @@
 #include <cmath>
 #include <limits>
 #include <numeric>
+#include <thread>
 
 namespace phx {
 
@@ -274,14 +275,22 @@ Multigrid buildMultigrid(const GridGeom& g, int denseMax) {
     if (Lc.n <= denseMax) {
         const int n = Lc.n;
         Lc.dense.assign((size_t)n * n, 0.0);
-        std::vector<double> b(n, 0.0), x(n, 0.0);
-        for (int jcol = 0; jcol < n; ++jcol) {
-            std::fill(b.begin(), b.end(), 0.0);
-            std::fill(x.begin(), x.end(), 0.0);
-            b[jcol] = 1.0;
-            for (int it = 0; it < 20; ++it) { gsSweep(Lc, b.data(), x.data(), true); gsSweep(Lc, b.data(), x.data(), false); }
-            for (int i = 0; i < n; ++i) Lc.dense[(size_t)i * n + jcol] = x[i];
-        }
+        // columns are independent: split them over the host's threads
+        auto cols = [&](int j0, int j1) {
+            std::vector<double> b(n, 0.0), x(n, 0.0);
+            for (int jcol = j0; jcol < j1; ++jcol) {
+                std::fill(b.begin(), b.end(), 0.0);
+                std::fill(x.begin(), x.end(), 0.0);
+                b[jcol] = 1.0;
+                for (int it = 0; it < 20; ++it) { gsSweep(Lc, b.data(), x.data(), true); gsSweep(Lc, b.data(), x.data(), false); }
+                for (int i = 0; i < n; ++i) Lc.dense[(size_t)i * n + jcol] = x[i];
+            }
+        };
+        int nt = (int)std::min<unsigned>(16, std::max(1u, std::thread::hardware_concurrency()));
+        if ((long long)n * n < 200000) nt = 1;
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nt; ++t) pool.emplace_back(cols, (int)((long long)n * t / nt), (int)((long long)n * (t + 1) / nt));
+        for (auto& th : pool) th.join();
     }
     return M;
 }

@@ -136,4 +136,25 @@ __global__ void k_mx_outer(const Scn<R>* __restrict__ S, int nscn, cudaGraphCond
     }
 }
 
+// per-scenario resets of the solve's scalar slots (one thread per scenario):
+// which 0: FP64 CG; 1: mixed refinement; 2: a bare V-cycle
+template <class R>
+__global__ void k_reset(const Scn<R>* __restrict__ S, Dom dom, int which) {
+    int s_, tile_;
+    locate(dom, blockIdx.x, s_, tile_);
+    if (threadIdx.x != 0) return;
+    double* sv = S[s_].sv;
+    sv[SV_DONE] = 0;
+    if (which == 2) return;
+    sv[SV_IT] = 0;
+    sv[SV_RMAX] = 0;
+    sv[SV_BMAX] = 0;
+    if (which == 1) {
+        sv[SV_ODONE] = 0;
+        sv[SV_OUTER] = 0;
+        sv[SV_ITTOT] = 0;
+        sv[SV_R64MAX] = 0;
+    }
+}
+
 }  // namespace phx

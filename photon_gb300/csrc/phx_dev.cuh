@@ -88,6 +88,7 @@ struct Scn {
     int nx, ny, nz, N, NX, NY, NZ;
     double dx, ox, oy, oz;
     double cfl, dtMaxP, tol, relTol;
+    const double* dtMaxArg;      // this step's dtMax argument (one slot per scenario of the batch)
     int maxIters;
     int radiationOn;
     double windSpeed, windSin, windCos, windExp;   // sin/cos of the wind direction taken on the host

@@ -179,9 +179,9 @@ __global__ void k_restrict(const Scn<R>* __restrict__ S, Dom dom, int l) {
 // forward + backward Gauss-Seidel sweeps (pressure_mg.cpp:258-266, 279).
 // One warp per row.
 template <class R>
-__global__ void k_coarse_dense(const Scn<R>* __restrict__ S, Dom dom, int l) {
+__global__ void k_coarse_dense(const Scn<R>* __restrict__ S, Dom dom) {
     PHX_PROLOGUE_ACTIVE(dom);
-    const Level<R>& L = g.lv[l];
+    const Level<R>& L = g.lv[g.nLevels - 1];
     const int row = tile_ * (TPB / 32) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (row >= L.n) return;
@@ -196,10 +196,10 @@ __global__ void k_coarse_dense(const Scn<R>* __restrict__ S, Dom dom, int l) {
 // sweeps, serially in one thread (used when the level is too large for a dense
 // operator)
 template <class R>
-__global__ void k_coarse_serial(const Scn<R>* __restrict__ S, Dom dom, int l) {
+__global__ void k_coarse_serial(const Scn<R>* __restrict__ S, Dom dom) {
     PHX_PROLOGUE_ACTIVE(dom);
     if (threadIdx.x != 0) return;
-    const Level<R>& L = g.lv[l];
+    const Level<R>& L = g.lv[g.nLevels - 1];
     for (int I = 0; I < L.n; ++I) L.x[I] = 0;
     for (int it = 0; it < 20; ++it)
         for (int dir = 0; dir < 2; ++dir)

@@ -67,7 +67,7 @@ __global__ void k_begin(const Scn<R>* __restrict__ S, Dom dom, int computeDt, do
     double* sv = g.sv;
     double dt;
     if (computeDt) {
-        double dtMax = sv[SV_DTMAX_ARG];
+        double dtMax = *g.dtMaxArg;
         dt = mn(dtMax, g.dtMaxP);
         dt = mn(dt, g.cfl * g.dx / mx(sv[SV_MAXVEL], 0.1));
         double alpha = sv[SV_MAXNU] * (1.0 + 1.0 / K_PR_T);

@@ -20,25 +20,31 @@ def _ptr(a):
     return ctypes.c_void_p(a.ctypes.data) if a is not None else None
 
 
+def make_grid(case):
+    """phx_grid for a case; returns (grid, arrays kept alive for the call)."""
+    g = PhxGrid()
+    g.nx, g.ny, g.nz = case.nx, case.ny, case.nz
+    g.dx, g.ox, g.oy, g.oz = case.dx, case.ox, case.oy, case.oz
+    pr = case.profile
+    g.cfl, g.dt_max, g.max_iters, g.tol, g.rel_tol = pr.cfl, pr.dtMax, pr.maxIters, pr.tol, pr.rel_tol
+    g.radiation_on, g.adiabatic_surfaces = int(case.radiationOn), int(case.adiabatic)
+    g.wind_speed, g.wind_from_deg, g.wind_exponent = case.wind
+    keep = {}
+    for n in ("blocked", "lx", "ly", "lz"):
+        keep[n] = np.ascontiguousarray(getattr(case, n), dtype=np.uint8)
+    for n in ("fx", "fy", "fz", "ax", "ay", "az"):
+        keep[n] = np.ascontiguousarray(getattr(case, n), dtype=np.float64)
+    for n, a in keep.items():
+        setattr(g, n, a.ctypes.data)
+    return g, keep
+
+
 class Solver:
     def __init__(self, case, precision: int = _lib.PREC_FP64, add_burners: bool = True):
         self.L = _lib.load()
         self.case = case
         self.h = ctypes.c_void_p()
-        g = PhxGrid()
-        g.nx, g.ny, g.nz = case.nx, case.ny, case.nz
-        g.dx, g.ox, g.oy, g.oz = case.dx, case.ox, case.oy, case.oz
-        pr = case.profile
-        g.cfl, g.dt_max, g.max_iters, g.tol, g.rel_tol = pr.cfl, pr.dtMax, pr.maxIters, pr.tol, pr.rel_tol
-        g.radiation_on, g.adiabatic_surfaces = int(case.radiationOn), int(case.adiabatic)
-        g.wind_speed, g.wind_from_deg, g.wind_exponent = case.wind
-        keep = {}
-        for n in ("blocked", "lx", "ly", "lz"):
-            keep[n] = np.ascontiguousarray(getattr(case, n), dtype=np.uint8)
-        for n in ("fx", "fy", "fz", "ax", "ay", "az"):
-            keep[n] = np.ascontiguousarray(getattr(case, n), dtype=np.float64)
-        for n, a in keep.items():
-            setattr(g, n, a.ctypes.data)
+        g, keep = make_grid(case)
         r = self.L.phx_create(ctypes.byref(g), precision, ctypes.byref(self.h))
         if r != 0:
             raise PhxError(r, self.L.phx_last_global_error().decode())
@@ -134,3 +140,108 @@ class Solver:
 
     def last_launches(self) -> int:
         return int(self.L.phx_last_step_launches(self.h))
+
+
+class Batch:
+    """Several scenarios stepped together by the same kernel launches (one CUDA
+    graph per step). Scenario indices are positions; removing one moves the
+    later ones down."""
+
+    def __init__(self, cases=(), precision: int = _lib.PREC_FP64, add_burners: bool = True):
+        self.L = _lib.load()
+        self.h = ctypes.c_void_p()
+        self.precision = precision
+        r = self.L.phx_create_batch(None, 0, precision, ctypes.byref(self.h))
+        if r != 0:
+            raise PhxError(r, self.L.phx_last_global_error().decode())
+        self.cases = []
+        for c in cases:
+            self.add(c, add_burners)
+
+    def close(self):
+        if self.h:
+            self.L.phx_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, r):
+        if r != 0:
+            raise PhxError(r, self.L.phx_last_error(self.h).decode())
+
+    def add(self, case, add_burners: bool = True) -> int:
+        g, keep = make_grid(case)
+        sid = ctypes.c_int(-1)
+        self._check(self.L.phx_batch_add(self.h, ctypes.byref(g), ctypes.byref(sid)))
+        self.cases.append(case)
+        if add_burners:
+            for b in case.burners:
+                idx = ctypes.c_int(-1)
+                self._check(self.L.phx_batch_add_burner(self.h, sid.value, b.x0, b.y0, b.x1, b.y1, b.z, b.peakW,
+                                                        b.rampS, b.start, b.duration, ctypes.byref(idx)))
+        return sid.value
+
+    def remove(self, s: int):
+        self._check(self.L.phx_batch_remove(self.h, s))
+        del self.cases[s]
+
+    def __len__(self):
+        return self.L.phx_batch_size(self.h)
+
+    def scenario_bytes(self, s: int) -> int:
+        return int(self.L.phx_batch_scenario_bytes(self.h, s))
+
+    def step(self, dtMax=None) -> np.ndarray:
+        """One step of every scenario; dtMax: scalar or one per scenario (default:
+        each scenario's profile dtMax). Returns each scenario's dt."""
+        n = len(self)
+        if dtMax is None:
+            dtm = np.array([c.profile.dtMax for c in self.cases], np.float64)
+        else:
+            dtm = np.broadcast_to(np.asarray(dtMax, np.float64), (n,)).copy()
+        out = np.zeros(n, np.float64)
+        self._check(self.L.phx_batch_step(self.h, _ptr(dtm), 0.0, _ptr(out)))
+        return out
+
+    def run(self, n: int, dtMax: float):
+        for _ in range(n):
+            self.step_fast(dtMax)
+
+    def step_fast(self, dtMax: float):
+        """One step of every scenario with one dtMax and no read-back."""
+        self._check(self.L.phx_batch_step(self.h, None, float(dtMax), None))
+
+    def get(self, s: int, name: str) -> np.ndarray:
+        fid = FIELD_ID[name]
+        n = self.L.phx_batch_field_count(self.h, s, fid)
+        dt = np.uint8 if name == "lit" else np.int32 if name == "zone" else np.float64
+        a = np.zeros(n, dt)
+        self._check(self.L.phx_batch_get_field(self.h, s, fid, _ptr(a), a.nbytes))
+        return a
+
+    def stats(self, s: int) -> dict:
+        st = PhxStats()
+        self._check(self.L.phx_batch_get_stats(self.h, s, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in PhxStats._fields_}
+
+    def device_bytes(self) -> int:
+        return int(self.L.phx_device_bytes(self.h))
+
+    def sync(self):
+        self._check(self.L.phx_sync(self.h))
+
+    def time_steps(self, n: int, dtMax: float, flush_l2: bool = False):
+        tot, nl = ctypes.c_double(), ctypes.c_int()
+        self._check(self.L.phx_time_steps(self.h, n, dtMax, int(flush_l2), ctypes.byref(tot), ctypes.byref(nl)))
+        return tot.value, nl.value
+
+    def profile_step(self, dtMax: float, flush_l2: bool = False) -> list:
+        cap = 128
+        arr = (_lib.PhxKernelTime * cap)()
+        n = ctypes.c_int()
+        self._check(self.L.phx_profile_step(self.h, dtMax, int(flush_l2), arr, cap, ctypes.byref(n)))
+        return [(arr[i].name.decode(), arr[i].launches, arr[i].ms) for i in range(min(n.value, cap))]
