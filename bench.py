@@ -318,6 +318,8 @@ def main():
     ap.add_argument("--workload", default="batch64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--spinup", type=int, default=SPINUP_STEPS, help="untimed steps before warm-up")
+    ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64"],
+                    help="which paths to time (the line's value is the mixed path unless only fp64 runs)")
     args = ap.parse_args()
     rank, world, local = rank_info()
     if args.impl == "reference":
@@ -333,8 +335,12 @@ def main():
     if L.phx_select_device(local) != 0:
         raise SystemExit("cannot select device %d" % local)
 
-    mixed = measure(args, _lib.PREC_MIXED, L, world, clocks=True)
-    fp64 = measure(args, _lib.PREC_FP64, L, world, clocks=False)
+    mixed = measure(args, _lib.PREC_MIXED, L, world, clocks=True) if args.precision in ("both", "mixed") else None
+    fp64 = measure(args, _lib.PREC_FP64, L, world, clocks=mixed is None) if args.precision in ("both", "fp64") else None
+    if mixed is None:           # FP64 only: it is the line's measurement
+        mixed = fp64
+    if fp64 is None:
+        fp64 = mixed
     cases = mixed["cases"]
 
     cpu = None

@@ -8,6 +8,7 @@
 #pragma once
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -49,6 +50,10 @@ static T* carve(char*& base, size_t& off, size_t n) {
 }
 
 // One scenario: host set-up results, its device arena and its descriptor.
+// mixed path: CG iterations between replacements of the FP32 recursive
+// residual by the FP64 residual b - A p64
+constexpr int REPLACE_EVERY = 10;
+
 template <class R>
 struct Scenario {
     static constexpr bool kMixed = std::is_same<R, float>::value;
@@ -213,6 +218,7 @@ struct Scenario {
         s.nZones = (int)Z.zoneP.size();
         s.nClosed = (int)Z.closed.size();
         s.mixed = kMixed ? 1 : 0;
+        s.replaceEvery = REPLACE_EVERY;
         PHX_TRY(putRaw(st, s.blocked, geo.blocked.data(), N));
         PHX_TRY(put(st, s.fx, geo.fx)); PHX_TRY(put(st, s.fy, geo.fy)); PHX_TRY(put(st, s.fz, geo.fz));
         PHX_TRY(put(st, s.ax, geo.ax)); PHX_TRY(put(st, s.ay, geo.ay)); PHX_TRY(put(st, s.az, geo.az));
@@ -285,9 +291,6 @@ public:
     // the float instantiation is the mixed path: FP32 fields and stencils, FP64
     // refinement of the pressure solve, FP64 dots and global sums
     static constexpr bool kMixed = std::is_same<R, float>::value;
-    static constexpr int INNER_MAX = 10;        // inner FP32 CG iterations per refinement pass
-    static constexpr double INNER_REL = 1e-4;   // inner stop relative to the pass's starting residual
-    static constexpr int OUTER_MAX = 40;
 
     std::vector<std::unique_ptr<Scenario<R>>> sc;
     cudaStream_t st = nullptr;
@@ -299,6 +302,10 @@ public:
     int* dDomStart = nullptr;    // D_COUNT x (cap + 1)
     double* dDtMax = nullptr;    // per-scenario dtMax of the step
     int* dLoop = nullptr;        // loop counters of the graph's while nodes
+    int* dTiles = nullptr;       // [D_COUNT][cap] tiles of each scenario per domain
+    int* dAStart = nullptr;      // [2][D_COUNT][cap + 1] active-tile prefixes (solving / replacing)
+    int* dATotal = nullptr;      // [2][D_COUNT]
+    ADom adom[2][D_COUNT];
     double* hPin = nullptr;      // pinned scratch for read-backs
     Dom dom[D_COUNT];
     int maxLevels = 0;
@@ -372,6 +379,9 @@ public:
                 dDomStart = carve<int>(base, off, (size_t)D_COUNT * (cap + 1));
                 dDtMax = carve<double>(base, off, cap);
                 dLoop = carve<int>(base, off, 4);
+                dTiles = carve<int>(base, off, (size_t)D_COUNT * cap);
+                dAStart = carve<int>(base, off, (size_t)2 * D_COUNT * (cap + 1));
+                dATotal = carve<int>(base, off, 2 * D_COUNT);
                 if (pass == 0) {
                     cudaError_t e = cudaMalloc(&tab, off + 256);
                     if (e != cudaSuccess) { tab = nullptr; err = "device allocation of the batch tables failed"; return PHX_ERR_OOM; }
@@ -380,6 +390,7 @@ public:
             }
         }
         std::vector<int> starts((size_t)D_COUNT * (n + 1), 0);
+        std::vector<int> tilesAll((size_t)D_COUNT * cap, 0);
         std::vector<R*> dd(2 * std::max(n, 1), nullptr);
         maxLevels = 0;
         anyClosed = false;
@@ -387,7 +398,10 @@ public:
         for (int s = 0; s < n; ++s) {
             Scenario<R>& S = *sc[s];
             S.tiles(t);
-            for (int d = 0; d < D_COUNT; ++d) starts[(size_t)d * (n + 1) + s + 1] = starts[(size_t)d * (n + 1) + s] + t[d];
+            for (int d = 0; d < D_COUNT; ++d) {
+                starts[(size_t)d * (n + 1) + s + 1] = starts[(size_t)d * (n + 1) + s] + t[d];
+                tilesAll[(size_t)d * cap + s] = t[d];
+            }
             dd[2 * s] = S.dbuf[0];
             dd[2 * s + 1] = S.dbuf[1];
             maxLevels = std::max(maxLevels, (int)S.MG.lv.size());
@@ -399,7 +413,14 @@ public:
             dom[d].nscn = n;
             dom[d].total = starts[(size_t)d * (n + 1) + n];
         }
+        for (int k = 0; k < 2; ++k)
+            for (int d = 0; d < D_COUNT; ++d) {
+                adom[k][d].start = dAStart + (size_t)(k * D_COUNT + d) * (cap + 1);
+                adom[k][d].total = dATotal + k * D_COUNT + d;
+                adom[k][d].nscn = n;
+            }
         PHX_CK(cudaMemcpyAsync(dDomStart, starts.data(), starts.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        PHX_CK(cudaMemcpyAsync(dTiles, tilesAll.data(), tilesAll.size() * sizeof(int), cudaMemcpyHostToDevice, st));
         if (n > 0) PHX_CK(cudaMemcpyAsync(dD, dd.data(), 2 * n * sizeof(R*), cudaMemcpyHostToDevice, st));
         tablesDirty = false;
         for (int s = 0; s < n; ++s) PHX_TRY(pushDescriptor(s, false));
@@ -500,6 +521,42 @@ public:
         ++launches;
     }
 
+    // persistent grid over the active tiles of domain d (solve kernels)
+    static constexpr int PERSIST_CTAS = 152 * 8;
+    template <class K, class... A>
+    void launchA(const char* name, int d, int threads, K kern, A... args) {
+        if (dom[d].total <= 0) return;
+        const int grid = std::min(dom[d].total, PERSIST_CTAS);
+        if (prof) {
+            if (evNext + 2 > (int)evPool.size()) {
+                for (int i = 0; i < 64; ++i) { cudaEvent_t e; cudaEventCreate(&e); evPool.push_back(e); }
+            }
+            cudaEventRecord(evPool[evNext], st);
+            kern<<<grid, threads, 0, st>>>(args...);
+            cudaEventRecord(evPool[evNext + 1], st);
+            evUse.push_back({name, evNext});
+            evNext += 2;
+        } else {
+            kern<<<grid, threads, 0, st>>>(args...);
+        }
+        ++launches;
+    }
+
+    ActiveTables activeTables() const {
+        ActiveTables t;
+        t.tiles = dTiles;
+        t.astart = dAStart;
+        t.atotal = dATotal;
+        t.nscn = nscn();
+        t.cap = cap;
+        t.ndom = D_COUNT;
+        return t;
+    }
+    void rebuildActive() {
+        k_active<R><<<1, 128, 0, st>>>(dS, activeTables());
+        ++launches;
+    }
+
     int collectProfile() {
         PHX_CK(cudaStreamSynchronize(st));
         for (auto& u : evUse) {
@@ -569,21 +626,21 @@ public:
     }
     void vcycleBody() {
         const Scn<R>* S = dS;
-        launch("k_gs0", D_HALF, TPB, k_gs0<R>, S, dom[D_HALF], 1, 1);
-        launch("k_res0_restrict", D_BLK, TPB, k_res0_restrict<R>, S, dom[D_BLK]);
+        launchA("k_gs0", D_HALF, TPB, k_gs0<R>, S, adom[0][D_HALF], 1, 1);
+        launchA("k_res0_restrict", D_BLK, TPB, k_res0_restrict<R>, S, adom[0][D_BLK]);
         for (int l = 1; l < maxLevels - 1; ++l) {
-            launch("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, dom[D_LV0 + l], l, 0);
-            launch("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, dom[D_LV0 + l], l, 1);
-            launch("k_residual", D_LV0 + l, TPB, k_residual<R>, S, dom[D_LV0 + l], l);
-            launch("k_restrict", D_RS0 + l, TPB, k_restrict<R>, S, dom[D_RS0 + l], l);
+            launchA("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, adom[0][D_LV0 + l], l, 0);
+            launchA("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, adom[0][D_LV0 + l], l, 1);
+            launchA("k_residual", D_LV0 + l, TPB, k_residual<R>, S, adom[0][D_LV0 + l], l);
+            launchA("k_restrict", D_RS0 + l, TPB, k_restrict<R>, S, adom[0][D_RS0 + l], l);
         }
-        launch("k_coarse_dense", D_CO_DENSE, TPB, k_coarse_dense<R>, S, dom[D_CO_DENSE]);
-        launch("k_coarse_serial", D_CO_SERIAL, 32, k_coarse_serial<R>, S, dom[D_CO_SERIAL]);
+        launchA("k_coarse_dense", D_CO_DENSE, TPB, k_coarse_dense<R>, S, adom[0][D_CO_DENSE]);
+        launchA("k_coarse_serial", D_CO_SERIAL, 32, k_coarse_serial<R>, S, adom[0][D_CO_SERIAL]);
         for (int l = maxLevels - 2; l >= 1; --l) {
-            launch("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, dom[D_LV0 + l], l, 2);
-            launch("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, dom[D_LV0 + l], l, 1);
+            launchA("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, adom[0][D_LV0 + l], l, 2);
+            launchA("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, adom[0][D_LV0 + l], l, 1);
         }
-        launch("k_gs0", D_HALF, TPB, k_gs0<R>, S, dom[D_HALF], 1, 2);
+        launchA("k_gs0", D_HALF, TPB, k_gs0<R>, S, adom[0][D_HALF], 1, 2);
     }
     // all scenarios' flag in slot `slot` set?
     int readAll(int slot, bool& all) {
@@ -599,18 +656,27 @@ public:
     void projectPrelude() {
         const Scn<R>* S = dS;
         launch("k_reset", D_ONE, 32, k_reset<R>, S, dom[D_ONE], 0);
+        rebuildActive();
         launch("k_rhs", D_CELLS, TPB, k_rhs<R>, S, dom[D_CELLS]);
-        launch("k_gs0", D_HALF, TPB, k_gs0<R>, S, dom[D_HALF], 0, 0);
+        launchA("k_gs0", D_HALF, TPB, k_gs0<R>, S, adom[0][D_HALF], 0, 0);
         vcycleBody();
-        launch("k_gs0_last_dot", D_CELLS, TPB, k_gs0_last_dot<R>, S, dom[D_CELLS], 0);
+        launchA("k_gs0_last_dot", D_CELLS, TPB, k_gs0_last_dot<R>, S, adom[0][D_CELLS], 0);
     }
-    // one CG iteration (src/sim/gasphase.cpp:605-625)
+    // one CG iteration (src/sim/gasphase.cpp:605-625). The mixed path can
+    // replace the recursive residual by the FP64 one before preconditioning,
+    // so its first red half sweep runs after that.
     void cgIteration() {
         const Scn<R>* S = dS;
-        launch("k_cg_apply", D_CELLS, TPB, k_cg_apply<R>, S, dom[D_CELLS], (R* const*)dD);
-        launch("k_cg_update", D_CELLS, TPB, k_cg_update<R>, S, dom[D_CELLS], (R* const*)dD);
+        launchA("k_cg_apply", D_CELLS, TPB, k_cg_apply<R>, S, adom[0][D_CELLS], (R* const*)dD);
+        launchA("k_cg_update", D_CELLS, TPB, k_cg_update<R>, S, adom[0][D_CELLS], (R* const*)dD, kMixed ? 0 : 1);
+        if (kMixed) {
+            launchA("k_mx_update", D_CELLS, TPB, k_mx_update<R>, S, adom[1][D_CELLS], 1);
+            launchA("k_mx_res64", D_CELLS, TPB, k_mx_res64<R>, S, adom[1][D_CELLS], 1);
+            launchA("k_mx_zone_proj", D_CZ, TPB, k_mx_zone_proj<R>, S, adom[1][D_CZ], 1);
+            launchA("k_gs0", D_HALF, TPB, k_gs0<R>, S, adom[0][D_HALF], 0, 0);
+        }
         vcycleBody();
-        launch("k_gs0_last_dot", D_CELLS, TPB, k_gs0_last_dot<R>, S, dom[D_CELLS], 1);
+        launchA("k_gs0_last_dot", D_CELLS, TPB, k_gs0_last_dot<R>, S, adom[0][D_CELLS], 1);
     }
     // zone mean removal and velocity correction (:629-676)
     void projectEpilogue() {
@@ -621,52 +687,20 @@ public:
         launch("k_velcorr", D_FY, TPB, k_velcorr<R>, S, dom[D_FY], 1);
         launch("k_velcorr", D_FZ, TPB, k_velcorr<R>, S, dom[D_FZ], 2);
     }
-    // ---- mixed path: FP64 refinement around the FP32 inner CG -------------------------
-    void mixedBegin() {
+    // ---- mixed path: the FP32 CG starts from the FP64 residual b - A p64 ---------------
+    void mixedPrelude() {
         const Scn<R>* S = dS;
-        launch("k_reset", D_ONE, 32, k_reset<R>, S, dom[D_ONE], 1);
+        launch("k_reset", D_ONE, 32, k_reset<R>, S, dom[D_ONE], 0);
+        rebuildActive();
         launch("k_rhs", D_CELLS, TPB, k_rhs<R>, S, dom[D_CELLS]);
-        launch("k_mx_res64", D_CELLS, TPB, k_mx_res64<R>, S, dom[D_CELLS]);
-        launch("k_mx_zone_proj", D_CZ, TPB, k_mx_zone_proj<R>, S, dom[D_CZ]);
-    }
-    // the inner solve's first V-cycle and CG set-up
-    void mixedInnerPrelude() {
-        const Scn<R>* S = dS;
-        launch("k_gs0", D_HALF, TPB, k_gs0<R>, S, dom[D_HALF], 0, 0);
+        launchA("k_mx_res64", D_CELLS, TPB, k_mx_res64<R>, S, adom[0][D_CELLS], 0);
+        launchA("k_mx_zone_proj", D_CZ, TPB, k_mx_zone_proj<R>, S, adom[0][D_CZ], 0);
+        launchA("k_gs0", D_HALF, TPB, k_gs0<R>, S, adom[0][D_HALF], 0, 0);
         vcycleBody();
-        launch("k_gs0_last_dot", D_CELLS, TPB, k_gs0_last_dot<R>, S, dom[D_CELLS], 0);
+        launchA("k_gs0_last_dot", D_CELLS, TPB, k_gs0_last_dot<R>, S, adom[0][D_CELLS], 0);
     }
-    // p64 += e, and the FP64 residual of the next pass
-    void mixedRefine() {
-        const Scn<R>* S = dS;
-        launch("k_mx_update", D_CELLS, TPB, k_mx_update<R>, S, dom[D_CELLS]);
-        launch("k_mx_res64", D_CELLS, TPB, k_mx_res64<R>, S, dom[D_CELLS]);
-        launch("k_mx_zone_proj", D_CZ, TPB, k_mx_zone_proj<R>, S, dom[D_CZ]);
-    }
-    void mixedOuterHost() {
-        k_mx_outer<R><<<1, 128, 0, st>>>(dS, nscn(), cudaGraphConditionalHandle{}, nullptr, 0, 0);
-        ++launches;
-    }
-    int stProjectMixed() {
-        mixedBegin();
-        mixedOuterHost();
-        bool odone = false;
-        PHX_TRY(readAll(SV_ODONE, odone));
-        for (int pass = 0; !odone && pass <= OUTER_MAX + 1; ++pass) {
-            mixedInnerPrelude();
-            bool done = false;
-            PHX_TRY(readAll(SV_DONE, done));
-            for (int it = 0; !done && it <= INNER_MAX + 1; ++it) {
-                cgIteration();
-                PHX_TRY(readAll(SV_DONE, done));
-            }
-            mixedRefine();
-            mixedOuterHost();
-            PHX_TRY(readAll(SV_ODONE, odone));
-        }
+    void mixedEpilogue() {
         launch("k_mx_final", D_CELLS, TPB, k_mx_final<R>, dS, dom[D_CELLS]);
-        projectEpilogue();
-        return PHX_OK;
     }
 
     int maxItersAll() const {
@@ -677,15 +711,17 @@ public:
 
     // host-driven CG loop: the stop test is read back after every iteration
     int stProject() {
-        if (kMixed) return stProjectMixed();
-        projectPrelude();
+        if (kMixed) mixedPrelude();
+        else projectPrelude();
         const int maxIt = maxItersAll();
         bool done = false;
         PHX_TRY(readAll(SV_DONE, done));
         for (int it = 0; !done && it <= maxIt + 1; ++it) {
+            rebuildActive();
             cgIteration();
             PHX_TRY(readAll(SV_DONE, done));
         }
+        if (kMixed) mixedEpilogue();
         projectEpilogue();
         return PHX_OK;
     }
@@ -709,9 +745,11 @@ public:
     // ---- captured step graph: the CG loops are device-side while nodes ---------------
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
-    cudaGraphConditionalHandle cgHandle{}, outerHandle{};
-    int outerKernels = 0, bodyKernels = 0, outerBodyKernels = 0;
-    bool useGraph = true;
+    cudaGraphConditionalHandle cgHandle{};
+    int outerKernels = 0, bodyKernels = 0;
+    // the step runs as one CUDA graph; PHX_NO_GRAPH=1 launches the same kernels
+    // one by one (kernels inside conditional graphs cannot be profiled by ncu)
+    bool useGraph = std::getenv("PHX_NO_GRAPH") == nullptr;
 
     void destroyGraph() {
         if (gexec) cudaGraphExecDestroy(gexec);
@@ -746,8 +784,7 @@ public:
         const int n = nscn();
         PHX_CK(cudaGraphCreate(&graph, 0));
         // conditional handles are created before the capture of the graph that holds their node
-        if (kMixed) PHX_CK(cudaGraphConditionalHandleCreate(&outerHandle, graph, 0, 0));
-        else PHX_CK(cudaGraphConditionalHandleCreate(&cgHandle, graph, 0, 0));
+        PHX_CK(cudaGraphConditionalHandleCreate(&cgHandle, graph, 0, 0));
         PHX_CK(cudaStreamBeginCaptureToGraph(st, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
         launches = 0;
         stBegin(true, 0.0);
@@ -757,79 +794,31 @@ public:
         stEnergy();
         stMomentum();
         stLeakage();
-        if (kMixed) {
-            PHX_TRY(captureMixedProject());
-        } else {
-            projectPrelude();
-            cudaMemsetAsync(dLoop, 0, sizeof(int), st);
-            const int capIt = maxItersAll() + 2;
-            k_cg_cond<R><<<1, 128, 0, st>>>(dS, n, cgHandle, dLoop, capIt);
-            ++launches;
-            cudaGraph_t body = nullptr;
-            PHX_TRY(addWhile(graph, cgHandle, &body));
-            projectEpilogue();
-            stAdvect();
-            stEnd();
-            cudaGraph_t outGraph = nullptr;
-            PHX_CK(cudaStreamEndCapture(st, &outGraph));
-            outerKernels = launches;
-            PHX_CK(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-            launches = 0;
-            cgIteration();
-            k_cg_cond<R><<<1, 128, 0, st>>>(dS, n, cgHandle, dLoop, capIt);
-            ++launches;
-            PHX_CK(cudaStreamEndCapture(st, &body));
-            bodyKernels = launches;
-        }
-        for (int s = 0; s < n; ++s) sc[s]->h = saved[s];
-        PHX_CK(cudaGraphInstantiate(&gexec, graph, 0));
-        return checkLaunch();
-    }
-
-    // mixed project in the step graph: while (refining) { inner prelude;
-    // while (inner CG) { iteration }; refine }. dLoop[0] bounds the refinement
-    // passes, dLoop[1] the inner iterations of a pass.
-    int captureMixedProject() {
-        const int n = nscn();
-        mixedBegin();
-        cudaMemsetAsync(dLoop, 0, 2 * sizeof(int), st);
-        const int capOuter = OUTER_MAX + 2, capInner = INNER_MAX + 2;
-        k_mx_outer<R><<<1, 128, 0, st>>>(dS, n, outerHandle, dLoop, capOuter, 1);
+        if (kMixed) mixedPrelude();
+        else projectPrelude();
+        cudaMemsetAsync(dLoop, 0, sizeof(int), st);
+        const int capIt = maxItersAll() + 2;
+        k_cg_cond<R><<<1, 128, 0, st>>>(dS, n, cgHandle, dLoop, capIt, activeTables(), 1);
         ++launches;
-        cudaGraph_t outerBody = nullptr;
-        PHX_TRY(addWhile(graph, outerHandle, &outerBody));
-        launch("k_mx_final", D_CELLS, TPB, k_mx_final<R>, dS, dom[D_CELLS]);
+        cudaGraph_t body = nullptr;
+        PHX_TRY(addWhile(graph, cgHandle, &body));
+        if (kMixed) mixedEpilogue();
         projectEpilogue();
         stAdvect();
         stEnd();
         cudaGraph_t outGraph = nullptr;
         PHX_CK(cudaStreamEndCapture(st, &outGraph));
         outerKernels = launches;
-        // refinement pass
-        PHX_CK(cudaGraphConditionalHandleCreate(&cgHandle, outerBody, 0, 0));
-        PHX_CK(cudaStreamBeginCaptureToGraph(st, outerBody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-        launches = 0;
-        cudaMemsetAsync(dLoop + 1, 0, sizeof(int), st);
-        mixedInnerPrelude();
-        k_cg_cond<R><<<1, 128, 0, st>>>(dS, n, cgHandle, dLoop + 1, capInner);
-        ++launches;
-        cudaGraph_t innerBody = nullptr;
-        PHX_TRY(addWhile(outerBody, cgHandle, &innerBody));
-        mixedRefine();
-        k_mx_outer<R><<<1, 128, 0, st>>>(dS, n, outerHandle, dLoop, capOuter, 1);
-        ++launches;
-        cudaGraph_t ob = nullptr;
-        PHX_CK(cudaStreamEndCapture(st, &ob));
-        outerBodyKernels = launches;
-        // inner CG iteration
-        PHX_CK(cudaStreamBeginCaptureToGraph(st, innerBody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        PHX_CK(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
         launches = 0;
         cgIteration();
-        k_cg_cond<R><<<1, 128, 0, st>>>(dS, n, cgHandle, dLoop + 1, capInner);
+        k_cg_cond<R><<<1, 128, 0, st>>>(dS, n, cgHandle, dLoop, capIt, activeTables(), 1);
         ++launches;
-        PHX_CK(cudaStreamEndCapture(st, &innerBody));
+        PHX_CK(cudaStreamEndCapture(st, &body));
         bodyKernels = launches;
-        return PHX_OK;
+        for (int s = 0; s < n; ++s) sc[s]->h = saved[s];
+        PHX_CK(cudaGraphInstantiate(&gexec, graph, 0));
+        return checkLaunch();
     }
 
     int graphStep(double dtMax, const double* per) {
@@ -840,22 +829,8 @@ public:
         return PHX_OK;
     }
 
-    // kernels the last graph step ran: the outer nodes plus the loop bodies per pass
+    // kernels the last graph step ran: the outer nodes plus the loop body per iteration
     int graphLaunchCount(int* out) {
-        if (kMixed) {
-            int lc[2] = {0, 0};
-            PHX_CK(cudaMemcpyAsync(lc, dLoop, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
-            double itTot = 0;
-            for (auto& S : sc) {
-                PHX_CK(cudaMemcpyAsync(hPin + 32, S->h.sv + SV_ITTOT, sizeof(double), cudaMemcpyDeviceToHost, st));
-                PHX_CK(cudaStreamSynchronize(st));
-                itTot = std::max(itTot, hPin[32]);
-            }
-            PHX_CK(cudaStreamSynchronize(st));
-            const int passes = std::max(0, lc[0] - 1);
-            *out = outerKernels + outerBodyKernels * passes + bodyKernels * ((int)itTot + passes);
-            return PHX_OK;
-        }
         int lc = 0;
         PHX_CK(cudaMemcpyAsync(&lc, dLoop, sizeof(int), cudaMemcpyDeviceToHost, st));
         PHX_CK(cudaStreamSynchronize(st));
@@ -925,9 +900,10 @@ public:
         const int N = S.geo.N();
         PHX_TRY(S.put(st, S.h.r, std::vector<double>(r, r + N)));
         launch("k_reset", D_ONE, 32, k_reset<R>, (const Scn<R>*)dS, dom[D_ONE], 2);
-        launch("k_gs0", D_HALF, TPB, k_gs0<R>, (const Scn<R>*)dS, dom[D_HALF], 0, 0);
+        rebuildActive();
+        launchA("k_gs0", D_HALF, TPB, k_gs0<R>, (const Scn<R>*)dS, adom[0][D_HALF], 0, 0);
         vcycleBody();
-        launch("k_gs0_last_dot", D_CELLS, TPB, k_gs0_last_dot<R>, (const Scn<R>*)dS, dom[D_CELLS], 2);
+        launchA("k_gs0_last_dot", D_CELLS, TPB, k_gs0_last_dot<R>, (const Scn<R>*)dS, adom[0][D_CELLS], 2);
         PHX_TRY(checkLaunch());
         return getReal(S.h.z, N, z);
     }
@@ -1025,7 +1001,7 @@ public:
         const double* sv = hPin + 4096;
         o->time = sv[SV_TIME]; o->dt = sv[SV_DT];
         o->max_vel = sv[SV_MAXVEL]; o->max_nu = sv[SV_MAXNU]; o->max_div = sv[SV_MAXDIV];
-        o->pressure_iters = kMixed ? (int)sv[SV_ITTOT] : (int)sv[SV_IT];
+        o->pressure_iters = (int)sv[SV_IT];
         o->pressure_residual = sv[SV_PRES]; o->pressure_rel_residual = sv[SV_PREL];
         o->hrr = sv[SV_HRR]; o->max_gas_t = sv[SV_MAXGAST]; o->burning_cells = (int)sv[SV_BURNING];
         o->fuel_in = sv[SV_FUELIN]; o->fuel_burned = sv[SV_FUELBURNED]; o->fuel_in_domain = sv[SV_FUELINDOMAIN];

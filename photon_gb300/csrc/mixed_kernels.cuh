@@ -12,13 +12,24 @@
 
 namespace phx {
 
-// r = b - A p64 in FP64; r (FP32) = r, inner iterate e = 0 (kept in p)
+// In-loop replacement kernels run for a scenario only when its last iteration
+// scheduled a replacement (SV_REPL) and it has not stopped; at the start of the
+// solve (inLoop 0) they always run.
 template <class R>
-__global__ void k_mx_res64(const Scn<R>* __restrict__ S, Dom dom) {
-    int s_, tile_;
-    locate(dom, blockIdx.x, s_, tile_);
-    const Scn<R>& g = S[s_];
-    if (g.sv[SV_ODONE] != 0) return;
+__device__ __forceinline__ bool replaceActive(const Scn<R>& g, int inLoop) {
+    return inLoop == 0 || (g.sv[SV_REPL] != 0 && g.sv[SV_DONE] == 0);
+}
+
+// r = b - A p64 in FP64 -> r (FP32); the FP32 iterate e (kept in p) restarts at 0
+template <class R>
+__global__ void k_mx_res64(const Scn<R>* __restrict__ S, ADom dom, int inLoop) {
+    const int tot_ = *dom.total;
+    for (int b_ = blockIdx.x; b_ < tot_; b_ += gridDim.x) {
+        int s_, tile_;
+        locate(dom, b_, s_, tile_);
+        const Scn<R>& g = S[s_];
+        if (!replaceActive(g, inLoop)) continue;
+        do {
     const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
     const int c = tile_ * TPB + threadIdx.x;
     double rm = 0;
@@ -45,19 +56,23 @@ __global__ void k_mx_res64(const Scn<R>* __restrict__ S, Dom dom) {
         if (!(z >= 0 && !g.zoneOpen[z])) rm = fabs(r);
     }
     blockMaxTo(g.sv + SV_R64MAX, rm);
+        } while (0);
+    }
 }
 
-// Closed zones make A singular (constants are its null space): the right-hand
-// side of the inner solve must have zero mean over each closed zone. In FP64
-// the step's b is consistent to rounding; its FP32 copy is not, so the mean of
-// the residual over each closed zone is removed before the inner solve (one
-// CTA per closed zone; FP64 sums).
+// Closed zones make A singular (constants are its null space): the residual
+// must have zero mean over each closed zone. In FP64 the step's b is
+// consistent to rounding; its FP32 copy is not, so the mean of the residual
+// over each closed zone is removed (one CTA per closed zone; FP64 sums).
 template <class R>
-__global__ void k_mx_zone_proj(const Scn<R>* __restrict__ S, Dom dom) {
-    int s_, tile_;
-    locate(dom, blockIdx.x, s_, tile_);
-    const Scn<R>& g = S[s_];
-    if (g.sv[SV_ODONE] != 0) return;
+__global__ void k_mx_zone_proj(const Scn<R>* __restrict__ S, ADom dom, int inLoop) {
+    const int tot_ = *dom.total;
+    for (int b_ = blockIdx.x; b_ < tot_; b_ += gridDim.x) {
+        int s_, tile_;
+        locate(dom, b_, s_, tile_);
+        const Scn<R>& g = S[s_];
+        if (!replaceActive(g, inLoop)) continue;
+        do {
     __shared__ double sh[32];
     __shared__ double meanSh;
     const int zi = tile_;
@@ -78,66 +93,43 @@ __global__ void k_mx_zone_proj(const Scn<R>* __restrict__ S, Dom dom) {
         }
     }
     blockMaxTo(g.sv + SV_R64MAX, rm);
+        } while (0);
+    }
 }
 
-// p64 += e after an inner solve
+// p64 += e: fold the FP32 iterate into the FP64 pressure
 template <class R>
-__global__ void k_mx_update(const Scn<R>* __restrict__ S, Dom dom) {
-    int s_, tile_;
-    locate(dom, blockIdx.x, s_, tile_);
-    const Scn<R>& g = S[s_];
-    if (g.sv[SV_ODONE] != 0) return;
+__global__ void k_mx_update(const Scn<R>* __restrict__ S, ADom dom, int inLoop) {
+    const int tot_ = *dom.total;
+    for (int b_ = blockIdx.x; b_ < tot_; b_ += gridDim.x) {
+        int s_, tile_;
+        locate(dom, b_, s_, tile_);
+        const Scn<R>& g = S[s_];
+        if (!replaceActive(g, inLoop)) continue;
+        do {
     const int c = tile_ * TPB + threadIdx.x;
     if (c < g.N && g.diag[c] > 0) g.p64[c] += (double)g.p[c];
+        } while (0);
+    }
 }
 
-// p (FP32, read by momentum and the velocity correction) = p64
+// end of the solve: p64 += e; p (FP32, read by momentum and the velocity
+// correction) = p64
 template <class R>
 __global__ void k_mx_final(const Scn<R>* __restrict__ S, Dom dom) {
     int s_, tile_;
     locate(dom, blockIdx.x, s_, tile_);
     const Scn<R>& g = S[s_];
     const int c = tile_ * TPB + threadIdx.x;
-    if (c < g.N) g.p[c] = (R)g.p64[c];
-}
-
-// refinement stop test per scenario, then the condition of the refinement
-// loop; also readies the inner CG (its stop flag and reference residual).
-// The pass counter bounds the loop whatever the flags say.
-template <class R>
-__global__ void k_mx_outer(const Scn<R>* __restrict__ S, int nscn, cudaGraphConditionalHandle handle, int* loopCount,
-                           int cap, int setCond) {
-    bool active = false;
-    for (int s = threadIdx.x; s < nscn; s += blockDim.x) {
-        const Scn<R>& g = S[s];
-        double* sv = g.sv;
-        if (sv[SV_ODONE] == 0) {
-            const double rmax = sv[SV_R64MAX];
-            const double rel = sv[SV_BMAX] > 0 ? rmax / sv[SV_BMAX] : 0.0;
-            const double res = rmax / sv[SV_INV];
-            sv[SV_PREL] = rel;
-            sv[SV_PRES] = res;
-            sv[SV_ITTOT] += sv[SV_IT];
-            sv[SV_OUTER] += 1;
-            bool more = rel > g.relTol && res > g.tol && sv[SV_OUTER] <= g.outerMax && rmax > 0;
-            if (!more) sv[SV_ODONE] = 1;
-            sv[SV_R0MAX] = rmax;
-            sv[SV_R64MAX] = 0;
-        }
-        sv[SV_DONE] = sv[SV_ODONE];   // the inner CG runs for the scenarios still refining
-        sv[SV_IT] = 0;
-        sv[SV_RMAX] = sv[SV_ODONE] != 0 ? 0.0 : sv[SV_R0MAX];   // max|r| at the inner start
-        active |= sv[SV_ODONE] == 0;
-    }
-    int any = __syncthreads_or(active);
-    if (threadIdx.x == 0 && setCond) {
-        int lc = ++(*loopCount);
-        cudaGraphSetConditional(handle, (any && lc <= cap) ? 1u : 0u);
-    }
+    if (c >= g.N) return;
+    double v = g.p64[c];
+    if (g.diag[c] > 0) v += (double)g.p[c];
+    g.p64[c] = v;
+    g.p[c] = (R)v;
 }
 
 // per-scenario resets of the solve's scalar slots (one thread per scenario):
-// which 0: FP64 CG; 1: mixed refinement; 2: a bare V-cycle
+// which 0: the CG of either path; 2: a bare V-cycle
 template <class R>
 __global__ void k_reset(const Scn<R>* __restrict__ S, Dom dom, int which) {
     int s_, tile_;
@@ -149,12 +141,8 @@ __global__ void k_reset(const Scn<R>* __restrict__ S, Dom dom, int which) {
     sv[SV_IT] = 0;
     sv[SV_RMAX] = 0;
     sv[SV_BMAX] = 0;
-    if (which == 1) {
-        sv[SV_ODONE] = 0;
-        sv[SV_OUTER] = 0;
-        sv[SV_ITTOT] = 0;
-        sv[SV_R64MAX] = 0;
-    }
+    sv[SV_R64MAX] = 0;
+    sv[SV_REPL] = 0;
 }
 
 }  // namespace phx

@@ -53,7 +53,7 @@ enum Slot {
     SV_PITERS, SV_PRES, SV_PREL, SV_HRR, SV_MAXGAST, SV_BURNING, SV_FUELIN, SV_FUELBURNED, SV_FUELINDOMAIN,
     SV_INV, SV_ACTIVE,
     // mixed path: FP64 refinement loop around the FP32 inner CG
-    SV_R64MAX, SV_R0MAX, SV_OUTER, SV_ODONE, SV_ITTOT,
+    SV_R64MAX, SV_R0MAX, SV_OUTER, SV_ODONE, SV_ITTOT, SV_REPL,
     SV_SRC_MF = 32,              // MAX_SRC injection amounts of this step (-1 = inactive)
     SV_COUNT = 64
 };
@@ -120,11 +120,9 @@ struct Scn {
     R* tmp[9];                   // turbulence: cell-centre velocities and filter passes
     // pressure solve
     R *b, *r, *z, *d, *q;
-    double* p64;                 // mixed path: FP64 pressure accumulated by the refinement loop
-    int mixed;                   // mixed path: the CG below is the inner FP32 solve
-    int innerMax;                // inner CG iterations per refinement
-    double innerRel;             // inner stop: max|r| <= innerRel * max|r| at the inner start
-    int outerMax;                // refinement passes per step
+    double* p64;                 // mixed path: FP64 pressure; the FP32 iterate p holds the part not yet folded in
+    int mixed;                   // mixed path: FP32 CG with FP64 residual replacement
+    int replaceEvery;            // mixed path: iterations between FP64 residual replacements
     int nLevels;
     Level<R> lv[MAX_LEVELS];
     // scalars and reductions
@@ -140,6 +138,25 @@ struct Dom {
     int nscn;
     int total;                   // CTAs of the launch
 };
+
+// the same over the scenarios still active in a solve: the prefix and the
+// total live in device memory and are rebuilt between iterations, so a
+// persistent grid loops over the tiles of unfinished scenarios only
+struct ADom {
+    const int* start;            // [nscn + 1], zero-width for finished scenarios
+    const int* total;
+    int nscn;
+};
+
+__device__ __forceinline__ void locate(const ADom& d, int b, int& s, int& tile) {
+    int lo = 0, hi = d.nscn - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (d.start[mid] <= b) lo = mid; else hi = mid - 1;
+    }
+    s = lo;
+    tile = b - d.start[lo];
+}
 
 __device__ __forceinline__ void locate(const Dom& d, int b, int& s, int& tile) {
     int lo = 0, hi = d.nscn - 1;

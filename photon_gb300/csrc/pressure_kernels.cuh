@@ -20,11 +20,19 @@
 
 namespace phx {
 
-#define PHX_PROLOGUE_ACTIVE(dom)          \
-    int s_, tile_;                        \
-    locate(dom, blockIdx.x, s_, tile_);   \
-    const Scn<R>& g = S[s_];              \
-    if (g.sv[SV_DONE] != 0) return;
+// Persistent loop over the active tiles of a domain: the body runs once per
+// (scenario, tile); `break` ends the current tile.
+#define PHX_TILES_BEGIN(ad)                                              \
+    const int tot_ = *(ad).total;                                        \
+    for (int b_ = blockIdx.x; b_ < tot_; b_ += gridDim.x) {              \
+        int s_, tile_;                                                   \
+        locate(ad, b_, s_, tile_);                                       \
+        const Scn<R>& g = S[s_];                                         \
+        if (g.sv[SV_DONE] != 0) continue;                                \
+        do {
+#define PHX_TILES_END \
+        } while (0);  \
+    }
 
 constexpr double OMEGA = 0.7;
 
@@ -32,19 +40,19 @@ constexpr double OMEGA = 0.7;
 // with b = r and x = z. mode 0: the other colour is still zero (x = b / diag);
 // mode 1: plain; mode 2: the other colour is first prolongated from level 1.
 template <class R>
-__global__ void k_gs0(const Scn<R>* __restrict__ S, Dom dom, int color, int mode) {
-    PHX_PROLOGUE_ACTIVE(dom);
+__global__ void k_gs0(const Scn<R>* __restrict__ S, ADom dom, int color, int mode) {
+    PHX_TILES_BEGIN(dom)
     const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
     const int hx = (nx + 1) >> 1;
     int t = tile_ * TPB + threadIdx.x;
-    if (t >= hx * ny * nz) return;
+    if (t >= hx * ny * nz) break;
     const int ii = t % hx, jk = t / hx, j = jk % ny, k = jk / ny;
     const int i = 2 * ii + ((j + k + color) & 1);
-    if (i >= nx) return;
+    if (i >= nx) break;
     const int c = i + nx * (j + ny * k);
     const double dg = g.diag[c];
     R* x = g.z;
-    if (dg <= 0) { x[c] = 0; return; }
+    if (dg <= 0) { x[c] = 0; break; }
     double s = g.r[c];
     if (mode != 0) {
         const int* agg = g.lv[0].agg;
@@ -63,17 +71,18 @@ __global__ void k_gs0(const Scn<R>* __restrict__ S, Dom dom, int color, int mode
         if (k < nz - 1) s += (double)g.a0z[c + sxy] * X(c + sxy);
     }
     x[c] = (R)(s / dg);
+    PHX_TILES_END
 }
 
 // level-0 residual (residualGrid, pressure_mg.cpp:217-235) and restriction to
 // level 1 (:285-286), one thread per 2x2x2 block
 template <class R>
-__global__ void k_res0_restrict(const Scn<R>* __restrict__ S, Dom dom) {
-    PHX_PROLOGUE_ACTIVE(dom);
+__global__ void k_res0_restrict(const Scn<R>* __restrict__ S, ADom dom) {
+    PHX_TILES_BEGIN(dom)
     const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
     const int bx = (nx + 1) >> 1, by = (ny + 1) >> 1, bz = (nz + 1) >> 1;
     int t = tile_ * TPB + threadIdx.x;
-    if (t >= bx * by * bz) return;
+    if (t >= bx * by * bz) break;
     const int bi = t % bx, bj = (t / bx) % by, bk = t / (bx * by);
     const R* x = g.z;
     const int* agg = g.lv[0].agg;
@@ -111,24 +120,25 @@ __global__ void k_res0_restrict(const Scn<R>* __restrict__ S, Dom dom) {
         }
     }
     for (int e = 0; e < na; ++e) cb[ids[e]] = (R)sums[e];
+    PHX_TILES_END
 }
 
 // damped Jacobi sweep on a coarse level (jacobi, pressure_mg.cpp:237-247).
 // mode 0: from x = 0, into y; mode 1: y -> x; mode 2: x plus the coarser
 // level's x prolongated (:290-297), into y.
 template <class R>
-__global__ void k_jacobi(const Scn<R>* __restrict__ S, Dom dom, int l, int mode) {
-    PHX_PROLOGUE_ACTIVE(dom);
+__global__ void k_jacobi(const Scn<R>* __restrict__ S, ADom dom, int l, int mode) {
+    PHX_TILES_BEGIN(dom)
     const Level<R>& L = g.lv[l];
     const int I = tile_ * TPB + threadIdx.x;
-    if (I >= L.n) return;
+    if (I >= L.n) break;
     R* out = mode == 1 ? L.x : L.y;
     const double dg = L.diag[I];
-    if (dg <= 0) { out[I] = 0; return; }
+    if (dg <= 0) { out[I] = 0; break; }
     if (mode == 0) {
         double s = L.b[I];
         out[I] = (R)((1 - OMEGA) * 0.0 + OMEGA * s / dg);
-        return;
+        break;
     }
     const R* in = mode == 1 ? L.y : L.x;
     const R* xc = mode == 2 ? g.lv[l + 1].x : nullptr;
@@ -141,16 +151,17 @@ __global__ void k_jacobi(const Scn<R>* __restrict__ S, Dom dom, int l, int mode)
     double s = L.b[I];
     for (int q = L.rowStart[I]; q < L.rowStart[I + 1]; ++q) s += (double)L.val[q] * X(L.col[q]);
     out[I] = (R)((1 - OMEGA) * X(I) + OMEGA * s / dg);
+    PHX_TILES_END
 }
 
 // residual of coarse level l (residualSparse, pressure_mg.cpp:248-257), one
 // thread per row, into the level's y buffer (free between the sweeps)
 template <class R>
-__global__ void k_residual(const Scn<R>* __restrict__ S, Dom dom, int l) {
-    PHX_PROLOGUE_ACTIVE(dom);
+__global__ void k_residual(const Scn<R>* __restrict__ S, ADom dom, int l) {
+    PHX_TILES_BEGIN(dom)
     const Level<R>& L = g.lv[l];
     const int I = tile_ * TPB + threadIdx.x;
-    if (I >= L.n) return;
+    if (I >= L.n) break;
     const double dg = L.diag[I];
     double r = 0;
     if (dg > 0) {
@@ -159,46 +170,49 @@ __global__ void k_residual(const Scn<R>* __restrict__ S, Dom dom, int l) {
         r = s;
     }
     L.y[I] = (R)r;
+    PHX_TILES_END
 }
 
 // restriction (pressure_mg.cpp:285-286): each unknown of level l+1 sums its
 // children's residuals in ascending order, the order of the reference's scatter
 template <class R>
-__global__ void k_restrict(const Scn<R>* __restrict__ S, Dom dom, int l) {
-    PHX_PROLOGUE_ACTIVE(dom);
+__global__ void k_restrict(const Scn<R>* __restrict__ S, ADom dom, int l) {
+    PHX_TILES_BEGIN(dom)
     const Level<R>& L = g.lv[l];
     const Level<R>& C = g.lv[l + 1];
     const int J = tile_ * TPB + threadIdx.x;
-    if (J >= C.n) return;
+    if (J >= C.n) break;
     double acc = 0.0;
     for (int e = L.childStart[J]; e < L.childStart[J + 1]; ++e) acc = (double)(R)(acc + (double)L.y[L.child[e]]);
     C.b[J] = (R)acc;
+    PHX_TILES_END
 }
 
 // coarsest level: x = M b with the dense operator of the reference's 20
 // forward + backward Gauss-Seidel sweeps (pressure_mg.cpp:258-266, 279).
 // One warp per row.
 template <class R>
-__global__ void k_coarse_dense(const Scn<R>* __restrict__ S, Dom dom) {
-    PHX_PROLOGUE_ACTIVE(dom);
+__global__ void k_coarse_dense(const Scn<R>* __restrict__ S, ADom dom) {
+    PHX_TILES_BEGIN(dom)
     const Level<R>& L = g.lv[g.nLevels - 1];
     const int row = tile_ * (TPB / 32) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
-    if (row >= L.n) return;
+    if (row >= L.n) break;
     const R* M = L.dense + (size_t)row * L.n;
     double acc = 0;
     for (int j = lane; j < L.n; j += 32) acc += (double)M[j] * (double)L.b[j];
     acc = warpSum(acc);
     if (lane == 0) L.x[row] = (R)acc;
+    PHX_TILES_END
 }
 
 // coarsest level solved as the reference does it: 20 forward + backward
 // sweeps, serially in one thread (used when the level is too large for a dense
 // operator)
 template <class R>
-__global__ void k_coarse_serial(const Scn<R>* __restrict__ S, Dom dom) {
-    PHX_PROLOGUE_ACTIVE(dom);
-    if (threadIdx.x != 0) return;
+__global__ void k_coarse_serial(const Scn<R>* __restrict__ S, ADom dom) {
+    PHX_TILES_BEGIN(dom)
+    if (threadIdx.x != 0) break;
     const Level<R>& L = g.lv[g.nLevels - 1];
     for (int I = 0; I < L.n; ++I) L.x[I] = 0;
     for (int it = 0; it < 20; ++it)
@@ -211,13 +225,13 @@ __global__ void k_coarse_serial(const Scn<R>* __restrict__ S, Dom dom) {
                 for (int q = L.rowStart[I]; q < L.rowStart[I + 1]; ++q) s += (double)L.val[q] * (double)L.x[L.col[q]];
                 L.x[I] = (R)(s / dg);
             }
+    PHX_TILES_END
 }
 
 // CG stop test of the reference (src/sim/gasphase.cpp:605) plus the optional
 // relative test max|r| <= relTol max|b|
 template <class R>
 __device__ __forceinline__ bool cgContinue(const Scn<R>& g, double res, double rmax, int it, double rz) {
-    if (g.mixed) return it < g.innerMax && rz > 0 && rmax > g.innerRel * g.sv[SV_R0MAX];
     double relStop = g.relTol > 0 ? g.relTol * g.sv[SV_BMAX] : -1.0;
     return res > g.tol && it < g.maxIters && rz > 0 && !(rmax <= relStop);
 }
@@ -227,8 +241,8 @@ __device__ __forceinline__ bool cgContinue(const Scn<R>& g, double res, double r
 // CTA of the scenario closes the iteration. phase 0: first preconditioning
 // before the loop; 1: inside the loop; 2: a bare V-cycle (no CG bookkeeping).
 template <class R>
-__global__ void k_gs0_last_dot(const Scn<R>* __restrict__ S, Dom dom, int phase) {
-    PHX_PROLOGUE_ACTIVE(dom);
+__global__ void k_gs0_last_dot(const Scn<R>* __restrict__ S, ADom dom, int phase) {
+    PHX_TILES_BEGIN(dom)
     const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
     const int c = tile_ * TPB + threadIdx.x;
     double dot = 0;
@@ -256,12 +270,10 @@ __global__ void k_gs0_last_dot(const Scn<R>* __restrict__ S, Dom dom, int phase)
         }
         dot = (double)g.r[c] * zc;
     }
-    if (phase == 2) return;
+    if (phase == 2) break;
     double tot;
     if (lastCtaSum(g, PS_RZ, tile_, ntilesOf(dom, s_), dot, &tot) && threadIdx.x == 0) {
         double* sv = g.sv;
-        const double rmax = sv[SV_RMAX];
-        const double res = rmax / sv[SV_INV];
         int it = (int)sv[SV_IT];
         if (phase == 0) {
             sv[SV_RZ] = tot;
@@ -272,11 +284,39 @@ __global__ void k_gs0_last_dot(const Scn<R>* __restrict__ S, Dom dom, int phase)
             it += 1;
         }
         sv[SV_IT] = it;
-        sv[SV_PRES] = res;
-        sv[SV_PREL] = sv[SV_BMAX] > 0 ? rmax / sv[SV_BMAX] : 0.0;
-        sv[SV_RMAX] = 0;
-        if (!cgContinue(g, res, rmax, it, sv[SV_RZ])) sv[SV_DONE] = 1;
+        if (!g.mixed) {
+            const double rmax = sv[SV_RMAX];
+            const double res = rmax / sv[SV_INV];
+            sv[SV_PRES] = res;
+            sv[SV_PREL] = sv[SV_BMAX] > 0 ? rmax / sv[SV_BMAX] : 0.0;
+            sv[SV_RMAX] = 0;
+            if (!cgContinue(g, res, rmax, it, sv[SV_RZ])) sv[SV_DONE] = 1;
+        } else {
+            // mixed: the stop test uses the FP64 residual, known where it was
+            // just replaced; the FP32 recursive residual schedules the next
+            // replacement (every replaceEvery iterations, or once it claims
+            // convergence)
+            const bool replaced = phase == 0 || sv[SV_REPL] != 0;
+            bool converged = false;
+            if (replaced) {
+                const double r64 = sv[SV_R64MAX];
+                const double res = r64 / sv[SV_INV];
+                const double rel = sv[SV_BMAX] > 0 ? r64 / sv[SV_BMAX] : 0.0;
+                sv[SV_PRES] = res;
+                sv[SV_PREL] = rel;
+                converged = !(res > g.tol) || (g.relTol > 0 && rel <= g.relTol) || !(r64 > 0);
+                sv[SV_R64MAX] = 0;
+            }
+            const bool stop = converged || it >= g.maxIters || !(sv[SV_RZ] > 0);
+            const double rrec = sv[SV_RMAX];
+            const bool claims = phase != 0 && ((g.relTol > 0 && rrec <= 2.0 * g.relTol * sv[SV_BMAX]) ||
+                                               rrec / sv[SV_INV] <= 0.5 * g.tol);
+            sv[SV_REPL] = (!stop && phase != 0 && ((it % g.replaceEvery) == 0 || claims)) ? 1.0 : 0.0;
+            sv[SV_RMAX] = 0;
+            if (stop) sv[SV_DONE] = 1;
+        }
     }
+    PHX_TILES_END
 }
 
 // q = A d with the search direction updated on the fly
@@ -284,8 +324,8 @@ __global__ void k_gs0_last_dot(const Scn<R>* __restrict__ S, Dom dom, int phase)
 // d.q partial sums; the last CTA computes alpha or stops on d.q <= 0 (:606-608).
 // d is double-buffered by iteration parity.
 template <class R>
-__global__ void k_cg_apply(const Scn<R>* __restrict__ S, Dom dom, R* const* dbuf) {
-    PHX_PROLOGUE_ACTIVE(dom);
+__global__ void k_cg_apply(const Scn<R>* __restrict__ S, ADom dom, R* const* dbuf) {
+    PHX_TILES_BEGIN(dom)
     const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
     const int c = tile_ * TPB + threadIdx.x;
     const int it = (int)g.sv[SV_IT];
@@ -322,14 +362,15 @@ __global__ void k_cg_apply(const Scn<R>* __restrict__ S, Dom dom, R* const* dbuf
         if (tot <= 0) g.sv[SV_DONE] = 1;
         else g.sv[SV_ALPHA] = g.sv[SV_RZ] / tot;
     }
+    PHX_TILES_END
 }
 
 // p += alpha d; r -= alpha q (src/sim/gasphase.cpp:609-615), max|r| for the
 // stop test (:592-602), and the first red half sweep of the next V-cycle
 // (x = r / diag, the black cells being zero)
 template <class R>
-__global__ void k_cg_update(const Scn<R>* __restrict__ S, Dom dom, R* const* dbuf) {
-    PHX_PROLOGUE_ACTIVE(dom);
+__global__ void k_cg_update(const Scn<R>* __restrict__ S, ADom dom, R* const* dbuf, int redSweep) {
+    PHX_TILES_BEGIN(dom)
     const int c = tile_ * TPB + threadIdx.x;
     double rm = 0;
     if (c < g.N) {
@@ -346,25 +387,61 @@ __global__ void k_cg_update(const Scn<R>* __restrict__ S, Dom dom, R* const* dbu
         rm = fabs(r);
         const int nx = g.nx, ny = g.ny;
         const int i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
-        if (((i + j + k) & 1) == 0) g.z[c] = dg > 0 ? (R)(r / dg) : (R)0;
+        if (redSweep && ((i + j + k) & 1) == 0) g.z[c] = dg > 0 ? (R)(r / dg) : (R)0;
     }
     blockMaxTo(g.sv + SV_RMAX, rm);
+    PHX_TILES_END
+}
+
+// Active-tile tables of the solve: for every domain, the prefix of the tiles
+// of the scenarios still solving (kind 0) and of those replacing their
+// residual this iteration (kind 1, mixed path).
+struct ActiveTables {
+    const int* tiles;            // [ndom][cap] tiles of each scenario
+    int* astart;                 // [2][ndom][cap + 1]
+    int* atotal;                 // [2][ndom]
+    int nscn, cap, ndom;
+};
+
+template <class R>
+__device__ void buildActive(const Scn<R>* __restrict__ S, const ActiveTables& t) {
+    for (int kd = threadIdx.x; kd < 2 * t.ndom; kd += blockDim.x) {
+        const int kind = kd / t.ndom, d = kd % t.ndom;
+        int* as = t.astart + (size_t)(kind * t.ndom + d) * (t.cap + 1);
+        int acc = 0;
+        as[0] = 0;
+        for (int s = 0; s < t.nscn; ++s) {
+            const double* sv = S[s].sv;
+            const bool on = sv[SV_DONE] == 0 && (kind == 0 || sv[SV_REPL] != 0);
+            acc += on ? t.tiles[(size_t)d * t.cap + s] : 0;
+            as[s + 1] = acc;
+        }
+        t.atotal[kind * t.ndom + d] = acc;
+    }
+}
+
+template <class R>
+__global__ void k_active(const Scn<R>* __restrict__ S, ActiveTables t) {
+    buildActive(S, t);
 }
 
 // Condition of the CG while-loop of the captured step graph: continue while
 // any scenario of the launch has not stopped. The loop counter bounds the
 // loop whatever the scenarios' flags say, so the graph always terminates.
+// Also rebuilds the active-tile tables for the next iteration.
 template <class R>
 __global__ void k_cg_cond(const Scn<R>* __restrict__ S, int nscn, cudaGraphConditionalHandle handle, int* loopCount,
-                          int cap) {
+                          int cap, ActiveTables t, int setCond) {
     bool active = false;
     for (int s = threadIdx.x; s < nscn; s += blockDim.x) active |= S[s].sv[SV_DONE] == 0;
     int any = __syncthreads_or(active);
-    if (threadIdx.x == 0) {
+    buildActive(S, t);
+    if (threadIdx.x == 0 && setCond) {
         int lc = ++(*loopCount);
         cudaGraphSetConditional(handle, (any && lc <= cap) ? 1u : 0u);
     }
 }
 
-#undef PHX_PROLOGUE_ACTIVE
+#undef PHX_TILES_BEGIN
+#undef PHX_TILES_END
 }  // namespace phx

@@ -54,6 +54,7 @@ __device__ bool lastCtaSum(const Scn<R>& g, int slot, int tile, int ntiles, doub
 }
 
 __device__ __forceinline__ int ntilesOf(const Dom& d, int s) { return __ldg(d.start + s + 1) - __ldg(d.start + s); }
+__device__ __forceinline__ int ntilesOf(const ADom& d, int s) { return d.start[s + 1] - d.start[s]; }
 
 // ---------------------------------------------------------------------------
 // Solver::stableDt (src/sim/gasphase.cpp:63-70) and the injection amounts of
@@ -591,7 +592,10 @@ __global__ void k_zone_mean(const Scn<R>* __restrict__ S, Dom dom) {
     __shared__ double sh[32];
     const int zi = tile_;
     double acc = 0;
-    for (int e = g.closedStart[zi] + threadIdx.x; e < g.closedStart[zi + 1]; e += blockDim.x) acc += (double)g.p[g.closedCells[e]];
+    for (int e = g.closedStart[zi] + threadIdx.x; e < g.closedStart[zi + 1]; e += blockDim.x) {
+        const int c = g.closedCells[e];
+        acc += g.p64 ? g.p64[c] : (double)g.p[c];   // mixed path: the FP64 pressure
+    }
     double sum = blockSum(acc, sh);
     if (threadIdx.x == 0) {
         double cnt = (double)(g.closedStart[zi + 1] - g.closedStart[zi]);
@@ -606,7 +610,13 @@ __global__ void k_zone_mean_sub(const Scn<R>* __restrict__ S, Dom dom) {
     int n = g.closedStart[g.nClosed];
     if (e >= n) return;
     int c = g.closedCells[e];
-    g.p[c] = (R)((double)g.p[c] - g.zoneMean[g.zone[c]]);
+    const double mean = g.zoneMean[g.zone[c]];
+    if (g.p64) {   // mixed path: the FP64 pressure is the solution; p follows it
+        g.p64[c] -= mean;
+        g.p[c] = (R)g.p64[c];
+    } else {
+        g.p[c] = (R)((double)g.p[c] - mean);
+    }
 }
 
 // velocity correction u -= dt/dx grad H on matrix faces, clamp, maxVel
