@@ -265,7 +265,7 @@ struct Scenario {
         t[D_ONE] = 1;
         t[D_CELLS] = cdiv(N, TPB);
         t[D_HALF] = cdiv((long long)((nx + 1) / 2) * ny * nz, TPB);
-        t[D_BLK] = cdiv((long long)((nx + 1) / 2) * ((ny + 1) / 2) * ((nz + 1) / 2), TPB);
+        t[D_BLK] = cdiv(nx, RB_X) * ((ny + 1) / 2) * ((nz + 1) / 2);   // 64 x 2 x 2 cells per tile
         t[D_FX] = cdiv(geo.NX(), TPB);
         t[D_FY] = cdiv(geo.NY(), TPB);
         t[D_FZ] = cdiv(geo.NZ(), TPB);
@@ -338,6 +338,7 @@ public:
 
     // ---- membership ---------------------------------------------------------------
     int addScenario(const phx_grid* g, int* id) override {
+        if (nscn() >= MAX_BATCH) { err = "batch is full (1024 scenarios)"; return PHX_ERR_BUDGET; }
         auto s = std::make_unique<Scenario<R>>();
         int r = s->setup(g);   // validation and host set-up first: no device needed to reject bad input
         if (r == PHX_OK) {

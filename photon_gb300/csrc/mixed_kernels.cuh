@@ -23,10 +23,13 @@ __device__ __forceinline__ bool replaceActive(const Scn<R>& g, int inLoop) {
 // r = b - A p64 in FP64 -> r (FP32); the FP32 iterate e (kept in p) restarts at 0
 template <class R>
 __global__ void k_mx_res64(const Scn<R>* __restrict__ S, ADom dom, int inLoop) {
-    const int tot_ = *dom.total;
+    __shared__ int sst_[MAX_BATCH + 1];
+    for (int i_ = threadIdx.x; i_ <= dom.nscn; i_ += blockDim.x) sst_[i_] = dom.start[i_];
+    __syncthreads();
+    const int tot_ = sst_[dom.nscn];
     for (int b_ = blockIdx.x; b_ < tot_; b_ += gridDim.x) {
         int s_, tile_;
-        locate(dom, b_, s_, tile_);
+        locateShared(sst_, dom.nscn, b_, s_, tile_);
         const Scn<R>& g = S[s_];
         if (!replaceActive(g, inLoop)) continue;
         do {
@@ -66,10 +69,13 @@ __global__ void k_mx_res64(const Scn<R>* __restrict__ S, ADom dom, int inLoop) {
 // over each closed zone is removed (one CTA per closed zone; FP64 sums).
 template <class R>
 __global__ void k_mx_zone_proj(const Scn<R>* __restrict__ S, ADom dom, int inLoop) {
-    const int tot_ = *dom.total;
+    __shared__ int sst_[MAX_BATCH + 1];
+    for (int i_ = threadIdx.x; i_ <= dom.nscn; i_ += blockDim.x) sst_[i_] = dom.start[i_];
+    __syncthreads();
+    const int tot_ = sst_[dom.nscn];
     for (int b_ = blockIdx.x; b_ < tot_; b_ += gridDim.x) {
         int s_, tile_;
-        locate(dom, b_, s_, tile_);
+        locateShared(sst_, dom.nscn, b_, s_, tile_);
         const Scn<R>& g = S[s_];
         if (!replaceActive(g, inLoop)) continue;
         do {
@@ -100,10 +106,13 @@ __global__ void k_mx_zone_proj(const Scn<R>* __restrict__ S, ADom dom, int inLoo
 // p64 += e: fold the FP32 iterate into the FP64 pressure
 template <class R>
 __global__ void k_mx_update(const Scn<R>* __restrict__ S, ADom dom, int inLoop) {
-    const int tot_ = *dom.total;
+    __shared__ int sst_[MAX_BATCH + 1];
+    for (int i_ = threadIdx.x; i_ <= dom.nscn; i_ += blockDim.x) sst_[i_] = dom.start[i_];
+    __syncthreads();
+    const int tot_ = sst_[dom.nscn];
     for (int b_ = blockIdx.x; b_ < tot_; b_ += gridDim.x) {
         int s_, tile_;
-        locate(dom, b_, s_, tile_);
+        locateShared(sst_, dom.nscn, b_, s_, tile_);
         const Scn<R>& g = S[s_];
         if (!replaceActive(g, inLoop)) continue;
         do {

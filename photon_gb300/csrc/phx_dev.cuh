@@ -45,6 +45,7 @@ constexpr int NSC = 10;          // transported scalars: T Yo Yf Ys Ya Yp Yc Yw 
 constexpr int MAX_SRC = 16;      // burners + ignitions per scenario
 constexpr int MAX_LEVELS = 12;   // multigrid levels (the reference's cap)
 constexpr int TPB = 256;         // threads per CTA of the cell/face kernels
+constexpr int MAX_BATCH = 1024;  // scenarios per batch (the persistent kernels keep their table in shared memory)
 
 // scalar slots of a scenario (double each)
 enum Slot {
@@ -147,6 +148,17 @@ struct ADom {
     const int* total;
     int nscn;
 };
+
+// binary search in a shared-memory copy of an active prefix
+__device__ __forceinline__ void locateShared(const int* st, int nscn, int b, int& s, int& tile) {
+    int lo = 0, hi = nscn - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (st[mid] <= b) lo = mid; else hi = mid - 1;
+    }
+    s = lo;
+    tile = b - st[lo];
+}
 
 __device__ __forceinline__ void locate(const ADom& d, int b, int& s, int& tile) {
     int lo = 0, hi = d.nscn - 1;

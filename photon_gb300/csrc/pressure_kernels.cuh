@@ -23,10 +23,14 @@ namespace phx {
 // Persistent loop over the active tiles of a domain: the body runs once per
 // (scenario, tile); `break` ends the current tile.
 #define PHX_TILES_BEGIN(ad)                                              \
-    const int tot_ = *(ad).total;                                        \
+    __shared__ int sst_[MAX_BATCH + 1];                                  \
+    for (int i_ = threadIdx.x; i_ <= (ad).nscn; i_ += blockDim.x)        \
+        sst_[i_] = (ad).start[i_];                                       \
+    __syncthreads();                                                     \
+    const int tot_ = sst_[(ad).nscn];                                    \
     for (int b_ = blockIdx.x; b_ < tot_; b_ += gridDim.x) {              \
         int s_, tile_;                                                   \
-        locate(ad, b_, s_, tile_);                                       \
+        locateShared(sst_, (ad).nscn, b_, s_, tile_);                    \
         const Scn<R>& g = S[s_];                                         \
         if (g.sv[SV_DONE] != 0) continue;                                \
         do {
@@ -75,51 +79,62 @@ __global__ void k_gs0(const Scn<R>* __restrict__ S, ADom dom, int color, int mod
 }
 
 // level-0 residual (residualGrid, pressure_mg.cpp:217-235) and restriction to
-// level 1 (:285-286), one thread per 2x2x2 block
+// level 1 (:285-286). A tile is 64 x 2 x 2 cells: each thread computes one
+// cell's residual (coalesced) into shared memory, then 32 threads sum the
+// 2x2x2 blocks of the tile per level-1 aggregate in ascending cell order --
+// the order of the reference's scatter (every aggregate lies in one block).
+constexpr int RB_X = 64;
 template <class R>
 __global__ void k_res0_restrict(const Scn<R>* __restrict__ S, ADom dom) {
+    __shared__ double rs[256];
+    __shared__ int ag[256];
     PHX_TILES_BEGIN(dom)
     const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
-    const int bx = (nx + 1) >> 1, by = (ny + 1) >> 1, bz = (nz + 1) >> 1;
-    int t = tile_ * TPB + threadIdx.x;
-    if (t >= bx * by * bz) break;
-    const int bi = t % bx, bj = (t / bx) % by, bk = t / (bx * by);
+    const int ntx = (nx + RB_X - 1) / RB_X, nty = (ny + 1) >> 1;
+    const int tx = tile_ % ntx, tj = (tile_ / ntx) % nty, tk = tile_ / (ntx * nty);
+    const int xi = threadIdx.x & (RB_X - 1), jj = (threadIdx.x >> 6) & 1, kk = threadIdx.x >> 7;
+    const int i = tx * RB_X + xi, j = 2 * tj + jj, k = 2 * tk + kk;
     const R* x = g.z;
-    const int* agg = g.lv[0].agg;
-    R* cb = g.lv[1].b;
-    int ids[8];
-    double sums[8];
-    int na = 0;
-    for (int dk = 0; dk < 2; ++dk) {
-        const int k = 2 * bk + dk;
-        if (k >= nz) break;
-        for (int dj = 0; dj < 2; ++dj) {
-            const int j = 2 * bj + dj;
-            if (j >= ny) break;
-            for (int di = 0; di < 2; ++di) {
-                const int i = 2 * bi + di;
-                if (i >= nx) break;
-                const int c = i + nx * (j + ny * k);
-                const int A = agg[c];
-                if (A < 0) continue;
-                const double dg = g.diag[c];
-                const int fx0 = i + (nx + 1) * (j + ny * k), fy0 = i + nx * (j + (ny + 1) * k);
-                double s = (double)g.r[c] - dg * (double)x[c];
-                if (i > 0) s += (double)g.a0x[fx0] * (double)x[c - 1];
-                if (i < nx - 1) s += (double)g.a0x[fx0 + 1] * (double)x[c + 1];
-                if (j > 0) s += (double)g.a0y[fy0] * (double)x[c - nx];
-                if (j < ny - 1) s += (double)g.a0y[fy0 + nx] * (double)x[c + nx];
-                if (k > 0) s += (double)g.a0z[c] * (double)x[c - sxy];
-                if (k < nz - 1) s += (double)g.a0z[c + sxy] * (double)x[c + sxy];
-                s = (double)(R)s;
-                int e = 0;
-                while (e < na && ids[e] != A) ++e;
-                if (e == na) { ids[na] = A; sums[na] = 0.0; ++na; }
-                sums[e] = (double)(R)(sums[e] + s);
-            }
+    double rv = 0;
+    int A = -1;
+    if (i < nx && j < ny && k < nz) {
+        const int c = i + nx * (j + ny * k);
+        A = g.lv[0].agg[c];
+        if (A >= 0) {
+            const double dg = g.diag[c];
+            const int fx0 = i + (nx + 1) * (j + ny * k), fy0 = i + nx * (j + (ny + 1) * k);
+            double s = (double)g.r[c] - dg * (double)x[c];
+            if (i > 0) s += (double)g.a0x[fx0] * (double)x[c - 1];
+            if (i < nx - 1) s += (double)g.a0x[fx0 + 1] * (double)x[c + 1];
+            if (j > 0) s += (double)g.a0y[fy0] * (double)x[c - nx];
+            if (j < ny - 1) s += (double)g.a0y[fy0 + nx] * (double)x[c + nx];
+            if (k > 0) s += (double)g.a0z[c] * (double)x[c - sxy];
+            if (k < nz - 1) s += (double)g.a0z[c + sxy] * (double)x[c + sxy];
+            rv = (double)(R)s;
         }
     }
-    for (int e = 0; e < na; ++e) cb[ids[e]] = (R)sums[e];
+    rs[threadIdx.x] = rv;
+    ag[threadIdx.x] = A;
+    __syncthreads();
+    if (threadIdx.x < RB_X / 2) {
+        R* cb = g.lv[1].b;
+        int ids[8];
+        double sums[8];
+        int na = 0;
+        for (int dk = 0; dk < 2; ++dk)
+            for (int dj = 0; dj < 2; ++dj)
+                for (int di = 0; di < 2; ++di) {
+                    const int q = dk * 128 + dj * 64 + 2 * threadIdx.x + di;
+                    const int a = ag[q];
+                    if (a < 0) continue;
+                    int e = 0;
+                    while (e < na && ids[e] != a) ++e;
+                    if (e == na) { ids[na] = a; sums[na] = 0.0; ++na; }
+                    sums[e] = (double)(R)(sums[e] + rs[q]);
+                }
+        for (int e = 0; e < na; ++e) cb[ids[e]] = (R)sums[e];
+    }
+    __syncthreads();
     PHX_TILES_END
 }
 
@@ -272,7 +287,7 @@ __global__ void k_gs0_last_dot(const Scn<R>* __restrict__ S, ADom dom, int phase
     }
     if (phase == 2) break;
     double tot;
-    if (lastCtaSum(g, PS_RZ, tile_, ntilesOf(dom, s_), dot, &tot) && threadIdx.x == 0) {
+    if (lastCtaSum(g, PS_RZ, tile_, (sst_[s_ + 1] - sst_[s_]), dot, &tot) && threadIdx.x == 0) {
         double* sv = g.sv;
         int it = (int)sv[SV_IT];
         if (phase == 0) {
@@ -357,7 +372,7 @@ __global__ void k_cg_apply(const Scn<R>* __restrict__ S, ADom dom, R* const* dbu
         }
     }
     double tot;
-    if (lastCtaSum(g, PS_DQ, tile_, ntilesOf(dom, s_), dot, &tot) && threadIdx.x == 0) {
+    if (lastCtaSum(g, PS_DQ, tile_, (sst_[s_ + 1] - sst_[s_]), dot, &tot) && threadIdx.x == 0) {
         g.sv[SV_DQ] = tot;
         if (tot <= 0) g.sv[SV_DONE] = 1;
         else g.sv[SV_ALPHA] = g.sv[SV_RZ] / tot;
