@@ -202,11 +202,62 @@ __device__ __forceinline__ double warpSum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     return v;
 }
+__device__ __forceinline__ float warpSum(float v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ float warpMax(float v) {
+    for (int o = 16; o > 0; o >>= 1) v = mx(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
 
 // CTA-wide max of non-negative values into *dst (one atomic per warp)
 __device__ __forceinline__ void blockMaxTo(double* dst, double v) {
     v = warpMax(v);
     if ((threadIdx.x & 31) == 0) atomicMaxPos(dst, v);
+}
+__device__ __forceinline__ void blockMaxTo(double* dst, float v) {
+    v = warpMax(v);
+    if ((threadIdx.x & 31) == 0) atomicMaxPos(dst, (double)v);
+}
+
+// Sums of the FP32 path: an unevaluated pair hi + lo of floats (about 48
+// significant bits) formed and added with FP32 instructions only -- the exact
+// product of Dekker (an FMA yields the rounding error of a*b) and Knuth's
+// TwoSum, i.e. the double-float arithmetic of Hida, Li & Bailey's QD library.
+// GB300 issues FP64 at a small fraction of its FP32 rate, so the dot products
+// of the FP32 CG keep FP64-grade accuracy at FP32 cost. The _rn intrinsics
+// keep the compiler from contracting the error terms.
+struct F2 {
+    float hi, lo;
+};
+__device__ __forceinline__ F2 f2prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return F2{p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ F2 f2add(F2 a, F2 b) {
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float v = __fsub_rn(s, a.hi);
+    const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, v)), __fsub_rn(b.hi, v));
+    const float t = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    const float hi = __fadd_rn(s, t);
+    return F2{hi, __fsub_rn(t, __fsub_rn(hi, s))};
+}
+__device__ __forceinline__ double f2value(F2 v) { return (double)v.hi + (double)v.lo; }
+
+// one term of a dot product in the accumulator of the arithmetic type
+__device__ __forceinline__ double dotTerm(double a, double b) { return a * b; }
+__device__ __forceinline__ F2 dotTerm(float a, float b) { return f2prod(a, b); }
+__device__ __forceinline__ double accAdd(double a, double b) { return a + b; }
+__device__ __forceinline__ F2 accAdd(F2 a, F2 b) { return f2add(a, b); }
+
+__device__ __forceinline__ F2 warpSum(F2 v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const F2 w{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
+        v = f2add(v, w);
+    }
+    return v;
 }
 
 // fixed-order CTA sum (the order depends only on the CTA size)
@@ -222,6 +273,22 @@ __device__ __forceinline__ double blockSum(double v, double* sh) {
         t = warpSum(t);
     }
     return t;   // valid in thread 0
+}
+// the same for double-float terms; the CTA total is rounded to double once
+__device__ __forceinline__ double blockSum(F2 v, double* sh) {
+    static_assert(sizeof(F2) == sizeof(double), "F2 shares the double scratch");
+    F2* shf = reinterpret_cast<F2*>(sh);
+    v = warpSum(v);
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (l == 0) shf[w] = v;
+    __syncthreads();
+    F2 t{0.f, 0.f};
+    if (w == 0) {
+        if (l < nw) t = shf[l];
+        t = warpSum(t);
+    }
+    return f2value(t);   // valid in thread 0
 }
 
 // Solver::windAt (src/sim/gasphase.cpp:52-61); NaN = no inflow on this face

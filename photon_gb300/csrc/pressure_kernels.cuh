@@ -40,11 +40,16 @@ namespace phx {
 
 constexpr double OMEGA = 0.7;
 
+// The solve kernels compute in the arithmetic type T = R of the path (FP64 or
+// FP32); dot products accumulate in Acc (double, or a double-float pair on
+// the FP32 path) and reach the per-scenario scalars as doubles.
+
 // level-0 Gauss-Seidel half sweep of one colour (gsColor, pressure_mg.cpp:195-216)
 // with b = r and x = z. mode 0: the other colour is still zero (x = b / diag);
 // mode 1: plain; mode 2: the other colour is first prolongated from level 1.
 template <class R>
 __global__ void k_gs0(const Scn<R>* __restrict__ S, ADom dom, int color, int mode) {
+    using T = R;
     PHX_TILES_BEGIN(dom)
     const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
     const int hx = (nx + 1) >> 1;
@@ -54,27 +59,27 @@ __global__ void k_gs0(const Scn<R>* __restrict__ S, ADom dom, int color, int mod
     const int i = 2 * ii + ((j + k + color) & 1);
     if (i >= nx) break;
     const int c = i + nx * (j + ny * k);
-    const double dg = g.diag[c];
+    const T dg = g.diag[c];
     R* x = g.z;
     if (dg <= 0) { x[c] = 0; break; }
-    double s = g.r[c];
+    T s = g.r[c];
     if (mode != 0) {
         const int* agg = g.lv[0].agg;
         const R* xc = g.lv[1].x;
-        auto X = [&](int n) -> double {
-            double v = x[n];
-            if (mode == 2) { int a = agg[n]; if (a >= 0) v = v + (double)xc[a]; }
+        auto X = [&](int n) -> T {
+            T v = x[n];
+            if (mode == 2) { int a = agg[n]; if (a >= 0) v = v + xc[a]; }
             return v;
         };
         const int fx0 = i + (nx + 1) * (j + ny * k), fy0 = i + nx * (j + (ny + 1) * k);
-        if (i > 0) s += (double)g.a0x[fx0] * X(c - 1);
-        if (i < nx - 1) s += (double)g.a0x[fx0 + 1] * X(c + 1);
-        if (j > 0) s += (double)g.a0y[fy0] * X(c - nx);
-        if (j < ny - 1) s += (double)g.a0y[fy0 + nx] * X(c + nx);
-        if (k > 0) s += (double)g.a0z[c] * X(c - sxy);
-        if (k < nz - 1) s += (double)g.a0z[c + sxy] * X(c + sxy);
+        if (i > 0) s += g.a0x[fx0] * X(c - 1);
+        if (i < nx - 1) s += g.a0x[fx0 + 1] * X(c + 1);
+        if (j > 0) s += g.a0y[fy0] * X(c - nx);
+        if (j < ny - 1) s += g.a0y[fy0 + nx] * X(c + nx);
+        if (k > 0) s += g.a0z[c] * X(c - sxy);
+        if (k < nz - 1) s += g.a0z[c + sxy] * X(c + sxy);
     }
-    x[c] = (R)(s / dg);
+    x[c] = s / dg;
     PHX_TILES_END
 }
 
@@ -86,7 +91,8 @@ __global__ void k_gs0(const Scn<R>* __restrict__ S, ADom dom, int color, int mod
 constexpr int RB_X = 64;
 template <class R>
 __global__ void k_res0_restrict(const Scn<R>* __restrict__ S, ADom dom) {
-    __shared__ double rs[256];
+    using T = R;
+    __shared__ T rs[256];
     __shared__ int ag[256];
     PHX_TILES_BEGIN(dom)
     const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
@@ -95,22 +101,22 @@ __global__ void k_res0_restrict(const Scn<R>* __restrict__ S, ADom dom) {
     const int xi = threadIdx.x & (RB_X - 1), jj = (threadIdx.x >> 6) & 1, kk = threadIdx.x >> 7;
     const int i = tx * RB_X + xi, j = 2 * tj + jj, k = 2 * tk + kk;
     const R* x = g.z;
-    double rv = 0;
+    T rv = 0;
     int A = -1;
     if (i < nx && j < ny && k < nz) {
         const int c = i + nx * (j + ny * k);
         A = g.lv[0].agg[c];
         if (A >= 0) {
-            const double dg = g.diag[c];
+            const T dg = g.diag[c];
             const int fx0 = i + (nx + 1) * (j + ny * k), fy0 = i + nx * (j + (ny + 1) * k);
-            double s = (double)g.r[c] - dg * (double)x[c];
-            if (i > 0) s += (double)g.a0x[fx0] * (double)x[c - 1];
-            if (i < nx - 1) s += (double)g.a0x[fx0 + 1] * (double)x[c + 1];
-            if (j > 0) s += (double)g.a0y[fy0] * (double)x[c - nx];
-            if (j < ny - 1) s += (double)g.a0y[fy0 + nx] * (double)x[c + nx];
-            if (k > 0) s += (double)g.a0z[c] * (double)x[c - sxy];
-            if (k < nz - 1) s += (double)g.a0z[c + sxy] * (double)x[c + sxy];
-            rv = (double)(R)s;
+            T s = g.r[c] - dg * x[c];
+            if (i > 0) s += g.a0x[fx0] * x[c - 1];
+            if (i < nx - 1) s += g.a0x[fx0 + 1] * x[c + 1];
+            if (j > 0) s += g.a0y[fy0] * x[c - nx];
+            if (j < ny - 1) s += g.a0y[fy0 + nx] * x[c + nx];
+            if (k > 0) s += g.a0z[c] * x[c - sxy];
+            if (k < nz - 1) s += g.a0z[c + sxy] * x[c + sxy];
+            rv = s;
         }
     }
     rs[threadIdx.x] = rv;
@@ -119,7 +125,7 @@ __global__ void k_res0_restrict(const Scn<R>* __restrict__ S, ADom dom) {
     if (threadIdx.x < RB_X / 2) {
         R* cb = g.lv[1].b;
         int ids[8];
-        double sums[8];
+        T sums[8];
         int na = 0;
         for (int dk = 0; dk < 2; ++dk)
             for (int dj = 0; dj < 2; ++dj)
@@ -129,10 +135,10 @@ __global__ void k_res0_restrict(const Scn<R>* __restrict__ S, ADom dom) {
                     if (a < 0) continue;
                     int e = 0;
                     while (e < na && ids[e] != a) ++e;
-                    if (e == na) { ids[na] = a; sums[na] = 0.0; ++na; }
-                    sums[e] = (double)(R)(sums[e] + rs[q]);
+                    if (e == na) { ids[na] = a; sums[na] = T(0); ++na; }
+                    sums[e] = sums[e] + rs[q];
                 }
-        for (int e = 0; e < na; ++e) cb[ids[e]] = (R)sums[e];
+        for (int e = 0; e < na; ++e) cb[ids[e]] = sums[e];
     }
     __syncthreads();
     PHX_TILES_END
@@ -143,29 +149,31 @@ __global__ void k_res0_restrict(const Scn<R>* __restrict__ S, ADom dom) {
 // level's x prolongated (:290-297), into y.
 template <class R>
 __global__ void k_jacobi(const Scn<R>* __restrict__ S, ADom dom, int l, int mode) {
+    using T = R;
     PHX_TILES_BEGIN(dom)
     const Level<R>& L = g.lv[l];
     const int I = tile_ * TPB + threadIdx.x;
     if (I >= L.n) break;
     R* out = mode == 1 ? L.x : L.y;
-    const double dg = L.diag[I];
+    const T dg = L.diag[I];
     if (dg <= 0) { out[I] = 0; break; }
+    const T om = T(OMEGA);
     if (mode == 0) {
-        double s = L.b[I];
-        out[I] = (R)((1 - OMEGA) * 0.0 + OMEGA * s / dg);
+        T s = L.b[I];
+        out[I] = (T(1) - om) * T(0) + om * s / dg;
         break;
     }
     const R* in = mode == 1 ? L.y : L.x;
     const R* xc = mode == 2 ? g.lv[l + 1].x : nullptr;
     const int* agg = L.agg;
-    auto X = [&](int n) -> double {
-        double v = in[n];
-        if (mode == 2) v = v + (double)xc[agg[n]];
+    auto X = [&](int n) -> T {
+        T v = in[n];
+        if (mode == 2) v = v + xc[agg[n]];
         return v;
     };
-    double s = L.b[I];
-    for (int q = L.rowStart[I]; q < L.rowStart[I + 1]; ++q) s += (double)L.val[q] * X(L.col[q]);
-    out[I] = (R)((1 - OMEGA) * X(I) + OMEGA * s / dg);
+    T s = L.b[I];
+    for (int q = L.rowStart[I]; q < L.rowStart[I + 1]; ++q) s += L.val[q] * X(L.col[q]);
+    out[I] = (T(1) - om) * X(I) + om * s / dg;
     PHX_TILES_END
 }
 
@@ -173,18 +181,19 @@ __global__ void k_jacobi(const Scn<R>* __restrict__ S, ADom dom, int l, int mode
 // thread per row, into the level's y buffer (free between the sweeps)
 template <class R>
 __global__ void k_residual(const Scn<R>* __restrict__ S, ADom dom, int l) {
+    using T = R;
     PHX_TILES_BEGIN(dom)
     const Level<R>& L = g.lv[l];
     const int I = tile_ * TPB + threadIdx.x;
     if (I >= L.n) break;
-    const double dg = L.diag[I];
-    double r = 0;
+    const T dg = L.diag[I];
+    T r = 0;
     if (dg > 0) {
-        double s = (double)L.b[I] - dg * (double)L.x[I];
-        for (int q = L.rowStart[I]; q < L.rowStart[I + 1]; ++q) s += (double)L.val[q] * (double)L.x[L.col[q]];
+        T s = L.b[I] - dg * L.x[I];
+        for (int q = L.rowStart[I]; q < L.rowStart[I + 1]; ++q) s += L.val[q] * L.x[L.col[q]];
         r = s;
     }
-    L.y[I] = (R)r;
+    L.y[I] = r;
     PHX_TILES_END
 }
 
@@ -192,14 +201,15 @@ __global__ void k_residual(const Scn<R>* __restrict__ S, ADom dom, int l) {
 // children's residuals in ascending order, the order of the reference's scatter
 template <class R>
 __global__ void k_restrict(const Scn<R>* __restrict__ S, ADom dom, int l) {
+    using T = R;
     PHX_TILES_BEGIN(dom)
     const Level<R>& L = g.lv[l];
     const Level<R>& C = g.lv[l + 1];
     const int J = tile_ * TPB + threadIdx.x;
     if (J >= C.n) break;
-    double acc = 0.0;
-    for (int e = L.childStart[J]; e < L.childStart[J + 1]; ++e) acc = (double)(R)(acc + (double)L.y[L.child[e]]);
-    C.b[J] = (R)acc;
+    T acc = 0;
+    for (int e = L.childStart[J]; e < L.childStart[J + 1]; ++e) acc = acc + L.y[L.child[e]];
+    C.b[J] = acc;
     PHX_TILES_END
 }
 
@@ -208,16 +218,17 @@ __global__ void k_restrict(const Scn<R>* __restrict__ S, ADom dom, int l) {
 // One warp per row.
 template <class R>
 __global__ void k_coarse_dense(const Scn<R>* __restrict__ S, ADom dom) {
+    using T = R;
     PHX_TILES_BEGIN(dom)
     const Level<R>& L = g.lv[g.nLevels - 1];
     const int row = tile_ * (TPB / 32) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (row >= L.n) break;
     const R* M = L.dense + (size_t)row * L.n;
-    double acc = 0;
-    for (int j = lane; j < L.n; j += 32) acc += (double)M[j] * (double)L.b[j];
+    T acc = 0;
+    for (int j = lane; j < L.n; j += 32) acc += M[j] * L.b[j];
     acc = warpSum(acc);
-    if (lane == 0) L.x[row] = (R)acc;
+    if (lane == 0) L.x[row] = acc;
     PHX_TILES_END
 }
 
@@ -226,6 +237,7 @@ __global__ void k_coarse_dense(const Scn<R>* __restrict__ S, ADom dom) {
 // operator)
 template <class R>
 __global__ void k_coarse_serial(const Scn<R>* __restrict__ S, ADom dom) {
+    using T = R;
     PHX_TILES_BEGIN(dom)
     if (threadIdx.x != 0) break;
     const Level<R>& L = g.lv[g.nLevels - 1];
@@ -234,11 +246,11 @@ __global__ void k_coarse_serial(const Scn<R>* __restrict__ S, ADom dom) {
         for (int dir = 0; dir < 2; ++dir)
             for (int t = 0; t < L.n; ++t) {
                 int I = dir == 0 ? t : L.n - 1 - t;
-                double dg = L.diag[I];
+                T dg = L.diag[I];
                 if (dg <= 0) { L.x[I] = 0; continue; }
-                double s = L.b[I];
-                for (int q = L.rowStart[I]; q < L.rowStart[I + 1]; ++q) s += (double)L.val[q] * (double)L.x[L.col[q]];
-                L.x[I] = (R)(s / dg);
+                T s = L.b[I];
+                for (int q = L.rowStart[I]; q < L.rowStart[I + 1]; ++q) s += L.val[q] * L.x[L.col[q]];
+                L.x[I] = s / dg;
             }
     PHX_TILES_END
 }
@@ -257,33 +269,36 @@ __device__ __forceinline__ bool cgContinue(const Scn<R>& g, double res, double r
 // before the loop; 1: inside the loop; 2: a bare V-cycle (no CG bookkeeping).
 template <class R>
 __global__ void k_gs0_last_dot(const Scn<R>* __restrict__ S, ADom dom, int phase) {
+    using T = R;
+    using Acc = decltype(dotTerm(T(0), T(0)));
     PHX_TILES_BEGIN(dom)
     const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
     const int c = tile_ * TPB + threadIdx.x;
-    double dot = 0;
+    Acc dot{};
     if (c < g.N) {
         const int i = c % nx, j = (c / nx) % ny, k = c / sxy;
         R* x = g.z;
-        double zc;
+        const T rc = g.r[c];
+        T zc;
         if (((i + j + k) & 1) == 0) {
-            const double dg = g.diag[c];
+            const T dg = g.diag[c];
             if (dg <= 0) zc = 0;
             else {
                 const int fx0 = i + (nx + 1) * (j + ny * k), fy0 = i + nx * (j + (ny + 1) * k);
-                double s = g.r[c];
-                if (i > 0) s += (double)g.a0x[fx0] * (double)x[c - 1];
-                if (i < nx - 1) s += (double)g.a0x[fx0 + 1] * (double)x[c + 1];
-                if (j > 0) s += (double)g.a0y[fy0] * (double)x[c - nx];
-                if (j < ny - 1) s += (double)g.a0y[fy0 + nx] * (double)x[c + nx];
-                if (k > 0) s += (double)g.a0z[c] * (double)x[c - sxy];
-                if (k < nz - 1) s += (double)g.a0z[c + sxy] * (double)x[c + sxy];
-                zc = (double)(R)(s / dg);
+                T s = rc;
+                if (i > 0) s += g.a0x[fx0] * x[c - 1];
+                if (i < nx - 1) s += g.a0x[fx0 + 1] * x[c + 1];
+                if (j > 0) s += g.a0y[fy0] * x[c - nx];
+                if (j < ny - 1) s += g.a0y[fy0 + nx] * x[c + nx];
+                if (k > 0) s += g.a0z[c] * x[c - sxy];
+                if (k < nz - 1) s += g.a0z[c + sxy] * x[c + sxy];
+                zc = s / dg;
             }
-            x[c] = (R)zc;
+            x[c] = zc;
         } else {
             zc = x[c];
         }
-        dot = (double)g.r[c] * zc;
+        dot = dotTerm(rc, zc);
     }
     if (phase == 2) break;
     double tot;
@@ -340,35 +355,35 @@ __global__ void k_gs0_last_dot(const Scn<R>* __restrict__ S, ADom dom, int phase
 // d is double-buffered by iteration parity.
 template <class R>
 __global__ void k_cg_apply(const Scn<R>* __restrict__ S, ADom dom, R* const* dbuf) {
+    using T = R;
+    using Acc = decltype(dotTerm(T(0), T(0)));
     PHX_TILES_BEGIN(dom)
     const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
     const int c = tile_ * TPB + threadIdx.x;
     const int it = (int)g.sv[SV_IT];
     const R* dprev = dbuf[2 * s_ + (it & 1)];
     R* dnew = dbuf[2 * s_ + ((it + 1) & 1)];
-    const double beta = g.sv[SV_BETA];
+    const T beta = (T)g.sv[SV_BETA];
     const R* z = g.z;
-    auto D = [&](int n) -> double {
-        return it == 0 ? (double)z[n] : (double)(R)((double)z[n] + (double)(R)(beta * (double)dprev[n]));
-    };
-    double dot = 0;
+    auto D = [&](int n) -> T { return it == 0 ? z[n] : (T)(z[n] + beta * dprev[n]); };
+    Acc dot{};
     if (c < g.N) {
-        const double dc = D(c);
-        dnew[c] = (R)dc;
-        const double dg = g.diag[c];
+        const T dc = D(c);
+        dnew[c] = dc;
+        const T dg = g.diag[c];
         if (dg <= 0) g.q[c] = 0;
         else {
             const int i = c % nx, j = (c / nx) % ny, k = c / sxy;
             const int fx0 = i + (nx + 1) * (j + ny * k), fy0 = i + nx * (j + (ny + 1) * k);
-            double s = dg * dc;
-            if (i > 0) s -= (double)g.a0x[fx0] * D(c - 1);
-            if (i < nx - 1) s -= (double)g.a0x[fx0 + 1] * D(c + 1);
-            if (j > 0) s -= (double)g.a0y[fy0] * D(c - nx);
-            if (j < ny - 1) s -= (double)g.a0y[fy0 + nx] * D(c + nx);
-            if (k > 0) s -= (double)g.a0z[c] * D(c - sxy);
-            if (k < nz - 1) s -= (double)g.a0z[c + sxy] * D(c + sxy);
-            g.q[c] = (R)s;
-            dot = (double)(R)s * dc;
+            T s = dg * dc;
+            if (i > 0) s -= g.a0x[fx0] * D(c - 1);
+            if (i < nx - 1) s -= g.a0x[fx0 + 1] * D(c + 1);
+            if (j > 0) s -= g.a0y[fy0] * D(c - nx);
+            if (j < ny - 1) s -= g.a0y[fy0 + nx] * D(c + nx);
+            if (k > 0) s -= g.a0z[c] * D(c - sxy);
+            if (k < nz - 1) s -= g.a0z[c + sxy] * D(c + sxy);
+            g.q[c] = s;
+            dot = dotTerm(s, dc);
         }
     }
     double tot;
@@ -385,24 +400,25 @@ __global__ void k_cg_apply(const Scn<R>* __restrict__ S, ADom dom, R* const* dbu
 // (x = r / diag, the black cells being zero)
 template <class R>
 __global__ void k_cg_update(const Scn<R>* __restrict__ S, ADom dom, R* const* dbuf, int redSweep) {
+    using T = R;
     PHX_TILES_BEGIN(dom)
     const int c = tile_ * TPB + threadIdx.x;
-    double rm = 0;
+    T rm = 0;
     if (c < g.N) {
         const int it = (int)g.sv[SV_IT];
         const R* d = dbuf[2 * s_ + ((it + 1) & 1)];
-        const double alpha = g.sv[SV_ALPHA];
-        const double dg = g.diag[c];
-        double r = g.r[c];
+        const T alpha = (T)g.sv[SV_ALPHA];
+        const T dg = g.diag[c];
+        T r = g.r[c];
         if (dg > 0) {
-            g.p[c] = (R)((double)g.p[c] + (double)(R)(alpha * (double)d[c]));
-            r = (double)(R)(r - (double)(R)(alpha * (double)g.q[c]));
-            g.r[c] = (R)r;
+            g.p[c] = g.p[c] + alpha * d[c];
+            r = r - alpha * g.q[c];
+            g.r[c] = r;
         }
         rm = fabs(r);
         const int nx = g.nx, ny = g.ny;
         const int i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
-        if (redSweep && ((i + j + k) & 1) == 0) g.z[c] = dg > 0 ? (R)(r / dg) : (R)0;
+        if (redSweep && ((i + j + k) & 1) == 0) g.z[c] = dg > 0 ? r / dg : T(0);
     }
     blockMaxTo(g.sv + SV_RMAX, rm);
     PHX_TILES_END

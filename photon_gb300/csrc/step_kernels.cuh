@@ -28,8 +28,8 @@ __device__ __forceinline__ double gasDensity(const Scn<R>& g, int c) {
 // order) and stores the partial; the CTA that finishes last sums the partials
 // in CTA order. Every thread of the CTA must call it. Returns true in every
 // thread of the last CTA, with the total in *total (thread 0).
-template <class R>
-__device__ bool lastCtaSum(const Scn<R>& g, int slot, int tile, int ntiles, double vThread, double* total) {
+template <class R, class V>
+__device__ bool lastCtaSum(const Scn<R>& g, int slot, int tile, int ntiles, V vThread, double* total) {
     __shared__ double sh[32];
     __shared__ int amLast;
     double v = blockSum(vThread, sh);
