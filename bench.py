@@ -95,6 +95,18 @@ def kernel_bytes(name: str, w: int):
     return table.get(name)
 
 
+def launched_cells(name: str, launches: int, iters, sizes) -> int:
+    """Cells processed by all launches of one kernel in one step. A scenario
+    that stopped after it CG iterations took part in it launches of q = A d and
+    of the update, and in it + 1 of the closing half sweep with r.z; every
+    other kernel runs over every cell at each launch."""
+    if name in ("k_cg_apply", "k_cg_update"):
+        return sum(i * n for i, n in zip(iters, sizes))
+    if name == "k_gs0_last_dot":
+        return sum((i + 1) * n for i, n in zip(iters, sizes))
+    return launches * sum(sizes)
+
+
 def measured_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -288,6 +300,7 @@ def measure(args, precision, L, world, clocks: bool):
     e2e_value = cells * args.steps * world / e2e_s
     # per-kernel device times of one step (outside the timed region) for the roofline
     prof = g.profile_step(dtMax, flush_l2=flush)
+    prof_iters = [g.stats(s)["pressure_iters"] for s in range(len(cases))]
     tot_prof = sum(p[2] for p in prof)
     top = max(prof, key=lambda p: p[2])
     w = 8 if precision == _lib.PREC_FP64 else 4
@@ -295,7 +308,10 @@ def measure(args, precision, L, world, clocks: bool):
     peak, peak_kind = measured_peak()
     roof = None
     if per_unit:
-        bytes_per_launch = per_unit * cells
+        # cells the kernel's launches of the profiled step processed: the CG
+        # kernels skip scenarios that have stopped iterating
+        units = launched_cells(top[0], top[1], prof_iters, [c.N for c in cases])
+        bytes_per_launch = per_unit * units / top[1]
         achieved = bytes_per_launch / (top[2] / top[1] / 1e3) / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": None, "kernel": top[0], "kernel_share": top[2] / tot_prof,

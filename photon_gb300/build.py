@@ -30,7 +30,7 @@ UNITS = {
     "api.cpp": [],
 }
 HEADERS = ["phx_dev.cuh", "step_kernels.cuh", "pressure_kernels.cuh", "engine.cuh", "engine.h", "host_setup.h",
-           "mixed_kernels.cuh", "engine_mixed.cuh"]
+           "mixed_kernels.cuh", "engine_mixed.cuh", "rowblock.cuh"]
 
 
 def _newer(target, deps):

@@ -18,6 +18,7 @@
 #include "engine.h"
 #include "host_setup.h"
 #include "mixed_kernels.cuh"
+#include "rowblock.cuh"
 
 namespace phx {
 
@@ -33,9 +34,11 @@ namespace phx {
 
 // dense coarse operators up to this many unknowns (n^2 reals)
 constexpr int DENSE_MAX = 4096;
+// dynamic shared memory of one CTA of the row-block kernels (the static part is about 4 KB)
+constexpr size_t RB_SMEM_MAX = 220 * 1024;
 
 enum DomId {
-    D_ONE = 0, D_CELLS, D_HALF, D_BLK, D_FX, D_FY, D_FZ, D_BX, D_BY, D_BZ, D_CZ, D_CC, D_CO_DENSE, D_CO_SERIAL,
+    D_ONE = 0, D_CELLS, D_HALF, D_BLK, D_FX, D_FY, D_FZ, D_BX, D_BY, D_BZ, D_CZ, D_CC, D_CO_DENSE, D_CO_SERIAL, D_RB,
     D_LV0,                       // D_LV0 + l: rows of level l when l is not the coarsest (1 <= l < 12)
     D_RS0 = D_LV0 + MAX_LEVELS,  // D_RS0 + l: rows of level l+1 for restriction from level l >= 1
     D_COUNT = D_RS0 + MAX_LEVELS
@@ -100,6 +103,10 @@ struct Scenario {
         for (auto v : geo.lz) geo.anyLeak |= v != 0;
         if (geo.anyLeak) {
             err = "crack faces (orifice-flow leakage) are not implemented in the GPU step yet";
+            return PHX_ERR_UNSUPPORTED;
+        }
+        if (rbApplySmem<R>(g->nx, g->ny) > RB_SMEM_MAX) {
+            err = "grid rows too long for the shared-memory tiles of the pressure kernels (nx = " + std::to_string(g->nx) + ")";
             return PHX_ERR_UNSUPPORTED;
         }
         cfl = g->cfl; dtMaxP = g->dt_max; tol = g->tol; relTol = g->rel_tol; maxIters = g->max_iters;
@@ -219,6 +226,8 @@ struct Scenario {
         s.nClosed = (int)Z.closed.size();
         s.mixed = kMixed ? 1 : 0;
         s.replaceEvery = REPLACE_EVERY;
+        s.tj = rowBlockRows<R>(geo.nx, geo.ny);
+        s.njb = (geo.ny + s.tj - 1) / s.tj;
         PHX_TRY(putRaw(st, s.blocked, geo.blocked.data(), N));
         PHX_TRY(put(st, s.fx, geo.fx)); PHX_TRY(put(st, s.fy, geo.fy)); PHX_TRY(put(st, s.fz, geo.fz));
         PHX_TRY(put(st, s.ax, geo.ax)); PHX_TRY(put(st, s.ay, geo.ay)); PHX_TRY(put(st, s.az, geo.az));
@@ -266,6 +275,7 @@ struct Scenario {
         t[D_CELLS] = cdiv(N, TPB);
         t[D_HALF] = cdiv((long long)((nx + 1) / 2) * ny * nz, TPB);
         t[D_BLK] = cdiv(nx, RB_X) * ((ny + 1) / 2) * ((nz + 1) / 2);   // 64 x 2 x 2 cells per tile
+        t[D_RB] = cdiv(ny, rowBlockRows<R>(nx, ny)) * cdiv(nz, RB_KZ);      // row blocks x plane blocks
         t[D_FX] = cdiv(geo.NX(), TPB);
         t[D_FY] = cdiv(geo.NY(), TPB);
         t[D_FZ] = cdiv(geo.NZ(), TPB);
@@ -305,6 +315,10 @@ public:
     int* dTiles = nullptr;       // [D_COUNT][cap] tiles of each scenario per domain
     int* dAStart = nullptr;      // [2][D_COUNT][cap + 1] active-tile prefixes (solving / replacing)
     int* dATotal = nullptr;      // [2][D_COUNT]
+    unsigned* dErr = nullptr;    // error word of the device side (bounded waits that ran out)
+    size_t rbSmem = 0;           // dynamic shared memory of the row-block kernels (max over the batch)
+    RbShape rbShape{0, 0};       // their slot and ring strides (max over the batch)
+    int rbGrid = 0;              // CTAs of their persistent grid
     ADom adom[2][D_COUNT];
     double* hPin = nullptr;      // pinned scratch for read-backs
     Dom dom[D_COUNT];
@@ -383,9 +397,11 @@ public:
                 dTiles = carve<int>(base, off, (size_t)D_COUNT * cap);
                 dAStart = carve<int>(base, off, (size_t)2 * D_COUNT * (cap + 1));
                 dATotal = carve<int>(base, off, 2 * D_COUNT);
+                dErr = carve<unsigned>(base, off, 4);
                 if (pass == 0) {
                     cudaError_t e = cudaMalloc(&tab, off + 256);
                     if (e != cudaSuccess) { tab = nullptr; err = "device allocation of the batch tables failed"; return PHX_ERR_OOM; }
+                    PHX_CK(cudaMemsetAsync(tab, 0, off + 256, st));
                     base = tab;
                 }
             }
@@ -395,6 +411,8 @@ public:
         std::vector<R*> dd(2 * std::max(n, 1), nullptr);
         maxLevels = 0;
         anyClosed = false;
+        rbSmem = 0;
+        rbShape = RbShape{0, 0};
         int t[D_COUNT];
         for (int s = 0; s < n; ++s) {
             Scenario<R>& S = *sc[s];
@@ -408,6 +426,12 @@ public:
             maxLevels = std::max(maxLevels, (int)S.MG.lv.size());
             anyClosed |= !S.Z.closed.empty();
             S.h.dtMaxArg = dDtMax + s;
+            S.h.errWord = dErr;
+            {
+                const ApplyLayout<R> L(S.geo.nx, rowBlockRows<R>(S.geo.nx, S.geo.ny));
+                rbShape.slot = std::max(rbShape.slot, L.slot);
+                rbShape.ring = std::max(rbShape.ring, L.ring);
+            }
         }
         for (int d = 0; d < D_COUNT; ++d) {
             dom[d].start = dDomStart + (size_t)d * (n + 1);
@@ -420,6 +444,22 @@ public:
                 adom[k][d].total = dATotal + k * D_COUNT + d;
                 adom[k][d].nscn = n;
             }
+        rbSmem = n > 0 ? rbApplySmem<R>(rbShape) : 0;
+        persistCtas = PERSIST_CTAS;
+        if (const char* cap = std::getenv("PHX_PERSIST_CTAS")) persistCtas = std::max(1, std::min(persistCtas, std::atoi(cap)));
+        if (rbSmem > RB_SMEM_MAX) {
+            err = "the batch's widest grids need more shared memory than a CTA has";
+            return PHX_ERR_UNSUPPORTED;
+        }
+        if (rbSmem > 0) {
+            int dev = 0, sms = 0, occ = 0;
+            PHX_CK(cudaGetDevice(&dev));
+            PHX_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            PHX_CK(cudaFuncSetAttribute(k_cg_apply_rb<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rbSmem));
+            PHX_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cg_apply_rb<R>, RB_THREADS, rbSmem));
+            rbGrid = sms * std::max(occ, 1);
+            if (const char* cap = std::getenv("PHX_PERSIST_CTAS")) rbGrid = std::max(1, std::min(rbGrid, std::atoi(cap)));
+        }
         PHX_CK(cudaMemcpyAsync(dDomStart, starts.data(), starts.size() * sizeof(int), cudaMemcpyHostToDevice, st));
         PHX_CK(cudaMemcpyAsync(dTiles, tilesAll.data(), tilesAll.size() * sizeof(int), cudaMemcpyHostToDevice, st));
         if (n > 0) PHX_CK(cudaMemcpyAsync(dD, dd.data(), 2 * n * sizeof(R*), cudaMemcpyHostToDevice, st));
@@ -524,10 +564,11 @@ public:
 
     // persistent grid over the active tiles of domain d (solve kernels)
     static constexpr int PERSIST_CTAS = 152 * 8;
+    int persistCtas = PERSIST_CTAS;   // PHX_PERSIST_CTAS caps it (tests: many tiles per CTA)
     template <class K, class... A>
     void launchA(const char* name, int d, int threads, K kern, A... args) {
         if (dom[d].total <= 0) return;
-        const int grid = std::min(dom[d].total, PERSIST_CTAS);
+        const int grid = std::min(dom[d].total, persistCtas);
         if (prof) {
             if (evNext + 2 > (int)evPool.size()) {
                 for (int i = 0; i < 64; ++i) { cudaEvent_t e; cudaEventCreate(&e); evPool.push_back(e); }
@@ -541,6 +582,39 @@ public:
             kern<<<grid, threads, 0, st>>>(args...);
         }
         ++launches;
+    }
+
+    // persistent grid over the active row-block tiles, with the staging ring in dynamic shared memory
+    template <class K, class... A>
+    void launchRB(const char* name, K kern, A... args) {
+        if (dom[D_RB].total <= 0) return;
+        const int grid = std::min(dom[D_RB].total, rbGrid);
+        if (prof) {
+            if (evNext + 2 > (int)evPool.size()) {
+                for (int i = 0; i < 64; ++i) { cudaEvent_t e; cudaEventCreate(&e); evPool.push_back(e); }
+            }
+            cudaEventRecord(evPool[evNext], st);
+            kern<<<grid, RB_THREADS, rbSmem, st>>>(args...);
+            cudaEventRecord(evPool[evNext + 1], st);
+            evUse.push_back({name, evNext});
+            evNext += 2;
+        } else {
+            kern<<<grid, RB_THREADS, rbSmem, st>>>(args...);
+        }
+        ++launches;
+    }
+
+    // the device error word: a bounded wait inside a kernel that ran out
+    int checkDeviceError() {
+        if (!dErr) return PHX_OK;
+        unsigned w = 0;
+        PHX_CK(cudaMemcpyAsync(&w, dErr, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        PHX_CK(cudaStreamSynchronize(st));
+        if (w) {
+            err = "a staged shared-memory copy did not arrive within its time limit (device error word " + std::to_string(w) + ")";
+            return PHX_ERR_CUDA;
+        }
+        return PHX_OK;
     }
 
     ActiveTables activeTables() const {
@@ -668,7 +742,7 @@ public:
     // so its first red half sweep runs after that.
     void cgIteration() {
         const Scn<R>* S = dS;
-        launchA("k_cg_apply", D_CELLS, TPB, k_cg_apply<R>, S, adom[0][D_CELLS], (R* const*)dD);
+        launchRB("k_cg_apply", k_cg_apply_rb<R>, S, adom[0][D_RB], (R* const*)dD, rbShape);
         launchA("k_cg_update", D_CELLS, TPB, k_cg_update<R>, S, adom[0][D_CELLS], (R* const*)dD, kMixed ? 0 : 1);
         if (kMixed) {
             launchA("k_mx_update", D_CELLS, TPB, k_mx_update<R>, S, adom[1][D_CELLS], 1);
@@ -868,6 +942,7 @@ public:
                 PHX_CK(cudaStreamSynchronize(st));
                 if (per) for (int s = 0; s < m; ++s) dtOut[(size_t)i * m + s] = hPin[16 + s % 4000];
                 else dtOut[i] = hPin[16];
+                PHX_TRY(checkDeviceError());
             }
         }
         return PHX_OK;
@@ -1029,7 +1104,7 @@ public:
     }
     int sync() override {
         if (st) PHX_CK(cudaStreamSynchronize(st));
-        return PHX_OK;
+        return checkDeviceError();
     }
     int lastLaunches() const override {
         if (useGraph && gexec) {
@@ -1070,7 +1145,7 @@ public:
         }
         if (totalMs) *totalMs = total;
         if (launchesOut) *launchesOut = nl;
-        return PHX_OK;
+        return checkDeviceError();
     }
 
     // one step with an event pair around every launch; per-kernel totals

@@ -126,6 +126,9 @@ struct Scn {
     int replaceEvery;            // mixed path: iterations between FP64 residual replacements
     int nLevels;
     Level<R> lv[MAX_LEVELS];
+    // row-block tiles of the level-0 pressure kernels: tj rows x RB_KZ planes, njb blocks along y
+    int tj, njb;
+    unsigned* errWord;           // the context's error word (a bounded wait that ran out sets bit 0)
     // scalars and reductions
     double* sv;
     double* part;                // PS_COUNT x partStride

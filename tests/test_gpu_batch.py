@@ -56,3 +56,26 @@ def test_batch_membership_change_keeps_results():
     for f in ("p", "T", "u", "Yf"):
         assert np.array_equal(B.get(0, f), ref[1].get(f)), f
         assert np.array_equal(B.get(1, f), ref[2].get(f)), f
+
+
+@pytest.mark.parametrize("precision", [_lib.PREC_FP64, _lib.PREC_MIXED])
+def test_batch_equals_alone_with_many_tiles_per_cta(precision, monkeypatch):
+    """Persistent grids capped at 3 CTAs: each CTA walks tiles of several
+    scenarios of different row lengths and plane counts in turn, so every
+    staging slot is reused across scenarios."""
+    monkeypatch.setenv("PHX_PERSIST_CTAS", "3")
+    cs = cases() + [casegen.house(30, 22, 34, 0.2, 5)]
+    cs[-1].profile.tol = 0.0
+    cs[-1].profile.rel_tol = 1e-8
+    B = Batch(cs, precision)
+    alone = [Solver(c, precision) for c in cs]
+    for step in range(6):
+        dts = B.step(0.02)
+        for s, g in enumerate(alone):
+            assert g.step(0.02) == dts[s]
+    for s, g in enumerate(alone):
+        for f in STATE:
+            a, b = B.get(s, f), g.get(f)
+            assert np.array_equal(a, b), (precision, s, f, float(np.max(np.abs(a - b))))
+        assert B.stats(s)["pressure_iters"] == g.stats()["pressure_iters"]
+        assert B.stats(s)["pressure_rel_residual"] <= 1e-8
