@@ -25,13 +25,13 @@ namespace phx {
 constexpr int RB_KZ = 16;          // planes per tile along z
 constexpr long long RB_WAIT_CYCLES = 2000000000LL;   // about one second at the GB300 clock
 
-// rows per tile for a grid of nx cells per row: about 512 cells per plane of
-// a tile on the FP32 path and 256 on the FP64 path (twice the bytes), even
+// rows per tile for a grid of nx cells per row: about 1024 cells per plane of
+// a tile on the FP32 path and 512 on the FP64 path (twice the bytes), even
 // (2x2x2 restriction blocks never straddle tiles), at least 2, at most ny
 // rounded up to even
 template <class R>
 __host__ __device__ inline int rowBlockRows(int nx, int ny) {
-    const int cells = sizeof(R) == 8 ? 256 : 512;
+    const int cells = sizeof(R) == 8 ? 512 : 1024;
     int tj = (cells / (nx > 0 ? nx : 1)) & ~1;
     if (tj < 2) tj = 2;
     const int cap = ny + (ny & 1);
@@ -48,14 +48,16 @@ __device__ __forceinline__ void fenceBarrierInit() { asm volatile("fence.mbarrie
 __device__ __forceinline__ void mbarArriveExpectTx(uint64_t* b, unsigned bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smemAddr(b)), "r"(bytes) : "memory");
 }
+// try_wait suspends the thread until the phase completes or the hint (ns)
+// runs out, so a waiting warp takes no issue slots from the working ones
 __device__ __forceinline__ bool mbarTryWait(uint64_t* b, unsigned parity) {
     unsigned ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(smemAddr(b)), "r"(parity)
+        : "r"(smemAddr(b)), "r"(parity), "r"(20000u)
         : "memory");
     return ok != 0;
 }
@@ -66,12 +68,16 @@ __device__ __forceinline__ void bulkLoad(void* dst, const void* src, unsigned by
                  : "memory");
 }
 
-// bounded wait for the phase of the given parity; false on time-out
-__device__ __forceinline__ bool mbarWaitBounded(uint64_t* b, unsigned parity) {
+// bounded wait for the phase of the given parity; false on time-out. Between
+// polls the warp sleeps for backoffNs so that a waiting warp (the producer is
+// usually ahead of the consumers) does not take issue slots from working ones.
+__device__ __forceinline__ bool mbarWaitBounded(uint64_t* b, unsigned parity, unsigned backoffNs = 0) {
     if (mbarTryWait(b, parity)) return true;
     const long long t0 = clock64();
-    while (!mbarTryWait(b, parity))
+    while (!mbarTryWait(b, parity)) {
         if (clock64() - t0 > RB_WAIT_CYCLES) return false;
+        if (backoffNs) __nanosleep(backoffNs);
+    }
     return true;
 }
 
@@ -257,7 +263,7 @@ __device__ void rbProducer(const Scn<R>* __restrict__ S, const int* sst, int nsc
             bool ok = true;
             if (lane == 0) {
                 if (*abortFlag) ok = false;
-                else if (q >= (unsigned)ST && !mbarWaitBounded(&empty[slot], ((q / ST) - 1) & 1)) {
+                else if (q >= (unsigned)ST && !mbarWaitBounded(&empty[slot], ((q / ST) - 1) & 1, 256)) {
                     ok = false;
                     *abortFlag = 1;
                     atomicOr(g.errWord, 2u);
@@ -294,15 +300,13 @@ drain:
 // ---------------------------------------------------------------------------------
 // q = A d with d = z + beta d (src/sim/gasphase.cpp:551-570, 620-622) and the
 // d.q partial sums (:606-608) on row-block tiles: the same arithmetic as
-// k_cg_apply. The FP32 path evaluates d at the 7 points of the stencil from the
-// staged z and d (cheap FMAs); the FP64 path, bound by the FP64 pipe, computes
-// d once per cell into a 4-plane ring in shared memory.
+// k_cg_apply. d is computed once per cell into a 4-plane ring in shared
+// memory (rows j0-1 .. j1), then the 7-point stencil reads the ring.
 //
 // Slot layout: {z, d_prev, diag, a0z, a0x, a0y}; z and d over rows j0-1 .. j1.
 template <class R>
 struct ApplyLayout {
-    static constexpr bool kRing = sizeof(R) == 8;
-    static constexpr int ST = kRing ? 4 : 6;
+    static constexpr int ST = 3;
     int cz, cc, cx, cy, slot, ring;
     __host__ __device__ ApplyLayout(int nx, int tj) {
         cz = stageCapacity<R>(tj + 2, nx);
@@ -310,25 +314,25 @@ struct ApplyLayout {
         cx = stageCapacity<R>(tj, nx + 1);
         cy = stageCapacity<R>(tj + 1, nx);
         slot = 2 * cz + 2 * cc + cx + cy;
-        ring = kRing ? roundUp((tj + 2) * nx, 4) : 0;
+        ring = roundUp((tj + 2) * nx, 4);
     }
-    __host__ __device__ size_t bytes() const { return ((size_t)ST * slot + 4 * (size_t)ring) * sizeof(R); }
 };
 
-template <class R>
-inline size_t rbApplySmem(int nx, int ny) {
-    return ApplyLayout<R>(nx, rowBlockRows<R>(nx, ny)).bytes();
-}
 template <class R>
 inline size_t rbApplySmem(const RbShape& sh) {
     return ((size_t)ApplyLayout<R>::ST * sh.slot + 4 * (size_t)sh.ring) * sizeof(R);
 }
+template <class R>
+inline size_t rbApplySmem(int nx, int ny) {
+    const ApplyLayout<R> L(nx, rowBlockRows<R>(nx, ny));
+    return rbApplySmem<R>(RbShape{L.slot, L.ring});
+}
 
 enum { SA_Z = 0, SA_D, SA_DIAG, SA_AZ, SA_AX, SA_AY, SA_COUNT };
 
-
 template <class R>
-__global__ void __launch_bounds__(RB_THREADS, 2) k_cg_apply_rb(const Scn<R>* __restrict__ S, ADom dom, R* const* dbuf, RbShape shape) {
+__global__ void __launch_bounds__(RB_THREADS, 2) k_cg_apply_rb(const Scn<R>* __restrict__ S, ADom dom, R* const* dbuf,
+                                                               RbShape shape) {
     using T = R;
     using Acc = decltype(dotTerm(T(0), T(0)));
     using LY = ApplyLayout<R>;
@@ -381,6 +385,7 @@ __global__ void __launch_bounds__(RB_THREADS, 2) k_cg_apply_rb(const Scn<R>* __r
     }
     // ---- consumers --------------------------------------------------------------
     const int tot = sst_[dom.nscn];
+    R* const ring = sm + (size_t)ST * shape.slot;
     unsigned seq = 0;
     for (int b = blockIdx.x; b < tot; b += gridDim.x) {
         int s, tile;
@@ -395,105 +400,86 @@ __global__ void __launch_bounds__(RB_THREADS, 2) k_cg_apply_rb(const Scn<R>* __r
         R* const dnew = dbuf[2 * s + ((it + 1) & 1)];
         R* const q = g.q;
         const int ncell = (t.j1 - j0) * nx;
-        // e / nx as umulhi(e, ceil(2^32 / nx)): exact for e, nx < 65536 (nx = 1 handled apart)
-        const unsigned magic = (unsigned)((0x100000000ULL + nx - 1) / nx);
-        // slot offsets of row j0 (z: row j0 - 1) of plane k
-        auto offC = [&](int k, int rowLo) { return (int)(((long long)k * t.sxy + (long long)rowLo * nx) & (EPV - 1)); };
-        auto offX = [&](int k) { return (int)(((long long)k * (nx + 1) * ny + (long long)j0 * (nx + 1)) & (EPV - 1)); };
-        auto offY = [&](int k) { return (int)(((long long)k * nx * (ny + 1) + (long long)j0 * nx) & (EPV - 1)); };
-        auto slotOf = [&](int k) { return sm + (size_t)((seq + (k - kLo)) % ST) * shape.slot; };
-        R* const ring = sm + (size_t)ST * shape.slot;
+        // e / nx as umulhi(e, ceil(2^32 / nx)): exact for e, nx < 65536 (nx = 1 apart)
+        const unsigned magic = nx == 1 ? 0u : (unsigned)((0x100000000ULL + nx - 1) / nx);
+        const int ringRa = max(j0 - 1, 0), ringRe = min(t.j1 + 1, ny);
+        // alignment offsets (mod EPV) of the first staged row of plane k: k * plane + row * pitch
+        const int mC = (int)(t.sxy & (EPV - 1)), mX = (int)(((long long)(nx + 1) * ny) & (EPV - 1));
+        const int mY = (int)(((long long)nx * (ny + 1)) & (EPV - 1));
+        const auto offMod = [](int k, int m, int rowTerm) { return ((k & (EPV - 1)) * m + rowTerm) & (EPV - 1); };
+        const int rC = (j0 * nx) & (EPV - 1), rCm = ((j0 - 1) * nx) & (EPV - 1);
+        const int rX = (j0 * (nx + 1)) & (EPV - 1), rY = rC;
         Acc dot{};
-        int waited = 0;
+        int waited = 0, released = 0;
         for (int kk = t.k0; kk < t.k1; ++kk) {
             const int ic = kk - kLo;
-            const int need = min(ic + 2, t.nPl);
-            for (; waited < need; ++waited) {
+            for (const int need = min(ic + 2, t.nPl); waited < need; ++waited) {
                 if (abortFlag) break;
                 const unsigned qn = seq + waited;
-                if (!mbarWaitBounded(&full[qn % ST], (qn / ST) & 1)) {
+                if (!mbarWaitBounded(&full[qn % ST], (qn / ST) & 1, 32)) {
                     abortFlag = 1;
                     atomicOr(g.errWord, 1u);
                 }
             }
-            if constexpr (LY::kRing) {
-                // d of the planes entering the ring (rows j0-1 .. j1), then one barrier
-                if (!abortFlag) {
-                    const int kFirst = kk == t.k0 ? kLo : kk + 1;
-                    for (int k = kFirst; k <= min(kk + 1, kHi); ++k) {
-                        const R* base = slotOf(k);
-                        const int ra = max(j0 - 1, 0), re = min(t.j1 + 1, ny);
-                        const int n = (re - ra) * nx;
-                        const int oz = offC(k, j0 - 1) + (ra - (j0 - 1)) * nx;
-                        R* out = ring + (size_t)(k & 3) * L.ring + (ra - (j0 - 1)) * nx;
-                        for (int e = threadIdx.x; e < n; e += RB_CTHREADS) {
-                            const T zv = base[oz + e];
-                            out[e] = useD ? (T)(zv + beta * base[L.cz + oz + e]) : zv;
-                        }
-                    }
-                }
-                consumerSync();
-            }
+            // d of the planes entering the ring (rows j0-1 .. j1)
             if (!abortFlag) {
-                const R* cur = slotOf(kk);
-                const R* nxt = kk + 1 <= kHi ? slotOf(kk + 1) : cur;
-                const R* prv = kk - 1 >= kLo ? slotOf(kk - 1) : cur;
-                const int oz0 = offC(kk, j0 - 1) + nx, ozm = offC(kk - 1, j0 - 1) + nx, ozp = offC(kk + 1, j0 - 1) + nx;
-                const int og = 2 * L.cz + offC(kk, j0), oZ = 2 * L.cz + L.cc + offC(kk, j0);
-                const int oZn = 2 * L.cz + L.cc + offC(kk + 1, j0);
-                const int ox = 2 * L.cz + 2 * L.cc + offX(kk), oy = 2 * L.cz + 2 * L.cc + L.cx + offY(kk);
-                const R* D0 = ring + (size_t)(kk & 3) * L.ring + nx;
-                const R* Dm = ring + (size_t)((kk + 3) & 3) * L.ring + nx;
-                const R* Dp = ring + (size_t)((kk + 1) & 3) * L.ring + nx;
+                for (int k = kk == t.k0 ? kLo : kk + 1; k <= min(kk + 1, kHi); ++k) {
+                    const R* base = sm + (size_t)((seq + (k - kLo)) % ST) * shape.slot;
+                    const int n = (ringRe - ringRa) * nx;
+                    const int oz = offMod(k, mC, rCm) + (ringRa - (j0 - 1)) * nx;
+                    const R* zs = base + oz;
+                    const R* ds = base + L.cz + oz;
+                    R* out = ring + (size_t)(k & 3) * shape.ring + (ringRa - (j0 - 1)) * nx;
+                    if (useD)
+                        for (int e = threadIdx.x; e < n; e += RB_CTHREADS) out[e] = (T)(zs[e] + beta * ds[e]);
+                    else
+                        for (int e = threadIdx.x; e < n; e += RB_CTHREADS) out[e] = zs[e];
+                }
+            }
+            consumerSync();
+            if (!abortFlag) {
+                const R* cur = sm + (size_t)((seq + ic) % ST) * shape.slot;
+                const R* nxt = kk + 1 <= kHi ? sm + (size_t)((seq + ic + 1) % ST) * shape.slot : cur;
+                const int oC = offMod(kk, mC, rC);
+                const R* dgp = cur + 2 * L.cz + oC;
+                const R* azp = cur + 2 * L.cz + L.cc + oC;
+                const R* azn = nxt + 2 * L.cz + L.cc + offMod(kk + 1, mC, rC);
+                const R* axp = cur + 2 * L.cz + 2 * L.cc + offMod(kk, mX, rX);
+                const R* ayp = cur + 2 * L.cz + 2 * L.cc + L.cx + offMod(kk, mY, rY);
+                const R* D0 = ring + (size_t)(kk & 3) * shape.ring + nx;
+                const R* Dm = ring + (size_t)((kk + 3) & 3) * shape.ring + nx;
+                const R* Dp = ring + (size_t)((kk + 1) & 3) * shape.ring + nx;
                 const long long cbase = (long long)kk * t.sxy + (long long)j0 * nx;
+                R* const dnp = dnew + cbase;
+                R* const qp = q + cbase;
+                const bool hasM = kk > 0, hasP = kk < nz - 1;
                 for (int e = threadIdx.x; e < ncell; e += RB_CTHREADS) {
-                    const int jj = nx == 1 ? e : (int)__umulhi((unsigned)e, magic), i = e - jj * nx, j = j0 + jj;
-                    const long long c = cbase + e;
-                    // d at cell e of plane k (slot base, z offset of row j0)
-                    auto Dz = [&](const R* base, int oz, int x) -> T {
-                        const T zv = base[oz + x];
-                        return useD ? (T)(zv + beta * base[L.cz + oz + x]) : zv;
-                    };
-                    T dc, dxm = 0, dxp = 0, dym = 0, dyp = 0, dzm = 0, dzp = 0;
-                    if constexpr (LY::kRing) {
-                        dc = D0[e];
-                        if (i > 0) dxm = D0[e - 1];
-                        if (i < nx - 1) dxp = D0[e + 1];
-                        if (j > 0) dym = D0[e - nx];
-                        if (j < ny - 1) dyp = D0[e + nx];
-                        if (kk > 0) dzm = Dm[e];
-                        if (kk < nz - 1) dzp = Dp[e];
-                    } else {
-                        dc = Dz(cur, oz0, e);
-                        if (i > 0) dxm = Dz(cur, oz0, e - 1);
-                        if (i < nx - 1) dxp = Dz(cur, oz0, e + 1);
-                        if (j > 0) dym = Dz(cur, oz0, e - nx);
-                        if (j < ny - 1) dyp = Dz(cur, oz0, e + nx);
-                        if (kk > 0) dzm = Dz(prv, ozm, e);
-                        if (kk < nz - 1) dzp = Dz(nxt, ozp, e);
-                    }
-                    dnew[c] = dc;
-                    const T dg = cur[og + e];
-                    if (dg <= 0) { q[c] = 0; continue; }
-                    const R* ax = cur + ox + jj * (nx + 1) + i;
+                    const int jj = nx == 1 ? e : (int)__umulhi((unsigned)e, magic);
+                    const int i = e - jj * nx, j = j0 + jj;
+                    const T dc = D0[e];
+                    dnp[e] = dc;
+                    const T dg = dgp[e];
+                    if (dg <= 0) { qp[e] = 0; continue; }
+                    const R* ax = axp + e + jj;   // a0x index jj * (nx + 1) + i
                     T sacc = dg * dc;
-                    if (i > 0) sacc -= ax[0] * dxm;
-                    if (i < nx - 1) sacc -= ax[1] * dxp;
-                    if (j > 0) sacc -= cur[oy + e] * dym;
-                    if (j < ny - 1) sacc -= cur[oy + e + nx] * dyp;
-                    if (kk > 0) sacc -= cur[oZ + e] * dzm;
-                    if (kk < nz - 1) sacc -= nxt[oZn + e] * dzp;
-                    q[c] = sacc;
+                    if (i > 0) sacc -= ax[0] * D0[e - 1];
+                    if (i < nx - 1) sacc -= ax[1] * D0[e + 1];
+                    if (j > 0) sacc -= ayp[e] * D0[e - nx];
+                    if (j < ny - 1) sacc -= ayp[e + nx] * D0[e + nx];
+                    if (hasM) sacc -= azp[e] * Dm[e];
+                    if (hasP) sacc -= azn[e] * Dp[e];
+                    qp[e] = sacc;
                     dot = accAdd(dot, dotTerm(sacc, dc));
                 }
             }
-            // plane kk - 1 is read by no later step
+            // planes up to kk are read by no later step
             __syncwarp();
-            if (lane == 0 && kk - 1 >= kLo) mbarArrive(&empty[(seq + ic - 1) % ST]);
+            if (lane == 0)
+                for (; released <= ic; ++released) mbarArrive(&empty[(seq + released) % ST]);
         }
         __syncwarp();
         if (lane == 0)
-            for (int idx = t.k1 - 1 - kLo; idx < t.nPl; ++idx) mbarArrive(&empty[(seq + idx) % ST]);
+            for (; released < t.nPl; ++released) mbarArrive(&empty[(seq + released) % ST]);
         seq += t.nPl;
         if (consumerSyncOr(abortFlag)) return;
         double total;
