@@ -105,7 +105,9 @@ struct Scenario {
             err = "crack faces (orifice-flow leakage) are not implemented in the GPU step yet";
             return PHX_ERR_UNSUPPORTED;
         }
-        if (rbApplySmem<R>(g->nx, g->ny) > RB_SMEM_MAX) {
+        RbShapes<R> one;
+        one.add(g->nx, g->ny);
+        if (one.maxSmem() > RB_SMEM_MAX) {
             err = "grid rows too long for the shared-memory tiles of the pressure kernels (nx = " + std::to_string(g->nx) + ")";
             return PHX_ERR_UNSUPPORTED;
         }
@@ -316,9 +318,13 @@ public:
     int* dAStart = nullptr;      // [2][D_COUNT][cap + 1] active-tile prefixes (solving / replacing)
     int* dATotal = nullptr;      // [2][D_COUNT]
     unsigned* dErr = nullptr;    // error word of the device side (bounded waits that ran out)
-    size_t rbSmem = 0;           // dynamic shared memory of the row-block kernels (max over the batch)
-    RbShape rbShape{0, 0};       // their slot and ring strides (max over the batch)
-    int rbGrid = 0;              // CTAs of their persistent grid
+    // launch shape of a row-block kernel: dynamic shared memory, persistent grid, slot strides
+    struct RbCfg {
+        size_t smem = 0;
+        int grid = 0;
+        RbShape shape{0, 0};
+    };
+    RbCfg cfgApply, cfgGs[3];
     ADom adom[2][D_COUNT];
     double* hPin = nullptr;      // pinned scratch for read-backs
     Dom dom[D_COUNT];
@@ -411,8 +417,7 @@ public:
         std::vector<R*> dd(2 * std::max(n, 1), nullptr);
         maxLevels = 0;
         anyClosed = false;
-        rbSmem = 0;
-        rbShape = RbShape{0, 0};
+        RbShapes<R> shp;
         int t[D_COUNT];
         for (int s = 0; s < n; ++s) {
             Scenario<R>& S = *sc[s];
@@ -427,11 +432,7 @@ public:
             anyClosed |= !S.Z.closed.empty();
             S.h.dtMaxArg = dDtMax + s;
             S.h.errWord = dErr;
-            {
-                const ApplyLayout<R> L(S.geo.nx, rowBlockRows<R>(S.geo.nx, S.geo.ny));
-                rbShape.slot = std::max(rbShape.slot, L.slot);
-                rbShape.ring = std::max(rbShape.ring, L.ring);
-            }
+            shp.add(S.geo.nx, S.geo.ny);
         }
         for (int d = 0; d < D_COUNT; ++d) {
             dom[d].start = dDomStart + (size_t)d * (n + 1);
@@ -444,21 +445,17 @@ public:
                 adom[k][d].total = dATotal + k * D_COUNT + d;
                 adom[k][d].nscn = n;
             }
-        rbSmem = n > 0 ? rbApplySmem<R>(rbShape) : 0;
         persistCtas = PERSIST_CTAS;
         if (const char* cap = std::getenv("PHX_PERSIST_CTAS")) persistCtas = std::max(1, std::min(persistCtas, std::atoi(cap)));
-        if (rbSmem > RB_SMEM_MAX) {
-            err = "the batch's widest grids need more shared memory than a CTA has";
-            return PHX_ERR_UNSUPPORTED;
-        }
-        if (rbSmem > 0) {
-            int dev = 0, sms = 0, occ = 0;
-            PHX_CK(cudaGetDevice(&dev));
-            PHX_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-            PHX_CK(cudaFuncSetAttribute(k_cg_apply_rb<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rbSmem));
-            PHX_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cg_apply_rb<R>, RB_THREADS, rbSmem));
-            rbGrid = sms * std::max(occ, 1);
-            if (const char* cap = std::getenv("PHX_PERSIST_CTAS")) rbGrid = std::max(1, std::min(rbGrid, std::atoi(cap)));
+        if (n > 0) {
+            if (shp.maxSmem() > RB_SMEM_MAX) {
+                err = "the batch's widest grids need more shared memory than a CTA has";
+                return PHX_ERR_UNSUPPORTED;
+            }
+            PHX_TRY(configRB(cfgApply, k_cg_apply_rb<R>, shp.apply, shp.smemApply()));
+            PHX_TRY(configRB(cfgGs[GS_PRE], k_gs_rb<R, GS_PRE>, shp.gs[GS_PRE], shp.smemGs(GS_PRE)));
+            PHX_TRY(configRB(cfgGs[GS_BLACK], k_gs_rb<R, GS_BLACK>, shp.gs[GS_BLACK], shp.smemGs(GS_BLACK)));
+            PHX_TRY(configRB(cfgGs[GS_RED], k_gs_rb<R, GS_RED>, shp.gs[GS_RED], shp.smemGs(GS_RED)));
         }
         PHX_CK(cudaMemcpyAsync(dDomStart, starts.data(), starts.size() * sizeof(int), cudaMemcpyHostToDevice, st));
         PHX_CK(cudaMemcpyAsync(dTiles, tilesAll.data(), tilesAll.size() * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -584,11 +581,26 @@ public:
         ++launches;
     }
 
+    // shared memory and persistent grid of a row-block kernel for the batch
+    template <class K>
+    int configRB(RbCfg& c, K kern, const RbShape& shape, size_t smem) {
+        int dev = 0, sms = 0, occ = 0;
+        PHX_CK(cudaGetDevice(&dev));
+        PHX_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        PHX_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        PHX_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, RB_THREADS, smem));
+        c.smem = smem;
+        c.shape = shape;
+        c.grid = std::min(sms * std::max(occ, 1), persistCtas);
+        return PHX_OK;
+    }
+
     // persistent grid over the active row-block tiles, with the staging ring in dynamic shared memory
     template <class K, class... A>
-    void launchRB(const char* name, K kern, A... args) {
+    void launchRB(const char* name, const RbCfg& c, K kern, A... args) {
         if (dom[D_RB].total <= 0) return;
-        const int grid = std::min(dom[D_RB].total, rbGrid);
+        const int grid = std::min(dom[D_RB].total, c.grid);
+        const size_t rbSmem = c.smem;
         if (prof) {
             if (evNext + 2 > (int)evPool.size()) {
                 for (int i = 0; i < 64; ++i) { cudaEvent_t e; cudaEventCreate(&e); evPool.push_back(e); }
@@ -699,9 +711,12 @@ public:
     void stLeakage() {
         launch("k_zone_integral", D_CZ, TPB, k_zone_integral<R>, (const Scn<R>*)dS, dom[D_CZ]);
     }
-    void vcycleBody() {
+    // one V-cycle z = M r (src/sim/pressure_mg.cpp:270-300) closed by the
+    // last red half sweep with r.z; phase 0: before the CG loop, 1: inside
+    // it, 2: a bare V-cycle
+    void vcycle(int phase) {
         const Scn<R>* S = dS;
-        launchA("k_gs0", D_HALF, TPB, k_gs0<R>, S, adom[0][D_HALF], 1, 1);
+        launchRB("k_gs_pre", cfgGs[GS_PRE], k_gs_rb<R, GS_PRE>, S, adom[0][D_RB], cfgGs[GS_PRE].shape, phase);
         launchA("k_res0_restrict", D_BLK, TPB, k_res0_restrict<R>, S, adom[0][D_BLK]);
         for (int l = 1; l < maxLevels - 1; ++l) {
             launchA("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, adom[0][D_LV0 + l], l, 0);
@@ -715,7 +730,8 @@ public:
             launchA("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, adom[0][D_LV0 + l], l, 2);
             launchA("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, adom[0][D_LV0 + l], l, 1);
         }
-        launchA("k_gs0", D_HALF, TPB, k_gs0<R>, S, adom[0][D_HALF], 1, 2);
+        launchRB("k_gs_black", cfgGs[GS_BLACK], k_gs_rb<R, GS_BLACK>, S, adom[0][D_RB], cfgGs[GS_BLACK].shape, phase);
+        launchRB("k_gs_red_dot", cfgGs[GS_RED], k_gs_rb<R, GS_RED>, S, adom[0][D_RB], cfgGs[GS_RED].shape, phase);
     }
     // all scenarios' flag in slot `slot` set?
     int readAll(int slot, bool& all) {
@@ -733,25 +749,21 @@ public:
         launch("k_reset", D_ONE, 32, k_reset<R>, S, dom[D_ONE], 0);
         rebuildActive();
         launch("k_rhs", D_CELLS, TPB, k_rhs<R>, S, dom[D_CELLS]);
-        launchA("k_gs0", D_HALF, TPB, k_gs0<R>, S, adom[0][D_HALF], 0, 0);
-        vcycleBody();
-        launchA("k_gs0_last_dot", D_CELLS, TPB, k_gs0_last_dot<R>, S, adom[0][D_CELLS], 0);
+        vcycle(0);
     }
     // one CG iteration (src/sim/gasphase.cpp:605-625). The mixed path can
     // replace the recursive residual by the FP64 one before preconditioning,
     // so its first red half sweep runs after that.
     void cgIteration() {
         const Scn<R>* S = dS;
-        launchRB("k_cg_apply", k_cg_apply_rb<R>, S, adom[0][D_RB], (R* const*)dD, rbShape);
-        launchA("k_cg_update", D_CELLS, TPB, k_cg_update<R>, S, adom[0][D_CELLS], (R* const*)dD, kMixed ? 0 : 1);
+        launchRB("k_cg_apply", cfgApply, k_cg_apply_rb<R>, S, adom[0][D_RB], (R* const*)dD, cfgApply.shape);
+        launchA("k_cg_update", D_CELLS, TPB, k_cg_update<R>, S, adom[0][D_CELLS], (R* const*)dD, 0);
         if (kMixed) {
             launchA("k_mx_update", D_CELLS, TPB, k_mx_update<R>, S, adom[1][D_CELLS], 1);
             launchA("k_mx_res64", D_CELLS, TPB, k_mx_res64<R>, S, adom[1][D_CELLS], 1);
             launchA("k_mx_zone_proj", D_CZ, TPB, k_mx_zone_proj<R>, S, adom[1][D_CZ], 1);
-            launchA("k_gs0", D_HALF, TPB, k_gs0<R>, S, adom[0][D_HALF], 0, 0);
         }
-        vcycleBody();
-        launchA("k_gs0_last_dot", D_CELLS, TPB, k_gs0_last_dot<R>, S, adom[0][D_CELLS], 1);
+        vcycle(1);
     }
     // zone mean removal and velocity correction (:629-676)
     void projectEpilogue() {
@@ -770,9 +782,7 @@ public:
         launch("k_rhs", D_CELLS, TPB, k_rhs<R>, S, dom[D_CELLS]);
         launchA("k_mx_res64", D_CELLS, TPB, k_mx_res64<R>, S, adom[0][D_CELLS], 0);
         launchA("k_mx_zone_proj", D_CZ, TPB, k_mx_zone_proj<R>, S, adom[0][D_CZ], 0);
-        launchA("k_gs0", D_HALF, TPB, k_gs0<R>, S, adom[0][D_HALF], 0, 0);
-        vcycleBody();
-        launchA("k_gs0_last_dot", D_CELLS, TPB, k_gs0_last_dot<R>, S, adom[0][D_CELLS], 0);
+        vcycle(0);
     }
     void mixedEpilogue() {
         launch("k_mx_final", D_CELLS, TPB, k_mx_final<R>, dS, dom[D_CELLS]);
@@ -977,9 +987,7 @@ public:
         PHX_TRY(S.put(st, S.h.r, std::vector<double>(r, r + N)));
         launch("k_reset", D_ONE, 32, k_reset<R>, (const Scn<R>*)dS, dom[D_ONE], 2);
         rebuildActive();
-        launchA("k_gs0", D_HALF, TPB, k_gs0<R>, (const Scn<R>*)dS, adom[0][D_HALF], 0, 0);
-        vcycleBody();
-        launchA("k_gs0_last_dot", D_CELLS, TPB, k_gs0_last_dot<R>, (const Scn<R>*)dS, adom[0][D_CELLS], 2);
+        vcycle(2);
         PHX_TRY(checkLaunch());
         return getReal(S.h.z, N, z);
     }

@@ -263,6 +263,55 @@ __device__ __forceinline__ bool cgContinue(const Scn<R>& g, double res, double r
     return res > g.tol && it < g.maxIters && rz > 0 && !(rmax <= relStop);
 }
 
+// closes a CG iteration in the last CTA of a scenario once r.z = tot is known:
+// beta, the iteration count and the stop test (src/sim/gasphase.cpp:589-605).
+// phase 0: first preconditioning before the loop; 1: inside the loop.
+template <class R>
+__device__ void closeCgIteration(const Scn<R>& g, int phase, double tot) {
+    double* sv = g.sv;
+    int it = (int)sv[SV_IT];
+    if (phase == 0) {
+        sv[SV_RZ] = tot;
+        it = 0;
+    } else {
+        sv[SV_BETA] = tot / sv[SV_RZ];
+        sv[SV_RZ] = tot;
+        it += 1;
+    }
+    sv[SV_IT] = it;
+    if (!g.mixed) {
+        const double rmax = sv[SV_RMAX];
+        const double res = rmax / sv[SV_INV];
+        sv[SV_PRES] = res;
+        sv[SV_PREL] = sv[SV_BMAX] > 0 ? rmax / sv[SV_BMAX] : 0.0;
+        sv[SV_RMAX] = 0;
+        if (!cgContinue(g, res, rmax, it, sv[SV_RZ])) sv[SV_DONE] = 1;
+    } else {
+        // mixed: the stop test uses the FP64 residual, known where it was
+        // just replaced; the FP32 recursive residual schedules the next
+        // replacement (every replaceEvery iterations, or once it claims
+        // convergence)
+        const bool replaced = phase == 0 || sv[SV_REPL] != 0;
+        bool converged = false;
+        if (replaced) {
+            const double r64 = sv[SV_R64MAX];
+            const double res = r64 / sv[SV_INV];
+            const double rel = sv[SV_BMAX] > 0 ? r64 / sv[SV_BMAX] : 0.0;
+            sv[SV_PRES] = res;
+            sv[SV_PREL] = rel;
+            converged = !(res > g.tol) || (g.relTol > 0 && rel <= g.relTol) || !(r64 > 0);
+            sv[SV_R64MAX] = 0;
+        }
+        const bool stop = converged || it >= g.maxIters || !(sv[SV_RZ] > 0);
+        const double rrec = sv[SV_RMAX];
+        const bool claims = phase != 0 && ((g.relTol > 0 && rrec <= 2.0 * g.relTol * sv[SV_BMAX]) ||
+                                           rrec / sv[SV_INV] <= 0.5 * g.tol);
+        sv[SV_REPL] = (!stop && phase != 0 && ((it % g.replaceEvery) == 0 || claims)) ? 1.0 : 0.0;
+        sv[SV_RMAX] = 0;
+        if (stop) sv[SV_DONE] = 1;
+    }
+}
+
 // last level-0 half sweep of the V-cycle (red, after black) fused with the
 // r.z dot product of the CG (dotRZ, src/sim/gasphase.cpp:582-588); the last
 // CTA of the scenario closes the iteration. phase 0: first preconditioning
@@ -302,50 +351,7 @@ __global__ void k_gs0_last_dot(const Scn<R>* __restrict__ S, ADom dom, int phase
     }
     if (phase == 2) break;
     double tot;
-    if (lastCtaSum(g, PS_RZ, tile_, (sst_[s_ + 1] - sst_[s_]), dot, &tot) && threadIdx.x == 0) {
-        double* sv = g.sv;
-        int it = (int)sv[SV_IT];
-        if (phase == 0) {
-            sv[SV_RZ] = tot;
-            it = 0;
-        } else {
-            sv[SV_BETA] = tot / sv[SV_RZ];
-            sv[SV_RZ] = tot;
-            it += 1;
-        }
-        sv[SV_IT] = it;
-        if (!g.mixed) {
-            const double rmax = sv[SV_RMAX];
-            const double res = rmax / sv[SV_INV];
-            sv[SV_PRES] = res;
-            sv[SV_PREL] = sv[SV_BMAX] > 0 ? rmax / sv[SV_BMAX] : 0.0;
-            sv[SV_RMAX] = 0;
-            if (!cgContinue(g, res, rmax, it, sv[SV_RZ])) sv[SV_DONE] = 1;
-        } else {
-            // mixed: the stop test uses the FP64 residual, known where it was
-            // just replaced; the FP32 recursive residual schedules the next
-            // replacement (every replaceEvery iterations, or once it claims
-            // convergence)
-            const bool replaced = phase == 0 || sv[SV_REPL] != 0;
-            bool converged = false;
-            if (replaced) {
-                const double r64 = sv[SV_R64MAX];
-                const double res = r64 / sv[SV_INV];
-                const double rel = sv[SV_BMAX] > 0 ? r64 / sv[SV_BMAX] : 0.0;
-                sv[SV_PRES] = res;
-                sv[SV_PREL] = rel;
-                converged = !(res > g.tol) || (g.relTol > 0 && rel <= g.relTol) || !(r64 > 0);
-                sv[SV_R64MAX] = 0;
-            }
-            const bool stop = converged || it >= g.maxIters || !(sv[SV_RZ] > 0);
-            const double rrec = sv[SV_RMAX];
-            const bool claims = phase != 0 && ((g.relTol > 0 && rrec <= 2.0 * g.relTol * sv[SV_BMAX]) ||
-                                               rrec / sv[SV_INV] <= 0.5 * g.tol);
-            sv[SV_REPL] = (!stop && phase != 0 && ((it % g.replaceEvery) == 0 || claims)) ? 1.0 : 0.0;
-            sv[SV_RMAX] = 0;
-            if (stop) sv[SV_DONE] = 1;
-        }
-    }
+    if (lastCtaSum(g, PS_RZ, tile_, (sst_[s_ + 1] - sst_[s_]), dot, &tot) && threadIdx.x == 0) closeCgIteration(g, phase, tot);
     PHX_TILES_END
 }
 

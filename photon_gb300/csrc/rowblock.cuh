@@ -83,69 +83,39 @@ __device__ __forceinline__ bool mbarWaitBounded(uint64_t* b, unsigned parity, un
 
 
 // One staged array of a plane slot: rows [rowLo, rowLo + rows) of plane k of
-// an array with `pitch` elements per row and `plane` elements per plane, at
-// element offset `off` of the slot. The slot holds element gidx at index
-// off + gidx - G0(k), G0(k) = the 16-byte aligned start of row rowLo.
+// an array with `pitch` elements of `esz` bytes per row and `plane` elements
+// per plane, at byte `off` of the slot. The slot holds element gidx at byte
+// off + (gidx - G0(k)) * esz, G0(k) = the 16-byte aligned start of row rowLo.
 struct StageDesc {
     const char* src;
     long long plane;             // elements per plane
     int pitch;                   // elements per row
     int rowLo, rows;             // nominal rows of the slot (rowLo may be negative at the grid's edge)
     int rowMin, rowMax;          // rows that exist: [rowMin, rowMax)
-    int off;                     // element offset of the array in the slot
+    int off;                     // byte offset of the array in the slot
+    int esz;                     // bytes per element (4 or 8)
 };
 
 __host__ __device__ inline long long floorTo(long long v, int m) { return v >= 0 ? v / m * m : -((-v + m - 1) / m) * m; }
 __host__ __device__ inline long long ceilTo(long long v, int m) { return floorTo(v + m - 1, m); }
 __host__ __device__ inline int roundUp(int v, int m) { return (v + m - 1) / m * m; }
 
-// slot capacity (elements) of `rows` rows of `pitch` elements, with the
-// alignment slack of both ends
-template <class R>
-__host__ __device__ inline int stageCapacity(int rows, int pitch) {
-    constexpr int EPV = 16 / (int)sizeof(R);
-    return roundUp(rows * pitch + 2 * EPV, EPV);
-}
+// slot bytes of `rows` rows of `pitch` elements of esz bytes, with the
+// alignment slack of both ends (a multiple of 16)
+__host__ __device__ inline int stageBytes(int rows, int pitch, int esz) { return roundUp(rows * pitch * esz + 32, 16); }
 
-// slot index of element (row, i) of plane k of a staged array
-template <class R>
-__device__ __forceinline__ int stageAt(const StageDesc& d, int k, int row, int i) {
-    constexpr int EPV = 16 / (int)sizeof(R);
-    const long long v = (long long)k * d.plane + (long long)d.rowLo * d.pitch;
-    return d.off + (int)(v & (EPV - 1)) + (row - d.rowLo) * d.pitch + i;
-}
-
-// total bytes of plane k over the descriptors, then the copies (thread 0)
-template <class R>
-__device__ __noinline__ void stagePlane(const StageDesc* ds, int n, int k, R* slot, uint64_t* bar) {
-    constexpr int EPV = 16 / (int)sizeof(R);
-    unsigned total = 0;
-    for (int q = 0; q < n; ++q) {
-        const StageDesc& d = ds[q];
-        const int a = max(d.rowLo, d.rowMin), e = min(d.rowLo + d.rows, d.rowMax);
-        if (a >= e || !d.src) continue;
-        const long long ga = floorTo((long long)k * d.plane + (long long)a * d.pitch, EPV);
-        const long long gb = ceilTo((long long)k * d.plane + (long long)e * d.pitch, EPV);
-        total += (unsigned)((gb - ga) * sizeof(R));
-    }
-    mbarArriveExpectTx(bar, total);
-    for (int q = 0; q < n; ++q) {
-        const StageDesc& d = ds[q];
-        const int a = max(d.rowLo, d.rowMin), e = min(d.rowLo + d.rows, d.rowMax);
-        if (a >= e || !d.src) continue;
-        const long long g0 = floorTo((long long)k * d.plane + (long long)d.rowLo * d.pitch, EPV);
-        const long long ga = floorTo((long long)k * d.plane + (long long)a * d.pitch, EPV);
-        const long long gb = ceilTo((long long)k * d.plane + (long long)e * d.pitch, EPV);
-        bulkLoad(slot + d.off + (ga - g0), d.src + ga * (long long)sizeof(R), (unsigned)((gb - ga) * sizeof(R)), bar);
-    }
+// element offset, within the slot array, of element 0 of row rowLo of plane k:
+// (k * plane + rowLo * pitch) mod (16 / esz), from small residues
+__device__ __forceinline__ int stageMod(int k, int planeMod, int rowTerm, int epv) {
+    return ((k & (epv - 1)) * planeMod + rowTerm) & (epv - 1);
 }
 
 // shared-memory shape of a launch: one slot stride for every tile of the
 // batch (the largest slot of its scenarios), so that planes of consecutive
 // tiles of different scenarios never overlap in the ring
 struct RbShape {
-    int slot;                    // elements per plane slot
-    int ring;                    // elements per plane of the d ring (FP64 path)
+    int slot;                    // bytes per plane slot
+    int ring;                    // bytes per plane of the consumers' ring
 };
 
 // ---- warp-specialised pipeline -------------------------------------------------
@@ -191,7 +161,7 @@ __device__ __forceinline__ double consumerSum(V v, double* sh) {
         V x{};
         if (l < RB_CONSUMERS) x = reinterpret_cast<V*>(sh)[l];
         x = warpSum(x);
-        if constexpr (sizeof(V) == sizeof(double) && !std::is_same<V, double>::value) t = f2value(x);
+        if constexpr (std::is_same<V, F2>::value) t = f2value(x);
         else t = (double)x;
     }
     consumerSync();   // sh is free again
@@ -223,30 +193,30 @@ __device__ bool lastCtaSumC(const Scn<R>& g, int slot, int tile, int ntiles, V v
     return true;
 }
 
-// geometry of a row-block tile
+// geometry of a row-block tile; the staged planes are [kLo, kHi] (the tile's
+// planes plus `halo` planes on each side, clipped to the grid)
 struct RbTile {
     int nx, ny, nz, j0, j1, k0, k1, kLo, kHi, nPl;
     long long sxy;
 };
 template <class R>
-__device__ __forceinline__ RbTile rbTile(const Scn<R>& g, int tile) {
+__device__ __forceinline__ RbTile rbTile(const Scn<R>& g, int tile, int halo = 1) {
     RbTile t;
     t.nx = g.nx; t.ny = g.ny; t.nz = g.nz;
     const int jb = tile % g.njb, kb = tile / g.njb;
     t.j0 = jb * g.tj; t.j1 = min(t.j0 + g.tj, t.ny);
     t.k0 = kb * RB_KZ; t.k1 = min(t.k0 + RB_KZ, t.nz);
-    t.kLo = max(t.k0 - 1, 0); t.kHi = min(t.k1, t.nz - 1);
+    t.kLo = max(t.k0 - halo, 0); t.kHi = min(t.k1 - 1 + halo, t.nz - 1);
     t.nPl = t.kHi - t.kLo + 1;
     t.sxy = (long long)t.nx * t.ny;
     return t;
 }
 
-// Producer warp: stage the planes of every tile of the CTA. Lane q < nd holds
-// descriptor q of the current tile, made by desc(lane, g, tile, t, d).
+// Producer warp: stage the planes of every tile of the CTA. Lane q holds
+// descriptor q of the current tile (desc returns false for unused lanes).
 template <class R, int ST, class DescFn>
-__device__ void rbProducer(const Scn<R>* __restrict__ S, const int* sst, int nscn, R* sm, int slotStride,
+__device__ void rbProducer(const Scn<R>* __restrict__ S, const int* sst, int nscn, char* sm, int slotStride, int halo,
                            uint64_t* full, uint64_t* empty, volatile int* abortFlag, DescFn desc) {
-    constexpr int EPV = 16 / (int)sizeof(R);
     const int lane = threadIdx.x & 31;
     const int tot = sst[nscn];
     unsigned seq = 0;
@@ -254,7 +224,7 @@ __device__ void rbProducer(const Scn<R>* __restrict__ S, const int* sst, int nsc
         int s, tile;
         locateShared(sst, nscn, b, s, tile);
         const Scn<R>& g = S[s];
-        const RbTile t = rbTile(g, tile);
+        const RbTile t = rbTile(g, tile, halo);
         StageDesc d{};
         const bool has = desc(lane, s, g, t, d);
         for (int idx = 0; idx < t.nPl; ++idx) {
@@ -272,21 +242,23 @@ __device__ void rbProducer(const Scn<R>* __restrict__ S, const int* sst, int nsc
             if (!__shfl_sync(0xffffffffu, ok, 0)) goto drain;
             {
                 const int k = t.kLo + idx;
+                const int epv = 16 / (d.esz > 0 ? d.esz : 16);
                 long long ga = 0, gb = 0, g0 = 0;
                 const int a = max(d.rowLo, d.rowMin), e = min(d.rowLo + d.rows, d.rowMax);
                 const bool live = has && d.src && a < e;
                 if (live) {
-                    g0 = floorTo((long long)k * d.plane + (long long)d.rowLo * d.pitch, EPV);
-                    ga = floorTo((long long)k * d.plane + (long long)a * d.pitch, EPV);
-                    gb = ceilTo((long long)k * d.plane + (long long)e * d.pitch, EPV);
+                    g0 = floorTo((long long)k * d.plane + (long long)d.rowLo * d.pitch, epv);
+                    ga = floorTo((long long)k * d.plane + (long long)a * d.pitch, epv);
+                    gb = ceilTo((long long)k * d.plane + (long long)e * d.pitch, epv);
                 }
-                unsigned bytes = live ? (unsigned)((gb - ga) * sizeof(R)) : 0u;
+                const unsigned bytes = live ? (unsigned)((gb - ga) * d.esz) : 0u;
                 unsigned total = bytes;
                 for (int o = 16; o > 0; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
                 if (lane == 0) mbarArriveExpectTx(&full[slot], total);
                 __syncwarp();
-                if (live) bulkLoad(sm + (size_t)slot * slotStride + d.off + (ga - g0), d.src + ga * (long long)sizeof(R), bytes,
-                                   &full[slot]);
+                if (live)
+                    bulkLoad(sm + (size_t)slot * slotStride + d.off + (ga - g0) * d.esz, d.src + ga * d.esz, bytes,
+                             &full[slot]);
             }
         }
         seq += t.nPl;
@@ -294,8 +266,67 @@ __device__ void rbProducer(const Scn<R>* __restrict__ S, const int* sst, int nsc
 drain:
     // no copy may be in flight when the CTA ends: wait for the last use of every slot
     if (lane == 0)
-        for (unsigned q = seq > (unsigned)ST ? seq - ST : 0; q < seq; ++q) mbarWaitBounded(&full[q % ST], (q / ST) & 1);
+        for (unsigned q = seq > (unsigned)ST ? seq - ST : 0; q < seq; ++q) mbarWaitBounded(&full[q % ST], (q / ST) & 1, 64);
 }
+
+// Consumer side of the slot ring for one tile: planes are waited in order and
+// released in order (one arrival per consumer warp).
+template <int ST>
+struct RbPipe {
+    uint64_t* full;
+    uint64_t* empty;
+    volatile int* abortFlag;
+    unsigned seq;                // planes of the CTA's earlier tiles
+    int nPl, waited, released;
+    // wait for planes [waited, idx] (idx clipped to the tile's planes)
+    __device__ __forceinline__ void waitThrough(int idx, unsigned* errWord) {
+        idx = min(idx, nPl - 1);
+        for (; waited <= idx; ++waited) {
+            if (*abortFlag) return;
+            const unsigned q = seq + waited;
+            if (!mbarWaitBounded(&full[q % ST], (q / ST) & 1, 32)) {
+                *abortFlag = 1;
+                atomicOr(errWord, 1u);
+            }
+        }
+    }
+    // release planes [released, idx]
+    __device__ __forceinline__ void releaseThrough(int idx) {
+        idx = min(idx, nPl - 1);
+        __syncwarp();
+        if ((threadIdx.x & 31) == 0)
+            for (int q = released; q <= idx; ++q) mbarArrive(&empty[(seq + q) % ST]);
+        released = max(released, idx + 1);
+    }
+    __device__ __forceinline__ int slotOf(int idx) const { return (int)((seq + idx) % ST); }
+};
+
+// common prologue of a row-block kernel: the active prefix and the barriers
+#define PHX_RB_PROLOGUE(ST)                                                   \
+    extern __shared__ __align__(128) unsigned char smraw[];                   \
+    __shared__ uint64_t full[ST], empty[ST];                                  \
+    __shared__ int sst_[MAX_BATCH + 1];                                       \
+    __shared__ volatile int abortFlag;                                        \
+    __shared__ int amLast;                                                    \
+    __shared__ double sh[RB_CONSUMERS];                                       \
+    for (int i_ = threadIdx.x; i_ <= dom.nscn; i_ += blockDim.x)              \
+        sst_[i_] = dom.start[i_];                                             \
+    if (threadIdx.x == 0) {                                                   \
+        for (int q_ = 0; q_ < ST; ++q_) {                                     \
+            mbarInit(&full[q_], 1);                                           \
+            mbarInit(&empty[q_], RB_CONSUMERS);                               \
+        }                                                                     \
+        fenceBarrierInit();                                                   \
+        abortFlag = 0;                                                        \
+    }                                                                         \
+    __syncthreads();                                                          \
+    char* const sm = reinterpret_cast<char*>(smraw);                          \
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;               \
+    (void)amLast; (void)sh; (void)lane;
+
+// e / nx as umulhi(e, ceil(2^32 / nx)): exact for e, nx < 65536 (nx = 1 apart)
+__device__ __forceinline__ unsigned divMagic(int nx) { return nx == 1 ? 0u : (unsigned)((0x100000000ULL + nx - 1) / nx); }
+__device__ __forceinline__ int divBy(int e, int nx, unsigned magic) { return nx == 1 ? e : (int)__umulhi((unsigned)e, magic); }
 
 // ---------------------------------------------------------------------------------
 // q = A d with d = z + beta d (src/sim/gasphase.cpp:551-570, 620-622) and the
@@ -307,25 +338,20 @@ drain:
 template <class R>
 struct ApplyLayout {
     static constexpr int ST = 3;
-    int cz, cc, cx, cy, slot, ring;
+    int bz, bc, bx, by, slot, ring;
     __host__ __device__ ApplyLayout(int nx, int tj) {
-        cz = stageCapacity<R>(tj + 2, nx);
-        cc = stageCapacity<R>(tj, nx);
-        cx = stageCapacity<R>(tj, nx + 1);
-        cy = stageCapacity<R>(tj + 1, nx);
-        slot = 2 * cz + 2 * cc + cx + cy;
-        ring = roundUp((tj + 2) * nx, 4);
+        bz = stageBytes(tj + 2, nx, sizeof(R));
+        bc = stageBytes(tj, nx, sizeof(R));
+        bx = stageBytes(tj, nx + 1, sizeof(R));
+        by = stageBytes(tj + 1, nx, sizeof(R));
+        slot = 2 * bz + 2 * bc + bx + by;
+        ring = roundUp((tj + 2) * nx * (int)sizeof(R), 16);
     }
 };
 
 template <class R>
 inline size_t rbApplySmem(const RbShape& sh) {
-    return ((size_t)ApplyLayout<R>::ST * sh.slot + 4 * (size_t)sh.ring) * sizeof(R);
-}
-template <class R>
-inline size_t rbApplySmem(int nx, int ny) {
-    const ApplyLayout<R> L(nx, rowBlockRows<R>(nx, ny));
-    return rbApplySmem<R>(RbShape{L.slot, L.ring});
+    return (size_t)ApplyLayout<R>::ST * sh.slot + 4 * (size_t)sh.ring;
 }
 
 enum { SA_Z = 0, SA_D, SA_DIAG, SA_AZ, SA_AX, SA_AY, SA_COUNT };
@@ -338,45 +364,31 @@ __global__ void __launch_bounds__(RB_THREADS, 2) k_cg_apply_rb(const Scn<R>* __r
     using LY = ApplyLayout<R>;
     constexpr int ST = LY::ST;
     constexpr int EPV = 16 / (int)sizeof(R);
-    extern __shared__ __align__(128) unsigned char smraw[];
-    __shared__ uint64_t full[ST], empty[ST];
-    __shared__ int sst_[MAX_BATCH + 1];
-    __shared__ volatile int abortFlag;
-    __shared__ int amLast;
-    __shared__ double sh[RB_CONSUMERS];
-    for (int i = threadIdx.x; i <= dom.nscn; i += blockDim.x) sst_[i] = dom.start[i];
-    if (threadIdx.x == 0) {
-        for (int q = 0; q < ST; ++q) {
-            mbarInit(&full[q], 1);
-            mbarInit(&empty[q], RB_CONSUMERS);
-        }
-        fenceBarrierInit();
-        abortFlag = 0;
-    }
-    __syncthreads();
-    R* const sm = reinterpret_cast<R*>(smraw);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int ES = (int)sizeof(R);
+    PHX_RB_PROLOGUE(ST)
     if (warp == RB_CONSUMERS) {
-        rbProducer<R, ST>(S, sst_, dom.nscn, sm, shape.slot, full, empty, &abortFlag,
+        rbProducer<R, ST>(S, sst_, dom.nscn, sm, shape.slot, 1, full, empty, &abortFlag,
                           [&](int ln, int s, const Scn<R>& g, const RbTile& t, StageDesc& d) {
                               const LY L(t.nx, g.tj);
                               const int it = (int)g.sv[SV_IT];
                               const int nx = t.nx, ny = t.ny, j0 = t.j0, tj = g.tj;
                               switch (ln) {
-                              case SA_Z: d = StageDesc{(const char*)g.z, t.sxy, nx, j0 - 1, tj + 2, 0, ny, 0}; return true;
+                              case SA_Z: d = StageDesc{(const char*)g.z, t.sxy, nx, j0 - 1, tj + 2, 0, ny, 0, ES}; return true;
                               case SA_D:
                                   d = StageDesc{it > 0 ? (const char*)dbuf[2 * s + (it & 1)] : nullptr, t.sxy, nx, j0 - 1,
-                                                tj + 2, 0, ny, L.cz};
+                                                tj + 2, 0, ny, L.bz, ES};
                                   return true;
-                              case SA_DIAG: d = StageDesc{(const char*)g.diag, t.sxy, nx, j0, tj, 0, ny, 2 * L.cz}; return true;
-                              case SA_AZ: d = StageDesc{(const char*)g.a0z, t.sxy, nx, j0, tj, 0, ny, 2 * L.cz + L.cc}; return true;
+                              case SA_DIAG: d = StageDesc{(const char*)g.diag, t.sxy, nx, j0, tj, 0, ny, 2 * L.bz, ES}; return true;
+                              case SA_AZ:
+                                  d = StageDesc{(const char*)g.a0z, t.sxy, nx, j0, tj, 0, ny, 2 * L.bz + L.bc, ES};
+                                  return true;
                               case SA_AX:
                                   d = StageDesc{(const char*)g.a0x, (long long)(nx + 1) * ny, nx + 1, j0, tj, 0, ny,
-                                                2 * L.cz + 2 * L.cc};
+                                                2 * L.bz + 2 * L.bc, ES};
                                   return true;
                               case SA_AY:
                                   d = StageDesc{(const char*)g.a0y, (long long)nx * (ny + 1), nx, j0, tj + 1, 0, ny + 1,
-                                                2 * L.cz + 2 * L.cc + L.cx};
+                                                2 * L.bz + 2 * L.bc + L.bx, ES};
                                   return true;
                               default: return false;
                               }
@@ -385,7 +397,7 @@ __global__ void __launch_bounds__(RB_THREADS, 2) k_cg_apply_rb(const Scn<R>* __r
     }
     // ---- consumers --------------------------------------------------------------
     const int tot = sst_[dom.nscn];
-    R* const ring = sm + (size_t)ST * shape.slot;
+    char* const ringB = sm + (size_t)ST * shape.slot;
     unsigned seq = 0;
     for (int b = blockIdx.x; b < tot; b += gridDim.x) {
         int s, tile;
@@ -400,36 +412,26 @@ __global__ void __launch_bounds__(RB_THREADS, 2) k_cg_apply_rb(const Scn<R>* __r
         R* const dnew = dbuf[2 * s + ((it + 1) & 1)];
         R* const q = g.q;
         const int ncell = (t.j1 - j0) * nx;
-        // e / nx as umulhi(e, ceil(2^32 / nx)): exact for e, nx < 65536 (nx = 1 apart)
-        const unsigned magic = nx == 1 ? 0u : (unsigned)((0x100000000ULL + nx - 1) / nx);
+        const unsigned magic = divMagic(nx);
         const int ringRa = max(j0 - 1, 0), ringRe = min(t.j1 + 1, ny);
-        // alignment offsets (mod EPV) of the first staged row of plane k: k * plane + row * pitch
         const int mC = (int)(t.sxy & (EPV - 1)), mX = (int)(((long long)(nx + 1) * ny) & (EPV - 1));
         const int mY = (int)(((long long)nx * (ny + 1)) & (EPV - 1));
-        const auto offMod = [](int k, int m, int rowTerm) { return ((k & (EPV - 1)) * m + rowTerm) & (EPV - 1); };
         const int rC = (j0 * nx) & (EPV - 1), rCm = ((j0 - 1) * nx) & (EPV - 1);
         const int rX = (j0 * (nx + 1)) & (EPV - 1), rY = rC;
+        RbPipe<ST> pipe{full, empty, &abortFlag, seq, t.nPl, 0, 0};
         Acc dot{};
-        int waited = 0, released = 0;
         for (int kk = t.k0; kk < t.k1; ++kk) {
             const int ic = kk - kLo;
-            for (const int need = min(ic + 2, t.nPl); waited < need; ++waited) {
-                if (abortFlag) break;
-                const unsigned qn = seq + waited;
-                if (!mbarWaitBounded(&full[qn % ST], (qn / ST) & 1, 32)) {
-                    abortFlag = 1;
-                    atomicOr(g.errWord, 1u);
-                }
-            }
+            pipe.waitThrough(ic + 1, g.errWord);
             // d of the planes entering the ring (rows j0-1 .. j1)
             if (!abortFlag) {
                 for (int k = kk == t.k0 ? kLo : kk + 1; k <= min(kk + 1, kHi); ++k) {
-                    const R* base = sm + (size_t)((seq + (k - kLo)) % ST) * shape.slot;
+                    const char* base = sm + (size_t)pipe.slotOf(k - kLo) * shape.slot;
                     const int n = (ringRe - ringRa) * nx;
-                    const int oz = offMod(k, mC, rCm) + (ringRa - (j0 - 1)) * nx;
-                    const R* zs = base + oz;
-                    const R* ds = base + L.cz + oz;
-                    R* out = ring + (size_t)(k & 3) * shape.ring + (ringRa - (j0 - 1)) * nx;
+                    const int oz = stageMod(k, mC, rCm, EPV) + (ringRa - (j0 - 1)) * nx;
+                    const R* zs = reinterpret_cast<const R*>(base) + oz;
+                    const R* ds = reinterpret_cast<const R*>(base + L.bz) + oz;
+                    R* out = reinterpret_cast<R*>(ringB + (size_t)(k & 3) * shape.ring) + (ringRa - (j0 - 1)) * nx;
                     if (useD)
                         for (int e = threadIdx.x; e < n; e += RB_CTHREADS) out[e] = (T)(zs[e] + beta * ds[e]);
                     else
@@ -438,23 +440,23 @@ __global__ void __launch_bounds__(RB_THREADS, 2) k_cg_apply_rb(const Scn<R>* __r
             }
             consumerSync();
             if (!abortFlag) {
-                const R* cur = sm + (size_t)((seq + ic) % ST) * shape.slot;
-                const R* nxt = kk + 1 <= kHi ? sm + (size_t)((seq + ic + 1) % ST) * shape.slot : cur;
-                const int oC = offMod(kk, mC, rC);
-                const R* dgp = cur + 2 * L.cz + oC;
-                const R* azp = cur + 2 * L.cz + L.cc + oC;
-                const R* azn = nxt + 2 * L.cz + L.cc + offMod(kk + 1, mC, rC);
-                const R* axp = cur + 2 * L.cz + 2 * L.cc + offMod(kk, mX, rX);
-                const R* ayp = cur + 2 * L.cz + 2 * L.cc + L.cx + offMod(kk, mY, rY);
-                const R* D0 = ring + (size_t)(kk & 3) * shape.ring + nx;
-                const R* Dm = ring + (size_t)((kk + 3) & 3) * shape.ring + nx;
-                const R* Dp = ring + (size_t)((kk + 1) & 3) * shape.ring + nx;
+                const char* cur = sm + (size_t)pipe.slotOf(ic) * shape.slot;
+                const char* nxt = kk + 1 <= kHi ? sm + (size_t)pipe.slotOf(ic + 1) * shape.slot : cur;
+                const int oC = stageMod(kk, mC, rC, EPV);
+                const R* dgp = reinterpret_cast<const R*>(cur + 2 * L.bz) + oC;
+                const R* azp = reinterpret_cast<const R*>(cur + 2 * L.bz + L.bc) + oC;
+                const R* azn = reinterpret_cast<const R*>(nxt + 2 * L.bz + L.bc) + stageMod(kk + 1, mC, rC, EPV);
+                const R* axp = reinterpret_cast<const R*>(cur + 2 * L.bz + 2 * L.bc) + stageMod(kk, mX, rX, EPV);
+                const R* ayp = reinterpret_cast<const R*>(cur + 2 * L.bz + 2 * L.bc + L.bx) + stageMod(kk, mY, rY, EPV);
+                const R* D0 = reinterpret_cast<const R*>(ringB + (size_t)(kk & 3) * shape.ring) + nx;
+                const R* Dm = reinterpret_cast<const R*>(ringB + (size_t)((kk + 3) & 3) * shape.ring) + nx;
+                const R* Dp = reinterpret_cast<const R*>(ringB + (size_t)((kk + 1) & 3) * shape.ring) + nx;
                 const long long cbase = (long long)kk * t.sxy + (long long)j0 * nx;
                 R* const dnp = dnew + cbase;
                 R* const qp = q + cbase;
                 const bool hasM = kk > 0, hasP = kk < nz - 1;
                 for (int e = threadIdx.x; e < ncell; e += RB_CTHREADS) {
-                    const int jj = nx == 1 ? e : (int)__umulhi((unsigned)e, magic);
+                    const int jj = divBy(e, nx, magic);
                     const int i = e - jj * nx, j = j0 + jj;
                     const T dc = D0[e];
                     dnp[e] = dc;
@@ -472,14 +474,9 @@ __global__ void __launch_bounds__(RB_THREADS, 2) k_cg_apply_rb(const Scn<R>* __r
                     dot = accAdd(dot, dotTerm(sacc, dc));
                 }
             }
-            // planes up to kk are read by no later step
-            __syncwarp();
-            if (lane == 0)
-                for (; released <= ic; ++released) mbarArrive(&empty[(seq + released) % ST]);
+            pipe.releaseThrough(ic);   // planes up to kk are read by no later step
         }
-        __syncwarp();
-        if (lane == 0)
-            for (; released < t.nPl; ++released) mbarArrive(&empty[(seq + released) % ST]);
+        pipe.releaseThrough(t.nPl - 1);
         seq += t.nPl;
         if (consumerSyncOr(abortFlag)) return;
         double total;
@@ -490,5 +487,255 @@ __global__ void __launch_bounds__(RB_THREADS, 2) k_cg_apply_rb(const Scn<R>* __r
         }
     }
 }
+
+}  // namespace phx
+
+namespace phx {
+
+// ---------------------------------------------------------------------------------
+// Level-0 Gauss-Seidel half sweeps of the V-cycle (gsColor, pressure_mg.cpp:195-216)
+// on row-block tiles; red cells have i + j + k even.
+//
+// GS_PRE   the pre-smoothing pair from x = 0: red = r / diag, then black from
+//          its red neighbours. The red values of the tile and its halo go to a
+//          4-plane ring, so each is divided once. Writes z on every cell.
+// GS_BLACK the post-smoothing black sweep after the prolongation
+//          (pressure_mg.cpp:290-297): the red neighbours are z + x_c[agg]; the
+//          ring holds them. Writes the black cells of z.
+// GS_RED   the last (red) half sweep fused with r.z (dotRZ,
+//          src/sim/gasphase.cpp:582-588); the last CTA of a scenario closes the
+//          CG iteration as k_gs0_last_dot does. Writes the red cells of z.
+enum { GS_PRE = 0, GS_BLACK = 1, GS_RED = 2 };
+
+template <class R, int MODE>
+struct GsLayout {
+    static constexpr int ST = MODE == GS_RED ? 4 : 3;
+    static constexpr int ES = (int)sizeof(R);
+    int oZ, oAG, oR, oDG, oAZ, oAX, oAY, slot, ring;
+    __host__ __device__ GsLayout(int nx, int tj) {
+        const int hr = MODE == GS_PRE ? tj + 2 : tj;   // rows of r and diag
+        int o = 0;
+        oZ = o;  o += MODE == GS_PRE ? 0 : stageBytes(tj + 2, nx, ES);
+        oAG = o; o += MODE == GS_BLACK ? stageBytes(tj + 2, nx, 4) : 0;
+        oR = o;  o += stageBytes(hr, nx, ES);
+        oDG = o; o += stageBytes(hr, nx, ES);
+        oAZ = o; o += stageBytes(tj, nx, ES);
+        oAX = o; o += stageBytes(tj, nx + 1, ES);
+        oAY = o; o += stageBytes(tj + 1, nx, ES);
+        slot = o;
+        ring = MODE == GS_RED ? 0 : roundUp((tj + 2) * nx * ES, 16);
+    }
+};
+
+template <class R, int MODE>
+inline size_t rbGsSmem(const RbShape& sh) {
+    return (size_t)GsLayout<R, MODE>::ST * sh.slot + 4 * (size_t)sh.ring;
+}
+
+enum { SG_Z = 0, SG_AG, SG_R, SG_DG, SG_AZ, SG_AX, SG_AY, SG_COUNT };
+
+template <class R, int MODE>
+__global__ void __launch_bounds__(RB_THREADS, 2) k_gs_rb(const Scn<R>* __restrict__ S, ADom dom, RbShape shape, int phase) {
+    using T = R;
+    using Acc = decltype(dotTerm(T(0), T(0)));
+    using LY = GsLayout<R, MODE>;
+    constexpr int ST = LY::ST;
+    constexpr int EPV = 16 / (int)sizeof(R);
+    constexpr int ES = (int)sizeof(R);
+    PHX_RB_PROLOGUE(ST)
+    if (warp == RB_CONSUMERS) {
+        rbProducer<R, ST>(S, sst_, dom.nscn, sm, shape.slot, 1, full, empty, &abortFlag,
+                          [&](int ln, int, const Scn<R>& g, const RbTile& t, StageDesc& d) {
+                              const LY L(t.nx, g.tj);
+                              const int nx = t.nx, ny = t.ny, j0 = t.j0, tj = g.tj;
+                              const int hlo = MODE == GS_PRE ? j0 - 1 : j0, hr = MODE == GS_PRE ? tj + 2 : tj;
+                              switch (ln) {
+                              case SG_Z:
+                                  if (MODE == GS_PRE) return false;
+                                  d = StageDesc{(const char*)g.z, t.sxy, nx, j0 - 1, tj + 2, 0, ny, L.oZ, ES};
+                                  return true;
+                              case SG_AG:
+                                  if (MODE != GS_BLACK) return false;
+                                  d = StageDesc{(const char*)g.lv[0].agg, t.sxy, nx, j0 - 1, tj + 2, 0, ny, L.oAG, 4};
+                                  return true;
+                              case SG_R: d = StageDesc{(const char*)g.r, t.sxy, nx, hlo, hr, 0, ny, L.oR, ES}; return true;
+                              case SG_DG: d = StageDesc{(const char*)g.diag, t.sxy, nx, hlo, hr, 0, ny, L.oDG, ES}; return true;
+                              case SG_AZ: d = StageDesc{(const char*)g.a0z, t.sxy, nx, j0, tj, 0, ny, L.oAZ, ES}; return true;
+                              case SG_AX:
+                                  d = StageDesc{(const char*)g.a0x, (long long)(nx + 1) * ny, nx + 1, j0, tj, 0, ny, L.oAX, ES};
+                                  return true;
+                              case SG_AY:
+                                  d = StageDesc{(const char*)g.a0y, (long long)nx * (ny + 1), nx, j0, tj + 1, 0, ny + 1, L.oAY, ES};
+                                  return true;
+                              default: return false;
+                              }
+                          });
+        return;
+    }
+    // ---- consumers --------------------------------------------------------------
+    const int tot = sst_[dom.nscn];
+    char* const ringB = sm + (size_t)ST * shape.slot;
+    unsigned seq = 0;
+    for (int b = blockIdx.x; b < tot; b += gridDim.x) {
+        int s, tile;
+        locateShared(sst_, dom.nscn, b, s, tile);
+        const Scn<R>& g = S[s];
+        const RbTile t = rbTile(g, tile);
+        const int nx = t.nx, ny = t.ny, nz = t.nz, j0 = t.j0, kLo = t.kLo, kHi = t.kHi;
+        const LY L(nx, g.tj);
+        R* const z = g.z;
+        const R* const xc = g.lv[1].x;
+        const int ncell = (t.j1 - j0) * nx;
+        const unsigned magic = divMagic(nx);
+        const int ringRa = max(j0 - 1, 0), ringRe = min(t.j1 + 1, ny);
+        const int mC = (int)(t.sxy & (EPV - 1)), mX = (int)(((long long)(nx + 1) * ny) & (EPV - 1));
+        const int mY = (int)(((long long)nx * (ny + 1)) & (EPV - 1)), mC4 = (int)(t.sxy & 3);
+        const int rC = (j0 * nx) & (EPV - 1), rCm = ((j0 - 1) * nx) & (EPV - 1), rCm4 = ((j0 - 1) * nx) & 3;
+        const int rX = (j0 * (nx + 1)) & (EPV - 1), rY = rC;
+        const int rH = MODE == GS_PRE ? rCm : rC;           // residue of the first row of r and diag
+        const int hOff = MODE == GS_PRE ? nx : 0;           // row j0 within the r and diag arrays
+        RbPipe<ST> pipe{full, empty, &abortFlag, seq, t.nPl, 0, 0};
+        Acc dot{};
+        for (int kk = t.k0; kk < t.k1; ++kk) {
+            const int ic = kk - kLo;
+            pipe.waitThrough(ic + 1, g.errWord);
+            if constexpr (MODE != GS_RED) {
+                // red values of the planes entering the ring (rows j0-1 .. j1)
+                if (!abortFlag) {
+                    for (int k = kk == t.k0 ? kLo : kk + 1; k <= min(kk + 1, kHi); ++k) {
+                        const char* base = sm + (size_t)pipe.slotOf(k - kLo) * shape.slot;
+                        const int n = (ringRe - ringRa) * nx;
+                        const int row0 = (ringRa - (j0 - 1)) * nx;   // ring index of row ringRa
+                        R* out = reinterpret_cast<R*>(ringB + (size_t)(k & 3) * shape.ring) + row0;
+                        if constexpr (MODE == GS_PRE) {
+                            const int o = stageMod(k, mC, rCm, EPV) + row0;
+                            const R* rs = reinterpret_cast<const R*>(base + L.oR) + o;
+                            const R* ds = reinterpret_cast<const R*>(base + L.oDG) + o;
+                            for (int e = threadIdx.x; e < n; e += RB_CTHREADS) {
+                                const int jj = divBy(e, nx, magic), i = e - jj * nx;
+                                if (((i + ringRa + jj + k) & 1) != 0) continue;
+                                const T dg = ds[e];
+                                out[e] = dg <= 0 ? T(0) : (T)(rs[e] / dg);
+                            }
+                        } else {
+                            const R* zs = reinterpret_cast<const R*>(base + L.oZ) + stageMod(k, mC, rCm, EPV) + row0;
+                            const int* as = reinterpret_cast<const int*>(base + L.oAG) + stageMod(k, mC4, rCm4, 4) + row0;
+                            for (int e = threadIdx.x; e < n; e += RB_CTHREADS) {
+                                const int jj = divBy(e, nx, magic), i = e - jj * nx;
+                                if (((i + ringRa + jj + k) & 1) != 0) continue;
+                                T v = zs[e];
+                                const int a = as[e];
+                                if (a >= 0) v = v + xc[a];
+                                out[e] = v;
+                            }
+                        }
+                    }
+                }
+                consumerSync();
+            }
+            if (!abortFlag) {
+                const char* cur = sm + (size_t)pipe.slotOf(ic) * shape.slot;
+                const char* nxt = kk + 1 <= kHi ? sm + (size_t)pipe.slotOf(ic + 1) * shape.slot : cur;
+                const char* prv = kk - 1 >= kLo ? sm + (size_t)pipe.slotOf(ic - 1) * shape.slot : cur;
+                const int oC = stageMod(kk, mC, rC, EPV);
+                const R* rp = reinterpret_cast<const R*>(cur + L.oR) + stageMod(kk, mC, rH, EPV) + hOff;
+                const R* dgp = reinterpret_cast<const R*>(cur + L.oDG) + stageMod(kk, mC, rH, EPV) + hOff;
+                const R* azp = reinterpret_cast<const R*>(cur + L.oAZ) + oC;
+                const R* azn = reinterpret_cast<const R*>(nxt + L.oAZ) + stageMod(kk + 1, mC, rC, EPV);
+                const R* axp = reinterpret_cast<const R*>(cur + L.oAX) + stageMod(kk, mX, rX, EPV);
+                const R* ayp = reinterpret_cast<const R*>(cur + L.oAY) + stageMod(kk, mY, rY, EPV);
+                // neighbour values: the ring (red values) or the staged z (GS_RED), at row j0
+                const R *X0, *Xm, *Xp;
+                if constexpr (MODE == GS_RED) {
+                    X0 = reinterpret_cast<const R*>(cur + L.oZ) + stageMod(kk, mC, rCm, EPV) + nx;
+                    Xm = reinterpret_cast<const R*>(prv + L.oZ) + stageMod(kk - 1, mC, rCm, EPV) + nx;
+                    Xp = reinterpret_cast<const R*>(nxt + L.oZ) + stageMod(kk + 1, mC, rCm, EPV) + nx;
+                } else {
+                    X0 = reinterpret_cast<const R*>(ringB + (size_t)(kk & 3) * shape.ring) + nx;
+                    Xm = reinterpret_cast<const R*>(ringB + (size_t)((kk + 3) & 3) * shape.ring) + nx;
+                    Xp = reinterpret_cast<const R*>(ringB + (size_t)((kk + 1) & 3) * shape.ring) + nx;
+                }
+                R* const zp = z + (long long)kk * t.sxy + (long long)j0 * nx;
+                const bool hasM = kk > 0, hasP = kk < nz - 1;
+                // the colour this sweep updates: black (odd) for GS_PRE and GS_BLACK, red for GS_RED
+                const int upd = MODE == GS_RED ? 0 : 1;
+                for (int e = threadIdx.x; e < ncell; e += RB_CTHREADS) {
+                    const int jj = divBy(e, nx, magic);
+                    const int i = e - jj * nx, j = j0 + jj;
+                    const bool mine = ((i + j + kk) & 1) == upd;
+                    T zc;
+                    if (mine) {
+                        const T dg = dgp[e];
+                        if (dg <= 0) zc = 0;
+                        else {
+                            const R* ax = axp + e + jj;   // a0x index jj * (nx + 1) + i
+                            T sacc = rp[e];
+                            if (i > 0) sacc += ax[0] * X0[e - 1];
+                            if (i < nx - 1) sacc += ax[1] * X0[e + 1];
+                            if (j > 0) sacc += ayp[e] * X0[e - nx];
+                            if (j < ny - 1) sacc += ayp[e + nx] * X0[e + nx];
+                            if (hasM) sacc += azp[e] * Xm[e];
+                            if (hasP) sacc += azn[e] * Xp[e];
+                            zc = sacc / dg;
+                        }
+                        zp[e] = zc;
+                    } else if constexpr (MODE == GS_PRE) {
+                        zc = X0[e];               // the red value of the ring
+                        zp[e] = zc;
+                    } else {
+                        zc = X0[e];               // GS_RED: the black value as staged
+                    }
+                    if constexpr (MODE == GS_RED) dot = accAdd(dot, dotTerm((T)rp[e], zc));
+                }
+            }
+            pipe.releaseThrough(MODE == GS_RED ? ic - 1 : ic);
+        }
+        pipe.releaseThrough(t.nPl - 1);
+        seq += t.nPl;
+        if (consumerSyncOr(abortFlag)) return;
+        if constexpr (MODE == GS_RED) {
+            if (phase == 2) continue;
+            double tot2;
+            if (lastCtaSumC(g, PS_RZ, tile, sst_[s + 1] - sst_[s], dot, &tot2, sh, &amLast) && threadIdx.x == 0)
+                closeCgIteration(g, phase, tot2);
+        }
+    }
+}
+
+}  // namespace phx
+
+namespace phx {
+
+// host side: the shared-memory shapes of the row-block kernels over a batch
+// (the largest slot and ring of its grids)
+template <class R>
+struct RbShapes {
+    RbShape apply{0, 0}, gs[3] = {RbShape{0, 0}, RbShape{0, 0}, RbShape{0, 0}};
+    static void grow(RbShape& a, int slot, int ring) {
+        a.slot = a.slot > slot ? a.slot : slot;
+        a.ring = a.ring > ring ? a.ring : ring;
+    }
+    void add(int nx, int ny) {
+        const int tj = rowBlockRows<R>(nx, ny);
+        const ApplyLayout<R> a(nx, tj);
+        grow(apply, a.slot, a.ring);
+        const GsLayout<R, GS_PRE> g0(nx, tj);
+        grow(gs[0], g0.slot, g0.ring);
+        const GsLayout<R, GS_BLACK> g1(nx, tj);
+        grow(gs[1], g1.slot, g1.ring);
+        const GsLayout<R, GS_RED> g2(nx, tj);
+        grow(gs[2], g2.slot, g2.ring);
+    }
+    size_t smemApply() const { return rbApplySmem<R>(apply); }
+    size_t smemGs(int m) const {
+        return m == GS_PRE ? rbGsSmem<R, GS_PRE>(gs[0]) : m == GS_BLACK ? rbGsSmem<R, GS_BLACK>(gs[1])
+                                                                        : rbGsSmem<R, GS_RED>(gs[2]);
+    }
+    size_t maxSmem() const {
+        size_t m = smemApply();
+        for (int i = 0; i < 3; ++i) m = m > smemGs(i) ? m : smemGs(i);
+        return m;
+    }
+};
 
 }  // namespace phx
