@@ -391,7 +391,9 @@ def main():
                          "cg_iters_last_step": {"min": min(fp64["iters"]), "max": max(fp64["iters"])},
                          "max_rel_residual_last_step": max(fp64["rels"]),
                          "gpu_launches": fp64["launches"], "roofline": fp64["roofline"], "e2e": fp64["e2e"],
-                         "latency": {"step_p50_ms": fp64["p50_ms"], "step_p99_ms": fp64["p99_ms"]}},
+                         "latency": {"step_p50_ms": fp64["p50_ms"], "step_p99_ms": fp64["p99_ms"]},
+                         "kernels": [{"name": p[0], "launches": p[1], "ms": round(p[2], 4)} for p in
+                                     sorted(fp64["prof"], key=lambda p: -p[2])[:10]]},
                 "mixed_over_fp64": mixed["value"] / fp64["value"],
                 "gpu_launches": mixed["launches"],
                 "roofline": mixed["roofline"],

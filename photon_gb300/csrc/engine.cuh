@@ -324,7 +324,7 @@ public:
         int grid = 0;
         RbShape shape{0, 0};
     };
-    RbCfg cfgApply, cfgGs[3];
+    RbCfg cfgApply, cfgGs[3], cfgRes;
     ADom adom[2][D_COUNT];
     double* hPin = nullptr;      // pinned scratch for read-backs
     Dom dom[D_COUNT];
@@ -456,6 +456,7 @@ public:
             PHX_TRY(configRB(cfgGs[GS_PRE], k_gs_rb<R, GS_PRE>, shp.gs[GS_PRE], shp.smemGs(GS_PRE)));
             PHX_TRY(configRB(cfgGs[GS_BLACK], k_gs_rb<R, GS_BLACK>, shp.gs[GS_BLACK], shp.smemGs(GS_BLACK)));
             PHX_TRY(configRB(cfgGs[GS_RED], k_gs_rb<R, GS_RED>, shp.gs[GS_RED], shp.smemGs(GS_RED)));
+            PHX_TRY(configRB(cfgRes, k_res_rb<R>, shp.res, shp.smemRes()));
         }
         PHX_CK(cudaMemcpyAsync(dDomStart, starts.data(), starts.size() * sizeof(int), cudaMemcpyHostToDevice, st));
         PHX_CK(cudaMemcpyAsync(dTiles, tilesAll.data(), tilesAll.size() * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -717,7 +718,7 @@ public:
     void vcycle(int phase) {
         const Scn<R>* S = dS;
         launchRB("k_gs_pre", cfgGs[GS_PRE], k_gs_rb<R, GS_PRE>, S, adom[0][D_RB], cfgGs[GS_PRE].shape, phase);
-        launchA("k_res0_restrict", D_BLK, TPB, k_res0_restrict<R>, S, adom[0][D_BLK]);
+        launchRB("k_res_restrict", cfgRes, k_res_rb<R>, S, adom[0][D_RB], cfgRes.shape);
         for (int l = 1; l < maxLevels - 1; ++l) {
             launchA("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, adom[0][D_LV0 + l], l, 0);
             launchA("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, adom[0][D_LV0 + l], l, 1);

@@ -706,11 +706,208 @@ __global__ void __launch_bounds__(RB_THREADS, 2) k_gs_rb(const Scn<R>* __restric
 
 namespace phx {
 
+// ---------------------------------------------------------------------------------
+// Level-0 residual (residualGrid, pressure_mg.cpp:217-235) and its restriction
+// to level 1 (:285-286) on row-block tiles. z of the tile and its halo rows
+// goes to a 4-plane ring; the residuals of an even plane wait in shared memory
+// (with their aggregate ids) until the odd plane above it is done, then one
+// thread per 2x2x2 block sums each level-1 aggregate's cells in ascending
+// cell order -- the order of the reference's scatter (an aggregate lies in one
+// block; tiles start on even rows and even planes).
+template <class R>
+struct ResLayout {
+    static constexpr int ST = 3;
+    static constexpr int ES = (int)sizeof(R);
+    int oZ, oAG, oR, oDG, oAZ, oAX, oAY, slot, ring, oRA, oRB, oGA, bytes;
+    __host__ __device__ ResLayout(int nx, int tj) {
+        int o = 0;
+        oZ = o;  o += stageBytes(tj + 2, nx, ES);
+        oAG = o; o += stageBytes(tj, nx, 4);
+        oR = o;  o += stageBytes(tj, nx, ES);
+        oDG = o; o += stageBytes(tj, nx, ES);
+        oAZ = o; o += stageBytes(tj, nx, ES);
+        oAX = o; o += stageBytes(tj, nx + 1, ES);
+        oAY = o; o += stageBytes(tj + 1, nx, ES);
+        slot = o;
+        ring = roundUp((tj + 2) * nx * ES, 16);
+        // after the ring: residuals of the even and odd plane, aggregate ids of the even plane
+        oRA = 0;
+        oRB = roundUp(tj * nx * ES, 16);
+        oGA = 2 * oRB;
+        bytes = oGA + roundUp(tj * nx * 4, 16);
+    }
+};
+
+template <class R>
+inline size_t rbResSmem(const RbShape& sh, int tail) {
+    return (size_t)ResLayout<R>::ST * sh.slot + 4 * (size_t)sh.ring + (size_t)tail;
+}
+
+template <class R>
+__global__ void __launch_bounds__(RB_THREADS, 1) k_res_rb(const Scn<R>* __restrict__ S, ADom dom, RbShape shape) {
+    using T = R;
+    using LY = ResLayout<R>;
+    constexpr int ST = LY::ST;
+    constexpr int EPV = 16 / (int)sizeof(R);
+    constexpr int ES = (int)sizeof(R);
+    PHX_RB_PROLOGUE(ST)
+    if (warp == RB_CONSUMERS) {
+        rbProducer<R, ST>(S, sst_, dom.nscn, sm, shape.slot, 1, full, empty, &abortFlag,
+                          [&](int ln, int, const Scn<R>& g, const RbTile& t, StageDesc& d) {
+                              const LY L(t.nx, g.tj);
+                              const int nx = t.nx, ny = t.ny, j0 = t.j0, tj = g.tj;
+                              switch (ln) {
+                              case SG_Z: d = StageDesc{(const char*)g.z, t.sxy, nx, j0 - 1, tj + 2, 0, ny, L.oZ, ES}; return true;
+                              case SG_AG: d = StageDesc{(const char*)g.lv[0].agg, t.sxy, nx, j0, tj, 0, ny, L.oAG, 4}; return true;
+                              case SG_R: d = StageDesc{(const char*)g.r, t.sxy, nx, j0, tj, 0, ny, L.oR, ES}; return true;
+                              case SG_DG: d = StageDesc{(const char*)g.diag, t.sxy, nx, j0, tj, 0, ny, L.oDG, ES}; return true;
+                              case SG_AZ: d = StageDesc{(const char*)g.a0z, t.sxy, nx, j0, tj, 0, ny, L.oAZ, ES}; return true;
+                              case SG_AX:
+                                  d = StageDesc{(const char*)g.a0x, (long long)(nx + 1) * ny, nx + 1, j0, tj, 0, ny, L.oAX, ES};
+                                  return true;
+                              case SG_AY:
+                                  d = StageDesc{(const char*)g.a0y, (long long)nx * (ny + 1), nx, j0, tj + 1, 0, ny + 1, L.oAY, ES};
+                                  return true;
+                              default: return false;
+                              }
+                          });
+        return;
+    }
+    // ---- consumers --------------------------------------------------------------
+    const int tot = sst_[dom.nscn];
+    char* const ringB = sm + (size_t)ST * shape.slot;
+    char* const tail = ringB + 4 * (size_t)shape.ring;
+    unsigned seq = 0;
+    for (int b = blockIdx.x; b < tot; b += gridDim.x) {
+        int s, tile;
+        locateShared(sst_, dom.nscn, b, s, tile);
+        const Scn<R>& g = S[s];
+        const RbTile t = rbTile(g, tile);
+        const int nx = t.nx, ny = t.ny, nz = t.nz, j0 = t.j0, kLo = t.kLo, kHi = t.kHi;
+        const LY L(nx, g.tj);
+        R* const cb = g.lv[1].b;
+        const int rows = t.j1 - j0, ncell = rows * nx;
+        const unsigned magic = divMagic(nx);
+        const int ringRa = max(j0 - 1, 0), ringRe = min(t.j1 + 1, ny);
+        const int mC = (int)(t.sxy & (EPV - 1)), mX = (int)(((long long)(nx + 1) * ny) & (EPV - 1));
+        const int mY = (int)(((long long)nx * (ny + 1)) & (EPV - 1)), mC4 = (int)(t.sxy & 3);
+        const int rC = (j0 * nx) & (EPV - 1), rCm = ((j0 - 1) * nx) & (EPV - 1), rC4 = (j0 * nx) & 3;
+        const int rX = (j0 * (nx + 1)) & (EPV - 1), rY = rC;
+        T* const RA = reinterpret_cast<T*>(tail + L.oRA);
+        T* const RB = reinterpret_cast<T*>(tail + L.oRB);
+        int* const GA = reinterpret_cast<int*>(tail + L.oGA);
+        const int hx = (nx + 1) >> 1, hy = (rows + 1) >> 1, nblk = hx * hy;
+        const unsigned magicHx = divMagic(hx);
+        RbPipe<ST> pipe{full, empty, &abortFlag, seq, t.nPl, 0, 0};
+        for (int kk = t.k0; kk < t.k1; ++kk) {
+            const int ic = kk - kLo;
+            pipe.waitThrough(ic + 1, g.errWord);
+            if (!abortFlag) {
+                for (int k = kk == t.k0 ? kLo : kk + 1; k <= min(kk + 1, kHi); ++k) {
+                    const char* base = sm + (size_t)pipe.slotOf(k - kLo) * shape.slot;
+                    const int n = (ringRe - ringRa) * nx;
+                    const int row0 = (ringRa - (j0 - 1)) * nx;
+                    const R* zs = reinterpret_cast<const R*>(base + L.oZ) + stageMod(k, mC, rCm, EPV) + row0;
+                    R* out = reinterpret_cast<R*>(ringB + (size_t)(k & 3) * shape.ring) + row0;
+                    for (int e = threadIdx.x; e < n; e += RB_CTHREADS) out[e] = zs[e];
+                }
+            }
+            consumerSync();
+            const bool odd = (kk & 1) != 0;
+            if (!abortFlag) {
+                const char* cur = sm + (size_t)pipe.slotOf(ic) * shape.slot;
+                const char* nxt = kk + 1 <= kHi ? sm + (size_t)pipe.slotOf(ic + 1) * shape.slot : cur;
+                const int oC = stageMod(kk, mC, rC, EPV);
+                const R* rp = reinterpret_cast<const R*>(cur + L.oR) + oC;
+                const R* dgp = reinterpret_cast<const R*>(cur + L.oDG) + oC;
+                const int* agp = reinterpret_cast<const int*>(cur + L.oAG) + stageMod(kk, mC4, rC4, 4);
+                const R* azp = reinterpret_cast<const R*>(cur + L.oAZ) + oC;
+                const R* azn = reinterpret_cast<const R*>(nxt + L.oAZ) + stageMod(kk + 1, mC, rC, EPV);
+                const R* axp = reinterpret_cast<const R*>(cur + L.oAX) + stageMod(kk, mX, rX, EPV);
+                const R* ayp = reinterpret_cast<const R*>(cur + L.oAY) + stageMod(kk, mY, rY, EPV);
+                const R* X0 = reinterpret_cast<const R*>(ringB + (size_t)(kk & 3) * shape.ring) + nx;
+                const R* Xm = reinterpret_cast<const R*>(ringB + (size_t)((kk + 3) & 3) * shape.ring) + nx;
+                const R* Xp = reinterpret_cast<const R*>(ringB + (size_t)((kk + 1) & 3) * shape.ring) + nx;
+                T* const RR = odd ? RB : RA;
+                const bool hasM = kk > 0, hasP = kk < nz - 1;
+                for (int e = threadIdx.x; e < ncell; e += RB_CTHREADS) {
+                    const int jj = divBy(e, nx, magic);
+                    const int i = e - jj * nx, j = j0 + jj;
+                    const int A = agp[e];
+                    T rv = 0;
+                    if (A >= 0) {
+                        const R* ax = axp + e + jj;
+                        T sacc = rp[e] - dgp[e] * X0[e];
+                        if (i > 0) sacc += ax[0] * X0[e - 1];
+                        if (i < nx - 1) sacc += ax[1] * X0[e + 1];
+                        if (j > 0) sacc += ayp[e] * X0[e - nx];
+                        if (j < ny - 1) sacc += ayp[e + nx] * X0[e + nx];
+                        if (hasM) sacc += azp[e] * Xm[e];
+                        if (hasP) sacc += azn[e] * Xp[e];
+                        rv = sacc;
+                    }
+                    RR[e] = rv;
+                    if (!odd) GA[e] = A;
+                }
+            }
+            // blocks close on odd planes, and on the grid's last plane when nz is odd
+            const bool close = odd || kk == nz - 1;
+            if (close) {
+                consumerSync();
+                if (!abortFlag) {
+                    const char* cur = sm + (size_t)pipe.slotOf(ic) * shape.slot;
+                    const int* agOdd = reinterpret_cast<const int*>(cur + L.oAG) + stageMod(kk, mC4, rC4, 4);
+                    for (int q = threadIdx.x; q < nblk; q += RB_CTHREADS) {
+                        const int by = divBy(q, hx, magicHx), bx = q - by * hx;
+                        int ag[8];
+                        T rv[8];
+#pragma unroll
+                        for (int m = 0; m < 8; ++m) {
+                            const int di = m & 1, dj = (m >> 1) & 1, dk = m >> 2;
+                            const int i = 2 * bx + di, jj = 2 * by + dj;
+                            const bool in = i < nx && jj < rows && (odd || dk == 0);
+                            const int e = jj * nx + i;
+                            // dk = 0: the even plane (or the lone last plane); dk = 1: the odd plane
+                            const bool useEven = !odd || dk == 0;
+                            ag[m] = in ? (useEven ? GA[e] : agOdd[e]) : -1;
+                            rv[m] = in ? (useEven ? RA[e] : RB[e]) : T(0);
+                        }
+#pragma unroll
+                        for (int m = 0; m < 8; ++m) {
+                            const int a = ag[m];
+                            bool first = a >= 0;
+#pragma unroll
+                            for (int p = 0; p < m; ++p) first = first && ag[p] != a;
+                            if (!first) continue;
+                            T acc = 0;
+#pragma unroll
+                            for (int p = m; p < 8; ++p)
+                                if (ag[p] == a) acc = acc + rv[p];
+                            cb[a] = acc;
+                        }
+                    }
+                }
+            }
+            pipe.releaseThrough(ic);
+            // RA / GA of an even plane are read at the next (odd) step: no barrier needed
+            // before they are rewritten, which happens two steps later after a consumerSync
+        }
+        pipe.releaseThrough(t.nPl - 1);
+        seq += t.nPl;
+        if (consumerSyncOr(abortFlag)) return;
+    }
+}
+
+}  // namespace phx
+
+namespace phx {
+
 // host side: the shared-memory shapes of the row-block kernels over a batch
 // (the largest slot and ring of its grids)
 template <class R>
 struct RbShapes {
-    RbShape apply{0, 0}, gs[3] = {RbShape{0, 0}, RbShape{0, 0}, RbShape{0, 0}};
+    RbShape apply{0, 0}, gs[3] = {RbShape{0, 0}, RbShape{0, 0}, RbShape{0, 0}}, res{0, 0};
+    int resTail = 0;
     static void grow(RbShape& a, int slot, int ring) {
         a.slot = a.slot > slot ? a.slot : slot;
         a.ring = a.ring > ring ? a.ring : ring;
@@ -725,7 +922,11 @@ struct RbShapes {
         grow(gs[1], g1.slot, g1.ring);
         const GsLayout<R, GS_RED> g2(nx, tj);
         grow(gs[2], g2.slot, g2.ring);
+        const ResLayout<R> rl(nx, tj);
+        grow(res, rl.slot, rl.ring);
+        resTail = resTail > rl.bytes ? resTail : rl.bytes;
     }
+    size_t smemRes() const { return rbResSmem<R>(res, resTail); }
     size_t smemApply() const { return rbApplySmem<R>(apply); }
     size_t smemGs(int m) const {
         return m == GS_PRE ? rbGsSmem<R, GS_PRE>(gs[0]) : m == GS_BLACK ? rbGsSmem<R, GS_BLACK>(gs[1])
@@ -734,7 +935,7 @@ struct RbShapes {
     size_t maxSmem() const {
         size_t m = smemApply();
         for (int i = 0; i < 3; ++i) m = m > smemGs(i) ? m : smemGs(i);
-        return m;
+        return m > smemRes() ? m : smemRes();
     }
 };
 
