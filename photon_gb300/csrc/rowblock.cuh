@@ -620,13 +620,30 @@ __global__ void __launch_bounds__(RB_THREADS, 2) k_gs_rb(const Scn<R>* __restric
                         } else {
                             const R* zs = reinterpret_cast<const R*>(base + L.oZ) + stageMod(k, mC, rCm, EPV) + row0;
                             const int* as = reinterpret_cast<const int*>(base + L.oAG) + stageMod(k, mC4, rCm4, 4) + row0;
-                            for (int e = threadIdx.x; e < n; e += RB_CTHREADS) {
-                                const int jj = divBy(e, nx, magic), i = e - jj * nx;
-                                if (((i + ringRa + jj + k) & 1) != 0) continue;
-                                T v = zs[e];
-                                const int a = as[e];
-                                if (a >= 0) v = v + xc[a];
-                                out[e] = v;
+                            // four cells per thread at a time, so that their gathers of
+                            // the coarse correction are in flight together
+                            for (int e0 = threadIdx.x; e0 < n; e0 += 4 * RB_CTHREADS) {
+                                T v[4], xv[4];
+                                int a[4];
+                                bool red[4];
+#pragma unroll
+                                for (int u = 0; u < 4; ++u) {
+                                    const int e = e0 + u * RB_CTHREADS;
+                                    red[u] = false;
+                                    a[u] = -1;
+                                    v[u] = T(0);
+                                    if (e < n) {
+                                        const int jj = divBy(e, nx, magic), i = e - jj * nx;
+                                        red[u] = ((i + ringRa + jj + k) & 1) == 0;
+                                        v[u] = zs[e];
+                                        a[u] = as[e];
+                                    }
+                                }
+#pragma unroll
+                                for (int u = 0; u < 4; ++u) xv[u] = (red[u] && a[u] >= 0) ? (T)xc[a[u]] : T(0);
+#pragma unroll
+                                for (int u = 0; u < 4; ++u)
+                                    if (red[u]) out[e0 + u * RB_CTHREADS] = a[u] >= 0 ? (T)(v[u] + xv[u]) : v[u];
                             }
                         }
                     }

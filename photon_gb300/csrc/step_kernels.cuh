@@ -683,6 +683,13 @@ __device__ __forceinline__ T superbee(T r) {
     return m;
 }
 
+// superbee(num / den) * den without the division (FP32 path): for den > 0
+// max(0, min(2 num, den), min(num, 2 den)); a negative den swaps min and max
+__device__ __forceinline__ float superbeeTimes(float num, float den) {
+    if (den > 0.f) return fmaxf(0.f, fmaxf(fminf(2.f * num, den), fminf(num, 2.f * den)));
+    return fminf(0.f, fminf(fmaxf(2.f * num, den), fmaxf(num, 2.f * den)));
+}
+
 template <class R>
 __global__ void k_advect(const Scn<R>* __restrict__ S, Dom dom) {
     using T = R;
@@ -693,10 +700,15 @@ __global__ void k_advect(const Scn<R>* __restrict__ S, Dom dom) {
         for (int q = 0; q < NSC; ++q) g.sc2[q][c] = g.sc[q][c];
         return;
     }
+    // The FP32 path (mixed precision) uses division-free forms of the same
+    // expressions: the limiter as superbeeTimes, 1/dx and 1/mden multiplied.
+    // The FP64 path keeps the reference's operations one for one.
+    constexpr bool kF32 = std::is_same<T, float>::value;
     const T amb[NSC] = {T(K_T0), T(K_YO2_AMB), T(0), T(0), T(0), T(0), T(K_YCO2_AMB), T(K_YH2O_AMB), T(0), T(0)};
     const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
     const int i = c % nx, j = (c / nx) % ny, k = c / sxy;
     const T dx = (T)g.dx;
+    const T invDx = T(1) / dx;
     const T dt = (T)g.sv[SV_DT];
     const T s = dt / dx;
     const int fa0 = i + (nx + 1) * (j + ny * k), fa1 = fa0 + 1;
@@ -731,11 +743,13 @@ __global__ void k_advect(const Scn<R>* __restrict__ S, Dom dom) {
         if (un[d] > T(0)) {
             T tu2 = opp[d] >= 0 ? Tf[opp[d]] : (opp[d] == -1 ? T(K_T0) : tc);
             T den = tn - tc;
-            tface = tc + (fabs(den) > T(1e-6) ? T(0.5) * superbee((tc - tu2) / den) * den : T(0));
+            if constexpr (kF32) tface = tc + (fabs(den) > T(1e-6) ? T(0.5) * superbeeTimes(tc - tu2, den) : T(0));
+            else tface = tc + (fabs(den) > T(1e-6) ? T(0.5) * superbee((tc - tu2) / den) * den : T(0));
         } else {
             T tu2 = nb2[d] >= 0 ? Tf[nb2[d]] : (nb2[d] == -1 ? T(K_T0) : tn);
             T den = tc - tn;
-            tface = tn + (fabs(den) > T(1e-6) ? T(0.5) * superbee((tn - tu2) / den) * den : T(0));
+            if constexpr (kF32) tface = tn + (fabs(den) > T(1e-6) ? T(0.5) * superbeeTimes(tn - tu2, den) : T(0));
+            else tface = tn + (fabs(den) > T(1e-6) ? T(0.5) * superbee((tn - tu2) / den) * den : T(0));
         }
         T pu = un[d] > T(0) ? g.Pb[c] : (nb[d] >= 0 ? g.Pb[nb[d]] : T(K_P0));
         rUp[d] = pu / (T(K_RS) * mx(tface, T(K_T_MIN)));
@@ -746,6 +760,14 @@ __global__ void k_advect(const Scn<R>* __restrict__ S, Dom dom) {
         rfd[d] = nb[d] >= 0 ? T(0.5) * (rc + rhoOf(g, nb[d])) : rc;
     }
     const bool conservative = mden > T(0.25) * rc;
+    // FP32 path: the per-face diffusion factors of the species
+    T kd[6], km[6];
+    if constexpr (kF32)
+        for (int d = 0; d < 6; ++d) {
+            kd[d] = fo[d] * Dd[d] * invDx;
+            km[d] = fo[d] * rfd[d] * Dd[d] * invDx;
+        }
+    const T invMden = T(1) / mden;
     for (int q = 0; q < NSC; ++q) {
         const R* F = g.sc[q];
         const T fc = F[c];
@@ -760,21 +782,36 @@ __global__ void k_advect(const Scn<R>* __restrict__ S, Dom dom) {
             if (flux > T(0)) {
                 T fu2 = opp[d] >= 0 ? F[opp[d]] : (opp[d] == -1 ? amb[q] : fc);
                 T den = fn - fc;
-                if (fabs(den) > T(1e-12)) face += T(0.5) * superbee((fc - fu2) / den) * den;
+                if constexpr (kF32) {
+                    if (fabs(den) > T(1e-12)) face += T(0.5) * superbeeTimes(fc - fu2, den);
+                } else {
+                    if (fabs(den) > T(1e-12)) face += T(0.5) * superbee((fc - fu2) / den) * den;
+                }
             } else if (flux < T(0)) {
                 T fu2 = nb2[d] >= 0 ? F[nb2[d]] : (nb2[d] == -1 ? amb[q] : fn);
                 T den = fc - fn;
                 face = fn;
-                if (fabs(den) > T(1e-12)) face += T(0.5) * superbee((fn - fu2) / den) * den;
+                if constexpr (kF32) {
+                    if (fabs(den) > T(1e-12)) face += T(0.5) * superbeeTimes(fn - fu2, den);
+                } else {
+                    if (fabs(den) > T(1e-12)) face += T(0.5) * superbee((fn - fu2) / den) * den;
+                }
             }
             acc -= flux * (face - fc);
             macc -= rUp[d] * flux * face;
             if (q > 0) {
-                acc += fo[d] * Dd[d] * (fn - fc) / dx;
-                macc += fo[d] * rfd[d] * Dd[d] * (fn - fc) / dx;
+                if constexpr (kF32) {
+                    acc += kd[d] * (fn - fc);
+                    macc += km[d] * (fn - fc);
+                } else {
+                    acc += fo[d] * Dd[d] * (fn - fc) / dx;
+                    macc += fo[d] * rfd[d] * Dd[d] * (fn - fc) / dx;
+                }
             }
         }
-        T val = conservative ? (rc * fc + s * macc) / mden : fc + s * acc;
+        T val;
+        if constexpr (kF32) val = conservative ? (rc * fc + s * macc) * invMden : fc + s * acc;
+        else val = conservative ? (rc * fc + s * macc) / mden : fc + s * acc;
         g.sc2[q][c] = clampd(val, lo, hi);
     }
 }
