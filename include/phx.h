@@ -167,6 +167,29 @@ int phx_profile_step(struct phx_ctx* ctx, double dt_max, int flush_l2, phx_kerne
 /* kernel launches of the last step */
 int phx_last_step_launches(const struct phx_ctx* ctx);
 
+/* gatherStats' sums of one scenario's current fields (src/sim/solver.cpp:884-915),
+ * recomputed without allocating device memory. No counterpart in the reference
+ * (its stats live in host memory). For callers that must not allocate at the
+ * time of the call: a watchdog or monitoring thread sampling a running batch
+ * whose device memory is committed to admitted scenarios under an HBM budget,
+ * or a real-time stepping loop where an allocation's implicit device
+ * synchronisation would stall the stepping stream.
+ * Fills hrr, fuel_in_domain, max_gas_t and burning_cells (the values
+ * phx_batch_get_stats reports after the step's gatherStats, when the fields
+ * have not changed since) and zeroes the other members; the context's own
+ * stats are not modified. Limits and rules:
+ *  - the scenario has at most 4,194,304 cells (PHX_ERR_INVALID beyond);
+ *  - the context has been stepped since its last membership change
+ *    (PHX_ERR_STATE otherwise: building its tables would allocate);
+ *  - the first call on a device does a one-time set-up (it looks up the
+ *    address of the function's device scratch); make it before any stream
+ *    capture begins;
+ *  - the device scratch is one array per device shared by all contexts: calls
+ *    that overlap in time (from several host threads, or on different
+ *    streams) race on it and give wrong results; serialise them.
+ * Runs on the context's stream and returns when the result is on the host. */
+int phx_gather_stats_noalloc(struct phx_ctx* ctx, int scenario, phx_stats* out);
+
 /* --- batches ---------------------------------------------------------------
  * A context can hold several scenarios of different grids; every kernel of a
  * step covers all of them (one launch per pass, one CUDA graph per step). The

@@ -27,7 +27,7 @@ SYMBOLS = ["phx_create", "phx_destroy", "phx_last_error", "phx_last_global_error
            "phx_time_steps", "phx_profile_step", "phx_last_step_launches", "phx_select_device", "phx_alloc_host",
            "phx_free_host", "phx_create_batch", "phx_batch_add", "phx_batch_remove", "phx_batch_size",
            "phx_batch_scenario_bytes", "phx_batch_add_burner", "phx_batch_step", "phx_batch_get_field",
-           "phx_batch_set_field", "phx_batch_field_count", "phx_batch_get_stats"]
+           "phx_batch_set_field", "phx_batch_field_count", "phx_batch_get_stats", "phx_gather_stats_noalloc"]
 
 
 class PhxGrid(ctypes.Structure):
@@ -96,6 +96,7 @@ def load():
     L.phx_time_steps.argtypes = [vp, i, d, i, ctypes.POINTER(d), ctypes.POINTER(i)]
     L.phx_profile_step.argtypes = [vp, d, i, ctypes.POINTER(PhxKernelTime), i, ctypes.POINTER(i)]
     L.phx_last_step_launches.argtypes = [vp]
+    L.phx_gather_stats_noalloc.argtypes = [vp, i, ctypes.POINTER(PhxStats)]
     L.phx_select_device.argtypes = [i]
     L.phx_create_batch.argtypes = [ctypes.POINTER(PhxGrid), i, i, ctypes.POINTER(vp)]
     L.phx_batch_add.argtypes = [vp, ctypes.POINTER(PhxGrid), ctypes.POINTER(i)]

@@ -28,6 +28,7 @@ UNITS = {
     "engine_mixed.cu": [],
     "host_setup.cpp": [],
     "api.cpp": [],
+    "noalloc.cu": ["--fmad=false"],
 }
 HEADERS = ["phx_dev.cuh", "step_kernels.cuh", "pressure_kernels.cuh", "engine.cuh", "engine.h", "host_setup.h",
            "mixed_kernels.cuh", "engine_mixed.cuh", "rowblock.cuh"]

@@ -199,6 +199,11 @@ int phx_profile_step(phx_ctx* c, double dt_max, int flush_l2, phx_kernel_time* o
 
 int phx_last_step_launches(const phx_ctx* c) { return c && c->impl ? c->impl->lastLaunches() : 0; }
 
+int phx_gather_stats_noalloc(phx_ctx* c, int scenario, phx_stats* out) {
+    if (!out) return fail(c, PHX_ERR_INVALID, "null stats");
+    return guarded(c, [&](phx::CtxBase* x) { return phx::gatherStatsNoAlloc(x, c->precision, scenario, out, x->err); });
+}
+
 int phx_select_device(int device) {
     cudaError_t e = cudaSetDevice(device);
     if (e != cudaSuccess) return fail(nullptr, PHX_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));

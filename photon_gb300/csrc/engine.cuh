@@ -1115,6 +1115,18 @@ public:
         if (st) PHX_CK(cudaStreamSynchronize(st));
         return checkDeviceError();
     }
+    int deviceView(int s, const void** descriptor, int* cells, void** stream) override {
+        PHX_TRY(checkScn(s));
+        if (tablesDirty || !dS) {
+            // building the tables would allocate: the caller steps (or syncs) the context first
+            err = "the context's device tables are not built yet: step the context once after adding scenarios";
+            return PHX_ERR_STATE;
+        }
+        *descriptor = dS + s;
+        *cells = sc[s]->geo.N();
+        *stream = (void*)st;
+        return PHX_OK;
+    }
     int lastLaunches() const override {
         if (useGraph && gexec) {
             int k = 0;

@@ -34,11 +34,17 @@ public:
     virtual int timeSteps(int n, double dtMax, int flushL2, double* totalMs, int* launches) = 0;
     virtual int profileStep(double dtMax, int flushL2, phx_kernel_time* out, int cap, int* count) = 0;
     virtual int lastLaunches() const = 0;
+    // device view of scenario s for kernels outside the engine: its descriptor
+    // in device memory, its cell count and the context's stream (as void*)
+    virtual int deviceView(int s, const void** descriptor, int* cells, void** stream) = 0;
     std::string err;
 };
 
 // empty engines (one translation unit per precision)
 CtxBase* makeCtxFp64();
 CtxBase* makeCtxMixed();
+
+// gatherStats sums of one scenario without any device allocation (noalloc.cu)
+int gatherStatsNoAlloc(CtxBase* ctx, int precision, int scenario, phx_stats* out, std::string& err);
 
 }  // namespace phx
