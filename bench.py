@@ -75,11 +75,12 @@ def kernel_bytes(name: str, w: int):
     table = {
         "k_advect": 18 * w + 1 + 10 * w,        # 10 scalars + u,v,w + fx,fy,fz + Pb,nu + blocked -> 10 scalars
         "k_momentum": 9 * w,                    # vel, 2 other components, fo, Pb, T, nu, p -> vel' (per face)
-        "k_gs0": 5 * w,                         # half sweep: r, diag, z of its colour, z of the other, coefficients
+        "k_gs_pre": 6 * w,                      # r, diag, 3 coefficients -> z
+        "k_gs_black": 6.5 * w + 4,              # r, diag, z, 3 coefficients, agg -> z (black)
+        "k_gs_red_dot": 6.5 * w,                # r, diag, z, 3 coefficients -> z (red), r.z
         "k_cg_apply": 8 * w,                    # z, d, diag, 3 coefficients -> d, q
-        "k_cg_update": 7.5 * w,                 # p, d, r, q, diag -> p, r, z(red)
-        "k_res0_restrict": 6 * w + 4,           # r, z, diag, 3 coefficients, agg
-        "k_gs0_last_dot": 6 * w,
+        "k_cg_update": 7 * w,                   # p, d, r, q, diag -> p, r
+        "k_res_restrict": 6 * w + 4,            # r, z, diag, 3 coefficients, agg
         "k_rhs": 13 * w + 1,
         "k_heat": 8 * w + 1,
         "k_energy": 6 * w + 1,
@@ -98,11 +99,11 @@ def kernel_bytes(name: str, w: int):
 def launched_cells(name: str, launches: int, iters, sizes) -> int:
     """Cells processed by all launches of one kernel in one step. A scenario
     that stopped after it CG iterations took part in it launches of q = A d and
-    of the update, and in it + 1 of the closing half sweep with r.z; every
-    other kernel runs over every cell at each launch."""
+    of the update, and in it + 1 V-cycles (level-0 sweeps and residual);
+    every other kernel runs over every cell at each launch."""
     if name in ("k_cg_apply", "k_cg_update"):
         return sum(i * n for i, n in zip(iters, sizes))
-    if name == "k_gs0_last_dot":
+    if name in ("k_gs_pre", "k_gs_black", "k_gs_red_dot", "k_res_restrict"):
         return sum((i + 1) * n for i, n in zip(iters, sizes))
     return launches * sum(sizes)
 
@@ -325,6 +326,79 @@ def measure(args, precision, L, world, clocks: bool):
             "p50_ms": pct(0.5), "p99_ms": pct(0.99)}
 
 
+def measure_serving(args, precision):
+    """Serving form: a Poisson stream of house requests (20k-1.32M cells,
+    seeded geometry, 10-500 kW burners) submitted by client threads at their
+    arrival times, admitted under a 150 GB HBM budget and stepped together by
+    one serving loop (continuous batching). The simulated durations of
+    30-300 s are scaled by args.serve_scale so the run ends in about a minute.
+    Returns throughput and p50/p99 step and completion latency."""
+    import threading
+    from photon_gb300 import casegen
+    from photon_gb300.serve import Server
+    reqs = casegen.serving_requests(args.serve_requests, args.serve_rate, seed=7)
+    for _, c in reqs:
+        c.profile.tol = 0.0
+        c.profile.rel_tol = REL_TOL
+    srv = Server(precision, hbm_budget_bytes=150 << 30)
+    ids = [None] * len(reqs)
+    arrival = [0.0] * len(reqs)
+    t0 = time.monotonic() + 0.5
+    lock = threading.Lock()
+    nxt = [0]
+
+    def client():
+        while True:
+            with lock:
+                k = nxt[0]
+                nxt[0] += 1
+            if k >= len(reqs):
+                return
+            at, c = reqs[k]
+            wait = t0 + at - time.monotonic()
+            if wait > 0:
+                time.sleep(wait)
+            arrival[k] = time.monotonic()
+            ids[k] = srv.submit(c, c.duration * args.serve_scale, c.profile.dtMax)
+
+    clients = [threading.Thread(target=client) for _ in range(4)]
+    for th in clients:
+        th.start()
+    step_ms = []
+    done = set()
+    tfirst = None
+    while len(done) < len(reqs):
+        c = srv.counts()
+        if c["queued"] == 0 and c["running"] == 0:
+            time.sleep(0.001)
+        else:
+            a = time.monotonic()
+            tfirst = tfirst or a
+            srv.step()
+            step_ms.append((time.monotonic() - a) * 1e3)
+        for k, rid in enumerate(ids):
+            if rid is not None and k not in done and srv.poll(rid)["state"] in ("done", "rejected"):
+                done.add(k)
+    tend = time.monotonic()
+    for th in clients:
+        th.join()
+    infos = [srv.poll(rid) for rid in ids]
+    cell_updates = srv.counts()["cell_updates"]
+    srv.close()
+    comp = sorted(i["t_done"] - a for i, a in zip(infos, arrival))
+    st = sorted(step_ms)
+    pct = lambda v, q: v[min(len(v) - 1, int(round(q * (len(v) - 1))))]
+    return {"value": cell_updates / (tend - tfirst), "unit": "cell-updates/s", "requests": len(reqs),
+            "rejected": sum(1 for i in infos if i["state"] == "rejected"),
+            "steps": len(step_ms), "wall_s": tend - tfirst,
+            "step_p50_ms": pct(st, 0.5), "step_p99_ms": pct(st, 0.99),
+            "completion_p50_s": pct(comp, 0.5), "completion_p99_s": pct(comp, 0.99),
+            "config": {"arrivals": "Poisson, %.1f requests/s" % args.serve_rate,
+                       "cells": "20k-1.32M log-uniform", "hbm_budget_gb": 150,
+                       "duration": "30-300 s simulated x %g" % args.serve_scale,
+                       "pressure_stop": "relative %g" % REL_TOL}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -334,6 +408,10 @@ def main():
     ap.add_argument("--workload", default="batch64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--spinup", type=int, default=SPINUP_STEPS, help="untimed steps before warm-up")
+    ap.add_argument("--serve-requests", type=int, default=32)
+    ap.add_argument("--serve-rate", type=float, default=8.0, help="request arrivals per second (Poisson)")
+    ap.add_argument("--serve-scale", type=float, default=0.01, help="scale of the 30-300 s simulated durations")
+    ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64"],
                     help="which paths to time (the line's value is the mixed path unless only fp64 runs)")
     args = ap.parse_args()
@@ -358,6 +436,13 @@ def main():
     if fp64 is None:
         fp64 = mixed
     cases = mixed["cases"]
+    serving = None
+    if not args.no_serving:
+        serving = {}
+        if args.precision in ("both", "mixed"):
+            serving["mixed"] = measure_serving(args, _lib.PREC_MIXED)
+        if args.precision in ("both", "fp64"):
+            serving["fp64"] = measure_serving(args, _lib.PREC_FP64)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -398,6 +483,7 @@ def main():
                 "gpu_launches": mixed["launches"],
                 "roofline": mixed["roofline"],
                 "cpu_baseline": cpu,
+                "serving": serving,
                 "clocks": mixed["clk"].summary(),
                 "kernels": [{"name": p[0], "launches": p[1], "ms": round(p[2], 4)} for p in
                             sorted(mixed["prof"], key=lambda p: -p[2])[:14]]}

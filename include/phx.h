@@ -167,6 +167,42 @@ int phx_profile_step(struct phx_ctx* ctx, double dt_max, int flush_l2, phx_kerne
 /* kernel launches of the last step */
 int phx_last_step_launches(const struct phx_ctx* ctx);
 
+/* ---- serving: continuous batching under an HBM budget -------------------------
+ * No counterpart in the reference (one Solver per process there). A server
+ * owns one batch context. Requests (a grid, its burners, a simulated duration
+ * and a dtMax) may be submitted from any host thread at any time; the
+ * submitting thread does the request's host set-up. phx_server_step, called
+ * by one stepping thread, admits queued requests in arrival order while their
+ * device bytes fit the budget and the batch has room, steps every running
+ * request once (all in the same kernel launches), and retires the requests
+ * whose simulated time reached their duration: their final fields are copied
+ * to host memory and their device memory is freed. */
+typedef struct phx_server phx_server;
+enum { PHX_REQ_QUEUED = 0, PHX_REQ_RUNNING = 1, PHX_REQ_DONE = 2, PHX_REQ_REJECTED = 3 };
+typedef struct phx_request_info {
+    int state;                   /* PHX_REQ_* */
+    int steps;                   /* steps run */
+    double sim_time, duration;   /* simulated seconds run / requested */
+    double t_submit, t_admit, t_done;   /* host steady-clock seconds */
+    size_t device_bytes;
+    long long cells;
+    phx_stats stats;             /* final stats (finished requests) */
+} phx_request_info;
+
+int phx_server_create(int precision, size_t hbm_budget_bytes, int max_scenarios, phx_server** out);
+void phx_server_destroy(phx_server* server);
+const char* phx_server_last_error(const phx_server* server);
+/* burners: n_burners x 9 doubles (x0 y0 x1 y1 z peak_w ramp_s start duration, as phx_add_burner) */
+int phx_server_submit(phx_server* server, const phx_grid* grid, const double* burners, int n_burners,
+                      double duration, double dt_max, int* request_id);
+int phx_server_step(phx_server* server, int* admitted, int* finished, int* running);
+int phx_server_poll(phx_server* server, int request_id, phx_request_info* out);
+/* fields of a running request (from the device) or of a finished one (u v w p T, the 9 species,
+ * nu, hrr, kept on the host); real fields as double */
+int phx_server_get_field(phx_server* server, int request_id, int field, void* host, size_t bytes);
+int phx_server_release(phx_server* server, int request_id);
+int phx_server_counts(phx_server* server, int* queued, int* running, size_t* used_bytes, long long* cell_updates);
+
 /* gatherStats' sums of one scenario's current fields (src/sim/solver.cpp:884-915),
  * recomputed without allocating device memory. No counterpart in the reference
  * (its stats live in host memory). For callers that must not allocate at the

@@ -27,7 +27,11 @@ SYMBOLS = ["phx_create", "phx_destroy", "phx_last_error", "phx_last_global_error
            "phx_time_steps", "phx_profile_step", "phx_last_step_launches", "phx_select_device", "phx_alloc_host",
            "phx_free_host", "phx_create_batch", "phx_batch_add", "phx_batch_remove", "phx_batch_size",
            "phx_batch_scenario_bytes", "phx_batch_add_burner", "phx_batch_step", "phx_batch_get_field",
-           "phx_batch_set_field", "phx_batch_field_count", "phx_batch_get_stats", "phx_gather_stats_noalloc"]
+           "phx_batch_set_field", "phx_batch_field_count", "phx_batch_get_stats", "phx_gather_stats_noalloc",
+           "phx_server_create", "phx_server_destroy", "phx_server_last_error", "phx_server_submit", "phx_server_step",
+           "phx_server_poll", "phx_server_get_field", "phx_server_release", "phx_server_counts"]
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_REJECTED = 0, 1, 2, 3
 
 
 class PhxGrid(ctypes.Structure):
@@ -51,6 +55,13 @@ class PhxStats(ctypes.Structure):
                 ("hrr", ctypes.c_double), ("max_gas_t", ctypes.c_double), ("burning_cells", ctypes.c_int),
                 ("fuel_in", ctypes.c_double), ("fuel_burned", ctypes.c_double), ("fuel_in_domain", ctypes.c_double),
                 ("zones", ctypes.c_int), ("leak_faces", ctypes.c_int)]
+
+
+class PhxRequestInfo(ctypes.Structure):
+    _fields_ = [("state", ctypes.c_int), ("steps", ctypes.c_int),
+                ("sim_time", ctypes.c_double), ("duration", ctypes.c_double),
+                ("t_submit", ctypes.c_double), ("t_admit", ctypes.c_double), ("t_done", ctypes.c_double),
+                ("device_bytes", ctypes.c_size_t), ("cells", ctypes.c_longlong), ("stats", PhxStats)]
 
 
 class PhxKernelTime(ctypes.Structure):
@@ -97,6 +108,18 @@ def load():
     L.phx_profile_step.argtypes = [vp, d, i, ctypes.POINTER(PhxKernelTime), i, ctypes.POINTER(i)]
     L.phx_last_step_launches.argtypes = [vp]
     L.phx_gather_stats_noalloc.argtypes = [vp, i, ctypes.POINTER(PhxStats)]
+    L.phx_server_create.argtypes = [i, sz, i, ctypes.POINTER(vp)]
+    L.phx_server_destroy.argtypes = [vp]
+    L.phx_server_destroy.restype = None
+    L.phx_server_last_error.argtypes = [vp]
+    L.phx_server_last_error.restype = ctypes.c_char_p
+    L.phx_server_submit.argtypes = [vp, ctypes.POINTER(PhxGrid), vp, i, d, d, ctypes.POINTER(i)]
+    L.phx_server_step.argtypes = [vp, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i)]
+    L.phx_server_poll.argtypes = [vp, i, ctypes.POINTER(PhxRequestInfo)]
+    L.phx_server_get_field.argtypes = [vp, i, i, vp, sz]
+    L.phx_server_release.argtypes = [vp, i]
+    L.phx_server_counts.argtypes = [vp, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(sz),
+                                    ctypes.POINTER(ctypes.c_longlong)]
     L.phx_select_device.argtypes = [i]
     L.phx_create_batch.argtypes = [ctypes.POINTER(PhxGrid), i, i, ctypes.POINTER(vp)]
     L.phx_batch_add.argtypes = [vp, ctypes.POINTER(PhxGrid), ctypes.POINTER(i)]

@@ -29,6 +29,7 @@ UNITS = {
     "host_setup.cpp": [],
     "api.cpp": [],
     "noalloc.cu": ["--fmad=false"],
+    "server.cpp": [],
 }
 HEADERS = ["phx_dev.cuh", "step_kernels.cuh", "pressure_kernels.cuh", "engine.cuh", "engine.h", "host_setup.h",
            "mixed_kernels.cuh", "engine_mixed.cuh", "rowblock.cuh"]

@@ -38,7 +38,7 @@ constexpr int DENSE_MAX = 4096;
 constexpr size_t RB_SMEM_MAX = 220 * 1024;
 
 enum DomId {
-    D_ONE = 0, D_CELLS, D_HALF, D_BLK, D_FX, D_FY, D_FZ, D_BX, D_BY, D_BZ, D_CZ, D_CC, D_CO_DENSE, D_CO_SERIAL, D_RB,
+    D_ONE = 0, D_CELLS, D_FX, D_FY, D_FZ, D_BX, D_BY, D_BZ, D_CZ, D_CC, D_CO_DENSE, D_CO_SERIAL, D_RB,
     D_LV0,                       // D_LV0 + l: rows of level l when l is not the coarsest (1 <= l < 12)
     D_RS0 = D_LV0 + MAX_LEVELS,  // D_RS0 + l: rows of level l+1 for restriction from level l >= 1
     D_COUNT = D_RS0 + MAX_LEVELS
@@ -275,8 +275,6 @@ struct Scenario {
         for (int d = 0; d < D_COUNT; ++d) t[d] = 0;
         t[D_ONE] = 1;
         t[D_CELLS] = cdiv(N, TPB);
-        t[D_HALF] = cdiv((long long)((nx + 1) / 2) * ny * nz, TPB);
-        t[D_BLK] = cdiv(nx, RB_X) * ((ny + 1) / 2) * ((nz + 1) / 2);   // 64 x 2 x 2 cells per tile
         t[D_RB] = cdiv(ny, rowBlockRows<R>(nx, ny)) * cdiv(nz, RB_KZ);      // row blocks x plane blocks
         t[D_FX] = cdiv(geo.NX(), TPB);
         t[D_FY] = cdiv(geo.NY(), TPB);
@@ -318,6 +316,7 @@ public:
     int* dAStart = nullptr;      // [2][D_COUNT][cap + 1] active-tile prefixes (solving / replacing)
     int* dATotal = nullptr;      // [2][D_COUNT]
     unsigned* dErr = nullptr;    // error word of the device side (bounded waits that ran out)
+    double* dTimes = nullptr;    // simulated time of each scenario (read-back staging)
     // launch shape of a row-block kernel: dynamic shared memory, persistent grid, slot strides
     struct RbCfg {
         size_t smem = 0;
@@ -359,19 +358,44 @@ public:
     // ---- membership ---------------------------------------------------------------
     int addScenario(const phx_grid* g, int* id) override {
         if (nscn() >= MAX_BATCH) { err = "batch is full (1024 scenarios)"; return PHX_ERR_BUDGET; }
+        size_t bytes = 0;
+        // validation and host set-up first: no device needed to reject bad input
+        void* p = prepare(g, &bytes, err);
+        if (!p) return lastPrepareStatus;
+        return admit(p, id);
+    }
+
+    int lastPrepareStatus = PHX_OK;
+    void* prepare(const phx_grid* g, size_t* bytes, std::string& e) override {
         auto s = std::make_unique<Scenario<R>>();
-        int r = s->setup(g);   // validation and host set-up first: no device needed to reject bad input
-        if (r == PHX_OK) {
-            r = initStream();
-            if (r != PHX_OK) return r;
-        }
-        if (r == PHX_OK) r = s->allocate();
+        const int r = s->setup(g);
+        lastPrepareStatus = r;
+        if (r != PHX_OK) { e = s->err; return nullptr; }
+        if (bytes) *bytes = s->layout(nullptr);
+        return s.release();
+    }
+    int admit(void* prepared, int* id) override {
+        std::unique_ptr<Scenario<R>> s(static_cast<Scenario<R>*>(prepared));
+        if (nscn() >= MAX_BATCH) { err = "batch is full (1024 scenarios)"; return PHX_ERR_BUDGET; }
+        PHX_TRY(initStream());
+        int r = s->allocate();
         if (r == PHX_OK) r = s->upload(st);
         if (r != PHX_OK) { err = s->err.empty() ? err : s->err; return r; }
         sc.push_back(std::move(s));
         if (id) *id = nscn() - 1;
         tablesDirty = true;
         return PHX_OK;
+    }
+    void discard(void* prepared) override { delete static_cast<Scenario<R>*>(prepared); }
+    int readTimes(double* out) override {
+        const int n = nscn();
+        if (n == 0) return PHX_OK;
+        PHX_TRY(ensureTables());
+        k_read_times<R><<<(n + 127) / 128, 128, 0, st>>>(dS, n, dTimes);
+        ++launches;
+        PHX_CK(cudaMemcpyAsync(out, dTimes, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+        PHX_CK(cudaStreamSynchronize(st));
+        return checkDeviceError();
     }
 
     int removeScenario(int s) override {
@@ -404,6 +428,7 @@ public:
                 dAStart = carve<int>(base, off, (size_t)2 * D_COUNT * (cap + 1));
                 dATotal = carve<int>(base, off, 2 * D_COUNT);
                 dErr = carve<unsigned>(base, off, 4);
+                dTimes = carve<double>(base, off, cap);
                 if (pass == 0) {
                     cudaError_t e = cudaMalloc(&tab, off + 256);
                     if (e != cudaSuccess) { tab = nullptr; err = "device allocation of the batch tables failed"; return PHX_ERR_OOM; }

@@ -37,6 +37,16 @@ public:
     // device view of scenario s for kernels outside the engine: its descriptor
     // in device memory, its cell count and the context's stream (as void*)
     virtual int deviceView(int s, const void** descriptor, int* cells, void** stream) = 0;
+    // two-phase admission for the serving loop: host set-up of a scenario
+    // (validation, zones, multigrid; no device work) with its device bytes,
+    // then its allocation and upload into the batch. prepare() may run on
+    // another host thread while the batch steps; a prepared scenario that is
+    // never admitted is released with discard().
+    virtual void* prepare(const phx_grid* g, size_t* bytes, std::string& err) = 0;
+    virtual int admit(void* prepared, int* id) = 0;
+    virtual void discard(void* prepared) = 0;
+    // simulated time of every scenario, one read-back for the batch
+    virtual int readTimes(double* out) = 0;
     std::string err;
 };
 

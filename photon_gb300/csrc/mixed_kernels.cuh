@@ -137,6 +137,13 @@ __global__ void k_mx_final(const Scn<R>* __restrict__ S, Dom dom) {
     g.p[c] = (R)v;
 }
 
+// simulated time of every scenario into one array (one read-back per batch)
+template <class R>
+__global__ void k_read_times(const Scn<R>* __restrict__ S, int n, double* out) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) out[s] = S[s].sv[SV_TIME];
+}
+
 // per-scenario resets of the solve's scalar slots (one thread per scenario):
 // which 0: the CG of either path; 2: a bare V-cycle
 template <class R>

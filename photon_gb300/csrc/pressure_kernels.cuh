@@ -2,11 +2,10 @@
 // (src/sim/pressure_mg.cpp:193-300) and the preconditioned CG loop
 // (src/sim/gasphase.cpp:551-626).
 //
-// Level 0 is the structured 7-point grid: red-black Gauss-Seidel half sweeps
-// (gsColor) are order independent, so each colour is one launch. The residual
-// and the restriction to level 1 run in one pass over 2x2x2 blocks: every
-// level-1 aggregate lies inside one block, so a thread sums its aggregates'
-// residuals in ascending cell order -- the order of the reference's scatter.
+// Level 0, the structured 7-point grid, runs on row-block tiles staged in
+// shared memory (rowblock.cuh: q = A d, the red-black half sweeps, the
+// residual with its restriction). This file holds the CG update, the coarse
+// levels and the active-tile tables.
 // Coarse levels are CSR rows: damped Jacobi (omega 0.7) and a gather of the
 // children's residuals in ascending order. The coarsest level's 20 forward +
 // backward Gauss-Seidel sweeps from x = 0 are a fixed linear map of b; it is
@@ -43,106 +42,6 @@ constexpr double OMEGA = 0.7;
 // The solve kernels compute in the arithmetic type T = R of the path (FP64 or
 // FP32); dot products accumulate in Acc (double, or a double-float pair on
 // the FP32 path) and reach the per-scenario scalars as doubles.
-
-// level-0 Gauss-Seidel half sweep of one colour (gsColor, pressure_mg.cpp:195-216)
-// with b = r and x = z. mode 0: the other colour is still zero (x = b / diag);
-// mode 1: plain; mode 2: the other colour is first prolongated from level 1.
-template <class R>
-__global__ void k_gs0(const Scn<R>* __restrict__ S, ADom dom, int color, int mode) {
-    using T = R;
-    PHX_TILES_BEGIN(dom)
-    const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
-    const int hx = (nx + 1) >> 1;
-    int t = tile_ * TPB + threadIdx.x;
-    if (t >= hx * ny * nz) break;
-    const int ii = t % hx, jk = t / hx, j = jk % ny, k = jk / ny;
-    const int i = 2 * ii + ((j + k + color) & 1);
-    if (i >= nx) break;
-    const int c = i + nx * (j + ny * k);
-    const T dg = g.diag[c];
-    R* x = g.z;
-    if (dg <= 0) { x[c] = 0; break; }
-    T s = g.r[c];
-    if (mode != 0) {
-        const int* agg = g.lv[0].agg;
-        const R* xc = g.lv[1].x;
-        auto X = [&](int n) -> T {
-            T v = x[n];
-            if (mode == 2) { int a = agg[n]; if (a >= 0) v = v + xc[a]; }
-            return v;
-        };
-        const int fx0 = i + (nx + 1) * (j + ny * k), fy0 = i + nx * (j + (ny + 1) * k);
-        if (i > 0) s += g.a0x[fx0] * X(c - 1);
-        if (i < nx - 1) s += g.a0x[fx0 + 1] * X(c + 1);
-        if (j > 0) s += g.a0y[fy0] * X(c - nx);
-        if (j < ny - 1) s += g.a0y[fy0 + nx] * X(c + nx);
-        if (k > 0) s += g.a0z[c] * X(c - sxy);
-        if (k < nz - 1) s += g.a0z[c + sxy] * X(c + sxy);
-    }
-    x[c] = s / dg;
-    PHX_TILES_END
-}
-
-// level-0 residual (residualGrid, pressure_mg.cpp:217-235) and restriction to
-// level 1 (:285-286). A tile is 64 x 2 x 2 cells: each thread computes one
-// cell's residual (coalesced) into shared memory, then 32 threads sum the
-// 2x2x2 blocks of the tile per level-1 aggregate in ascending cell order --
-// the order of the reference's scatter (every aggregate lies in one block).
-constexpr int RB_X = 64;
-template <class R>
-__global__ void k_res0_restrict(const Scn<R>* __restrict__ S, ADom dom) {
-    using T = R;
-    __shared__ T rs[256];
-    __shared__ int ag[256];
-    PHX_TILES_BEGIN(dom)
-    const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
-    const int ntx = (nx + RB_X - 1) / RB_X, nty = (ny + 1) >> 1;
-    const int tx = tile_ % ntx, tj = (tile_ / ntx) % nty, tk = tile_ / (ntx * nty);
-    const int xi = threadIdx.x & (RB_X - 1), jj = (threadIdx.x >> 6) & 1, kk = threadIdx.x >> 7;
-    const int i = tx * RB_X + xi, j = 2 * tj + jj, k = 2 * tk + kk;
-    const R* x = g.z;
-    T rv = 0;
-    int A = -1;
-    if (i < nx && j < ny && k < nz) {
-        const int c = i + nx * (j + ny * k);
-        A = g.lv[0].agg[c];
-        if (A >= 0) {
-            const T dg = g.diag[c];
-            const int fx0 = i + (nx + 1) * (j + ny * k), fy0 = i + nx * (j + (ny + 1) * k);
-            T s = g.r[c] - dg * x[c];
-            if (i > 0) s += g.a0x[fx0] * x[c - 1];
-            if (i < nx - 1) s += g.a0x[fx0 + 1] * x[c + 1];
-            if (j > 0) s += g.a0y[fy0] * x[c - nx];
-            if (j < ny - 1) s += g.a0y[fy0 + nx] * x[c + nx];
-            if (k > 0) s += g.a0z[c] * x[c - sxy];
-            if (k < nz - 1) s += g.a0z[c + sxy] * x[c + sxy];
-            rv = s;
-        }
-    }
-    rs[threadIdx.x] = rv;
-    ag[threadIdx.x] = A;
-    __syncthreads();
-    if (threadIdx.x < RB_X / 2) {
-        R* cb = g.lv[1].b;
-        int ids[8];
-        T sums[8];
-        int na = 0;
-        for (int dk = 0; dk < 2; ++dk)
-            for (int dj = 0; dj < 2; ++dj)
-                for (int di = 0; di < 2; ++di) {
-                    const int q = dk * 128 + dj * 64 + 2 * threadIdx.x + di;
-                    const int a = ag[q];
-                    if (a < 0) continue;
-                    int e = 0;
-                    while (e < na && ids[e] != a) ++e;
-                    if (e == na) { ids[na] = a; sums[na] = T(0); ++na; }
-                    sums[e] = sums[e] + rs[q];
-                }
-        for (int e = 0; e < na; ++e) cb[ids[e]] = sums[e];
-    }
-    __syncthreads();
-    PHX_TILES_END
-}
 
 // damped Jacobi sweep on a coarse level (jacobi, pressure_mg.cpp:237-247).
 // mode 0: from x = 0, into y; mode 1: y -> x; mode 2: x plus the coarser
@@ -310,95 +209,6 @@ __device__ void closeCgIteration(const Scn<R>& g, int phase, double tot) {
         sv[SV_RMAX] = 0;
         if (stop) sv[SV_DONE] = 1;
     }
-}
-
-// last level-0 half sweep of the V-cycle (red, after black) fused with the
-// r.z dot product of the CG (dotRZ, src/sim/gasphase.cpp:582-588); the last
-// CTA of the scenario closes the iteration. phase 0: first preconditioning
-// before the loop; 1: inside the loop; 2: a bare V-cycle (no CG bookkeeping).
-template <class R>
-__global__ void k_gs0_last_dot(const Scn<R>* __restrict__ S, ADom dom, int phase) {
-    using T = R;
-    using Acc = decltype(dotTerm(T(0), T(0)));
-    PHX_TILES_BEGIN(dom)
-    const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
-    const int c = tile_ * TPB + threadIdx.x;
-    Acc dot{};
-    if (c < g.N) {
-        const int i = c % nx, j = (c / nx) % ny, k = c / sxy;
-        R* x = g.z;
-        const T rc = g.r[c];
-        T zc;
-        if (((i + j + k) & 1) == 0) {
-            const T dg = g.diag[c];
-            if (dg <= 0) zc = 0;
-            else {
-                const int fx0 = i + (nx + 1) * (j + ny * k), fy0 = i + nx * (j + (ny + 1) * k);
-                T s = rc;
-                if (i > 0) s += g.a0x[fx0] * x[c - 1];
-                if (i < nx - 1) s += g.a0x[fx0 + 1] * x[c + 1];
-                if (j > 0) s += g.a0y[fy0] * x[c - nx];
-                if (j < ny - 1) s += g.a0y[fy0 + nx] * x[c + nx];
-                if (k > 0) s += g.a0z[c] * x[c - sxy];
-                if (k < nz - 1) s += g.a0z[c + sxy] * x[c + sxy];
-                zc = s / dg;
-            }
-            x[c] = zc;
-        } else {
-            zc = x[c];
-        }
-        dot = dotTerm(rc, zc);
-    }
-    if (phase == 2) break;
-    double tot;
-    if (lastCtaSum(g, PS_RZ, tile_, (sst_[s_ + 1] - sst_[s_]), dot, &tot) && threadIdx.x == 0) closeCgIteration(g, phase, tot);
-    PHX_TILES_END
-}
-
-// q = A d with the search direction updated on the fly
-// (d = z + beta d, src/sim/gasphase.cpp:620-622, and apply :551-570), and the
-// d.q partial sums; the last CTA computes alpha or stops on d.q <= 0 (:606-608).
-// d is double-buffered by iteration parity.
-template <class R>
-__global__ void k_cg_apply(const Scn<R>* __restrict__ S, ADom dom, R* const* dbuf) {
-    using T = R;
-    using Acc = decltype(dotTerm(T(0), T(0)));
-    PHX_TILES_BEGIN(dom)
-    const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
-    const int c = tile_ * TPB + threadIdx.x;
-    const int it = (int)g.sv[SV_IT];
-    const R* dprev = dbuf[2 * s_ + (it & 1)];
-    R* dnew = dbuf[2 * s_ + ((it + 1) & 1)];
-    const T beta = (T)g.sv[SV_BETA];
-    const R* z = g.z;
-    auto D = [&](int n) -> T { return it == 0 ? z[n] : (T)(z[n] + beta * dprev[n]); };
-    Acc dot{};
-    if (c < g.N) {
-        const T dc = D(c);
-        dnew[c] = dc;
-        const T dg = g.diag[c];
-        if (dg <= 0) g.q[c] = 0;
-        else {
-            const int i = c % nx, j = (c / nx) % ny, k = c / sxy;
-            const int fx0 = i + (nx + 1) * (j + ny * k), fy0 = i + nx * (j + (ny + 1) * k);
-            T s = dg * dc;
-            if (i > 0) s -= g.a0x[fx0] * D(c - 1);
-            if (i < nx - 1) s -= g.a0x[fx0 + 1] * D(c + 1);
-            if (j > 0) s -= g.a0y[fy0] * D(c - nx);
-            if (j < ny - 1) s -= g.a0y[fy0 + nx] * D(c + nx);
-            if (k > 0) s -= g.a0z[c] * D(c - sxy);
-            if (k < nz - 1) s -= g.a0z[c + sxy] * D(c + sxy);
-            g.q[c] = s;
-            dot = dotTerm(s, dc);
-        }
-    }
-    double tot;
-    if (lastCtaSum(g, PS_DQ, tile_, (sst_[s_ + 1] - sst_[s_]), dot, &tot) && threadIdx.x == 0) {
-        g.sv[SV_DQ] = tot;
-        if (tot <= 0) g.sv[SV_DONE] = 1;
-        else g.sv[SV_ALPHA] = g.sv[SV_RZ] / tot;
-    }
-    PHX_TILES_END
 }
 
 // p += alpha d; r -= alpha q (src/sim/gasphase.cpp:609-615), max|r| for the

@@ -331,7 +331,7 @@ __device__ __forceinline__ int divBy(int e, int nx, unsigned magic) { return nx 
 // ---------------------------------------------------------------------------------
 // q = A d with d = z + beta d (src/sim/gasphase.cpp:551-570, 620-622) and the
 // d.q partial sums (:606-608) on row-block tiles: the same arithmetic as
-// k_cg_apply. d is computed once per cell into a 4-plane ring in shared
+// the reference. d is computed once per cell into a 4-plane ring in shared
 // memory (rows j0-1 .. j1), then the 7-point stencil reads the ring.
 //
 // Slot layout: {z, d_prev, diag, a0z, a0x, a0y}; z and d over rows j0-1 .. j1.
@@ -504,7 +504,7 @@ namespace phx {
 //          ring holds them. Writes the black cells of z.
 // GS_RED   the last (red) half sweep fused with r.z (dotRZ,
 //          src/sim/gasphase.cpp:582-588); the last CTA of a scenario closes the
-//          CG iteration as k_gs0_last_dot does. Writes the red cells of z.
+//          CG iteration (closeCgIteration). Writes the red cells of z.
 enum { GS_PRE = 0, GS_BLACK = 1, GS_RED = 2 };
 
 template <class R, int MODE>
