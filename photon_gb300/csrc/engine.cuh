@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <string>
 #include <type_traits>
@@ -34,8 +35,6 @@ namespace phx {
 
 // dense coarse operators up to this many unknowns (n^2 reals)
 constexpr int DENSE_MAX = 4096;
-// dynamic shared memory of one CTA of the row-block kernels (the static part is about 4 KB)
-constexpr size_t RB_SMEM_MAX = 220 * 1024;
 
 enum DomId {
     D_ONE = 0, D_CELLS, D_FX, D_FY, D_FZ, D_BX, D_BY, D_BZ, D_CZ, D_CC, D_CO_DENSE, D_CO_SERIAL, D_RB,
@@ -107,7 +106,7 @@ struct Scenario {
         }
         RbShapes<R> one;
         one.add(g->nx, g->ny);
-        if (one.maxSmem() > RB_SMEM_MAX) {
+        if (!one.finish()) {
             err = "grid rows too long for the shared-memory tiles of the pressure kernels (nx = " + std::to_string(g->nx) + ")";
             return PHX_ERR_UNSUPPORTED;
         }
@@ -317,11 +316,12 @@ public:
     int* dATotal = nullptr;      // [2][D_COUNT]
     unsigned* dErr = nullptr;    // error word of the device side (bounded waits that ran out)
     double* dTimes = nullptr;    // simulated time of each scenario (read-back staging)
+    int* dAllTotal = nullptr;    // the row-block tile total of the batch (every tile active), for tuning runs
     // launch shape of a row-block kernel: dynamic shared memory, persistent grid, slot strides
     struct RbCfg {
         size_t smem = 0;
         int grid = 0;
-        RbShape shape{0, 0};
+        RbShape shape{0, 0, 0};
     };
     RbCfg cfgApply, cfgGs[3], cfgRes;
     ADom adom[2][D_COUNT];
@@ -429,6 +429,7 @@ public:
                 dATotal = carve<int>(base, off, 2 * D_COUNT);
                 dErr = carve<unsigned>(base, off, 4);
                 dTimes = carve<double>(base, off, cap);
+                dAllTotal = carve<int>(base, off, 4);
                 if (pass == 0) {
                     cudaError_t e = cudaMalloc(&tab, off + 256);
                     if (e != cudaSuccess) { tab = nullptr; err = "device allocation of the batch tables failed"; return PHX_ERR_OOM; }
@@ -473,22 +474,120 @@ public:
         persistCtas = PERSIST_CTAS;
         if (const char* cap = std::getenv("PHX_PERSIST_CTAS")) persistCtas = std::max(1, std::min(persistCtas, std::atoi(cap)));
         if (n > 0) {
-            if (shp.maxSmem() > RB_SMEM_MAX) {
+            if (!shp.finish()) {
                 err = "the batch's widest grids need more shared memory than a CTA has";
                 return PHX_ERR_UNSUPPORTED;
             }
-            PHX_TRY(configRB(cfgApply, k_cg_apply_rb<R>, shp.apply, shp.smemApply()));
-            PHX_TRY(configRB(cfgGs[GS_PRE], k_gs_rb<R, GS_PRE>, shp.gs[GS_PRE], shp.smemGs(GS_PRE)));
-            PHX_TRY(configRB(cfgGs[GS_BLACK], k_gs_rb<R, GS_BLACK>, shp.gs[GS_BLACK], shp.smemGs(GS_BLACK)));
-            PHX_TRY(configRB(cfgGs[GS_RED], k_gs_rb<R, GS_RED>, shp.gs[GS_RED], shp.smemGs(GS_RED)));
-            PHX_TRY(configRB(cfgRes, k_res_rb<R>, shp.res, shp.smemRes()));
         }
         PHX_CK(cudaMemcpyAsync(dDomStart, starts.data(), starts.size() * sizeof(int), cudaMemcpyHostToDevice, st));
         PHX_CK(cudaMemcpyAsync(dTiles, tilesAll.data(), tilesAll.size() * sizeof(int), cudaMemcpyHostToDevice, st));
         if (n > 0) PHX_CK(cudaMemcpyAsync(dD, dd.data(), 2 * n * sizeof(R*), cudaMemcpyHostToDevice, st));
         tablesDirty = false;
         for (int s = 0; s < n; ++s) PHX_TRY(pushDescriptor(s, false));
+        const int allTotal = dom[D_RB].total;
+        PHX_CK(cudaMemcpyAsync(dAllTotal, &allTotal, sizeof(int), cudaMemcpyHostToDevice, st));
         PHX_CK(cudaStreamSynchronize(st));
+        if (n > 0) PHX_TRY(tuneRowBlocks(shp));
+        return PHX_OK;
+    }
+
+    // ---- launch shapes of the row-block kernels -----------------------------------------
+    // The slot count of each kernel's staging ring (and with it how many CTAs
+    // share an SM) is tuned on the batch itself: every candidate that fits an
+    // SM's shared memory is timed on all tiles of the batch (the kernels only
+    // write scratch that the next projection recomputes), and the fastest is
+    // kept, cached per kernel and slot shape. The results do not depend on the
+    // choice. PHX_NO_AUTOTUNE=1 takes the first candidate that fits two CTAs
+    // per SM instead.
+    std::map<std::string, int> tuneCache;
+    int tuneRowBlocks(const RbShapes<R>& shp) {
+        const Scn<R>* S = dS;
+        const ADom all{dom[D_RB].start, dAllTotal, nscn()};
+        PHX_TRY(tuneRB("apply", cfgApply, k_cg_apply_rb<R>, shp.apply, 0, ApplyLayout<R>::MIN_ST,
+                       [&](const RbShape& sh, size_t smem, int grid) {
+                           k_cg_apply_rb<R><<<grid, RB_THREADS, smem, st>>>(S, all, (R* const*)dD, sh);
+                       }));
+        PHX_TRY(tuneRB("gs_pre", cfgGs[GS_PRE], k_gs_rb<R, GS_PRE>, shp.gs[GS_PRE], 0, GsLayout<R, GS_PRE>::MIN_ST,
+                       [&](const RbShape& sh, size_t smem, int grid) {
+                           k_gs_rb<R, GS_PRE><<<grid, RB_THREADS, smem, st>>>(S, all, sh, 2);
+                       }));
+        PHX_TRY(tuneRB("gs_black", cfgGs[GS_BLACK], k_gs_rb<R, GS_BLACK>, shp.gs[GS_BLACK], 0,
+                       GsLayout<R, GS_BLACK>::MIN_ST, [&](const RbShape& sh, size_t smem, int grid) {
+                           k_gs_rb<R, GS_BLACK><<<grid, RB_THREADS, smem, st>>>(S, all, sh, 2);
+                       }));
+        PHX_TRY(tuneRB("gs_red", cfgGs[GS_RED], k_gs_rb<R, GS_RED>, shp.gs[GS_RED], 0, GsLayout<R, GS_RED>::MIN_ST,
+                       [&](const RbShape& sh, size_t smem, int grid) {
+                           k_gs_rb<R, GS_RED><<<grid, RB_THREADS, smem, st>>>(S, all, sh, 2);
+                       }));
+        PHX_TRY(tuneRB("res", cfgRes, k_res_rb<R>, shp.res, shp.resTail, ResLayout<R>::MIN_ST,
+                       [&](const RbShape& sh, size_t smem, int grid) {
+                           k_res_rb<R><<<grid, RB_THREADS, smem, st>>>(S, all, sh);
+                       }));
+        return PHX_OK;
+    }
+
+    template <class K, class Launch>
+    int tuneRB(const char* name, RbCfg& c, K kern, RbShape shape, int tail, int minSt, Launch launchFn) {
+        int dev = 0, sms = 0;
+        PHX_CK(cudaGetDevice(&dev));
+        PHX_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        const size_t maxSmem = RB_SM_SMEM - RB_STATIC_SMEM;
+        PHX_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)maxSmem));
+        std::vector<int> cands;
+        for (int k = minSt; k <= RB_MAX_ST; ++k) {
+            RbShape sh = shape;
+            sh.st = k;
+            if (rbSmem(sh, tail) <= maxSmem) cands.push_back(k);
+        }
+        if (cands.empty()) {
+            err = std::string("the batch's widest grids need more shared memory than an SM has (") + name + ")";
+            return PHX_ERR_UNSUPPORTED;
+        }
+        auto gridFor = [&](size_t smem, int* grid) -> int {
+            int occ = 0;
+            PHX_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, RB_THREADS, smem));
+            *grid = std::min(sms * std::max(occ, 1), persistCtas);
+            return PHX_OK;
+        };
+        // default: the deepest ring that still lets two CTAs share an SM, else one more slot than the minimum
+        int best = cands.front() + (cands.size() > 1 ? 1 : 0);
+        for (int k : cands) {
+            RbShape sh = shape;
+            sh.st = k;
+            if (rbSmem(sh, tail) <= RB_SM_SMEM / 2 - RB_STATIC_SMEM) best = k;
+        }
+        const std::string key = std::string(name) + ":" + std::to_string(shape.slot) + ":" + std::to_string(shape.ring) +
+                                ":" + std::to_string(tail);
+        auto hit = tuneCache.find(key);
+        if (hit != tuneCache.end()) {
+            best = hit->second;
+        } else if (std::getenv("PHX_NO_AUTOTUNE") == nullptr && dom[D_RB].total > 0 && cands.size() > 1) {
+            float bestMs = 1e30f;
+            for (int k : cands) {
+                RbShape sh = shape;
+                sh.st = k;
+                const size_t smem = rbSmem(sh, tail);
+                int grid = 0;
+                PHX_TRY(gridFor(smem, &grid));
+                grid = std::min(grid, dom[D_RB].total);
+                launchFn(sh, smem, grid);
+                PHX_CK(cudaEventRecord(ev[2], st));
+                launchFn(sh, smem, grid);
+                launchFn(sh, smem, grid);
+                PHX_CK(cudaEventRecord(ev[3], st));
+                PHX_CK(cudaEventSynchronize(ev[3]));
+                float ms = 0;
+                PHX_CK(cudaEventElapsedTime(&ms, ev[2], ev[3]));
+                if (ms < bestMs) { bestMs = ms; best = k; }
+            }
+            PHX_TRY(checkLaunch());
+            PHX_TRY(checkDeviceError());
+            tuneCache[key] = best;
+        }
+        shape.st = best;
+        c.shape = shape;
+        c.smem = rbSmem(shape, tail);
+        PHX_TRY(gridFor(c.smem, &c.grid));
         return PHX_OK;
     }
 
@@ -605,20 +704,6 @@ public:
             kern<<<grid, threads, 0, st>>>(args...);
         }
         ++launches;
-    }
-
-    // shared memory and persistent grid of a row-block kernel for the batch
-    template <class K>
-    int configRB(RbCfg& c, K kern, const RbShape& shape, size_t smem) {
-        int dev = 0, sms = 0, occ = 0;
-        PHX_CK(cudaGetDevice(&dev));
-        PHX_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        PHX_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        PHX_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, RB_THREADS, smem));
-        c.smem = smem;
-        c.shape = shape;
-        c.grid = std::min(sms * std::max(occ, 1), persistCtas);
-        return PHX_OK;
     }
 
     // persistent grid over the active row-block tiles, with the staging ring in dynamic shared memory

@@ -116,7 +116,9 @@ __device__ __forceinline__ int stageMod(int k, int planeMod, int rowTerm, int ep
 struct RbShape {
     int slot;                    // bytes per plane slot
     int ring;                    // bytes per plane of the consumers' ring
+    int st;                      // slots of the staging ring (chosen per launch from the shared-memory budget)
 };
+constexpr int RB_MAX_ST = 8;
 
 // ---- warp-specialised pipeline -------------------------------------------------
 // A CTA of a row-block kernel is RB_CONSUMERS consumer warps plus one producer
@@ -214,9 +216,9 @@ __device__ __forceinline__ RbTile rbTile(const Scn<R>& g, int tile, int halo = 1
 
 // Producer warp: stage the planes of every tile of the CTA. Lane q holds
 // descriptor q of the current tile (desc returns false for unused lanes).
-template <class R, int ST, class DescFn>
-__device__ void rbProducer(const Scn<R>* __restrict__ S, const int* sst, int nscn, char* sm, int slotStride, int halo,
-                           uint64_t* full, uint64_t* empty, volatile int* abortFlag, DescFn desc) {
+template <class R, class DescFn>
+__device__ void rbProducer(const Scn<R>* __restrict__ S, const int* sst, int nscn, char* sm, int slotStride, int ST,
+                           int halo, uint64_t* full, uint64_t* empty, volatile int* abortFlag, DescFn desc) {
     const int lane = threadIdx.x & 31;
     const int tot = sst[nscn];
     unsigned seq = 0;
@@ -271,13 +273,13 @@ drain:
 
 // Consumer side of the slot ring for one tile: planes are waited in order and
 // released in order (one arrival per consumer warp).
-template <int ST>
 struct RbPipe {
     uint64_t* full;
     uint64_t* empty;
     volatile int* abortFlag;
     unsigned seq;                // planes of the CTA's earlier tiles
     int nPl, waited, released;
+    unsigned ST;                 // slots of the ring
     // wait for planes [waited, idx] (idx clipped to the tile's planes)
     __device__ __forceinline__ void waitThrough(int idx, unsigned* errWord) {
         idx = min(idx, nPl - 1);
@@ -302,9 +304,9 @@ struct RbPipe {
 };
 
 // common prologue of a row-block kernel: the active prefix and the barriers
-#define PHX_RB_PROLOGUE(ST)                                                   \
+#define PHX_RB_PROLOGUE()                                                     \
     extern __shared__ __align__(128) unsigned char smraw[];                   \
-    __shared__ uint64_t full[ST], empty[ST];                                  \
+    __shared__ uint64_t full[RB_MAX_ST], empty[RB_MAX_ST];                    \
     __shared__ int sst_[MAX_BATCH + 1];                                       \
     __shared__ volatile int abortFlag;                                        \
     __shared__ int amLast;                                                    \
@@ -312,7 +314,7 @@ struct RbPipe {
     for (int i_ = threadIdx.x; i_ <= dom.nscn; i_ += blockDim.x)              \
         sst_[i_] = dom.start[i_];                                             \
     if (threadIdx.x == 0) {                                                   \
-        for (int q_ = 0; q_ < ST; ++q_) {                                     \
+        for (int q_ = 0; q_ < RB_MAX_ST; ++q_) {                              \
             mbarInit(&full[q_], 1);                                           \
             mbarInit(&empty[q_], RB_CONSUMERS);                               \
         }                                                                     \
@@ -337,7 +339,7 @@ __device__ __forceinline__ int divBy(int e, int nx, unsigned magic) { return nx 
 // Slot layout: {z, d_prev, diag, a0z, a0x, a0y}; z and d over rows j0-1 .. j1.
 template <class R>
 struct ApplyLayout {
-    static constexpr int ST = 3;
+    static constexpr int MIN_ST = 3;
     int bz, bc, bx, by, slot, ring;
     __host__ __device__ ApplyLayout(int nx, int tj) {
         bz = stageBytes(tj + 2, nx, sizeof(R));
@@ -349,10 +351,9 @@ struct ApplyLayout {
     }
 };
 
-template <class R>
-inline size_t rbApplySmem(const RbShape& sh) {
-    return (size_t)ApplyLayout<R>::ST * sh.slot + 4 * (size_t)sh.ring;
-}
+// dynamic shared memory of a row-block launch: the staging ring, the
+// consumers' 4-plane ring and a kernel's own tail
+inline size_t rbSmem(const RbShape& sh, int tail = 0) { return (size_t)sh.st * sh.slot + 4 * (size_t)sh.ring + (size_t)tail; }
 
 enum { SA_Z = 0, SA_D, SA_DIAG, SA_AZ, SA_AX, SA_AY, SA_COUNT };
 
@@ -362,12 +363,12 @@ __global__ void __launch_bounds__(RB_THREADS, 2) k_cg_apply_rb(const Scn<R>* __r
     using T = R;
     using Acc = decltype(dotTerm(T(0), T(0)));
     using LY = ApplyLayout<R>;
-    constexpr int ST = LY::ST;
+    const int ST = shape.st;
     constexpr int EPV = 16 / (int)sizeof(R);
     constexpr int ES = (int)sizeof(R);
-    PHX_RB_PROLOGUE(ST)
+    PHX_RB_PROLOGUE()
     if (warp == RB_CONSUMERS) {
-        rbProducer<R, ST>(S, sst_, dom.nscn, sm, shape.slot, 1, full, empty, &abortFlag,
+        rbProducer<R>(S, sst_, dom.nscn, sm, shape.slot, ST, 1, full, empty, &abortFlag,
                           [&](int ln, int s, const Scn<R>& g, const RbTile& t, StageDesc& d) {
                               const LY L(t.nx, g.tj);
                               const int it = (int)g.sv[SV_IT];
@@ -418,7 +419,7 @@ __global__ void __launch_bounds__(RB_THREADS, 2) k_cg_apply_rb(const Scn<R>* __r
         const int mY = (int)(((long long)nx * (ny + 1)) & (EPV - 1));
         const int rC = (j0 * nx) & (EPV - 1), rCm = ((j0 - 1) * nx) & (EPV - 1);
         const int rX = (j0 * (nx + 1)) & (EPV - 1), rY = rC;
-        RbPipe<ST> pipe{full, empty, &abortFlag, seq, t.nPl, 0, 0};
+        RbPipe pipe{full, empty, &abortFlag, seq, t.nPl, 0, 0, (unsigned)ST};
         Acc dot{};
         for (int kk = t.k0; kk < t.k1; ++kk) {
             const int ic = kk - kLo;
@@ -509,7 +510,7 @@ enum { GS_PRE = 0, GS_BLACK = 1, GS_RED = 2 };
 
 template <class R, int MODE>
 struct GsLayout {
-    static constexpr int ST = MODE == GS_RED ? 4 : 3;
+    static constexpr int MIN_ST = MODE == GS_RED ? 4 : 3;
     static constexpr int ES = (int)sizeof(R);
     int oZ, oAG, oR, oDG, oAZ, oAX, oAY, slot, ring;
     __host__ __device__ GsLayout(int nx, int tj) {
@@ -527,24 +528,27 @@ struct GsLayout {
     }
 };
 
-template <class R, int MODE>
-inline size_t rbGsSmem(const RbShape& sh) {
-    return (size_t)GsLayout<R, MODE>::ST * sh.slot + 4 * (size_t)sh.ring;
-}
 
 enum { SG_Z = 0, SG_AG, SG_R, SG_DG, SG_AZ, SG_AX, SG_AY, SG_COUNT };
+
+// the sweeps' division by the diagonal: IEEE on the FP64 path (the
+// reference's operation), the fast reciprocal-based division on the FP32
+// path (a preconditioner; diagonals are far from the range where it loses
+// accuracy)
+__device__ __forceinline__ double gsDiv(double a, double b) { return a / b; }
+__device__ __forceinline__ float gsDiv(float a, float b) { return __fdividef(a, b); }
 
 template <class R, int MODE>
 __global__ void __launch_bounds__(RB_THREADS, 2) k_gs_rb(const Scn<R>* __restrict__ S, ADom dom, RbShape shape, int phase) {
     using T = R;
     using Acc = decltype(dotTerm(T(0), T(0)));
     using LY = GsLayout<R, MODE>;
-    constexpr int ST = LY::ST;
+    const int ST = shape.st;
     constexpr int EPV = 16 / (int)sizeof(R);
     constexpr int ES = (int)sizeof(R);
-    PHX_RB_PROLOGUE(ST)
+    PHX_RB_PROLOGUE()
     if (warp == RB_CONSUMERS) {
-        rbProducer<R, ST>(S, sst_, dom.nscn, sm, shape.slot, 1, full, empty, &abortFlag,
+        rbProducer<R>(S, sst_, dom.nscn, sm, shape.slot, ST, 1, full, empty, &abortFlag,
                           [&](int ln, int, const Scn<R>& g, const RbTile& t, StageDesc& d) {
                               const LY L(t.nx, g.tj);
                               const int nx = t.nx, ny = t.ny, j0 = t.j0, tj = g.tj;
@@ -592,58 +596,65 @@ __global__ void __launch_bounds__(RB_THREADS, 2) k_gs_rb(const Scn<R>* __restric
         const int mY = (int)(((long long)nx * (ny + 1)) & (EPV - 1)), mC4 = (int)(t.sxy & 3);
         const int rC = (j0 * nx) & (EPV - 1), rCm = ((j0 - 1) * nx) & (EPV - 1), rCm4 = ((j0 - 1) * nx) & 3;
         const int rX = (j0 * (nx + 1)) & (EPV - 1), rY = rC;
+        const int hx = (nx + 1) >> 1;                       // pairs of cells per row
+        const unsigned magicHx = divMagic(hx);
         const int rH = MODE == GS_PRE ? rCm : rC;           // residue of the first row of r and diag
         const int hOff = MODE == GS_PRE ? nx : 0;           // row j0 within the r and diag arrays
-        RbPipe<ST> pipe{full, empty, &abortFlag, seq, t.nPl, 0, 0};
+        RbPipe pipe{full, empty, &abortFlag, seq, t.nPl, 0, 0, (unsigned)ST};
         Acc dot{};
         for (int kk = t.k0; kk < t.k1; ++kk) {
             const int ic = kk - kLo;
             pipe.waitThrough(ic + 1, g.errWord);
             if constexpr (MODE != GS_RED) {
-                // red values of the planes entering the ring (rows j0-1 .. j1)
+                // red values of the planes entering the ring (rows j0-1 .. j1), one
+                // per pair of cells (2m, 2m+1) of a row
                 if (!abortFlag) {
                     for (int k = kk == t.k0 ? kLo : kk + 1; k <= min(kk + 1, kHi); ++k) {
                         const char* base = sm + (size_t)pipe.slotOf(k - kLo) * shape.slot;
-                        const int n = (ringRe - ringRa) * nx;
+                        const int np = (ringRe - ringRa) * hx;
                         const int row0 = (ringRa - (j0 - 1)) * nx;   // ring index of row ringRa
                         R* out = reinterpret_cast<R*>(ringB + (size_t)(k & 3) * shape.ring) + row0;
                         if constexpr (MODE == GS_PRE) {
                             const int o = stageMod(k, mC, rCm, EPV) + row0;
                             const R* rs = reinterpret_cast<const R*>(base + L.oR) + o;
                             const R* ds = reinterpret_cast<const R*>(base + L.oDG) + o;
-                            for (int e = threadIdx.x; e < n; e += RB_CTHREADS) {
-                                const int jj = divBy(e, nx, magic), i = e - jj * nx;
-                                if (((i + ringRa + jj + k) & 1) != 0) continue;
+                            for (int p = threadIdx.x; p < np; p += RB_CTHREADS) {
+                                const int jr = divBy(p, hx, magicHx), m = p - jr * hx;
+                                const int i = 2 * m + ((ringRa + jr + k) & 1);
+                                if (i >= nx) continue;
+                                const int e = jr * nx + i;
                                 const T dg = ds[e];
-                                out[e] = dg <= 0 ? T(0) : (T)(rs[e] / dg);
+                                out[e] = dg <= 0 ? T(0) : gsDiv(rs[e], dg);
                             }
                         } else {
                             const R* zs = reinterpret_cast<const R*>(base + L.oZ) + stageMod(k, mC, rCm, EPV) + row0;
                             const int* as = reinterpret_cast<const int*>(base + L.oAG) + stageMod(k, mC4, rCm4, 4) + row0;
-                            // four cells per thread at a time, so that their gathers of
+                            // four pairs per thread at a time, so that their gathers of
                             // the coarse correction are in flight together
-                            for (int e0 = threadIdx.x; e0 < n; e0 += 4 * RB_CTHREADS) {
+                            for (int p0 = threadIdx.x; p0 < np; p0 += 4 * RB_CTHREADS) {
                                 T v[4], xv[4];
-                                int a[4];
-                                bool red[4];
+                                int a[4], ee[4];
 #pragma unroll
                                 for (int u = 0; u < 4; ++u) {
-                                    const int e = e0 + u * RB_CTHREADS;
-                                    red[u] = false;
+                                    const int p = p0 + u * RB_CTHREADS;
+                                    ee[u] = -1;
                                     a[u] = -1;
                                     v[u] = T(0);
-                                    if (e < n) {
-                                        const int jj = divBy(e, nx, magic), i = e - jj * nx;
-                                        red[u] = ((i + ringRa + jj + k) & 1) == 0;
-                                        v[u] = zs[e];
-                                        a[u] = as[e];
+                                    if (p < np) {
+                                        const int jr = divBy(p, hx, magicHx), m = p - jr * hx;
+                                        const int i = 2 * m + ((ringRa + jr + k) & 1);
+                                        if (i < nx) {
+                                            ee[u] = jr * nx + i;
+                                            v[u] = zs[ee[u]];
+                                            a[u] = as[ee[u]];
+                                        }
                                     }
                                 }
 #pragma unroll
-                                for (int u = 0; u < 4; ++u) xv[u] = (red[u] && a[u] >= 0) ? (T)xc[a[u]] : T(0);
+                                for (int u = 0; u < 4; ++u) xv[u] = a[u] >= 0 ? (T)xc[a[u]] : T(0);
 #pragma unroll
                                 for (int u = 0; u < 4; ++u)
-                                    if (red[u]) out[e0 + u * RB_CTHREADS] = a[u] >= 0 ? (T)(v[u] + xv[u]) : v[u];
+                                    if (ee[u] >= 0) out[ee[u]] = a[u] >= 0 ? (T)(v[u] + xv[u]) : v[u];
                             }
                         }
                     }
@@ -676,33 +687,36 @@ __global__ void __launch_bounds__(RB_THREADS, 2) k_gs_rb(const Scn<R>* __restric
                 const bool hasM = kk > 0, hasP = kk < nz - 1;
                 // the colour this sweep updates: black (odd) for GS_PRE and GS_BLACK, red for GS_RED
                 const int upd = MODE == GS_RED ? 0 : 1;
-                for (int e = threadIdx.x; e < ncell; e += RB_CTHREADS) {
-                    const int jj = divBy(e, nx, magic);
-                    const int i = e - jj * nx, j = j0 + jj;
-                    const bool mine = ((i + j + kk) & 1) == upd;
-                    T zc;
-                    if (mine) {
+                const int np = (t.j1 - j0) * hx;
+                // one pair of cells (2m, 2m+1) of a row per thread: one is updated,
+                // the other (GS_PRE: its red value; GS_RED: its r.z term) is passed on
+                for (int p = threadIdx.x; p < np; p += RB_CTHREADS) {
+                    const int jj = divBy(p, hx, magicHx), m = p - jj * hx;
+                    const int j = j0 + jj;
+                    const int iu = 2 * m + ((j + kk + upd) & 1), io = 4 * m + 1 - iu;
+                    if (iu < nx) {
+                        const int e = jj * nx + iu;
                         const T dg = dgp[e];
-                        if (dg <= 0) zc = 0;
-                        else {
+                        T zc = 0;
+                        if (dg > 0) {
                             const R* ax = axp + e + jj;   // a0x index jj * (nx + 1) + i
                             T sacc = rp[e];
-                            if (i > 0) sacc += ax[0] * X0[e - 1];
-                            if (i < nx - 1) sacc += ax[1] * X0[e + 1];
+                            if (iu > 0) sacc += ax[0] * X0[e - 1];
+                            if (iu < nx - 1) sacc += ax[1] * X0[e + 1];
                             if (j > 0) sacc += ayp[e] * X0[e - nx];
                             if (j < ny - 1) sacc += ayp[e + nx] * X0[e + nx];
                             if (hasM) sacc += azp[e] * Xm[e];
                             if (hasP) sacc += azn[e] * Xp[e];
-                            zc = sacc / dg;
+                            zc = gsDiv(sacc, dg);
                         }
                         zp[e] = zc;
-                    } else if constexpr (MODE == GS_PRE) {
-                        zc = X0[e];               // the red value of the ring
-                        zp[e] = zc;
-                    } else {
-                        zc = X0[e];               // GS_RED: the black value as staged
+                        if constexpr (MODE == GS_RED) dot = accAdd(dot, dotTerm((T)rp[e], zc));
                     }
-                    if constexpr (MODE == GS_RED) dot = accAdd(dot, dotTerm((T)rp[e], zc));
+                    if (io < nx) {
+                        const int e = jj * nx + io;
+                        if constexpr (MODE == GS_PRE) zp[e] = X0[e];                       // the red value of the ring
+                        if constexpr (MODE == GS_RED) dot = accAdd(dot, dotTerm((T)rp[e], (T)X0[e]));   // staged black
+                    }
                 }
             }
             pipe.releaseThrough(MODE == GS_RED ? ic - 1 : ic);
@@ -733,7 +747,7 @@ namespace phx {
 // block; tiles start on even rows and even planes).
 template <class R>
 struct ResLayout {
-    static constexpr int ST = 3;
+    static constexpr int MIN_ST = 3;
     static constexpr int ES = (int)sizeof(R);
     int oZ, oAG, oR, oDG, oAZ, oAX, oAY, slot, ring, oRA, oRB, oGA, bytes;
     __host__ __device__ ResLayout(int nx, int tj) {
@@ -755,21 +769,17 @@ struct ResLayout {
     }
 };
 
-template <class R>
-inline size_t rbResSmem(const RbShape& sh, int tail) {
-    return (size_t)ResLayout<R>::ST * sh.slot + 4 * (size_t)sh.ring + (size_t)tail;
-}
 
 template <class R>
 __global__ void __launch_bounds__(RB_THREADS, 1) k_res_rb(const Scn<R>* __restrict__ S, ADom dom, RbShape shape) {
     using T = R;
     using LY = ResLayout<R>;
-    constexpr int ST = LY::ST;
+    const int ST = shape.st;
     constexpr int EPV = 16 / (int)sizeof(R);
     constexpr int ES = (int)sizeof(R);
-    PHX_RB_PROLOGUE(ST)
+    PHX_RB_PROLOGUE()
     if (warp == RB_CONSUMERS) {
-        rbProducer<R, ST>(S, sst_, dom.nscn, sm, shape.slot, 1, full, empty, &abortFlag,
+        rbProducer<R>(S, sst_, dom.nscn, sm, shape.slot, ST, 1, full, empty, &abortFlag,
                           [&](int ln, int, const Scn<R>& g, const RbTile& t, StageDesc& d) {
                               const LY L(t.nx, g.tj);
                               const int nx = t.nx, ny = t.ny, j0 = t.j0, tj = g.tj;
@@ -815,7 +825,7 @@ __global__ void __launch_bounds__(RB_THREADS, 1) k_res_rb(const Scn<R>* __restri
         int* const GA = reinterpret_cast<int*>(tail + L.oGA);
         const int hx = (nx + 1) >> 1, hy = (rows + 1) >> 1, nblk = hx * hy;
         const unsigned magicHx = divMagic(hx);
-        RbPipe<ST> pipe{full, empty, &abortFlag, seq, t.nPl, 0, 0};
+        RbPipe pipe{full, empty, &abortFlag, seq, t.nPl, 0, 0, (unsigned)ST};
         for (int kk = t.k0; kk < t.k1; ++kk) {
             const int ic = kk - kLo;
             pipe.waitThrough(ic + 1, g.errWord);
@@ -920,10 +930,16 @@ __global__ void __launch_bounds__(RB_THREADS, 1) k_res_rb(const Scn<R>* __restri
 namespace phx {
 
 // host side: the shared-memory shapes of the row-block kernels over a batch
-// (the largest slot and ring of its grids)
+// (the largest slot and ring of its grids), and the number of staging slots
+// of each kernel. The slot count is chosen from the shared memory of an SM:
+// for one or two CTAs per SM, as many slots as fit (up to RB_MAX_ST), keeping
+// the configuration with the most bytes in flight per SM (slots beyond the
+// ones the stencil holds resident, times CTAs per SM).
+constexpr size_t RB_SM_SMEM = 228 * 1024;      // shared memory of a GB300 SM
+constexpr size_t RB_STATIC_SMEM = 6 * 1024;    // the kernels' static shared memory, rounded up
 template <class R>
 struct RbShapes {
-    RbShape apply{0, 0}, gs[3] = {RbShape{0, 0}, RbShape{0, 0}, RbShape{0, 0}}, res{0, 0};
+    RbShape apply{0, 0, 0}, gs[3] = {RbShape{0, 0, 0}, RbShape{0, 0, 0}, RbShape{0, 0, 0}}, res{0, 0, 0};
     int resTail = 0;
     static void grow(RbShape& a, int slot, int ring) {
         a.slot = a.slot > slot ? a.slot : slot;
@@ -943,17 +959,34 @@ struct RbShapes {
         grow(res, rl.slot, rl.ring);
         resTail = resTail > rl.bytes ? resTail : rl.bytes;
     }
-    size_t smemRes() const { return rbResSmem<R>(res, resTail); }
-    size_t smemApply() const { return rbApplySmem<R>(apply); }
-    size_t smemGs(int m) const {
-        return m == GS_PRE ? rbGsSmem<R, GS_PRE>(gs[0]) : m == GS_BLACK ? rbGsSmem<R, GS_BLACK>(gs[1])
-                                                                        : rbGsSmem<R, GS_RED>(gs[2]);
+    // slots for one kernel (0 if even one CTA per SM cannot hold minSt slots)
+    static int pickSlots(const RbShape& sh, int tail, int minSt) {
+        int best = 0;
+        size_t bestFlight = 0;
+        for (int ctas = 2; ctas >= 1; --ctas) {
+            const size_t per = RB_SM_SMEM / ctas - RB_STATIC_SMEM;
+            const size_t fixed = 4 * (size_t)sh.ring + (size_t)tail;
+            if (sh.slot <= 0 || per <= fixed) continue;
+            int st = (int)((per - fixed) / (size_t)sh.slot);
+            if (st > RB_MAX_ST) st = RB_MAX_ST;
+            if (st < minSt) continue;
+            const size_t flight = (size_t)ctas * (size_t)(st - minSt + 1) * (size_t)sh.slot;
+            if (flight > bestFlight) { bestFlight = flight; best = st; }
+        }
+        return best;
     }
-    size_t maxSmem() const {
-        size_t m = smemApply();
-        for (int i = 0; i < 3; ++i) m = m > smemGs(i) ? m : smemGs(i);
-        return m > smemRes() ? m : smemRes();
+    // fills the slot counts; false if a kernel does not fit
+    bool finish() {
+        apply.st = pickSlots(apply, 0, ApplyLayout<R>::MIN_ST);
+        gs[0].st = pickSlots(gs[0], 0, GsLayout<R, GS_PRE>::MIN_ST);
+        gs[1].st = pickSlots(gs[1], 0, GsLayout<R, GS_BLACK>::MIN_ST);
+        gs[2].st = pickSlots(gs[2], 0, GsLayout<R, GS_RED>::MIN_ST);
+        res.st = pickSlots(res, resTail, ResLayout<R>::MIN_ST);
+        return apply.st && gs[0].st && gs[1].st && gs[2].st && res.st;
     }
+    size_t smemApply() const { return rbSmem(apply); }
+    size_t smemGs(int m) const { return rbSmem(gs[m]); }
+    size_t smemRes() const { return rbSmem(res, resTail); }
 };
 
 }  // namespace phx
