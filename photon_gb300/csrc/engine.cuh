@@ -289,7 +289,7 @@ struct Scenario {
         t[D_CO_SERIAL] = Lc.dense.empty() ? 1 : 0;
         for (int l = 1; l < MAX_LEVELS; ++l) {
             t[D_LV0 + l] = (l < nl - 1) ? cdiv(MG.lv[l].n, TPB) : 0;
-            t[D_RS0 + l] = (l + 1 <= nl - 1) ? cdiv(MG.lv[l + 1].n, TPB) : 0;
+            t[D_RS0 + l] = (l + 1 <= nl - 1) ? cdiv(MG.lv[l + 1].n, TPB / RRJ_LANES) : 0;   // 8 lanes per unknown
         }
     }
 };
@@ -829,11 +829,12 @@ public:
         const Scn<R>* S = dS;
         launchRB("k_gs_pre", cfgGs[GS_PRE], k_gs_rb<R, GS_PRE>, S, adom[0][D_RB], cfgGs[GS_PRE].shape, phase);
         launchRB("k_res_restrict", cfgRes, k_res_rb<R>, S, adom[0][D_RB], cfgRes.shape);
+        // down: level 1's first Jacobi sweep; then per level its second sweep and
+        // its residual restricted to level l+1 with l+1's first sweep
+        launchA("k_jacobi", D_LV0 + 1, TPB, k_jacobi<R>, S, adom[0][D_LV0 + 1], 1, 0);
         for (int l = 1; l < maxLevels - 1; ++l) {
-            launchA("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, adom[0][D_LV0 + l], l, 0);
             launchA("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, adom[0][D_LV0 + l], l, 1);
-            launchA("k_residual", D_LV0 + l, TPB, k_residual<R>, S, adom[0][D_LV0 + l], l);
-            launchA("k_restrict", D_RS0 + l, TPB, k_restrict<R>, S, adom[0][D_RS0 + l], l);
+            launchA("k_res_restrict_jac0", D_RS0 + l, TPB, k_res_restrict_jac0<R>, S, adom[0][D_RS0 + l], l);
         }
         launchA("k_coarse_dense", D_CO_DENSE, TPB, k_coarse_dense<R>, S, adom[0][D_CO_DENSE]);
         launchA("k_coarse_serial", D_CO_SERIAL, 32, k_coarse_serial<R>, S, adom[0][D_CO_SERIAL]);

@@ -112,6 +112,58 @@ __global__ void k_restrict(const Scn<R>* __restrict__ S, ADom dom, int l) {
     PHX_TILES_END
 }
 
+// residual of level l fused with its restriction to level l+1 and the first
+// (from-zero) Jacobi sweep of level l+1 (pressure_mg.cpp:248-257, 285-286,
+// 237-247). Eight lanes serve one unknown J of level l+1: they compute the
+// residuals of J's children eight at a time (children in ascending order),
+// and the group's first lane sums them in that order -- the order of the
+// reference's scatter -- then sets y_J = omega b_J / diag_J unless level l+1
+// is the coarsest.
+constexpr int RRJ_LANES = 8;
+template <class R>
+__global__ void k_res_restrict_jac0(const Scn<R>* __restrict__ S, ADom dom, int l) {
+    using T = R;
+    PHX_TILES_BEGIN(dom)
+    const Level<R>& L = g.lv[l];
+    const Level<R>& C = g.lv[l + 1];
+    const int J = tile_ * (TPB / RRJ_LANES) + (threadIdx.x / RRJ_LANES);
+    const int c = threadIdx.x % RRJ_LANES;
+    const int groupLane0 = threadIdx.x & 31 & ~(RRJ_LANES - 1);
+    int nch = 0, e0 = 0;
+    if (J < C.n) {
+        e0 = L.childStart[J];
+        nch = L.childStart[J + 1] - e0;
+    }
+    const int chunks = __reduce_max_sync(0xffffffffu, (nch + RRJ_LANES - 1) / RRJ_LANES);
+    T acc = 0;
+    for (int ch = 0; ch < chunks; ++ch) {
+        const int idx = ch * RRJ_LANES + c;
+        T r = 0;
+        if (idx < nch) {
+            const int I = L.child[e0 + idx];
+            const T dg = L.diag[I];
+            if (dg > 0) {
+                T s = L.b[I] - dg * L.x[I];
+                for (int q = L.rowStart[I]; q < L.rowStart[I + 1]; ++q) s += L.val[q] * L.x[L.col[q]];
+                r = s;
+            }
+        }
+        for (int q = 0; q < RRJ_LANES; ++q) {
+            const T rq = __shfl_sync(0xffffffffu, r, groupLane0 + q);
+            if (ch * RRJ_LANES + q < nch) acc = acc + rq;
+        }
+    }
+    if (J < C.n && c == 0) {
+        C.b[J] = acc;
+        if (l + 1 < g.nLevels - 1) {
+            const T dc = C.diag[J];
+            const T om = T(OMEGA);
+            C.y[J] = dc <= 0 ? T(0) : (T(1) - om) * T(0) + om * acc / dc;
+        }
+    }
+    PHX_TILES_END
+}
+
 // coarsest level: x = M b with the dense operator of the reference's 20
 // forward + backward Gauss-Seidel sweeps (pressure_mg.cpp:258-266, 279).
 // One warp per row.
