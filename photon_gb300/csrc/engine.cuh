@@ -748,10 +748,16 @@ public:
         t.nscn = nscn();
         t.cap = cap;
         t.ndom = D_COUNT;
+        // the domains of the solve's persistent kernels (kind 0: solving, kind 1: replacing)
+        int n = 0;
+        auto add = [&](int kind, int d) { if (n < 32) t.list[n++] = (short)(kind * D_COUNT + d); };
+        add(0, D_CELLS); add(0, D_CZ); add(0, D_RB); add(0, D_CO_DENSE); add(0, D_CO_SERIAL);
+        for (int l = 1; l < maxLevels - 1 && l < MAX_LEVELS; ++l) { add(0, D_LV0 + l); add(0, D_RS0 + l); }
+        add(1, D_CELLS); add(1, D_CZ);
+        t.nlist = n;
         return t;
-    }
-    void rebuildActive() {
-        k_active<R><<<1, 128, 0, st>>>(dS, activeTables());
+    }    void rebuildActive() {
+        k_active<R><<<1, 256, 0, st>>>(dS, activeTables());
         ++launches;
     }
 
@@ -995,7 +1001,7 @@ public:
         else projectPrelude();
         cudaMemsetAsync(dLoop, 0, sizeof(int), st);
         const int capIt = maxItersAll() + 2;
-        k_cg_cond<R><<<1, 128, 0, st>>>(dS, n, cgHandle, dLoop, capIt, activeTables(), 1);
+        k_cg_cond<R><<<1, 256, 0, st>>>(dS, n, cgHandle, dLoop, capIt, activeTables(), 1);
         ++launches;
         cudaGraph_t body = nullptr;
         PHX_TRY(addWhile(graph, cgHandle, &body));
@@ -1009,7 +1015,7 @@ public:
         PHX_CK(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
         launches = 0;
         cgIteration();
-        k_cg_cond<R><<<1, 128, 0, st>>>(dS, n, cgHandle, dLoop, capIt, activeTables(), 1);
+        k_cg_cond<R><<<1, 256, 0, st>>>(dS, n, cgHandle, dLoop, capIt, activeTables(), 1);
         ++launches;
         PHX_CK(cudaStreamEndCapture(st, &body));
         bodyKernels = launches;

@@ -300,22 +300,43 @@ struct ActiveTables {
     int* astart;                 // [2][ndom][cap + 1]
     int* atotal;                 // [2][ndom]
     int nscn, cap, ndom;
+    int nlist;                   // the (kind, domain) prefixes the solve's persistent kernels use
+    short list[32];              // kind * ndom + domain
 };
 
+// One warp per listed (kind, domain): the scenarios' flags are read once into
+// shared memory, then each warp scans its domain's tile counts 32 scenarios at
+// a time (warp shuffles), so the rebuild costs a few microseconds for any batch.
+// Every thread of the block must call it.
 template <class R>
 __device__ void buildActive(const Scn<R>* __restrict__ S, const ActiveTables& t) {
-    for (int kd = threadIdx.x; kd < 2 * t.ndom; kd += blockDim.x) {
+    __shared__ unsigned char on[2][MAX_BATCH];
+    for (int s = threadIdx.x; s < t.nscn; s += blockDim.x) {
+        const double* sv = S[s].sv;
+        const bool solving = sv[SV_DONE] == 0;
+        on[0][s] = solving;
+        on[1][s] = solving && sv[SV_REPL] != 0;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int li = threadIdx.x >> 5; li < t.nlist; li += nw) {
+        const int kd = t.list[li];
         const int kind = kd / t.ndom, d = kd % t.ndom;
-        int* as = t.astart + (size_t)(kind * t.ndom + d) * (t.cap + 1);
-        int acc = 0;
-        as[0] = 0;
-        for (int s = 0; s < t.nscn; ++s) {
-            const double* sv = S[s].sv;
-            const bool on = sv[SV_DONE] == 0 && (kind == 0 || sv[SV_REPL] != 0);
-            acc += on ? t.tiles[(size_t)d * t.cap + s] : 0;
-            as[s + 1] = acc;
+        int* as = t.astart + (size_t)kd * (t.cap + 1);
+        const int* tl = t.tiles + (size_t)d * t.cap;
+        int base = 0;
+        if (lane == 0) as[0] = 0;
+        for (int s0 = 0; s0 < t.nscn; s0 += 32) {
+            const int s = s0 + lane;
+            int v = (s < t.nscn && on[kind][s]) ? tl[s] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int u = __shfl_up_sync(0xffffffffu, v, o);
+                if (lane >= o) v += u;
+            }
+            if (s < t.nscn) as[s + 1] = base + v;
+            base += __shfl_sync(0xffffffffu, v, 31);
         }
-        t.atotal[kind * t.ndom + d] = acc;
+        if (lane == 0) t.atotal[kd] = base;
     }
 }
 
