@@ -25,13 +25,16 @@ namespace phx {
 constexpr int RB_KZ = 16;          // planes per tile along z
 constexpr long long RB_WAIT_CYCLES = 2000000000LL;   // about one second at the GB300 clock
 
-// rows per tile for a grid of nx cells per row: about 1024 cells per plane of
-// a tile on the FP32 path and 512 on the FP64 path (twice the bytes), even
+// rows per tile for a grid of nx cells per row: about 768 cells per plane of
+// a tile on the FP32 path and 384 on the FP64 path (twice the bytes), even
 // (2x2x2 restriction blocks never straddle tiles), at least 2, at most ny
-// rounded up to even
+// rounded up to even. 768 is the measured best of 512 / 768 / 1024 on the
+// 64-scenario batch: the wider planes favour q = A d and the sweeps with a
+// ring, the narrower ones let the residual and the prolongated sweep (the
+// largest slots) run two CTAs per SM.
 template <class R>
 __host__ __device__ inline int rowBlockRows(int nx, int ny) {
-    const int cells = sizeof(R) == 8 ? 512 : 1024;
+    const int cells = sizeof(R) == 8 ? 384 : 768;
     int tj = (cells / (nx > 0 ? nx : 1)) & ~1;
     if (tj < 2) tj = 2;
     const int cap = ny + (ny & 1);
