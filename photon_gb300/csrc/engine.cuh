@@ -37,7 +37,7 @@ namespace phx {
 constexpr int DENSE_MAX = 4096;
 
 enum DomId {
-    D_ONE = 0, D_CELLS, D_FX, D_FY, D_FZ, D_BX, D_BY, D_BZ, D_CZ, D_CC, D_CO_DENSE, D_CO_SERIAL, D_RB,
+    D_ONE = 0, D_CELLS, D_FX, D_FY, D_FZ, D_BX, D_BY, D_BZ, D_CZ, D_CC, D_CO_DENSE, D_CO_SERIAL, D_RB, D_QUAD,
     D_LV0,                       // D_LV0 + l: rows of level l when l is not the coarsest (1 <= l < 12)
     D_RS0 = D_LV0 + MAX_LEVELS,  // D_RS0 + l: rows of level l+1 for restriction from level l >= 1
     D_COUNT = D_RS0 + MAX_LEVELS
@@ -227,6 +227,7 @@ struct Scenario {
         s.nClosed = (int)Z.closed.size();
         s.mixed = kMixed ? 1 : 0;
         s.replaceEvery = REPLACE_EVERY;
+        s.fp16Scratch = kMixed && std::getenv("PHX_FP16_SCRATCH") != nullptr;
         s.tj = rowBlockRows<R>(geo.nx, geo.ny);
         s.njb = (geo.ny + s.tj - 1) / s.tj;
         PHX_TRY(putRaw(st, s.blocked, geo.blocked.data(), N));
@@ -275,6 +276,7 @@ struct Scenario {
         t[D_ONE] = 1;
         t[D_CELLS] = cdiv(N, TPB);
         t[D_RB] = cdiv(ny, rowBlockRows<R>(nx, ny)) * cdiv(nz, RB_KZ);      // row blocks x plane blocks
+        t[D_QUAD] = cdiv(N, TPB * CG_QUAD);                                 // 4 cells per thread
         t[D_FX] = cdiv(geo.NX(), TPB);
         t[D_FY] = cdiv(geo.NY(), TPB);
         t[D_FZ] = cdiv(geo.NZ(), TPB);
@@ -751,7 +753,7 @@ public:
         // the domains of the solve's persistent kernels (kind 0: solving, kind 1: replacing)
         int n = 0;
         auto add = [&](int kind, int d) { if (n < 32) t.list[n++] = (short)(kind * D_COUNT + d); };
-        add(0, D_CELLS); add(0, D_CZ); add(0, D_RB); add(0, D_CO_DENSE); add(0, D_CO_SERIAL);
+        add(0, D_CELLS); add(0, D_CZ); add(0, D_RB); add(0, D_QUAD); add(0, D_CO_DENSE); add(0, D_CO_SERIAL);
         for (int l = 1; l < maxLevels - 1 && l < MAX_LEVELS; ++l) { add(0, D_LV0 + l); add(0, D_RS0 + l); }
         add(1, D_CELLS); add(1, D_CZ);
         t.nlist = n;
@@ -875,7 +877,7 @@ public:
     void cgIteration() {
         const Scn<R>* S = dS;
         launchRB("k_cg_apply", cfgApply, k_cg_apply_rb<R>, S, adom[0][D_RB], (R* const*)dD, cfgApply.shape);
-        launchA("k_cg_update", D_CELLS, TPB, k_cg_update<R>, S, adom[0][D_CELLS], (R* const*)dD, 0);
+        launchA("k_cg_update", D_QUAD, TPB, k_cg_update<R>, S, adom[0][D_QUAD], (R* const*)dD);
         if (kMixed) {
             launchA("k_mx_update", D_CELLS, TPB, k_mx_update<R>, S, adom[1][D_CELLS], 1);
             launchA("k_mx_res64", D_CELLS, TPB, k_mx_res64<R>, S, adom[1][D_CELLS], 1);

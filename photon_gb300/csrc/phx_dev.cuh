@@ -8,6 +8,7 @@
 // with CTA b of the launch mapped to (scenario, tile) by a prefix table.
 #pragma once
 #include <cstdint>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 namespace phx {
@@ -124,6 +125,7 @@ struct Scn {
     double* p64;                 // mixed path: FP64 pressure; the FP32 iterate p holds the part not yet folded in
     int mixed;                   // mixed path: FP32 CG with FP64 residual replacement
     int replaceEvery;            // mixed path: iterations between FP64 residual replacements
+    int fp16Scratch;             // mixed path: Jacobi scratch rounded to FP16 (an accuracy study; off by default)
     int nLevels;
     Level<R> lv[MAX_LEVELS];
     // row-block tiles of the level-0 pressure kernels: tj rows x RB_KZ planes, njb blocks along y

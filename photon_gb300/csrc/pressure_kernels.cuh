@@ -39,6 +39,16 @@ namespace phx {
 
 constexpr double OMEGA = 0.7;
 
+// the Jacobi sweeps' scratch value (y, between the two sweeps of a level),
+// rounded to FP16 when the context studies FP16 scratch storage
+template <class R>
+__device__ __forceinline__ R scratchRound(const Scn<R>& g, R v) {
+    if constexpr (sizeof(R) == 4) {
+        if (g.fp16Scratch) return __half2float(__float2half_rn(v));
+    }
+    return v;
+}
+
 // The solve kernels compute in the arithmetic type T = R of the path (FP64 or
 // FP32); dot products accumulate in Acc (double, or a double-float pair on
 // the FP32 path) and reach the per-scenario scalars as doubles.
@@ -59,7 +69,7 @@ __global__ void k_jacobi(const Scn<R>* __restrict__ S, ADom dom, int l, int mode
     const T om = T(OMEGA);
     if (mode == 0) {
         T s = L.b[I];
-        out[I] = (T(1) - om) * T(0) + om * s / dg;
+        out[I] = scratchRound(g, (T(1) - om) * T(0) + om * s / dg);
         break;
     }
     const R* in = mode == 1 ? L.y : L.x;
@@ -72,7 +82,8 @@ __global__ void k_jacobi(const Scn<R>* __restrict__ S, ADom dom, int l, int mode
     };
     T s = L.b[I];
     for (int q = L.rowStart[I]; q < L.rowStart[I + 1]; ++q) s += L.val[q] * X(L.col[q]);
-    out[I] = (T(1) - om) * X(I) + om * s / dg;
+    const T v = (T(1) - om) * X(I) + om * s / dg;
+    out[I] = mode == 1 ? v : scratchRound(g, v);
     PHX_TILES_END
 }
 
@@ -158,7 +169,7 @@ __global__ void k_res_restrict_jac0(const Scn<R>* __restrict__ S, ADom dom, int 
         if (l + 1 < g.nLevels - 1) {
             const T dc = C.diag[J];
             const T om = T(OMEGA);
-            C.y[J] = dc <= 0 ? T(0) : (T(1) - om) * T(0) + om * acc / dc;
+            C.y[J] = dc <= 0 ? T(0) : scratchRound(g, (T(1) - om) * T(0) + om * acc / dc);
         }
     }
     PHX_TILES_END
@@ -263,30 +274,62 @@ __device__ void closeCgIteration(const Scn<R>& g, int phase, double tot) {
     }
 }
 
-// p += alpha d; r -= alpha q (src/sim/gasphase.cpp:609-615), max|r| for the
-// stop test (:592-602), and the first red half sweep of the next V-cycle
-// (x = r / diag, the black cells being zero)
+// p += alpha d; r -= alpha q (src/sim/gasphase.cpp:609-615) and max|r| for
+// the stop test (:592-602). Four consecutive cells per thread (a tile is 1024
+// cells, so a thread's quad starts on a 16-byte boundary on the FP32 path and
+// is moved with vector loads and stores).
+constexpr int CG_QUAD = 4;
 template <class R>
-__global__ void k_cg_update(const Scn<R>* __restrict__ S, ADom dom, R* const* dbuf, int redSweep) {
+__device__ __forceinline__ void cgUpdateCell(R* p, R* r, const R* d, const R* q, const R* diag, R alpha, int c, R& rm) {
+    const R dg = diag[c];
+    R rv = r[c];
+    if (dg > 0) {
+        p[c] = p[c] + alpha * d[c];
+        rv = rv - alpha * q[c];
+        r[c] = rv;
+    }
+    rm = mx(rm, (R)fabs(rv));
+}
+
+template <class R>
+__global__ void k_cg_update(const Scn<R>* __restrict__ S, ADom dom, R* const* dbuf) {
     using T = R;
     PHX_TILES_BEGIN(dom)
-    const int c = tile_ * TPB + threadIdx.x;
+    const int c0 = (tile_ * TPB + threadIdx.x) * CG_QUAD;
     T rm = 0;
-    if (c < g.N) {
+    if (c0 < g.N) {
         const int it = (int)g.sv[SV_IT];
         const R* d = dbuf[2 * s_ + ((it + 1) & 1)];
         const T alpha = (T)g.sv[SV_ALPHA];
-        const T dg = g.diag[c];
-        T r = g.r[c];
-        if (dg > 0) {
-            g.p[c] = g.p[c] + alpha * d[c];
-            r = r - alpha * g.q[c];
-            g.r[c] = r;
+        if constexpr (sizeof(R) == 4) {
+            if (c0 + CG_QUAD <= g.N) {
+                const float4 dg = *reinterpret_cast<const float4*>(g.diag + c0);
+                const float4 dv = *reinterpret_cast<const float4*>(d + c0);
+                const float4 qv = *reinterpret_cast<const float4*>(g.q + c0);
+                float4 pv = *reinterpret_cast<const float4*>(g.p + c0);
+                float4 rv = *reinterpret_cast<const float4*>(g.r + c0);
+                const float* dgs = &dg.x;
+                const float* ds = &dv.x;
+                const float* qs = &qv.x;
+                float* ps = &pv.x;
+                float* rs = &rv.x;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (dgs[u] > 0) {
+                        ps[u] = ps[u] + alpha * ds[u];
+                        rs[u] = rs[u] - alpha * qs[u];
+                    }
+                    rm = mx(rm, (T)fabsf(rs[u]));
+                }
+                *reinterpret_cast<float4*>(g.p + c0) = pv;
+                *reinterpret_cast<float4*>(g.r + c0) = rv;
+            } else {
+                for (int c = c0; c < g.N; ++c) cgUpdateCell<R>(g.p, g.r, d, g.q, g.diag, alpha, c, rm);
+            }
+        } else {
+            const int c1 = min(c0 + CG_QUAD, g.N);
+            for (int c = c0; c < c1; ++c) cgUpdateCell<R>(g.p, g.r, d, g.q, g.diag, alpha, c, rm);
         }
-        rm = fabs(r);
-        const int nx = g.nx, ny = g.ny;
-        const int i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
-        if (redSweep && ((i + j + k) & 1) == 0) g.z[c] = dg > 0 ? r / dg : T(0);
     }
     blockMaxTo(g.sv + SV_RMAX, rm);
     PHX_TILES_END
