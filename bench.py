@@ -39,6 +39,23 @@ def rank_info():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def max_over_ranks(t_s: float) -> float:
+    """The timed region of the slowest rank (replicas: each rank steps its own
+    batch; the whole job's rate is all ranks' cell-updates over this time)."""
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return t_s
+    import torch
+    t = torch.tensor([t_s], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t[0])
+
+
+def whole_job_rate(cells: int, steps: int, world: int, t_s: float) -> float:
+    """cell-updates/s of N replicas of the workload over the slowest rank's time"""
+    return cells * steps * world / t_s
+
+
 def make_workloads(name: str):
     """list of cases of a workload"""
     from photon_gb300 import casegen
@@ -276,13 +293,8 @@ def measure(args, precision, L, world, clocks: bool):
     if clocks:
         clk.__exit__()
     g.sync()
-    t_s = sum(step_ms) / 1e3
-    if dist:
-        import torch
-        t = torch.tensor([t_s], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_s = float(t[0])
-    value = cells * args.steps * world / t_s
+    t_s = max_over_ranks(sum(step_ms) / 1e3)
+    value = whole_job_rate(cells, args.steps, world, t_s)
     iters = [g.stats(s)["pressure_iters"] for s in range(len(cases))]
     rels = [g.stats(s)["pressure_rel_residual"] for s in range(len(cases))]
     # e2e through the C ABI: per step, the dtMax of every scenario goes down
