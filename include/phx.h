@@ -78,6 +78,7 @@ enum {
     PHX_FIELD_LIT,      /* uint8 */
     PHX_FIELD_ZONE,     /* int32, read only */
     PHX_FIELD_RHS, PHX_FIELD_CGR, PHX_FIELD_CGZ,
+    PHX_FIELD_ZONEP,    /* double per zone: background pressure (Solver::zoneP, src/sim/solver.h:262) */
     PHX_FIELD_COUNT
 };
 

@@ -15,7 +15,7 @@ PHX_OK, PHX_ERR_INVALID, PHX_ERR_UNSUPPORTED, PHX_ERR_OOM, PHX_ERR_CUDA, PHX_ERR
 PREC_FP64, PREC_MIXED = 0, 1
 
 FIELDS = ["u", "v", "w", "p", "S", "T", "Yo", "Yf", "Ys", "Ya", "Yp", "Yc", "Yw", "Yco", "Yai", "nu", "Pb", "Q", "Qr",
-          "hrr", "massSrc", "lit", "zone", "rhs", "cgR", "cgZ"]
+          "hrr", "massSrc", "lit", "zone", "rhs", "cgR", "cgZ", "zoneP"]
 FIELD_ID = {n: i for i, n in enumerate(FIELDS)}
 STAGES = ["begin", "combustion", "turbulence", "heat", "energy", "momentum", "leakage", "project", "advect", "end"]
 STAGE_ID = {n: i for i, n in enumerate(STAGES)}

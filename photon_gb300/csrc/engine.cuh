@@ -37,7 +37,7 @@ namespace phx {
 constexpr int DENSE_MAX = 4096;
 
 enum DomId {
-    D_ONE = 0, D_CELLS, D_FX, D_FY, D_FZ, D_BX, D_BY, D_BZ, D_CZ, D_CC, D_CO_DENSE, D_CO_SERIAL, D_RB, D_QUAD,
+    D_ONE = 0, D_CELLS, D_FX, D_FY, D_FZ, D_BX, D_BY, D_BZ, D_CZ, D_CC, D_CO_DENSE, D_CO_SERIAL, D_RB, D_QUAD, D_LEAK,
     D_LV0,                       // D_LV0 + l: rows of level l when l is not the coarsest (1 <= l < 12)
     D_RS0 = D_LV0 + MAX_LEVELS,  // D_RS0 + l: rows of level l+1 for restriction from level l >= 1
     D_COUNT = D_RS0 + MAX_LEVELS
@@ -100,10 +100,6 @@ struct Scenario {
         for (auto v : geo.lx) geo.anyLeak |= v != 0;
         for (auto v : geo.ly) geo.anyLeak |= v != 0;
         for (auto v : geo.lz) geo.anyLeak |= v != 0;
-        if (geo.anyLeak) {
-            err = "crack faces (orifice-flow leakage) are not implemented in the GPU step yet";
-            return PHX_ERR_UNSUPPORTED;
-        }
         RbShapes<R> one;
         one.add(g->nx, g->ny);
         if (!one.finish()) {
@@ -116,7 +112,50 @@ struct Scenario {
         Pb0.assign(NN, 101325.0);
         Z = computeZones(geo, Pb0);
         MG = buildMultigrid(geo, DENSE_MAX);
+        buildLeakFaces();
         return PHX_OK;
+    }
+
+    // leak faces in the reference's order (axis, then face index) that touch no
+    // blocked cell, and per zone its faces to other zones (src/sim/gasphase.cpp:410-445)
+    std::vector<int> leak;       // 4 per face: axis, f, a, b
+    std::vector<int> leakZStart, leakZList;
+    void buildLeakFaces() {
+        leak.clear();
+        const int nx = geo.nx, ny = geo.ny, nz = geo.nz;
+        for (int axis = 0; axis < 3 && geo.anyLeak; ++axis) {
+            const std::vector<uint8_t>& lk = axis == 0 ? geo.lx : axis == 1 ? geo.ly : geo.lz;
+            const int dX = nx + (axis == 0), dY = ny + (axis == 1);
+            const int ncell = axis == 0 ? nx : axis == 1 ? ny : nz;
+            for (int f = 0; f < (int)lk.size(); ++f) {
+                if (!lk[f]) continue;
+                const int i = f % dX, j = (f / dX) % dY, k = f / (dX * dY);
+                int id[3] = {i, j, k}, a[3] = {i, j, k};
+                a[axis] -= 1;
+                const int ca = a[axis] >= 0 ? geo.cell(a[0], a[1], a[2]) : -1;
+                const int cb = id[axis] < ncell ? geo.cell(i, j, k) : -1;
+                if ((ca >= 0 && geo.blocked[ca]) || (cb >= 0 && geo.blocked[cb])) continue;
+                leak.insert(leak.end(), {axis, f, ca, cb});
+            }
+        }
+        const int nZ = (int)Z.zoneP.size(), nf = (int)leak.size() / 4;
+        leakZStart.assign(nZ + 1, 0);
+        auto zoneOf = [&](int c) { return c >= 0 ? Z.zone[c] : -1; };
+        for (int q = 0; q < nf; ++q) {
+            const int za = zoneOf(leak[4 * q + 2]), zb = zoneOf(leak[4 * q + 3]);
+            if (za == zb) continue;
+            if (za >= 0) leakZStart[za + 1]++;
+            if (zb >= 0) leakZStart[zb + 1]++;
+        }
+        for (int z = 0; z < nZ; ++z) leakZStart[z + 1] += leakZStart[z];
+        leakZList.assign(leakZStart[nZ], 0);
+        std::vector<int> fill(nZ, 0);
+        for (int q = 0; q < nf; ++q) {
+            const int za = zoneOf(leak[4 * q + 2]), zb = zoneOf(leak[4 * q + 3]);
+            if (za == zb) continue;
+            if (za >= 0) leakZList[leakZStart[za] + fill[za]++] = q;
+            if (zb >= 0) leakZList[leakZStart[zb] + fill[zb]++] = q;
+        }
     }
 
     // device bytes the scenario will take (the arena layout without memory)
@@ -130,7 +169,9 @@ struct Scenario {
         s.fx = carve<R>(base, off, NX); s.fy = carve<R>(base, off, NY); s.fz = carve<R>(base, off, NZ);
         s.ax = carve<R>(base, off, NX); s.ay = carve<R>(base, off, NY); s.az = carve<R>(base, off, NZ);
         s.a0x = carve<R>(base, off, NX); s.a0y = carve<R>(base, off, NY); s.a0z = carve<R>(base, off, NZ);
-        s.lx = nullptr; s.ly = nullptr; s.lz = nullptr;
+        s.lx = geo.anyLeak ? carve<uint8_t>(base, off, NX) : nullptr;
+        s.ly = geo.anyLeak ? carve<uint8_t>(base, off, NY) : nullptr;
+        s.lz = geo.anyLeak ? carve<uint8_t>(base, off, NZ) : nullptr;
         s.diag = carve<R>(base, off, N);
         s.zone = carve<int>(base, off, N);
         const int nZ = (int)Z.zoneP.size(), nC = (int)Z.closed.size();
@@ -143,6 +184,13 @@ struct Scenario {
         s.zoneDP = carve<double>(base, off, nZ + 1);
         s.zoneShift = carve<double>(base, off, nZ + 1);
         s.zoneMean = carve<double>(base, off, nZ + 1);
+        s.nLeak = (int)leak.size() / 4;
+        s.leak = carve<int4>(base, off, s.nLeak + 1);
+        s.leakZStart = carve<int>(base, off, leakZStart.size() + 1);
+        s.leakZList = carve<int>(base, off, leakZList.size() + 1);
+        s.leakQ = carve<double>(base, off, s.nLeak + 1);
+        s.zonePnew = carve<double>(base, off, nZ + 1);
+        s.zoneDInt = carve<double>(base, off, nZ + 1);
         s.u = carve<R>(base, off, NX); s.v = carve<R>(base, off, NY); s.w = carve<R>(base, off, NZ);
         s.u2 = carve<R>(base, off, NX); s.v2 = carve<R>(base, off, NY); s.w2 = carve<R>(base, off, NZ);
         for (int q = 0; q < NSC; ++q) { s.sc[q] = carve<R>(base, off, N); s.sc2[q] = carve<R>(base, off, N); }
@@ -242,6 +290,14 @@ struct Scenario {
         PHX_TRY(putRaw(st, s.closedCells, Z.closedCells.data(), Z.closedCells.size()));
         PHX_TRY(putRaw(st, s.zoneP, Z.zoneP.data(), Z.zoneP.size()));
         PHX_TRY(putRaw(st, s.zoneVol, Z.zoneVol.data(), Z.zoneVol.size()));
+        if (geo.anyLeak) {
+            PHX_TRY(putRaw(st, s.lx, geo.lx.data(), geo.lx.size()));
+            PHX_TRY(putRaw(st, s.ly, geo.ly.data(), geo.ly.size()));
+            PHX_TRY(putRaw(st, s.lz, geo.lz.data(), geo.lz.size()));
+        }
+        if (!leak.empty()) PHX_TRY(putRaw(st, s.leak, reinterpret_cast<const int4*>(leak.data()), leak.size() / 4));
+        PHX_TRY(putRaw(st, s.leakZStart, leakZStart.data(), leakZStart.size()));
+        PHX_TRY(putRaw(st, s.leakZList, leakZList.data(), leakZList.size()));
         // initial state (src/sim/discretize.cpp:28-31)
         const double amb[NSC] = {K_T0, K_YO2_AMB, 0, 0, 0, 0, K_YCO2_AMB, K_YH2O_AMB, 0, 0};
         for (int q = 0; q < NSC; ++q) {
@@ -277,6 +333,7 @@ struct Scenario {
         t[D_CELLS] = cdiv(N, TPB);
         t[D_RB] = cdiv(ny, rowBlockRows<R>(nx, ny)) * cdiv(nz, RB_KZ);      // row blocks x plane blocks
         t[D_QUAD] = cdiv(N, TPB * CG_QUAD);                                 // 4 cells per thread
+        t[D_LEAK] = cdiv((long long)leak.size() / 4, TPB);
         t[D_FX] = cdiv(geo.NX(), TPB);
         t[D_FY] = cdiv(geo.NY(), TPB);
         t[D_FZ] = cdiv(geo.NZ(), TPB);
@@ -331,6 +388,7 @@ public:
     Dom dom[D_COUNT];
     int maxLevels = 0;
     bool anyClosed = false;
+    bool anyLeak = false;
     bool tablesDirty = true;
     int launches = 0;
     cudaEvent_t ev[4] = {};
@@ -445,6 +503,7 @@ public:
         std::vector<R*> dd(2 * std::max(n, 1), nullptr);
         maxLevels = 0;
         anyClosed = false;
+        anyLeak = false;
         RbShapes<R> shp;
         int t[D_COUNT];
         for (int s = 0; s < n; ++s) {
@@ -458,6 +517,7 @@ public:
             dd[2 * s + 1] = S.dbuf[1];
             maxLevels = std::max(maxLevels, (int)S.MG.lv.size());
             anyClosed |= !S.Z.closed.empty();
+            anyLeak |= !S.leak.empty();
             S.h.dtMaxArg = dDtMax + s;
             S.h.errWord = dErr;
             shp.add(S.geo.nx, S.geo.ny);
@@ -829,6 +889,10 @@ public:
     }
     void stLeakage() {
         launch("k_zone_integral", D_CZ, TPB, k_zone_integral<R>, (const Scn<R>*)dS, dom[D_CZ]);
+        if (anyLeak) {
+            launch("k_leak_faces", D_LEAK, TPB, k_leak_faces<R>, (const Scn<R>*)dS, dom[D_LEAK]);
+            launch("k_leak_finish", D_CZ, TPB, k_leak_finish<R>, (const Scn<R>*)dS, dom[D_CZ]);
+        }
     }
     // one V-cycle z = M r (src/sim/pressure_mg.cpp:270-300) closed by the
     // last red half sweep with r.z; phase 0: before the CG loop, 1: inside
@@ -1149,6 +1213,7 @@ public:
         case PHX_FIELD_CGZ: *p = h.z; *n = N; return true;
         case PHX_FIELD_LIT: *p = h.lit; *n = N; *type = 1; return true;
         case PHX_FIELD_ZONE: *p = (void*)h.zone; *n = N; *type = 2; return true;
+        case PHX_FIELD_ZONEP: *p = (void*)h.zoneP; *n = S.Z.zoneP.size(); *type = 3; return true;
         default:
             if (f >= PHX_FIELD_T && f <= PHX_FIELD_YAI) { *p = h.sc[f - PHX_FIELD_T]; *n = N; return true; }
             return false;
@@ -1167,7 +1232,7 @@ public:
         size_t n;
         int t;
         if (!fieldPtr(s, f, &p, &n, &t)) { err = "unknown field or scenario"; return PHX_ERR_INVALID; }
-        size_t want = n * (t == 0 ? sizeof(double) : t == 1 ? 1 : 4);
+        size_t want = n * (t == 0 || t == 3 ? sizeof(double) : t == 1 ? 1 : 4);
         if (bytes != want) { err = "field size mismatch: expected " + std::to_string(want) + " bytes"; return PHX_ERR_INVALID; }
         if (kMixed && f == PHX_FIELD_P) {   // the FP64 pressure of the refinement loop
             PHX_CK(cudaMemcpyAsync(host, sc[s]->h.p64, bytes, cudaMemcpyDeviceToHost, st));
@@ -1185,7 +1250,7 @@ public:
         size_t n;
         int t;
         if (!fieldPtr(s, f, &p, &n, &t) || f == PHX_FIELD_ZONE) { err = "unknown or read-only field"; return PHX_ERR_INVALID; }
-        size_t want = n * (t == 0 ? sizeof(double) : t == 1 ? 1 : 4);
+        size_t want = n * (t == 0 || t == 3 ? sizeof(double) : t == 1 ? 1 : 4);
         if (bytes != want) { err = "field size mismatch: expected " + std::to_string(want) + " bytes"; return PHX_ERR_INVALID; }
         Scenario<R>& S = *sc[s];
         if (t == 0) {
@@ -1209,7 +1274,7 @@ public:
         o->pressure_residual = sv[SV_PRES]; o->pressure_rel_residual = sv[SV_PREL];
         o->hrr = sv[SV_HRR]; o->max_gas_t = sv[SV_MAXGAST]; o->burning_cells = (int)sv[SV_BURNING];
         o->fuel_in = sv[SV_FUELIN]; o->fuel_burned = sv[SV_FUELBURNED]; o->fuel_in_domain = sv[SV_FUELINDOMAIN];
-        o->zones = (int)sc[s]->Z.zoneP.size(); o->leak_faces = 0;
+        o->zones = (int)sc[s]->Z.zoneP.size(); o->leak_faces = (int)sc[s]->leak.size() / 4;
         return PHX_OK;
     }
 

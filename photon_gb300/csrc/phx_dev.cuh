@@ -113,6 +113,13 @@ struct Scn {
     double* zoneDP;
     double* zoneShift;
     double* zoneMean;
+    // crack faces (the leakage network, src/sim/gasphase.cpp:410-499)
+    int nLeak;                   // leak faces (0: none)
+    const int4* leak;            // per face: axis, face index, cell a (-1 outside), cell b
+    const int *leakZStart, *leakZList;   // per zone: its leak faces to other zones, ascending
+    double* leakQ;               // m3/s through each leak face this step (a -> b)
+    double* zonePnew;            // the implicit end-of-step pressure of each closed zone
+    double* zoneDInt;            // the zone integral of S
     // state
     R *u, *v, *w, *u2, *v2, *w2;
     R* sc[NSC];                  // current scalars

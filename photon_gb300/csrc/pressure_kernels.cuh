@@ -53,24 +53,30 @@ __device__ __forceinline__ R scratchRound(const Scn<R>& g, R v) {
 // FP32); dot products accumulate in Acc (double, or a double-float pair on
 // the FP32 path) and reach the per-scenario scalars as doubles.
 
+// ---- coarse levels ------------------------------------------------------------------
+// Each coarse-level pass is a per-tile device function run by a persistent
+// kernel over the active tiles; a tile function returns early where the tile
+// ends. (Running all coarse passes as phases of one cooperative kernel with
+// grid barriers was measured slower on the 64-scenario batch: the barriers
+// cost more than the launches they save inside the step graph.)
+
 // damped Jacobi sweep on a coarse level (jacobi, pressure_mg.cpp:237-247).
 // mode 0: from x = 0, into y; mode 1: y -> x; mode 2: x plus the coarser
 // level's x prolongated (:290-297), into y.
 template <class R>
-__global__ void k_jacobi(const Scn<R>* __restrict__ S, ADom dom, int l, int mode) {
+__device__ __forceinline__ void jacobiTile(const Scn<R>& g, int tile, int l, int mode) {
     using T = R;
-    PHX_TILES_BEGIN(dom)
     const Level<R>& L = g.lv[l];
-    const int I = tile_ * TPB + threadIdx.x;
-    if (I >= L.n) break;
+    const int I = tile * TPB + threadIdx.x;
+    if (I >= L.n) return;
     R* out = mode == 1 ? L.x : L.y;
     const T dg = L.diag[I];
-    if (dg <= 0) { out[I] = 0; break; }
+    if (dg <= 0) { out[I] = 0; return; }
     const T om = T(OMEGA);
     if (mode == 0) {
         T s = L.b[I];
         out[I] = scratchRound(g, (T(1) - om) * T(0) + om * s / dg);
-        break;
+        return;
     }
     const R* in = mode == 1 ? L.y : L.x;
     const R* xc = mode == 2 ? g.lv[l + 1].x : nullptr;
@@ -84,43 +90,6 @@ __global__ void k_jacobi(const Scn<R>* __restrict__ S, ADom dom, int l, int mode
     for (int q = L.rowStart[I]; q < L.rowStart[I + 1]; ++q) s += L.val[q] * X(L.col[q]);
     const T v = (T(1) - om) * X(I) + om * s / dg;
     out[I] = mode == 1 ? v : scratchRound(g, v);
-    PHX_TILES_END
-}
-
-// residual of coarse level l (residualSparse, pressure_mg.cpp:248-257), one
-// thread per row, into the level's y buffer (free between the sweeps)
-template <class R>
-__global__ void k_residual(const Scn<R>* __restrict__ S, ADom dom, int l) {
-    using T = R;
-    PHX_TILES_BEGIN(dom)
-    const Level<R>& L = g.lv[l];
-    const int I = tile_ * TPB + threadIdx.x;
-    if (I >= L.n) break;
-    const T dg = L.diag[I];
-    T r = 0;
-    if (dg > 0) {
-        T s = L.b[I] - dg * L.x[I];
-        for (int q = L.rowStart[I]; q < L.rowStart[I + 1]; ++q) s += L.val[q] * L.x[L.col[q]];
-        r = s;
-    }
-    L.y[I] = r;
-    PHX_TILES_END
-}
-
-// restriction (pressure_mg.cpp:285-286): each unknown of level l+1 sums its
-// children's residuals in ascending order, the order of the reference's scatter
-template <class R>
-__global__ void k_restrict(const Scn<R>* __restrict__ S, ADom dom, int l) {
-    using T = R;
-    PHX_TILES_BEGIN(dom)
-    const Level<R>& L = g.lv[l];
-    const Level<R>& C = g.lv[l + 1];
-    const int J = tile_ * TPB + threadIdx.x;
-    if (J >= C.n) break;
-    T acc = 0;
-    for (int e = L.childStart[J]; e < L.childStart[J + 1]; ++e) acc = acc + L.y[L.child[e]];
-    C.b[J] = acc;
-    PHX_TILES_END
 }
 
 // residual of level l fused with its restriction to level l+1 and the first
@@ -129,15 +98,14 @@ __global__ void k_restrict(const Scn<R>* __restrict__ S, ADom dom, int l) {
 // residuals of J's children eight at a time (children in ascending order),
 // and the group's first lane sums them in that order -- the order of the
 // reference's scatter -- then sets y_J = omega b_J / diag_J unless level l+1
-// is the coarsest.
+// is the coarsest. Every thread of the tile takes part (warp shuffles).
 constexpr int RRJ_LANES = 8;
 template <class R>
-__global__ void k_res_restrict_jac0(const Scn<R>* __restrict__ S, ADom dom, int l) {
+__device__ __forceinline__ void resRestrictJac0Tile(const Scn<R>& g, int tile, int l) {
     using T = R;
-    PHX_TILES_BEGIN(dom)
     const Level<R>& L = g.lv[l];
     const Level<R>& C = g.lv[l + 1];
-    const int J = tile_ * (TPB / RRJ_LANES) + (threadIdx.x / RRJ_LANES);
+    const int J = tile * (TPB / RRJ_LANES) + (threadIdx.x / RRJ_LANES);
     const int c = threadIdx.x % RRJ_LANES;
     const int groupLane0 = threadIdx.x & 31 & ~(RRJ_LANES - 1);
     int nch = 0, e0 = 0;
@@ -172,36 +140,32 @@ __global__ void k_res_restrict_jac0(const Scn<R>* __restrict__ S, ADom dom, int 
             C.y[J] = dc <= 0 ? T(0) : scratchRound(g, (T(1) - om) * T(0) + om * acc / dc);
         }
     }
-    PHX_TILES_END
 }
 
 // coarsest level: x = M b with the dense operator of the reference's 20
 // forward + backward Gauss-Seidel sweeps (pressure_mg.cpp:258-266, 279).
 // One warp per row.
 template <class R>
-__global__ void k_coarse_dense(const Scn<R>* __restrict__ S, ADom dom) {
+__device__ __forceinline__ void coarseDenseTile(const Scn<R>& g, int tile) {
     using T = R;
-    PHX_TILES_BEGIN(dom)
     const Level<R>& L = g.lv[g.nLevels - 1];
-    const int row = tile_ * (TPB / 32) + (threadIdx.x >> 5);
+    const int row = tile * (TPB / 32) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
-    if (row >= L.n) break;
+    if (row >= L.n) return;
     const R* M = L.dense + (size_t)row * L.n;
     T acc = 0;
     for (int j = lane; j < L.n; j += 32) acc += M[j] * L.b[j];
     acc = warpSum(acc);
     if (lane == 0) L.x[row] = acc;
-    PHX_TILES_END
 }
 
 // coarsest level solved as the reference does it: 20 forward + backward
 // sweeps, serially in one thread (used when the level is too large for a dense
 // operator)
 template <class R>
-__global__ void k_coarse_serial(const Scn<R>* __restrict__ S, ADom dom) {
+__device__ __forceinline__ void coarseSerialTile(const Scn<R>& g) {
     using T = R;
-    PHX_TILES_BEGIN(dom)
-    if (threadIdx.x != 0) break;
+    if (threadIdx.x != 0) return;
     const Level<R>& L = g.lv[g.nLevels - 1];
     for (int I = 0; I < L.n; ++I) L.x[I] = 0;
     for (int it = 0; it < 20; ++it)
@@ -214,6 +178,30 @@ __global__ void k_coarse_serial(const Scn<R>* __restrict__ S, ADom dom) {
                 for (int q = L.rowStart[I]; q < L.rowStart[I + 1]; ++q) s += L.val[q] * L.x[L.col[q]];
                 L.x[I] = s / dg;
             }
+}
+
+template <class R>
+__global__ void k_jacobi(const Scn<R>* __restrict__ S, ADom dom, int l, int mode) {
+    PHX_TILES_BEGIN(dom)
+    jacobiTile(g, tile_, l, mode);
+    PHX_TILES_END
+}
+template <class R>
+__global__ void k_res_restrict_jac0(const Scn<R>* __restrict__ S, ADom dom, int l) {
+    PHX_TILES_BEGIN(dom)
+    resRestrictJac0Tile(g, tile_, l);
+    PHX_TILES_END
+}
+template <class R>
+__global__ void k_coarse_dense(const Scn<R>* __restrict__ S, ADom dom) {
+    PHX_TILES_BEGIN(dom)
+    coarseDenseTile(g, tile_);
+    PHX_TILES_END
+}
+template <class R>
+__global__ void k_coarse_serial(const Scn<R>* __restrict__ S, ADom dom) {
+    PHX_TILES_BEGIN(dom)
+    coarseSerialTile(g);
     PHX_TILES_END
 }
 

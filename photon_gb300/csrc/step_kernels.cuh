@@ -494,13 +494,30 @@ __global__ void k_mom_bnd(const Scn<R>* __restrict__ S, Dom dom, int comp) {
 }
 
 // ---------------------------------------------------------------------------
-// Solver::leakage without crack faces (src/sim/gasphase.cpp:403-409, 486-498):
-// per closed zone the integral of S, the zone's pressure-rise rate and the
-// divergence shift. One CTA per closed zone; FP64 sums in either path.
+// Solver::leakage (src/sim/gasphase.cpp:403-499). k_zone_integral: per closed
+// zone (one CTA each) the integral of S and, with crack faces, the implicit
+// end-of-step zone pressure by the reference's 40-step bisection of the
+// zone's mass balance against the orifice flow through its leak faces (each
+// evaluation sums the zone's faces with a fixed-order CTA reduction).
+// k_leak_faces: the relaxed orifice velocity of every leak face and its volume
+// flow. k_leak_finish: per closed zone the pressure-rise rate and the
+// divergence shift. FP64 arithmetic in either path (a few hundred faces).
+constexpr double K_CD_LEAK = 1.0, K_LEAK_VMAX = 40.0;
+
+__device__ __forceinline__ double leakFlow(double dp, double rhoUp) {   // m/s, positive a -> b
+    const double sgn = dp >= 0 ? 1.0 : -1.0;
+    return sgn * mn(K_LEAK_VMAX, K_CD_LEAK * sqrt(2.0 * fabs(dp) / mx(rhoUp, 0.05)));
+}
+template <class R>
+__device__ __forceinline__ double leakOpenFrac(const Scn<R>& g, const int4& lf) {
+    return (double)(lf.x == 0 ? g.fx : lf.x == 1 ? g.fy : g.fz)[lf.y];
+}
+
 template <class R>
 __global__ void k_zone_integral(const Scn<R>* __restrict__ S, Dom dom) {
     PHX_PROLOGUE(dom);
     __shared__ double sh[32];
+    __shared__ double bcast;
     const int zi = tile_;
     const int z = g.closedZone[zi];
     const double V = g.dx * g.dx * g.dx;
@@ -510,9 +527,96 @@ __global__ void k_zone_integral(const Scn<R>* __restrict__ S, Dom dom) {
         acc += (double)g.S[c] * V;
     }
     double dInt = blockSum(acc, sh);
+    if (threadIdx.x == 0) bcast = dInt;
+    __syncthreads();
+    dInt = bcast;
+    const double Vz = g.zoneVol[z];
+    if (g.nLeak == 0) {
+        if (threadIdx.x == 0) {
+            double out = 0.0;
+            g.zoneDP[z] = K_GAMMA * g.zoneP[z] * (double)(dInt - out) / Vz;
+            g.zoneShift[z] = (double)(dInt - out) / Vz;
+        }
+        return;
+    }
+    const double P = g.zoneP[z], dt = g.sv[SV_DT], A = g.dx * g.dx;
+    const int e0 = g.leakZStart[z], e1 = g.leakZStart[z + 1];
+    // residual of the zone's mass balance at trial pressure Pt (every thread)
+    auto resid = [&](double Pt) {
+        double acc2 = 0;
+        for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+            const int4 lf = g.leak[g.leakZList[e]];
+            const bool zIsA = lf.z >= 0 && g.zone[lf.z] == z;
+            const int other = zIsA ? lf.w : lf.z;
+            const double Po = other >= 0 && g.zone[other] >= 0 ? g.zoneP[g.zone[other]] : K_P0;
+            const double dp = Pt - Po;
+            const int up = dp >= 0 ? (zIsA ? lf.z : lf.w) : other;
+            const double rho = up >= 0 ? gasDensity(g, up) : K_P0 / (K_RS * K_T0);
+            acc2 += leakOpenFrac(g, lf) * A * fabs(leakFlow(dp, rho)) * (dp >= 0 ? 1 : -1);
+        }
+        const double out = blockSum(acc2, sh);
+        __syncthreads();
+        if (threadIdx.x == 0) bcast = out;
+        __syncthreads();
+        return Pt - P - dt * K_GAMMA * P / Vz * (double)(dInt - bcast);
+    };
+    double lo = P - 20000.0, hi = P + 20000.0, Pnew;
+    const double rlo = resid(lo), rhi = resid(hi);
+    if (rlo > 0 || rhi < 0) {
+        Pnew = P;
+    } else {
+        for (int it = 0; it < 40; ++it) {
+            const double mid = 0.5 * (lo + hi);
+            if (resid(mid) > 0) hi = mid; else lo = mid;
+        }
+        Pnew = 0.5 * (lo + hi);
+    }
     if (threadIdx.x == 0) {
-        double Vz = g.zoneVol[z];
-        double out = 0.0;
+        g.zonePnew[z] = Pnew;
+        g.zoneDInt[z] = dInt;
+    }
+}
+
+// one thread per leak face (src/sim/gasphase.cpp:475-486)
+template <class R>
+__global__ void k_leak_faces(const Scn<R>* __restrict__ S, Dom dom) {
+    PHX_PROLOGUE(dom);
+    const int q = tile_ * TPB + threadIdx.x;
+    if (q >= g.nLeak) return;
+    const int4 lf = g.leak[q];
+    auto Pz = [&](int c) -> double {
+        if (c < 0 || g.zone[c] < 0) return K_P0;
+        const int zc = g.zone[c];
+        return g.zoneOpen[zc] ? g.zoneP[zc] : g.zonePnew[zc];
+    };
+    const double rho0 = K_P0 / (K_RS * K_T0);
+    const double pa = Pz(lf.z), pb = Pz(lf.w);
+    const double ra = lf.z >= 0 ? gasDensity(g, lf.z) : rho0, rb = lf.w >= 0 ? gasDensity(g, lf.w) : rho0;
+    const double Ha = lf.z >= 0 ? (double)g.p[lf.z] : 0, Hb = lf.w >= 0 ? (double)g.p[lf.w] : 0;
+    const double dp = (pa - pb) + 0.5 * (ra + rb) * (Ha - Hb);
+    const double un = leakFlow(dp, dp >= 0 ? ra : rb);
+    R* vel = lf.x == 0 ? g.u : lf.x == 1 ? g.v : g.w;
+    vel[lf.y] = (R)(0.5 * ((double)vel[lf.y] + un));
+    g.leakQ[q] = leakOpenFrac(g, lf) * (g.dx * g.dx) * (double)vel[lf.y];
+}
+
+// per closed zone: the net flow out through its leak faces, the zone's
+// pressure-rise rate and the divergence shift (src/sim/gasphase.cpp:484-498)
+template <class R>
+__global__ void k_leak_finish(const Scn<R>* __restrict__ S, Dom dom) {
+    PHX_PROLOGUE(dom);
+    __shared__ double sh[32];
+    const int z = g.closedZone[tile_];
+    double acc = 0;
+    for (int e = g.leakZStart[z] + threadIdx.x; e < g.leakZStart[z + 1]; e += blockDim.x) {
+        const int q = g.leakZList[e];
+        const int4 lf = g.leak[q];
+        const bool zIsA = lf.z >= 0 && g.zone[lf.z] == z;
+        acc += zIsA ? g.leakQ[q] : -g.leakQ[q];
+    }
+    const double out = blockSum(acc, sh);
+    if (threadIdx.x == 0) {
+        const double Vz = g.zoneVol[z], dInt = g.zoneDInt[z];
         g.zoneDP[z] = K_GAMMA * g.zoneP[z] * (double)(dInt - out) / Vz;
         g.zoneShift[z] = (double)(dInt - out) / Vz;
     }
