@@ -77,7 +77,9 @@ public:
     // state, filled from the device by sync()
     float time = 0;
     std::vector<float> u, v, w, p, S, T, Yo, Yf, Ys, Ya, Yp, Yc, Yw, Yco, Yai, nu, Pb, Q, Qr, hrr, massSrc;
+    std::vector<uint8_t> lit;
     std::vector<int> zone;
+    std::vector<float> zoneP;
     SimStats stats;
     float maxVel = 0, maxNu = 0, maxDiv = 0;
     int pressureIters = 0;
@@ -155,8 +157,11 @@ public:
         get(PHX_FIELD_YA, Ya); get(PHX_FIELD_YP, Yp); get(PHX_FIELD_YC, Yc); get(PHX_FIELD_YW, Yw);
         get(PHX_FIELD_YCO, Yco); get(PHX_FIELD_YAI, Yai); get(PHX_FIELD_NU, nu); get(PHX_FIELD_PB, Pb);
         get(PHX_FIELD_Q, Q); get(PHX_FIELD_QR, Qr); get(PHX_FIELD_HRR, hrr); get(PHX_FIELD_MASSSRC, massSrc);
+        get(PHX_FIELD_ZONEP, zoneP);
         zone.resize(phx_field_count(ctx_, PHX_FIELD_ZONE));
         check(phx_get_field(ctx_, PHX_FIELD_ZONE, zone.data(), zone.size() * sizeof(int)));
+        lit.resize(phx_field_count(ctx_, PHX_FIELD_LIT));
+        check(phx_get_field(ctx_, PHX_FIELD_LIT, lit.data(), lit.size()));
         readScalars();
     }
 
@@ -166,6 +171,50 @@ public:
         put(PHX_FIELD_T, T); put(PHX_FIELD_YO, Yo); put(PHX_FIELD_YF, Yf); put(PHX_FIELD_YS, Ys);
         put(PHX_FIELD_YA, Ya); put(PHX_FIELD_YP, Yp); put(PHX_FIELD_YC, Yc); put(PHX_FIELD_YW, Yw);
         put(PHX_FIELD_YCO, Yco); put(PHX_FIELD_YAI, Yai);
+    }
+
+    // Checkpoint interop. A checkpoint is written and read by the host
+    // photon::Solver (saveState / loadState, src/sim/state.cpp:62-195); these
+    // two move the gas-phase part of that state between the GPU and any host
+    // object with photon::Solver's public members (u v w p S T Yo Yf Ys Ya Yp
+    // Yc Yw Yco Yai nu Pb hrr lit zone zoneP, time, maxVel, maxNu, maxDiv,
+    // stats). The host's zone tables must exist (they do after its first step
+    // or a loadState): zones depend on the geometry only, and the host's
+    // numbering is the GPU's.
+    template <class Host>
+    void exportTo(Host& h) {
+        sync();
+        auto cp = [](auto& dst, const auto& src) { dst.assign(src.begin(), src.end()); };
+        cp(h.u, u); cp(h.v, v); cp(h.w, w); cp(h.p, p); cp(h.S, S);
+        cp(h.T, T); cp(h.Yo, Yo); cp(h.Yf, Yf); cp(h.Ys, Ys); cp(h.Ya, Ya); cp(h.Yp, Yp);
+        cp(h.Yc, Yc); cp(h.Yw, Yw); cp(h.Yco, Yco); cp(h.Yai, Yai); cp(h.nu, nu); cp(h.Pb, Pb);
+        cp(h.hrr, hrr); cp(h.lit, lit); cp(h.zoneP, zoneP);
+        h.time = time; h.maxVel = maxVel; h.maxNu = maxNu; h.maxDiv = maxDiv;
+        h.stats.hrr = stats.hrr; h.stats.maxGasT = stats.maxGasT; h.stats.burningCells = stats.burningCells;
+        h.stats.fuelIn = stats.fuelIn; h.stats.fuelBurned = stats.fuelBurned; h.stats.fuelInDomain = stats.fuelInDomain;
+    }
+    // The reverse, after the host loaded a checkpoint; false with a message when
+    // the host's grid or zone count is not this solver's.
+    template <class Host>
+    bool importFrom(const Host& h, std::string& err) {
+        if (h.nx != nx || h.ny != ny || h.nz != nz || h.dx != dx) { err = "state grid does not match this solver's grid"; return false; }
+        if (h.zoneP.size() != phx_field_count(ctx_, PHX_FIELD_ZONEP)) { err = "state zone count does not match"; return false; }
+        auto cp = [](auto& dst, const auto& src) { dst.assign(src.begin(), src.end()); };
+        cp(u, h.u); cp(v, h.v); cp(w, h.w); cp(p, h.p); cp(S, h.S);
+        cp(T, h.T); cp(Yo, h.Yo); cp(Yf, h.Yf); cp(Ys, h.Ys); cp(Ya, h.Ya); cp(Yp, h.Yp);
+        cp(Yc, h.Yc); cp(Yw, h.Yw); cp(Yco, h.Yco); cp(Yai, h.Yai); cp(nu, h.nu); cp(Pb, h.Pb);
+        cp(hrr, h.hrr); cp(lit, h.lit); cp(zoneP, h.zoneP);
+        push();
+        put(PHX_FIELD_S, S); put(PHX_FIELD_NU, nu); put(PHX_FIELD_PB, Pb); put(PHX_FIELD_HRR, hrr);
+        put(PHX_FIELD_ZONEP, zoneP);
+        if (!lit.empty()) check(phx_set_field(ctx_, PHX_FIELD_LIT, lit.data(), lit.size()));
+        phx_stats s{};
+        s.time = h.time; s.max_vel = h.maxVel; s.max_nu = h.maxNu; s.max_div = h.maxDiv;
+        s.hrr = h.stats.hrr; s.max_gas_t = h.stats.maxGasT; s.burning_cells = h.stats.burningCells;
+        s.fuel_in = h.stats.fuelIn; s.fuel_burned = h.stats.fuelBurned; s.fuel_in_domain = h.stats.fuelInDomain;
+        check(phx_set_stats(ctx_, &s));
+        readScalars();
+        return true;
     }
 
     phx_ctx* handle() const { return ctx_; }

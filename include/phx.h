@@ -145,6 +145,11 @@ size_t phx_field_count(const struct phx_ctx* ctx, int field);
 int phx_get_stats(struct phx_ctx* ctx, phx_stats* out);
 /* time, maxVel, maxNu, maxDiv as read by the next stableDt */
 int phx_set_scalars(struct phx_ctx* ctx, double time, double max_vel, double max_nu, double max_div);
+/* Restore what a checkpoint holds besides the fields (Solver::loadState,
+ * src/sim/state.cpp:144-145,186: time, maxVel, maxNu and the SimStats): time,
+ * max_vel, max_nu, max_div, hrr, max_gas_t, burning_cells and the cumulative
+ * fuel_in, fuel_burned, fuel_in_domain. The other members of *in are ignored. */
+int phx_set_stats(struct phx_ctx* ctx, const phx_stats* in);
 /* device bytes this context holds */
 size_t phx_device_bytes(const struct phx_ctx* ctx);
 /* wait for the context's stream */
@@ -246,6 +251,7 @@ int phx_batch_get_field(struct phx_ctx* ctx, int scenario, int field, void* host
 int phx_batch_set_field(struct phx_ctx* ctx, int scenario, int field, const void* host, size_t bytes);
 size_t phx_batch_field_count(const struct phx_ctx* ctx, int scenario, int field);
 int phx_batch_get_stats(struct phx_ctx* ctx, int scenario, phx_stats* out);
+int phx_batch_set_stats(struct phx_ctx* ctx, int scenario, const phx_stats* in);
 
 /* --- process-level helpers ------------------------------------------------
  * select the CUDA device later contexts of this thread are created on */

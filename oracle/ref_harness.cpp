@@ -16,6 +16,7 @@
 #include "sim/solver.h"
 
 #include <chrono>
+#include <cstdio>
 #include <cstring>
 #include <string>
 #include <thread>
@@ -316,5 +317,31 @@ void ref_mg_get(void* h, int l, int* agg, int* rowStart, int* col, double* val, 
 }
 
 double ref_phase_ms(void* h, int i) { return ((Ctx*)h)->s->phaseMs[i]; }
+
+// the order of ref_scalars' first four, then hrr, maxGasT, burningCells,
+// fuelIn, fuelBurned, fuelInDomain
+void ref_set_stats(void* h, const double* v) {
+    Solver& s = *((Ctx*)h)->s;
+    s.time = (float)v[0]; s.maxVel = (float)v[1]; s.maxNu = (float)v[2]; s.maxDiv = (float)v[3];
+    s.stats.hrr = (float)v[4]; s.stats.maxGasT = (float)v[5]; s.stats.burningCells = (int)v[6];
+    s.stats.fuelIn = v[7]; s.stats.fuelBurned = v[8]; s.stats.fuelInDomain = v[9];
+}
+
+// the zone tables Solver::step builds on its first call (src/sim/gasphase.cpp:111-158)
+void ref_compute_zones(void* h) { ((Ctx*)h)->s->computeZones(); }
+
+// Solver::saveState / Solver::loadState (src/sim/state.cpp:62-195); 0 on success
+int ref_save_state(void* h, const char* path, char* err, int errLen) {
+    std::string e;
+    if (((Ctx*)h)->s->saveState(path, e)) return 0;
+    std::snprintf(err, errLen, "%s", e.c_str());
+    return -1;
+}
+int ref_load_state(void* h, const char* path, char* err, int errLen) {
+    std::string e;
+    if (((Ctx*)h)->s->loadState(path, e)) return 0;
+    std::snprintf(err, errLen, "%s", e.c_str());
+    return -1;
+}
 
 } // extern "C"

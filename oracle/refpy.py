@@ -66,6 +66,10 @@ def load(bits: int = 64):
     L.ref_mg_get.argtypes = [vp, i, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     L.ref_phase_ms.restype = d
     L.ref_phase_ms.argtypes = [vp, i]
+    L.ref_set_stats.argtypes = [vp, ctypes.c_void_p]
+    L.ref_compute_zones.argtypes = [vp]
+    L.ref_save_state.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, i]
+    L.ref_load_state.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, i]
     _LIBS[bits] = L
     return L
 
@@ -172,6 +176,32 @@ class RefSolver:
 
     def set_scalars(self, time, maxVel, maxNu, maxDiv):
         self.L.ref_set_scalars(self.h, time, maxVel, maxNu, maxDiv)
+
+    # stats under the names of the GPU library's phx_stats
+    _STATS = (("time", "time"), ("max_vel", "maxVel"), ("max_nu", "maxNu"), ("max_div", "maxDiv"), ("hrr", "hrr"),
+              ("max_gas_t", "maxGasT"), ("burning_cells", "burningCells"), ("fuel_in", "fuelIn"),
+              ("fuel_burned", "fuelBurned"), ("fuel_in_domain", "fuelInDomain"))
+
+    def stats(self) -> dict:
+        sc = self.scalars()
+        return {k: int(sc[r]) if k == "burning_cells" else sc[r] for k, r in self._STATS}
+
+    def set_stats(self, st: dict):
+        v = (ctypes.c_double * len(self._STATS))(*[float(st[k]) for k, _ in self._STATS])
+        self.L.ref_set_stats(self.h, v)
+
+    def compute_zones(self):
+        self.L.ref_compute_zones(self.h)
+
+    def save_state(self, path: str):
+        err = ctypes.create_string_buffer(512)
+        if self.L.ref_save_state(self.h, path.encode(), err, 512) != 0:
+            raise RuntimeError(err.value.decode())
+
+    def load_state(self, path: str):
+        err = ctypes.create_string_buffer(512)
+        if self.L.ref_load_state(self.h, path.encode(), err, 512) != 0:
+            raise RuntimeError(err.value.decode())
 
     def mg(self):
         """Multigrid hierarchy: list of dicts (n, agg, rowStart, col, val, diag)."""

@@ -23,11 +23,11 @@ STAGE_ID = {n: i for i, n in enumerate(STAGES)}
 # exported symbols, as declared in include/phx.h
 SYMBOLS = ["phx_create", "phx_destroy", "phx_last_error", "phx_last_global_error", "phx_abi_version", "phx_add_burner",
            "phx_add_ignition", "phx_step", "phx_run", "phx_stage", "phx_precondition", "phx_get_field",
-           "phx_set_field", "phx_field_count", "phx_get_stats", "phx_set_scalars", "phx_device_bytes", "phx_sync",
+           "phx_set_field", "phx_field_count", "phx_get_stats", "phx_set_scalars", "phx_set_stats", "phx_device_bytes", "phx_sync",
            "phx_time_steps", "phx_profile_step", "phx_last_step_launches", "phx_select_device", "phx_alloc_host",
            "phx_free_host", "phx_create_batch", "phx_batch_add", "phx_batch_remove", "phx_batch_size",
            "phx_batch_scenario_bytes", "phx_batch_add_burner", "phx_batch_step", "phx_batch_get_field",
-           "phx_batch_set_field", "phx_batch_field_count", "phx_batch_get_stats", "phx_gather_stats_noalloc",
+           "phx_batch_set_field", "phx_batch_field_count", "phx_batch_get_stats", "phx_batch_set_stats", "phx_gather_stats_noalloc",
            "phx_server_create", "phx_server_destroy", "phx_server_last_error", "phx_server_submit", "phx_server_step",
            "phx_server_poll", "phx_server_get_field", "phx_server_release", "phx_server_counts"]
 
@@ -101,6 +101,7 @@ def load():
     L.phx_field_count.argtypes = [vp, i]
     L.phx_get_stats.argtypes = [vp, ctypes.POINTER(PhxStats)]
     L.phx_set_scalars.argtypes = [vp, d, d, d, d]
+    L.phx_set_stats.argtypes = [vp, ctypes.POINTER(PhxStats)]
     L.phx_device_bytes.restype = sz
     L.phx_device_bytes.argtypes = [vp]
     L.phx_sync.argtypes = [vp]
@@ -134,6 +135,7 @@ def load():
     L.phx_batch_field_count.restype = sz
     L.phx_batch_field_count.argtypes = [vp, i, i]
     L.phx_batch_get_stats.argtypes = [vp, i, ctypes.POINTER(PhxStats)]
+    L.phx_batch_set_stats.argtypes = [vp, i, ctypes.POINTER(PhxStats)]
     L.phx_alloc_host.restype = vp
     L.phx_alloc_host.argtypes = [sz]
     L.phx_free_host.argtypes = [vp]

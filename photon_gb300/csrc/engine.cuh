@@ -1290,6 +1290,20 @@ public:
         return PHX_OK;
     }
 
+    // the scalar slots a checkpoint restores (src/sim/state.cpp:144-145,186)
+    int setStats(int s, const phx_stats* in) override {
+        PHX_TRY(checkScn(s));
+        const int slot[10] = {SV_TIME, SV_MAXVEL, SV_MAXNU, SV_MAXDIV, SV_HRR, SV_MAXGAST, SV_BURNING,
+                              SV_FUELIN, SV_FUELBURNED, SV_FUELINDOMAIN};
+        const double v[10] = {in->time, in->max_vel, in->max_nu, in->max_div, in->hrr, in->max_gas_t,
+                              (double)in->burning_cells, in->fuel_in, in->fuel_burned, in->fuel_in_domain};
+        double* sv = sc[s]->h.sv;
+        for (int q = 0; q < 10; ++q)
+            PHX_CK(cudaMemcpyAsync(sv + slot[q], &v[q], sizeof(double), cudaMemcpyHostToDevice, st));
+        PHX_CK(cudaStreamSynchronize(st));
+        return PHX_OK;
+    }
+
     size_t deviceBytes() const override {
         size_t b = 0;
         for (auto& S : sc) b += S->arenaBytes;

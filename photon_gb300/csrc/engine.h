@@ -28,6 +28,7 @@ public:
     virtual int setField(int s, int field, const void* host, size_t bytes) = 0;
     virtual size_t fieldCount(int s, int field) const = 0;
     virtual int getStats(int s, phx_stats* out) = 0;
+    virtual int setStats(int s, const phx_stats* in) = 0;
     virtual int setScalars(int s, double time, double maxVel, double maxNu, double maxDiv) = 0;
     virtual size_t deviceBytes() const = 0;
     virtual int sync() = 0;

@@ -39,6 +39,15 @@ def make_grid(case):
     return g, keep
 
 
+# the gas-phase fields of a checkpoint, in the order Solver::saveState writes
+# them (src/sim/state.cpp:75-79); geometry and solid-phase state stay on the host
+CHECKPOINT_FIELDS = ("u", "v", "w", "p", "S", "T", "Yo", "Yf", "Ys", "Ya", "Yp", "Yc", "Yw", "Yco", "Yai",
+                     "nu", "Pb", "zoneP", "hrr", "lit")
+# the stats a checkpoint restores (time, maxVel, maxNu and SimStats)
+STAT_KEYS = ("time", "max_vel", "max_nu", "max_div", "hrr", "max_gas_t", "burning_cells", "fuel_in",
+             "fuel_burned", "fuel_in_domain")
+
+
 class Solver:
     def __init__(self, case, precision: int = _lib.PREC_FP64, add_burners: bool = True):
         self.L = _lib.load()
@@ -117,6 +126,31 @@ class Solver:
 
     def set_scalars(self, time, maxVel, maxNu, maxDiv):
         self._check(self.L.phx_set_scalars(self.h, time, maxVel, maxNu, maxDiv))
+
+    def set_stats(self, st: dict):
+        """Restore the scalars a checkpoint holds (keys as stats() returns them)."""
+        s = PhxStats()
+        for k in STAT_KEYS:
+            setattr(s, k, int(st[k]) if k == "burning_cells" else float(st[k]))
+        self._check(self.L.phx_set_stats(self.h, ctypes.byref(s)))
+
+    def export_state(self, host):
+        """Copy the gas-phase state into `host` (get/set by field name,
+        set_stats), e.g. a host solver about to write a checkpoint
+        (Solver::saveState, src/sim/state.cpp:62-121). The host's zone tables
+        must exist; zones depend on the geometry only."""
+        for f in CHECKPOINT_FIELDS:
+            host.set(f, self.get(f))
+        host.set_stats(self.stats())
+
+    def import_state(self, host):
+        """The reverse of export_state, after `host` loaded a checkpoint
+        (Solver::loadState, src/sim/state.cpp:123-195)."""
+        if len(host.get("zoneP")) != len(self.get("zoneP")):
+            raise PhxError(_lib.PHX_ERR_INVALID, "state zone count does not match")
+        for f in CHECKPOINT_FIELDS:
+            self.set(f, host.get(f))
+        self.set_stats(host.stats())
 
     def device_bytes(self) -> int:
         return int(self.L.phx_device_bytes(self.h))

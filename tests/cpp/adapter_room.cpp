@@ -2,18 +2,40 @@
 // reference's gas-phase tests (src/tests/test_main.cpp:420-433) as a closed box
 // at 20 cm with an open doorway, a 100 kW burner, 40 steps; prints one line of
 // results for the test to check.
+//
+// With a second argument "checkpoint" it then moves the state through a host
+// object with photon::Solver's public state members (what saveState writes,
+// src/sim/state.cpp:62-121) into a second GPU solver, checks that the fields
+// arrive unchanged, steps both solvers 10 more steps and prints the largest
+// relative difference of their temperature and velocity fields.
+#include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <string>
+#include <vector>
 
 #include "photon_gpu/solver.hpp"
 
-int main(int argc, char** argv) {
-    photon_gpu::Solver s;
+// the members of photon::Solver a checkpoint's gas phase consists of
+struct HostState {
+    int nx = 0, ny = 0, nz = 0;
+    float dx = 0;
+    float time = 0, maxVel = 0, maxNu = 0, maxDiv = 0;
+    std::vector<float> u, v, w, p, S, T, Yo, Yf, Ys, Ya, Yp, Yc, Yw, Yco, Yai, nu, Pb, hrr, zoneP;
+    std::vector<uint8_t> lit;
+    struct {
+        float hrr = 0, maxGasT = 0;
+        int burningCells = 0;
+        double fuelIn = 0, fuelBurned = 0, fuelInDomain = 0;
+    } stats;
+};
+
+static bool setupRoom(photon_gpu::Solver& s, bool mixed) {
     s.profile = photon_gpu::FidelityProfile::realtime();
     s.radiationOn = false;
     s.adiabaticSurfaces = true;
-    if (argc > 1 && std::string(argv[1]) == "mixed") s.precision = photon_gpu::Solver::Precision::Mixed;
+    if (mixed) s.precision = photon_gpu::Solver::Precision::Mixed;
     const int nx = 18, ny = 12, nz = 12;
     s.setGrid(nx, ny, nz, 0.2f);
     // closed walls and ceiling, one doorway in the x = 0 wall (j 4..7, k 0..9)
@@ -31,16 +53,50 @@ int main(int argc, char** argv) {
     for (int j = 0; j < ny; ++j)
         for (int i = 0; i < nx; ++i) s.fz[s.zface(i, j, nz)] = s.az[s.zface(i, j, nz)] = 0.f;
     std::string err;
-    if (!s.build(err)) { std::printf("build failed: %s\n", err.c_str()); return 1; }
+    if (!s.build(err)) { std::printf("build failed: %s\n", err.c_str()); return false; }
     photon_gpu::Burner b;
     b.x0 = 2.4f; b.y0 = 1.0f; b.x1 = 2.8f; b.y1 = 1.4f; b.z = 0; b.peakW = 100e3f;
-    if (s.addBurner(b) < 0) { std::printf("burner rejected\n"); return 1; }
+    if (s.addBurner(b) < 0) { std::printf("burner rejected\n"); return false; }
+    return true;
+}
+
+static double maxRel(const std::vector<float>& a, const std::vector<float>& b) {
+    double num = 0, den = 0;
+    for (size_t i = 0; i < a.size(); ++i) {
+        num = std::max(num, (double)std::fabs(a[i] - b[i]));
+        den = std::max(den, (double)std::fabs(b[i]));
+    }
+    return den > 0 ? num / den : num;
+}
+
+int main(int argc, char** argv) {
+    const bool mixed = argc > 1 && std::string(argv[1]) == "mixed";
+    const bool ckpt = argc > 2 && std::string(argv[2]) == "checkpoint";
+    photon_gpu::Solver s;
+    if (!setupRoom(s, mixed)) return 1;
     float t = 0;
     for (int i = 0; i < 40; ++i) t += s.step(0.05f);
     s.sync();
     float maxT = 0;
     for (float v : s.T) maxT = std::fmax(maxT, v);
-    std::printf("time %.6f hrr %.3f maxT %.3f iters %d fuelIn %.9f maxVel %.6f cells %zu\n", t, s.stats.hrr, maxT,
+    std::printf("time %.6f hrr %.3f maxT %.3f iters %d fuelIn %.9f maxVel %.6f cells %zu", t, s.stats.hrr, maxT,
                 s.pressureIters, s.stats.fuelIn, s.maxVel, s.T.size());
+    if (ckpt) {
+        HostState h;
+        h.nx = s.nx; h.ny = s.ny; h.nz = s.nz; h.dx = s.dx;
+        s.exportTo(h);
+        photon_gpu::Solver r;
+        if (!setupRoom(r, mixed)) return 1;
+        std::string err;
+        if (!r.importFrom(h, err)) { std::printf("\nimport failed: %s\n", err.c_str()); return 1; }
+        r.sync();
+        const bool same = r.u == h.u && r.v == h.v && r.w == h.w && r.p == h.p && r.T == h.T && r.Yf == h.Yf &&
+                          r.zoneP == h.zoneP && r.lit == h.lit && r.time == h.time && r.stats.fuelIn == h.stats.fuelIn;
+        for (int i = 0; i < 10; ++i) { s.step(0.05f); r.step(0.05f); }
+        s.sync(); r.sync();
+        const double d = std::max({maxRel(r.T, s.T), maxRel(r.u, s.u), maxRel(r.v, s.v), maxRel(r.w, s.w)});
+        std::printf(" ckpt_same %d ckpt_maxrel %.3e ckpt_dtime %.3e", same ? 1 : 0, d, (double)std::fabs(r.time - s.time));
+    }
+    std::printf("\n");
     return 0;
 }

@@ -37,3 +37,19 @@ def test_adapter_runs_room(mode):
     assert float(vals["maxT"]) > 400          # the burner heats the room
     assert float(vals["hrr"]) > 10e3          # and burns
     assert int(vals["cells"]) == 18 * 12 * 12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+def test_adapter_checkpoint_round_trip(mode):
+    """exportTo / importFrom through a host object shaped like photon::Solver:
+    the fields arrive unchanged, and the resumed solver tracks the original
+    (the host holds FP32 fields, as the reference does, so the FP64 state is
+    rounded once on the way)."""
+    exe = compile_adapter()
+    out = subprocess.run([exe, mode, "checkpoint"], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    vals = dict(zip(out.stdout.split()[0::2], out.stdout.split()[1::2]))
+    assert int(vals["ckpt_same"]) == 1
+    assert float(vals["ckpt_dtime"]) < 1e-5
+    assert float(vals["ckpt_maxrel"]) < 1e-3
