@@ -424,6 +424,52 @@ def measure_serving(args, precision):
                        "pressure_stop": "relative %g" % REL_TOL}}
 
 
+def measure_radiation(args, cpu_baseline: bool):
+    """The radiation trace (phx_rad_trace; Solver::traceRadiation,
+    src/sim/radiation.cpp:181-319) on the seeded 144x104x88 house at 0.1 m
+    (1.32 M cells) with its synthetic element set (casegen.rad_workload): device
+    time of the trace kernels (CUDA events) and the end-to-end call with its
+    host copies, per precision; the oracle's single-threaded restatement on a
+    sample of the elements as the CPU baseline."""
+    from photon_gb300 import _lib, casegen
+    from photon_gb300.solver import Solver
+    c = casegen.house_fine(1)
+    w = casegen.rad_workload(c)
+    el, wl = _lib.rad_elements(w["elements"]), _lib.rad_walls(w["walls"])
+    rays = int(32 * np.count_nonzero(el["sphere"])) + 16 * int(np.count_nonzero(el["sphere"] == 0))
+    out = {"workload": "house %dx%dx%d at %.1f m (%d cells), %d elements, %d walls" % (
+        c.nx, c.ny, c.nz, c.dx, c.N, len(el), len(wl)), "rays_per_trace_approx": rays}
+    for name, prec in (("mixed", _lib.PREC_MIXED), ("fp64", _lib.PREC_FP64)):
+        g = Solver(c, prec)
+        for f, a in w["gas"].items():
+            g.set(f, a)
+        for _ in range(max(3, args.warmup)):
+            g.rad_trace(el, wl, w["solidT"])
+        dev, wall = [], []
+        for _ in range(10):
+            t = time.perf_counter()
+            g.rad_trace(el, wl, w["solidT"])
+            wall.append((time.perf_counter() - t) * 1e3)
+            dev.append(g.rad_last_ms())
+        g.close()
+        out[name] = {"device_ms": float(np.median(dev)), "e2e_ms": float(np.median(wall)),
+                     "traces_per_s": 1e3 / float(np.median(dev)),
+                     "h2d_bytes": int(el.nbytes + wl.nbytes + w["solidT"].nbytes),
+                     "d2h_bytes": int(len(el) * 8 + c.N * 8)}
+    if cpu_baseline:
+        from oracle import oraclepy
+        k = max(1, len(el) // 16)
+        sub = w["elements"][:k]
+        t = time.perf_counter()
+        oraclepy.rad_trace((c.nx, c.ny, c.nz), (c.dx, c.ox, c.oy, c.oz), c.blocked, w["gas"], sub, w["walls"],
+                           w["solidT"])
+        ms = (time.perf_counter() - t) * 1e3 * len(el) / k
+        out["cpu_baseline"] = {"ms_per_trace": ms, "cores": 1, "kind": "port",
+                               "sample": "oracle restatement, first %d of %d elements, scaled by element count" %
+                                         (k, len(el))}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -437,6 +483,7 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=8.0, help="request arrivals per second (Poisson)")
     ap.add_argument("--serve-scale", type=float, default=0.01, help="scale of the 30-300 s simulated durations")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-radiation", action="store_true")
     ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64"],
                     help="which paths to time (the line's value is the mixed path unless only fp64 runs)")
     args = ap.parse_args()
@@ -468,6 +515,10 @@ def main():
             serving["mixed"] = measure_serving(args, _lib.PREC_MIXED)
         if args.precision in ("both", "fp64"):
             serving["fp64"] = measure_serving(args, _lib.PREC_FP64)
+
+    radiation = None
+    if rank == 0 and not args.no_radiation:
+        radiation = measure_radiation(args, not args.no_cpu_baseline)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -509,6 +560,7 @@ def main():
                 "roofline": mixed["roofline"],
                 "cpu_baseline": cpu,
                 "serving": serving,
+                "radiation_trace": radiation,
                 "clocks": mixed["clk"].summary(),
                 "kernels": [{"name": p[0], "launches": p[1], "ms": round(p[2], 4)} for p in
                             sorted(mixed["prof"], key=lambda p: -p[2])[:14]]}

@@ -253,6 +253,43 @@ size_t phx_batch_field_count(const struct phx_ctx* ctx, int scenario, int field)
 int phx_batch_get_stats(struct phx_ctx* ctx, int scenario, phx_stats* out);
 int phx_batch_set_stats(struct phx_ctx* ctx, int scenario, const phx_stats* in);
 
+/* --- radiation trace -------------------------------------------------------
+ * Replaces Solver::traceRadiation (src/sim/radiation.cpp:181-319): rays from
+ * every radiating surface element over the gas fields resident on the device,
+ * in the reference's four bands and 32 directions. The radiating elements and
+ * the wall and solid temperatures come from the host (they belong to the
+ * solid phase, src/sim/radiation.cpp:104-164 builds them); the gas fields
+ * (T, soot, H2O, CO2, background pressure, heat release, blocked cells) are
+ * the scenario's own. The FP64 context traces in FP64, the mixed context in
+ * FP32 (the reference's own precision). */
+typedef struct phx_rad_elem {
+    double o[3];          /* ray origin, m (RadElem::o) */
+    double n[3];          /* outward unit normal; unused for porous fuel */
+    double area;          /* m2 */
+    double emissivity;    /* Solver::elemEmissivity */
+    double temperature;   /* K, Solver::elemTemp */
+    int sphere;           /* porous fuel: rays over the full sphere */
+    int skip_own_cell;    /* porous fuel: the ray does not absorb in its own start cell */
+} phx_rad_elem;
+typedef struct phx_rad_wall {  /* an intact barrier (Solver::barrierOn + barrierIntact) */
+    int axis;             /* 0 x-face, 1 y-face, 2 z-face */
+    int face;             /* index into that axis' face arrays */
+    double t_lower;       /* K, surface seen from the cell below the face along the axis */
+    double t_upper;       /* K, surface seen from the cell above it */
+} phx_rad_wall;
+/* rad_abs (n_elems, W absorbed by each element) and rad_gas (cells, W gained
+ * by each gas cell; may be NULL) are host arrays. solid_t (cells, K; NULL =
+ * ambient everywhere) is the temperature a ray sees where it enters a blocked
+ * cell. At most one wall per face. Results do not depend on the order of the
+ * walls; rad_gas sums its rays' contributions in an unspecified order. */
+int phx_rad_trace(struct phx_ctx* ctx, const phx_rad_elem* elems, int n_elems, const phx_rad_wall* walls,
+                  int n_walls, const double* solid_t, double* rad_abs, double* rad_gas);
+int phx_batch_rad_trace(struct phx_ctx* ctx, int scenario, const phx_rad_elem* elems, int n_elems,
+                        const phx_rad_wall* walls, int n_walls, const double* solid_t, double* rad_abs,
+                        double* rad_gas);
+/* device time (ms, CUDA events) of the last trace's kernels on this context */
+double phx_rad_last_ms(const struct phx_ctx* ctx);
+
 /* --- process-level helpers ------------------------------------------------
  * select the CUDA device later contexts of this thread are created on */
 int phx_select_device(int device);

@@ -68,8 +68,34 @@ def load():
     L.orc_mg_levels.argtypes = [vp]
     L.orc_mg_info.argtypes = [vp, i, ctypes.c_void_p]
     L.orc_mg_get.argtypes = [vp, i, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    vpp = ctypes.c_void_p
+    L.orc_rad_trace.argtypes = [i, i, i, d, d, d, d, vpp, vpp, vpp, vpp, vpp, vpp, vpp, i, vpp, i, vpp, vpp, vpp, vpp]
     _L = L
     return L
+
+
+RAD_GAS_FIELDS = ("T", "Ys", "Yw", "Yc", "Pb", "hrr")
+
+
+def rad_trace(dims, geo, blocked, gas: dict, elements, walls, solidT):
+    """Solver::traceRadiation (src/sim/radiation.cpp:181-319) over flat inputs:
+    dims (nx, ny, nz), geo (dx, ox, oy, oz), gas fields by name (T Ys Yw Yc Pb
+    hrr), elements (n x 11), walls (m x 4), solidT (N). Returns (radAbs, radGas)."""
+    L = load()
+    nx, ny, nz = (int(v) for v in dims)
+    dx, ox, oy, oz = (float(v) for v in geo)
+    n = nx * ny * nz
+    bl = np.ascontiguousarray(blocked, np.uint8)
+    g = [np.ascontiguousarray(gas[f], np.float64) for f in RAD_GAS_FIELDS]
+    el = np.ascontiguousarray(elements, np.float64).reshape(-1, 11)
+    wl = np.ascontiguousarray(walls, np.float64).reshape(-1, 4)
+    st = np.ascontiguousarray(solidT, np.float64)
+    assert bl.size == n and st.size == n and all(a.size == n for a in g)
+    ab = np.zeros(len(el), np.float64)
+    gas_out = np.zeros(n, np.float64)
+    L.orc_rad_trace(nx, ny, nz, dx, ox, oy, oz, _ptr(bl), *[_ptr(a) for a in g], len(el), _ptr(el), len(wl),
+                    _ptr(wl), _ptr(st), _ptr(ab), _ptr(gas_out))
+    return ab, gas_out
 
 
 def _ptr(a):

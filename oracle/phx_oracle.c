@@ -1514,3 +1514,197 @@ void orc_mg_get(Orc* o, int l, int* agg, int* rowStart, int* col, double* val, d
     }
     memcpy(diag, L->diag, L->n * sizeof(double));
 }
+
+/* ------------------------------------------------------------------------
+ * Radiation trace (src/sim/radiation.cpp). Constants of :41-51; the
+ * reference's PI is the literal 3.14159265 (:44), not M_PI.
+ * ------------------------------------------------------------------------ */
+#define RAD_NB 4
+#define RAD_DIRS 32
+#define RAD_BLOCKS 24
+static const double RAD_PI = 3.14159265;
+static const double RAD_MAXLEN = 8.0, RAD_SIGMA = 5.670374e-8, RAD_T0 = 293.15;
+static const double RAD_EDGE[RAD_NB + 1] = {0.0, 2.7, 8.0, 14.0, 1e9};
+static const double RAD_LAMBDA[RAD_NB] = {1.5, 4.5, 11.0, 25.0};
+static const double RAD_GAS[RAD_NB] = {0.05, 3.0, 0.1, 6.0};
+static const double RAD_SOOT_C = 5.5, RAD_SOOT_DENSITY = 1800.0, RAD_T_FLAME = 1400.0, RAD_CHI_R = 0.35;
+
+/* fraction of blackbody emission below lambda*T (um K): Chang & Rhee series (:54-63) */
+static double rad_planck_below(double lambdaT) {
+    if (lambdaT <= 0) return 0;
+    if (lambdaT > 1e8) return 1;
+    double x = 14388.0 / lambdaT, s = 0;
+    for (int n = 1; n <= 12; ++n) {
+        double xn = x * n, dn = (double)n;
+        s += exp(-xn) / n * (x * x * x + 3 * x * x / n + 6 * x / (dn * n) + 6 / (dn * n * n));
+    }
+    double v = 1.0 - 15.0 / (RAD_PI * RAD_PI * RAD_PI * RAD_PI) * s;
+    return v < 0.0 ? 0.0 : v > 1.0 ? 1.0 : v;
+}
+static void rad_band_fractions(double T, double f[RAD_NB]) {   /* :64-71 */
+    double prev = 0;
+    for (int b = 0; b < RAD_NB; ++b) {
+        double up = b == RAD_NB - 1 ? 1.0 : rad_planck_below(RAD_EDGE[b + 1] * T);
+        f[b] = up - prev;
+        prev = up;
+    }
+}
+/* band emissive power relative to ambient, W/m2 (:73-81) */
+static void rad_band_power(double T, double out[RAD_NB]) {
+    double f0[RAD_NB], f[RAD_NB];
+    rad_band_fractions(RAD_T0, f0);
+    rad_band_fractions(T, f);
+    double a = T * T, a0 = RAD_T0 * RAD_T0;
+    for (int b = 0; b < RAD_NB; ++b) out[b] = RAD_SIGMA * (f[b] * a * a - f0[b] * a0 * a0);
+}
+
+void orc_rad_trace(int nx, int ny, int nz, double dx, double ox, double oy, double oz, const uint8_t* blocked,
+                   const double* T, const double* Ys, const double* Yw, const double* Yc, const double* Pb,
+                   const double* hrr, int nElem, const double* elem, int nWall, const double* wall,
+                   const double* solidT, double* radAbs, double* radGas) {
+    const long N = (long)nx * ny * nz;
+    const long NF[3] = {(long)(nx + 1) * ny * nz, (long)nx * (ny + 1) * nz, (long)nx * ny * (nz + 1)};
+    /* directions: golden-spiral points on the sphere (:84-96) */
+    double dir[RAD_DIRS][3];
+    const double ga = RAD_PI * (3.0 - sqrt(5.0));
+    for (int i = 0; i < RAD_DIRS; ++i) {
+        double z = 1.0 - 2.0 * (i + 0.5) / RAD_DIRS;
+        double r = sqrt(fmax(0.0, 1 - z * z));
+        dir[i][0] = r * cos(ga * i); dir[i][1] = r * sin(ga * i); dir[i][2] = z;
+    }
+    const double dW = 4.0 * RAD_PI / RAD_DIRS;
+    /* per-cell absorption coefficient and source function per band (:193-222) */
+    double* kap = calloc((size_t)N * RAD_NB, sizeof(double));
+    double* src = calloc((size_t)N * RAD_NB, sizeof(double));
+    uint8_t* flame = calloc((size_t)N, 1);
+    double fFlame[RAD_NB];
+    rad_band_fractions(RAD_T_FLAME, fFlame);
+    for (long c = 0; c < N; ++c) {
+        if (blocked[c]) continue;
+        double rho = Pb[c] / (287.0 * T[c]);
+        double fv = rho * Ys[c] / RAD_SOOT_DENSITY;
+        double pg = (Yw[c] * 28.96 / 18.02 + Yc[c] * 28.96 / 44.01) * Pb[c] / 101325.0;
+        double Eb[RAD_NB], k[RAD_NB];
+        rad_band_power(T[c], Eb);
+        double jfTot = hrr[c] > 0 ? RAD_CHI_R * hrr[c] / (4.0 * RAD_PI) : 0.0;
+        double jTot = 0;
+        for (int q = 0; q < RAD_NB; ++q) {
+            k[q] = RAD_SOOT_C * fv / (RAD_LAMBDA[q] * 1e-6) + RAD_GAS[q] * pg + 1e-4;
+            jTot += k[q] * Eb[q] / RAD_PI;
+        }
+        int fl = jfTot > jTot;
+        flame[c] = (uint8_t)fl;
+        for (int q = 0; q < RAD_NB; ++q) {
+            double j = fl ? jfTot * fFlame[q] : k[q] * Eb[q] / RAD_PI;
+            kap[c * RAD_NB + q] = k[q];
+            src[c * RAD_NB + q] = j / k[q];
+        }
+    }
+    /* wall per face (Solver::barrierOn + barrierIntact, src/sim/solver.cpp:51-62) */
+    int* wallOf[3];
+    for (int a = 0; a < 3; ++a) {
+        wallOf[a] = malloc((size_t)NF[a] * sizeof(int));
+        for (long f = 0; f < NF[a]; ++f) wallOf[a][f] = -1;
+    }
+    for (int w = 0; w < nWall; ++w) wallOf[(int)wall[4 * w]][(long)wall[4 * w + 1]] = w;
+
+    double* gb = malloc((size_t)N * sizeof(double));
+    for (long c = 0; c < N; ++c) radGas[c] = 0;
+    const int dim[3] = {nx, ny, nz};
+    for (int blk = 0; blk < RAD_BLOCKS; ++blk) {   /* :223-306 */
+        for (long c = 0; c < N; ++c) gb[c] = 0;
+        int e0 = (int)((long)nElem * blk / RAD_BLOCKS), e1 = (int)((long)nElem * (blk + 1) / RAD_BLOCKS);
+        for (int ei = e0; ei < e1; ++ei) {
+            const double* el = elem + 11 * ei;
+            const double* n = el + 3;
+            const double area = el[6], eps = el[7], temp = el[8];
+            const int sphere = el[9] != 0, skipOwn = el[10] != 0;
+            double Is[RAD_NB];
+            rad_band_power(temp, Is);
+            for (int q = 0; q < RAD_NB; ++q) Is[q] *= eps / RAD_PI;
+            double wsum = 0;
+            if (!sphere)
+                for (int d = 0; d < RAD_DIRS; ++d) {
+                    double cs = dir[d][0] * n[0] + dir[d][1] * n[1] + dir[d][2] * n[2];
+                    if (cs > 0) wsum += cs * dW;
+                }
+            double norm = sphere ? 1.0 : (wsum > 0 ? RAD_PI / wsum : 0.0);
+            double absorbed = 0;
+            for (int d = 0; d < RAD_DIRS; ++d) {
+                double w;
+                if (sphere) w = dW * 0.25 * area;
+                else {
+                    double cs = dir[d][0] * n[0] + dir[d][1] * n[1] + dir[d][2] * n[2];
+                    if (cs <= 0) continue;
+                    w = cs * dW * norm * area;
+                }
+                /* Amanatides-Woo march from the element origin */
+                double p[3] = {(el[0] - ox) / dx, (el[1] - oy) / dx, (el[2] - oz) / dx};
+                int ci[3] = {(int)floor(p[0]), (int)floor(p[1]), (int)floor(p[2])};
+                if (ci[0] < 0 || ci[1] < 0 || ci[2] < 0 || ci[0] >= nx || ci[1] >= ny || ci[2] >= nz) continue;
+                int stp[3];
+                double tMax[3], tDel[3];
+                for (int a = 0; a < 3; ++a) {
+                    double dv = dir[d][a];
+                    if (dv > 1e-9) { stp[a] = 1; tMax[a] = (ci[a] + 1 - p[a]) / dv; tDel[a] = 1 / dv; }
+                    else if (dv < -1e-9) { stp[a] = -1; tMax[a] = (p[a] - ci[a]) / -dv; tDel[a] = -1 / dv; }
+                    else { stp[a] = 0; tMax[a] = 1e30; tDel[a] = 1e30; }
+                }
+                double t = 0, tau[RAD_NB] = {1, 1, 1, 1}, I[RAD_NB] = {0, 0, 0, 0}, Iend[RAD_NB] = {0, 0, 0, 0};
+                const double tEnd = RAD_MAXLEN / dx;
+                long c = ci[0] + (long)nx * (ci[1] + (long)ny * ci[2]);
+                const long skip = skipOwn ? c : -1;
+                for (;;) {
+                    int a = tMax[0] < tMax[1] ? (tMax[0] < tMax[2] ? 0 : 2) : (tMax[1] < tMax[2] ? 1 : 2);
+                    double tn = tEnd < tMax[a] ? tEnd : tMax[a];
+                    double ds = (tn - t) * dx;
+                    if (ds > 0 && !blocked[c] && c != skip) {
+                        double g = 0;
+                        for (int q = 0; q < RAD_NB; ++q) {
+                            double x = kap[c * RAD_NB + q] * ds;
+                            double att = x < 1e-3 ? x * (1 - 0.5 * x) : 1.0 - exp(-x);
+                            double fromCell = tau[q] * src[c * RAD_NB + q] * att;
+                            I[q] += fromCell;
+                            g += Is[q] * tau[q] * att - (flame[c] ? 0.0 : eps * fromCell);
+                            tau[q] *= 1.0 - att;
+                        }
+                        gb[c] += w * g;
+                    }
+                    t = tn;
+                    if (t >= tEnd || (tau[0] < 1e-3 && tau[1] < 1e-3 && tau[2] < 1e-3 && tau[3] < 1e-3)) break;
+                    /* the face crossed: the upper face of c along a when stepping up */
+                    int up = stp[a] > 0;
+                    int fi[3] = {ci[0], ci[1], ci[2]};
+                    fi[a] += up;
+                    long f = a == 0 ? fi[0] + (long)(nx + 1) * (fi[1] + (long)ny * fi[2])
+                           : a == 1 ? fi[0] + (long)nx * (fi[1] + (long)(ny + 1) * fi[2])
+                                    : fi[0] + (long)nx * (fi[1] + (long)ny * fi[2]);
+                    int wi = wallOf[a][f];
+                    if (wi >= 0) {
+                        /* c is the lower cell of its upper face, the upper cell of its lower face */
+                        rad_band_power(wall[4 * wi + (up ? 2 : 3)], Iend);
+                        for (int q = 0; q < RAD_NB; ++q) Iend[q] *= 0.9 / RAD_PI;
+                        break;
+                    }
+                    ci[a] += stp[a];
+                    if (ci[a] < 0 || ci[a] >= dim[a]) break;
+                    long nb = ci[0] + (long)nx * (ci[1] + (long)ny * ci[2]);
+                    if (blocked[nb]) {
+                        rad_band_power(solidT[nb], Iend);
+                        for (int q = 0; q < RAD_NB; ++q) Iend[q] *= 0.9 / RAD_PI;
+                        break;
+                    }
+                    c = nb;
+                    tMax[a] += tDel[a];
+                }
+                double It = 0;
+                for (int q = 0; q < RAD_NB; ++q) It += I[q] + tau[q] * Iend[q];
+                absorbed += eps * w * It;
+            }
+            radAbs[ei] = absorbed;
+        }
+        for (long c = 0; c < N; ++c) radGas[c] += gb[c];
+    }
+    free(gb); free(kap); free(src); free(flame);
+    for (int a = 0; a < 3; ++a) free(wallOf[a]);
+}

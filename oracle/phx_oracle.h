@@ -47,6 +47,20 @@ int orc_mg_levels(Orc* o);
 void orc_mg_info(Orc* o, int l, int* info);
 void orc_mg_get(Orc* o, int l, int* agg, int* rowStart, int* col, double* val, double* diag);
 
+/* Radiation trace, Solver::traceRadiation (src/sim/radiation.cpp:181-319),
+ * over flat inputs: the gas fields it reads (N each); nElem elements of 11
+ * doubles (origin[3], normal[3], area, emissivity, temperature, sphere flag,
+ * skip-own-cell flag: porous fuel); nWall intact barriers of 4 doubles (axis,
+ * face, surface temperature seen from the lower cell, from the upper cell);
+ * solidT (N): the temperature a ray sees where it enters a blocked cell.
+ * Outputs: radAbs (nElem, W absorbed by each element), radGas (N, W gained by
+ * each gas cell). Elements run in the reference's 24 blocks, each with its own
+ * gas buffer, the buffers summed in block order. */
+void orc_rad_trace(int nx, int ny, int nz, double dx, double ox, double oy, double oz, const uint8_t* blocked,
+                   const double* T, const double* Ys, const double* Yw, const double* Yc, const double* Pb,
+                   const double* hrr, int nElem, const double* elem, int nWall, const double* wall,
+                   const double* solidT, double* radAbs, double* radGas);
+
 #ifdef __cplusplus
 }
 #endif

@@ -330,6 +330,51 @@ void ref_set_stats(void* h, const double* v) {
 // the zone tables Solver::step builds on its first call (src/sim/gasphase.cpp:111-158)
 void ref_compute_zones(void* h) { ((Ctx*)h)->s->computeZones(); }
 
+// Radiation trace inputs in the flat form the GPU trace takes
+// (src/sim/radiation.cpp:104-193): the elements buildRadElements makes, with
+// their emissivity and temperature; every intact barrier as a wall with the
+// surface temperature seen from its lower and its upper cell; the solid
+// temperature of every cell. counts = {elements, walls}.
+void ref_rad_counts(void* h, int* counts) {
+    Solver& s = *((Ctx*)h)->s;
+    s.buildRadElements();
+    int nw = 0;
+    for (int b = 0; b < (int)s.barriers.size(); ++b) nw += s.barrierIntact(b) ? 1 : 0;
+    counts[0] = (int)s.radElems_.size();
+    counts[1] = nw;
+}
+// elem: 11 per element (o[3], n[3], area, eps, temp, sphere, skip own cell);
+// wall: 4 per wall (axis, face, T seen from the lower cell, from the upper);
+// solidT: N
+void ref_rad_export(void* h, double* elem, double* wall, double* solidT) {
+    Solver& s = *((Ctx*)h)->s;
+    s.buildRadElements();
+    for (size_t e = 0; e < s.radElems_.size(); ++e) {
+        const RadElem& r = s.radElems_[e];
+        double* o = elem + 11 * e;
+        for (int q = 0; q < 3; ++q) { o[q] = r.o[q]; o[3 + q] = r.n[q]; }
+        o[6] = r.area; o[7] = s.elemEmissivity(r); o[8] = s.elemTemp(r); o[9] = r.sphere ? 1 : 0;
+        o[10] = r.kind == 2 ? 1 : 0;
+    }
+    int w = 0;
+    for (int b = 0; b < (int)s.barriers.size(); ++b) {
+        if (!s.barrierIntact(b)) continue;
+        const Barrier& br = s.barriers[b];
+        double* o = wall + 4 * w++;
+        o[0] = br.axis; o[1] = br.face;
+        o[2] = br.T[br.cellOn(0) == br.cellA ? 0 : 1];
+        o[3] = br.T[br.cellOn(0) == br.cellB ? 0 : 1];
+    }
+    for (int c = 0; c < s.N; ++c) solidT[c] = s.fuelT[c];
+}
+// Solver::traceRadiation (src/sim/radiation.cpp:181-319): radAbs per element (W), radGas per cell (W)
+void ref_rad_trace(void* h, double* radAbs, double* radGas) {
+    Solver& s = *((Ctx*)h)->s;
+    s.traceRadiation();
+    for (size_t e = 0; e < s.radAbs_.size(); ++e) radAbs[e] = s.radAbs_[e];
+    for (int c = 0; c < s.N; ++c) radGas[c] = s.radGas_[c];
+}
+
 // Solver::saveState / Solver::loadState (src/sim/state.cpp:62-195); 0 on success
 int ref_save_state(void* h, const char* path, char* err, int errLen) {
     std::string e;

@@ -67,6 +67,9 @@ def load(bits: int = 64):
     L.ref_phase_ms.restype = d
     L.ref_phase_ms.argtypes = [vp, i]
     L.ref_set_stats.argtypes = [vp, ctypes.c_void_p]
+    L.ref_rad_counts.argtypes = [vp, ctypes.c_void_p]
+    L.ref_rad_export.argtypes = [vp, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    L.ref_rad_trace.argtypes = [vp, ctypes.c_void_p, ctypes.c_void_p]
     L.ref_compute_zones.argtypes = [vp]
     L.ref_save_state.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, i]
     L.ref_load_state.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, i]
@@ -189,6 +192,29 @@ class RefSolver:
     def set_stats(self, st: dict):
         v = (ctypes.c_double * len(self._STATS))(*[float(st[k]) for k, _ in self._STATS])
         self.L.ref_set_stats(self.h, v)
+
+    def rad_inputs(self) -> dict:
+        """The radiation trace's inputs in flat form: elements (n x 11: o, n,
+        area, eps, temp, sphere, skip own cell), walls (m x 4: axis, face, T
+        from the lower cell, T from the upper cell), solidT (N)."""
+        cnt = (ctypes.c_int * 2)()
+        self.L.ref_rad_counts(self.h, cnt)
+        elem = np.zeros((cnt[0], 11), np.float64)
+        wall = np.zeros((cnt[1], 4), np.float64)
+        (nx, ny, nz, n), _ = self.grid()
+        solid = np.zeros(n, np.float64)
+        self.L.ref_rad_export(self.h, _ptr(elem), _ptr(wall), _ptr(solid))
+        return {"elements": elem, "walls": wall, "solidT": solid}
+
+    def rad_trace(self):
+        """Run Solver::traceRadiation; returns (radAbs per element, radGas per cell)."""
+        cnt = (ctypes.c_int * 2)()
+        self.L.ref_rad_counts(self.h, cnt)
+        (nx, ny, nz, n), _ = self.grid()
+        ab = np.zeros(cnt[0], np.float64)
+        gas = np.zeros(n, np.float64)
+        self.L.ref_rad_trace(self.h, _ptr(ab), _ptr(gas))
+        return ab, gas
 
     def compute_zones(self):
         self.L.ref_compute_zones(self.h)

@@ -8,6 +8,8 @@ from __future__ import annotations
 import ctypes
 import os
 
+import numpy as np
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libphx.so")
 
@@ -24,7 +26,7 @@ STAGE_ID = {n: i for i, n in enumerate(STAGES)}
 SYMBOLS = ["phx_create", "phx_destroy", "phx_last_error", "phx_last_global_error", "phx_abi_version", "phx_add_burner",
            "phx_add_ignition", "phx_step", "phx_run", "phx_stage", "phx_precondition", "phx_get_field",
            "phx_set_field", "phx_field_count", "phx_get_stats", "phx_set_scalars", "phx_set_stats", "phx_device_bytes", "phx_sync",
-           "phx_time_steps", "phx_profile_step", "phx_last_step_launches", "phx_select_device", "phx_alloc_host",
+           "phx_time_steps", "phx_profile_step", "phx_last_step_launches", "phx_rad_trace", "phx_batch_rad_trace", "phx_rad_last_ms", "phx_select_device", "phx_alloc_host",
            "phx_free_host", "phx_create_batch", "phx_batch_add", "phx_batch_remove", "phx_batch_size",
            "phx_batch_scenario_bytes", "phx_batch_add_burner", "phx_batch_step", "phx_batch_get_field",
            "phx_batch_set_field", "phx_batch_field_count", "phx_batch_get_stats", "phx_batch_set_stats", "phx_gather_stats_noalloc",
@@ -45,6 +47,37 @@ class PhxGrid(ctypes.Structure):
                 ("fx", ctypes.c_void_p), ("fy", ctypes.c_void_p), ("fz", ctypes.c_void_p),
                 ("ax", ctypes.c_void_p), ("ay", ctypes.c_void_p), ("az", ctypes.c_void_p),
                 ("lx", ctypes.c_void_p), ("ly", ctypes.c_void_p), ("lz", ctypes.c_void_p)]
+
+
+# phx_rad_elem and phx_rad_wall as numpy record types (same layout as the C structs)
+RAD_ELEM_DTYPE = np.dtype([("o", "<f8", (3,)), ("n", "<f8", (3,)), ("area", "<f8"), ("emissivity", "<f8"),
+                           ("temperature", "<f8"), ("sphere", "<i4"), ("skip_own_cell", "<i4")], align=True)
+RAD_WALL_DTYPE = np.dtype([("axis", "<i4"), ("face", "<i4"), ("t_lower", "<f8"), ("t_upper", "<f8")], align=True)
+
+
+def rad_elements(a) -> np.ndarray:
+    """phx_rad_elem records from an (n, 11) array (o, n, area, emissivity,
+    temperature, sphere, skip own cell) or records already."""
+    if isinstance(a, np.ndarray) and a.dtype == RAD_ELEM_DTYPE:
+        return np.ascontiguousarray(a)
+    a = np.asarray(a, np.float64).reshape(-1, 11)
+    r = np.zeros(len(a), RAD_ELEM_DTYPE)
+    r["o"], r["n"] = a[:, 0:3], a[:, 3:6]
+    r["area"], r["emissivity"], r["temperature"] = a[:, 6], a[:, 7], a[:, 8]
+    r["sphere"], r["skip_own_cell"] = a[:, 9].astype(np.int32), a[:, 10].astype(np.int32)
+    return r
+
+
+def rad_walls(a) -> np.ndarray:
+    """phx_rad_wall records from an (m, 4) array (axis, face, T from the lower
+    cell, T from the upper cell) or records already."""
+    if isinstance(a, np.ndarray) and a.dtype == RAD_WALL_DTYPE:
+        return np.ascontiguousarray(a)
+    a = np.asarray(a, np.float64).reshape(-1, 4)
+    r = np.zeros(len(a), RAD_WALL_DTYPE)
+    r["axis"], r["face"] = a[:, 0].astype(np.int32), a[:, 1].astype(np.int32)
+    r["t_lower"], r["t_upper"] = a[:, 2], a[:, 3]
+    return r
 
 
 class PhxStats(ctypes.Structure):
@@ -136,6 +169,10 @@ def load():
     L.phx_batch_field_count.argtypes = [vp, i, i]
     L.phx_batch_get_stats.argtypes = [vp, i, ctypes.POINTER(PhxStats)]
     L.phx_batch_set_stats.argtypes = [vp, i, ctypes.POINTER(PhxStats)]
+    L.phx_rad_trace.argtypes = [vp, vp, i, vp, i, vp, vp, vp]
+    L.phx_batch_rad_trace.argtypes = [vp, i, vp, i, vp, i, vp, vp, vp]
+    L.phx_rad_last_ms.restype = d
+    L.phx_rad_last_ms.argtypes = [vp]
     L.phx_alloc_host.restype = vp
     L.phx_alloc_host.argtypes = [sz]
     L.phx_free_host.argtypes = [vp]

@@ -145,6 +145,13 @@ def _finish(name, blocked3, fx, fy, fz, dx, origin, burners, profile, duration, 
                 burners=burners, profile=profile, duration=duration, seed=seed, radiationOn=radiationOn)
 
 
+def from_blocked(name: str, blocked3: np.ndarray, dx: float, origin=(0.0, 0.0, 0.0)) -> Case:
+    """A case of the given solid mask [nz, ny, nx] with no barriers and no
+    burners: faces open except next to solid cells and at the ground."""
+    fx, fy, fz = faces_from_blocked(blocked3)
+    return _finish(name, np.asarray(blocked3, np.uint8), fx, fy, fz, dx, origin, [], Profile.reference(), 60.0, 0)
+
+
 def single_room(peakW: float = 100e3, profile: Profile | None = None) -> Case:
     """36x24x24 cells at 0.1 m: closed box, 0.8 x 2.0 m doorway in the x = 0 wall."""
     nx, ny, nz, dx = 36, 24, 24, 0.1
@@ -323,3 +330,96 @@ def tiny_room(nx=12, ny=10, nz=9, dx=0.2, peakW=60e3, doorway=True, seed=0) -> C
     burners = [Burner((ci - 1) * dx, (cj - 1) * dx, (ci + 1) * dx, (cj + 1) * dx, 0.0, peakW)] if peakW > 0 else []
     return _finish("tiny_room_%dx%dx%d" % (nx, ny, nz), blocked, fx, fy, fz, dx, (0.0, 0.0, 0.0), burners,
                    Profile.reference(), 10.0, seed)
+
+
+def rad_workload(case: Case, seed: int = 3, wall_frac: float = 0.02, porous_frac: float = 0.01) -> dict:
+    """Seeded inputs of a radiation trace on `case`, shaped like what
+    Solver::buildRadElements and the solid phase hand the trace
+    (src/sim/radiation.cpp:104-164): a hot plume with flame cells over the
+    first burner (or the domain centre); an element on every gas-facing side
+    of every solid cell; a random share of the interior gas-gas faces as
+    intact walls, with an element on each side; a random share of the gas
+    cells as porous fuel (full-sphere elements that skip their own cell).
+    Returns the gas fields (T Ys Yw Yc Pb hrr), elements (n x 11), walls
+    (m x 4) and solidT (N)."""
+    rng = np.random.default_rng(seed)
+    nx, ny, nz, dx = case.nx, case.ny, case.nz, case.dx
+    ox, oy, oz = case.ox, case.oy, case.oz
+    b3 = case.blocked.reshape(nz, ny, nx).astype(bool)
+    k3, j3, i3 = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    xc, yc, zc = ox + (i3 + 0.5) * dx, oy + (j3 + 0.5) * dx, oz + (k3 + 0.5) * dx
+    if case.burners:
+        b = case.burners[0]
+        px, py = 0.5 * (b.x0 + b.x1), 0.5 * (b.y0 + b.y1)
+    else:
+        px, py = ox + 0.5 * nx * dx, oy + 0.5 * ny * dx
+    r2 = (xc - px) ** 2 + (yc - py) ** 2
+    plume = np.exp(-r2 / 0.5) * np.clip(1.2 - 0.25 * (zc - oz), 0.2, 1.0)
+    layer = np.clip((zc - oz - 1.2) / 1.2, 0, 1) * 0.35
+    heat = np.maximum(plume, layer)
+    T = 293.15 + 900.0 * heat
+    hrr = np.where(plume > 0.6, 2.0e6 * plume, 0.0)
+    Ys = 0.004 * heat
+    Yw = 0.0073 + 0.05 * heat
+    Yc = 0.0006 + 0.08 * heat
+    Pb = np.full(T.shape, 101325.0)
+    for a in (T, hrr, Ys, Yw, Yc):
+        a[b3] = 0.0 if a is not T else 293.15
+    gas = {"T": T.ravel(), "Ys": Ys.ravel(), "Yw": Yw.ravel(), "Yc": Yc.ravel(), "Pb": Pb.ravel(), "hrr": hrr.ravel()}
+    solidT = np.where(b3, 293.15 + 500.0 * heat + 50.0 * rng.random(b3.shape), 293.15).ravel()
+
+    elems = []
+    A = dx * dx
+    # solid cell faces seen from gas (kind 1)
+    for axis in range(3):
+        for sgn in (-1, 1):
+            sh = [0, 0, 0]
+            sh[2 - axis] = sgn
+            nb = np.zeros_like(b3)
+            src = [slice(None)] * 3
+            dst = [slice(None)] * 3
+            if sgn > 0:
+                src[2 - axis], dst[2 - axis] = slice(1, None), slice(0, -1)
+            else:
+                src[2 - axis], dst[2 - axis] = slice(0, -1), slice(1, None)
+            nbb = np.ones_like(b3)            # outside the domain counts as no gas neighbour
+            nbb[tuple(dst)] = b3[tuple(src)]
+            exposed = b3 & ~nbb
+            kk, jj, ii = np.nonzero(exposed)
+            n = np.zeros((len(kk), 3))
+            n[:, axis] = sgn
+            o = np.stack([ox + (ii + 0.5) * dx, oy + (jj + 0.5) * dx, oz + (kk + 0.5) * dx], 1) + n * (0.5 * dx + 1e-3)
+            t = solidT.reshape(nz, ny, nx)[kk, jj, ii]
+            e = np.zeros((len(kk), 11))
+            e[:, 0:3], e[:, 3:6], e[:, 6], e[:, 7], e[:, 8] = o, n, A, 0.9, t
+            elems.append(e)
+    # walls on interior gas-gas faces (kind 0 on each side)
+    walls = []
+    for axis, nf in ((0, (nz, ny, nx + 1)), (1, (nz, ny + 1, nx)), (2, (nz + 1, ny, nx))):
+        lo = [slice(None)] * 3
+        hi = [slice(None)] * 3
+        lo[2 - axis], hi[2 - axis] = slice(0, -1), slice(1, None)
+        both = ~b3[tuple(lo)] & ~b3[tuple(hi)]
+        kk, jj, ii = np.nonzero(both & (rng.random(both.shape) < wall_frac))
+        fi = [ii, jj, kk]
+        fi[axis] = fi[axis] + 1                   # the face above the lower cell
+        face = fi[0] + nf[2] * (fi[1] + nf[1] * fi[2])
+        tl = 293.15 + 600.0 * heat[kk, jj, ii] * rng.random(len(kk))
+        tu = 293.15 + 600.0 * heat[kk, jj, ii] * rng.random(len(kk))
+        walls.append(np.stack([np.full(len(kk), axis), face, tl, tu], 1))
+        for side, t in ((-1, tl), (1, tu)):
+            n = np.zeros((len(kk), 3))
+            n[:, axis] = side
+            fc = np.stack([ox + (ii + 0.5) * dx, oy + (jj + 0.5) * dx, oz + (kk + 0.5) * dx], 1)
+            fc[:, axis] += 0.5 * dx                 # the face plane
+            e = np.zeros((len(kk), 11))
+            e[:, 0:3], e[:, 3:6], e[:, 6], e[:, 7], e[:, 8] = fc + n * 1e-3, n, A, 0.85, t
+            elems.append(e)
+    # porous fuel in gas cells (kind 2)
+    kk, jj, ii = np.nonzero(~b3 & (rng.random(b3.shape) < porous_frac))
+    e = np.zeros((len(kk), 11))
+    e[:, 0:3] = np.stack([ox + (ii + 0.5) * dx, oy + (jj + 0.5) * dx, oz + (kk + 0.5) * dx], 1)
+    e[:, 6] = np.minimum(rng.uniform(0.2, 8.0, len(kk)) * A, 4 * A)
+    e[:, 7], e[:, 8], e[:, 9], e[:, 10] = 0.8, T[kk, jj, ii], 1, 1
+    elems.append(e)
+    return {"gas": gas, "elements": np.concatenate(elems), "walls": np.concatenate(walls), "solidT": solidT}

@@ -205,6 +205,18 @@ int phx_profile_step(phx_ctx* c, double dt_max, int flush_l2, phx_kernel_time* o
 
 int phx_last_step_launches(const phx_ctx* c) { return c && c->impl ? c->impl->lastLaunches() : 0; }
 
+int phx_batch_rad_trace(phx_ctx* c, int s, const phx_rad_elem* elems, int n_elems, const phx_rad_wall* walls,
+                        int n_walls, const double* solid_t, double* rad_abs, double* rad_gas) {
+    return guarded(c, [&](phx::CtxBase* x) {
+        return x->radTrace(s, elems, n_elems, walls, n_walls, solid_t, rad_abs, rad_gas);
+    });
+}
+int phx_rad_trace(phx_ctx* c, const phx_rad_elem* elems, int n_elems, const phx_rad_wall* walls, int n_walls,
+                  const double* solid_t, double* rad_abs, double* rad_gas) {
+    return phx_batch_rad_trace(c, 0, elems, n_elems, walls, n_walls, solid_t, rad_abs, rad_gas);
+}
+double phx_rad_last_ms(const phx_ctx* c) { return c && c->impl ? c->impl->radLastMs() : 0.0; }
+
 int phx_gather_stats_noalloc(phx_ctx* c, int scenario, phx_stats* out) {
     if (!out) return fail(c, PHX_ERR_INVALID, "null stats");
     return guarded(c, [&](phx::CtxBase* x) { return phx::gatherStatsNoAlloc(x, c->precision, scenario, out, x->err); });

@@ -19,6 +19,7 @@
 #include "engine.h"
 #include "host_setup.h"
 #include "mixed_kernels.cuh"
+#include "radiation.cuh"
 #include "rowblock.cuh"
 
 namespace phx {
@@ -393,8 +394,24 @@ public:
     int launches = 0;
     cudaEvent_t ev[4] = {};
 
+    // radiation trace work space, grown on demand (traces are seconds of
+    // simulated time apart)
+    struct RadWork {
+        enum { EL, WL, WALLI, ABS, WALLOF, CELLS, FLAGS, SOLIDT, GAS, KC, NBUF };
+        void* buf[NBUF] = {};
+        size_t cap[NBUF] = {};
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        double lastMs = 0;
+        void release() {
+            for (void* p : buf) if (p) cudaFree(p);
+            if (e0) cudaEventDestroy(e0);
+            if (e1) cudaEventDestroy(e1);
+        }
+    } rad;
+
     ~Ctx() override {
         if (st) cudaStreamSynchronize(st);
+        rad.release();
         destroyGraph();
         sc.clear();
         if (tab) cudaFree(tab);
@@ -447,6 +464,106 @@ public:
         return PHX_OK;
     }
     void discard(void* prepared) override { delete static_cast<Scenario<R>*>(prepared); }
+    // Solver::traceRadiation (src/sim/radiation.cpp:181-319) for scenario s
+    int radTrace(int s, const phx_rad_elem* el, int nE, const phx_rad_wall* wl, int nW, const double* solidT,
+                 double* radAbs, double* radGas) override {
+        PHX_TRY(checkScn(s));
+        if (nE < 0 || nW < 0 || (nE > 0 && (!el || !radAbs)) || (nW > 0 && !wl)) {
+            err = "invalid radiation trace arguments";
+            return PHX_ERR_INVALID;
+        }
+        const Scenario<R>& S = *sc[s];
+        const int nx = S.geo.nx, ny = S.geo.ny, nz = S.geo.nz;
+        const size_t N = (size_t)nx * ny * nz;
+        const size_t NF[3] = {(size_t)(nx + 1) * ny * nz, (size_t)nx * (ny + 1) * nz, (size_t)nx * ny * (nz + 1)};
+        {   // at most one wall per face, every face in range
+            std::vector<size_t> key(nW);
+            for (int w = 0; w < nW; ++w) {
+                if (wl[w].axis < 0 || wl[w].axis > 2 || wl[w].face < 0 || (size_t)wl[w].face >= NF[wl[w].axis]) {
+                    err = "radiation wall " + std::to_string(w) + ": axis or face out of range";
+                    return PHX_ERR_INVALID;
+                }
+                key[w] = (wl[w].axis == 0 ? 0 : wl[w].axis == 1 ? NF[0] : NF[0] + NF[1]) + (size_t)wl[w].face;
+            }
+            std::sort(key.begin(), key.end());
+            for (int w = 1; w < nW; ++w)
+                if (key[w] == key[w - 1]) { err = "two radiation walls on one face"; return PHX_ERR_INVALID; }
+        }
+        PHX_TRY(ensureTables());
+        PHX_TRY(initStream());
+        // buffer b holds at least `bytes` (device memory is allocated here only)
+        auto grow = [&](int b, size_t bytes) -> int {
+            bytes = std::max<size_t>(bytes, 16);
+            if (rad.buf[b] && rad.cap[b] >= bytes) return PHX_OK;
+            if (rad.buf[b]) { PHX_CK(cudaStreamSynchronize(st)); cudaFree(rad.buf[b]); rad.buf[b] = nullptr; rad.cap[b] = 0; }
+            if (cudaMalloc(&rad.buf[b], bytes) != cudaSuccess) {
+                cudaGetLastError();
+                rad.buf[b] = nullptr;
+                err = "out of device memory for the radiation trace";
+                return PHX_ERR_OOM;
+            }
+            rad.cap[b] = bytes;
+            return PHX_OK;
+        };
+        const size_t nF = NF[0] + NF[1] + NF[2];
+        PHX_TRY(grow(RadWork::EL, nE * sizeof(phx_rad_elem)));
+        PHX_TRY(grow(RadWork::ABS, nE * sizeof(double)));
+        PHX_TRY(grow(RadWork::WL, nW * sizeof(phx_rad_wall)));
+        PHX_TRY(grow(RadWork::WALLI, nW * 8 * sizeof(R)));
+        PHX_TRY(grow(RadWork::WALLOF, nF * sizeof(int)));
+        PHX_TRY(grow(RadWork::CELLS, N * sizeof(RadCell<R>)));
+        PHX_TRY(grow(RadWork::FLAGS, N));
+        PHX_TRY(grow(RadWork::SOLIDT, N * sizeof(double)));
+        PHX_TRY(grow(RadWork::GAS, N * sizeof(R)));
+        PHX_TRY(grow(RadWork::KC, sizeof(RadConst<R>)));
+        if (!rad.e0) {
+            PHX_CK(cudaEventCreate(&rad.e0));
+            PHX_CK(cudaEventCreate(&rad.e1));
+        }
+        phx_rad_elem* dEl = static_cast<phx_rad_elem*>(rad.buf[RadWork::EL]);
+        phx_rad_wall* dWl = static_cast<phx_rad_wall*>(rad.buf[RadWork::WL]);
+        R* dWallI = static_cast<R*>(rad.buf[RadWork::WALLI]);
+        double* dAbs = static_cast<double*>(rad.buf[RadWork::ABS]);
+        int* dWallOf = static_cast<int*>(rad.buf[RadWork::WALLOF]);
+        RadCell<R>* dCells = static_cast<RadCell<R>*>(rad.buf[RadWork::CELLS]);
+        uint8_t* dFlags = static_cast<uint8_t*>(rad.buf[RadWork::FLAGS]);
+        double* dSolid = static_cast<double*>(rad.buf[RadWork::SOLIDT]);
+        R* dGas = static_cast<R*>(rad.buf[RadWork::GAS]);
+        RadConst<R>* dKc = static_cast<RadConst<R>*>(rad.buf[RadWork::KC]);
+        if (nE) PHX_CK(cudaMemcpyAsync(dEl, el, nE * sizeof(phx_rad_elem), cudaMemcpyHostToDevice, st));
+        if (nW) PHX_CK(cudaMemcpyAsync(dWl, wl, nW * sizeof(phx_rad_wall), cudaMemcpyHostToDevice, st));
+        if (solidT) PHX_CK(cudaMemcpyAsync(dSolid, solidT, N * sizeof(double), cudaMemcpyHostToDevice, st));
+        PHX_CK(cudaMemsetAsync(dWallOf, 0xff, nF * sizeof(int), st));
+        PHX_CK(cudaMemsetAsync(dGas, 0, N * sizeof(R), st));
+        PHX_CK(cudaEventRecord(rad.e0, st));
+        k_rad_setup<R><<<1, 32, 0, st>>>(dKc);
+        if (nW) k_rad_walls<R><<<(nW + 127) / 128, 128, 0, st>>>(dWl, nW, (int)NF[0], (int)NF[1], dWallOf, dWallI, dKc);
+        k_rad_cells<R><<<(unsigned)((N + 255) / 256), 256, 0, st>>>(dS, s, solidT ? dSolid : nullptr, dCells, dFlags,
+                                                                    dKc);
+        if (nE)
+            k_rad_trace<R><<<(nE + RAD_WARPS - 1) / RAD_WARPS, RAD_WARPS * 32, 0, st>>>(
+                dS, s, dEl, nE, dCells, dFlags, dWallOf, dWallI, dKc, dGas, dAbs);
+        PHX_CK(cudaGetLastError());
+        PHX_CK(cudaEventRecord(rad.e1, st));
+        if (nE) PHX_CK(cudaMemcpyAsync(radAbs, dAbs, nE * sizeof(double), cudaMemcpyDeviceToHost, st));
+        std::vector<R> gasHost;
+        if (radGas) {
+            if (std::is_same<R, double>::value)
+                PHX_CK(cudaMemcpyAsync(radGas, dGas, N * sizeof(double), cudaMemcpyDeviceToHost, st));
+            else {
+                gasHost.resize(N);
+                PHX_CK(cudaMemcpyAsync(gasHost.data(), dGas, N * sizeof(R), cudaMemcpyDeviceToHost, st));
+            }
+        }
+        PHX_CK(cudaStreamSynchronize(st));
+        if (!gasHost.empty()) for (size_t c = 0; c < N; ++c) radGas[c] = (double)gasHost[c];
+        float ms = 0;
+        PHX_CK(cudaEventElapsedTime(&ms, rad.e0, rad.e1));
+        rad.lastMs = ms;
+        return checkDeviceError();
+    }
+    double radLastMs() const override { return rad.lastMs; }
+
     int readTimes(double* out) override {
         const int n = nscn();
         if (n == 0) return PHX_OK;

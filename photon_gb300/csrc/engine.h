@@ -48,6 +48,9 @@ public:
     virtual void discard(void* prepared) = 0;
     // simulated time of every scenario, one read-back for the batch
     virtual int readTimes(double* out) = 0;
+    virtual int radTrace(int s, const phx_rad_elem* el, int nE, const phx_rad_wall* wl, int nW, const double* solidT,
+                         double* radAbs, double* radGas) = 0;
+    virtual double radLastMs() const = 0;
     std::string err;
 };
 

@@ -152,6 +152,28 @@ class Solver:
             self.set(f, host.get(f))
         self.set_stats(host.stats())
 
+    def rad_trace(self, elements, walls, solid_t=None, gas: bool = True):
+        """Solver::traceRadiation (src/sim/radiation.cpp:181-319) on the GPU over
+        this context's gas fields: elements (phx_rad_elem records or an (n, 11)
+        array), walls (phx_rad_wall records or an (m, 4) array), solid_t (N, K,
+        or None for ambient). Returns (radAbs per element, radGas per cell or
+        None); rad_last_ms() is the device time of its kernels."""
+        el, wl = _lib.rad_elements(elements), _lib.rad_walls(walls)
+        n = len(self.get("T"))
+        st = None if solid_t is None else np.ascontiguousarray(solid_t, np.float64)
+        if st is not None and st.size != n:
+            raise PhxError(_lib.PHX_ERR_INVALID, "solid_t needs one value per cell")
+        ab = np.zeros(len(el), np.float64)
+        g = np.zeros(n, np.float64) if gas else None
+        self._check(self.L.phx_rad_trace(self.h, el.ctypes.data if len(el) else None, len(el),
+                                         wl.ctypes.data if len(wl) else None, len(wl),
+                                         None if st is None else st.ctypes.data, ab.ctypes.data,
+                                         None if g is None else g.ctypes.data))
+        return ab, g
+
+    def rad_last_ms(self) -> float:
+        return float(self.L.phx_rad_last_ms(self.h))
+
     def device_bytes(self) -> int:
         return int(self.L.phx_device_bytes(self.h))
 

@@ -9,7 +9,9 @@ import pytest
 from oracle.oraclepy import OracleSolver
 from photon_gb300 import casegen
 
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+# the step fixtures (rad_*.npz hold the radiation trace's, tests/test_oracle_rad.py)
+GOLDEN = sorted(p for p in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz"))
+                if not os.path.basename(p).startswith("rad_"))
 
 
 def case_from_golden(g):
