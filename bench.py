@@ -470,6 +470,48 @@ def measure_radiation(args, cpu_baseline: bool):
     return out
 
 
+def measure_volume(args, cpu_baseline: bool):
+    """The headless smoke and flame render (phx_vol_render; the viewer's
+    VOL_FS shader) of the 1.32 M-cell house with the synthetic trace fields at
+    1280x720: device time (CUDA events) and the end-to-end call; the oracle's
+    C restatement of the shader on a band of rows as the CPU baseline."""
+    from photon_gb300 import _lib, casegen, render
+    from photon_gb300.solver import Solver
+    c = casegen.house_fine(1)
+    w = casegen.rad_workload(c)
+    g = Solver(c, _lib.PREC_MIXED)
+    gas = dict(w["gas"])
+    gas["Ys"] = gas["Ys"] * 0.01
+    for f, a in gas.items():
+        g.set(f, a)
+    g.set("Ya", 0.5 * gas["Ys"])
+    cx, cy = c.ox + c.nx * c.dx / 2, c.oy + c.ny * c.dx / 2
+    p = render.camera(c, eye=(cx - 14, cy - 16, 9.0), target=(cx, cy, 2.0), width=1280, height=720,
+                      lights=render.fire_lights(c, gas["hrr"]), slice_z=1.5)
+    for _ in range(max(3, args.warmup)):
+        g.vol_render(p)
+    dev, wall = [], []
+    for _ in range(10):
+        t = time.perf_counter()
+        g.vol_render(p)
+        wall.append((time.perf_counter() - t) * 1e3)
+        dev.append(g.vol_last_ms())
+    out = {"workload": "house %dx%dx%d at %.1f m, 1280x720, smoke + fire + slice, step 0.3 dx" % (
+        c.nx, c.ny, c.nz, c.dx), "device_ms": float(np.median(dev)), "e2e_ms": float(np.median(wall)),
+        "frames_per_s": 1e3 / float(np.median(dev)), "d2h_bytes": 1280 * 720 * 12}
+    if cpu_baseline:
+        from oracle import oraclepy
+        vol = oraclepy.pack_volume(c.blocked, g.get("T"), g.get("Ys"), g.get("Ya"), g.get("Pb"), g.get("hrr"))
+        r0, r1 = 360 - 24, 360 + 24
+        t = time.perf_counter()
+        oraclepy.vol_render(c, vol, p, rows=(r0, r1))
+        out["cpu_baseline"] = {"ms_per_frame": (time.perf_counter() - t) * 1e3 * 720 / (r1 - r0), "cores": 1,
+                               "kind": "port", "sample": "oracle restatement of the shader, rows %d-%d of 720, "
+                                                         "scaled by row count" % (r0, r1)}
+    g.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -516,9 +558,10 @@ def main():
         if args.precision in ("both", "fp64"):
             serving["fp64"] = measure_serving(args, _lib.PREC_FP64)
 
-    radiation = None
+    radiation = volume = None
     if rank == 0 and not args.no_radiation:
         radiation = measure_radiation(args, not args.no_cpu_baseline)
+        volume = measure_volume(args, not args.no_cpu_baseline)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -561,6 +604,7 @@ def main():
                 "cpu_baseline": cpu,
                 "serving": serving,
                 "radiation_trace": radiation,
+                "volume_render": volume,
                 "clocks": mixed["clk"].summary(),
                 "kernels": [{"name": p[0], "launches": p[1], "ms": round(p[2], 4)} for p in
                             sorted(mixed["prof"], key=lambda p: -p[2])[:14]]}

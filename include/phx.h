@@ -290,6 +290,35 @@ int phx_batch_rad_trace(struct phx_ctx* ctx, int scenario, const phx_rad_elem* e
 /* device time (ms, CUDA events) of the last trace's kernels on this context */
 double phx_rad_last_ms(const struct phx_ctx* ctx);
 
+/* --- smoke and flame volume render --------------------------------------------
+ * The viewer's volume ray march (the VOL_FS shader, src/render/renderer.cpp:
+ * 119-283, over the volume Viewer::uploadVolume packs, src/app/viewer.cpp:
+ * 941-949) into a host RGB image, without a window or GL. The members mirror
+ * the shader's uniforms; the volume box is the scenario's grid. */
+typedef struct phx_vol_params {
+    int width, height;        /* pixels */
+    float inv_vp[16];         /* inverse view-projection matrix, column-major (uInvVP) */
+    float eye[3];             /* camera position, m (uEye) */
+    float step;               /* march step, m (uStep; the viewer uses 0.3 dx) */
+    float clip_z;             /* cut-away height, m (uClipZ) */
+    float slice_z;            /* temperature slice plane height, m (uSliceZ) */
+    float t_min, t_max;       /* slice colour range, K (uTMin, uTMax) */
+    int smoke, slice, fire;   /* switches (uSmoke, uSlice, uFire) */
+    float time;               /* s, animates the display-only noise (uTime) */
+    float smoke_scale;        /* uSmokeScale */
+    float sun_dir[3];         /* unit vector towards the sun (uSunDir) */
+    int n_lights;             /* fire lights in use, 0-8 (uNumLights) */
+    float lights[8][4];       /* x, y, z, intensity (uLights) */
+    float background[3];      /* colour of the scene behind the volume (uColor) */
+} phx_vol_params;
+/* rgb: width*height*3 floats, rows from the bottom (GL window order). depth:
+ * width*height scene depths in [0, 1] (uDepth), or NULL for no scene. */
+int phx_vol_render(struct phx_ctx* ctx, const phx_vol_params* params, const float* depth, float* rgb);
+int phx_batch_vol_render(struct phx_ctx* ctx, int scenario, const phx_vol_params* params, const float* depth,
+                         float* rgb);
+/* device time (ms, CUDA events) of the last render's kernels on this context */
+double phx_vol_last_ms(const struct phx_ctx* ctx);
+
 /* --- process-level helpers ------------------------------------------------
  * select the CUDA device later contexts of this thread are created on */
 int phx_select_device(int device);

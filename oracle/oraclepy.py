@@ -70,6 +70,8 @@ def load():
     L.orc_mg_get.argtypes = [vp, i, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     vpp = ctypes.c_void_p
     L.orc_rad_trace.argtypes = [i, i, i, d, d, d, d, vpp, vpp, vpp, vpp, vpp, vpp, vpp, i, vpp, i, vpp, vpp, vpp, vpp]
+    L.orc_vol_render.argtypes = [i, i, i, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, vpp, vpp,
+                                 vpp, vpp, i, i]
     _L = L
     return L
 
@@ -96,6 +98,31 @@ def rad_trace(dims, geo, blocked, gas: dict, elements, walls, solidT):
     L.orc_rad_trace(nx, ny, nz, dx, ox, oy, oz, _ptr(bl), *[_ptr(a) for a in g], len(el), _ptr(el), len(wl),
                     _ptr(wl), _ptr(st), _ptr(ab), _ptr(gas_out))
     return ab, gas_out
+
+
+def vol_render(case, vol: np.ndarray, params, depth=None, rows=None) -> np.ndarray:
+    """The viewer's volume shader restated in C (orc_vol_render) over vol
+    (N x 4 float32: soot density, aerosol density, T, heat release) with the
+    uniforms of a photon_gb300._lib.PhxVolParams. rows: (first, end) to render
+    a band of rows (the rest stays 0). Returns (height, width, 3) float32."""
+    L = load()
+    v = np.ascontiguousarray(vol, np.float32).reshape(-1, 4)
+    rgb = np.zeros((params.height, params.width, 3), np.float32)
+    d = None if depth is None else np.ascontiguousarray(depth, np.float32)
+    r0, r1 = rows if rows else (0, params.height)
+    L.orc_vol_render(case.nx, case.ny, case.nz, float(case.dx), float(case.ox), float(case.oy), float(case.oz),
+                     _ptr(v), ctypes.byref(params), None if d is None else _ptr(d), _ptr(rgb), int(r0), int(r1))
+    return rgb
+
+
+def pack_volume(blocked, T, Ys, Ya, Pb, hrr) -> np.ndarray:
+    """Viewer::uploadVolume's packing (src/app/viewer.cpp:941-949) in FP32."""
+    T32 = np.asarray(T).astype(np.float32)
+    rho = np.asarray(Pb).astype(np.float32) / (np.float32(287.0) * T32)
+    v = np.stack([np.asarray(Ys).astype(np.float32) * rho, np.asarray(Ya).astype(np.float32) * rho, T32,
+                  np.asarray(hrr).astype(np.float32)], 1)
+    v[np.asarray(blocked) != 0] = 0
+    return v
 
 
 def _ptr(a):

@@ -1708,3 +1708,216 @@ void orc_rad_trace(int nx, int ny, int nz, double dx, double ox, double oy, doub
     free(gb); free(kap); free(src); free(flame);
     for (int a = 0; a < 3; ++a) free(wallOf[a]);
 }
+
+/* ------------------------------------------------------------------------
+ * Volume ray march of the viewer (src/render/renderer.cpp:119-283) in FP32.
+ * GLSL built-ins follow the GLSL 3.30 definitions (mix = x(1-a) + ya,
+ * smoothstep, fract = x - floor x); the 3D texture is sampled with linear
+ * filtering and clamp-to-edge addressing (src/render/renderer.cpp:406-413).
+ * ------------------------------------------------------------------------ */
+typedef struct { float x, y, z; } ov3;
+static ov3 o3(float a, float b, float c) { ov3 r = {a, b, c}; return r; }
+static ov3 oadd(ov3 a, ov3 b) { return o3(a.x + b.x, a.y + b.y, a.z + b.z); }
+static ov3 osub(ov3 a, ov3 b) { return o3(a.x - b.x, a.y - b.y, a.z - b.z); }
+static ov3 omul(ov3 a, float s) { return o3(a.x * s, a.y * s, a.z * s); }
+static ov3 omulv(ov3 a, ov3 b) { return o3(a.x * b.x, a.y * b.y, a.z * b.z); }
+static float odot(ov3 a, ov3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static float ofract(float x) { return x - floorf(x); }
+static float oclamp(float x, float a, float b) { return fminf(fmaxf(x, a), b); }
+static float omix(float a, float b, float t) { return a * (1.0f - t) + b * t; }
+static ov3 omix3(ov3 a, ov3 b, float t) { return oadd(omul(a, 1.0f - t), omul(b, t)); }
+static float osmooth(float e0, float e1, float x) {
+    float t = oclamp((x - e0) / (e1 - e0), 0.0f, 1.0f);
+    return t * t * (3.0f - 2.0f * t);
+}
+static ov3 oheatmap(float t) {
+    t = oclamp(t, 0.0f, 1.0f);
+    ov3 c0 = o3(0.10f, 0.15f, 0.55f), c1 = o3(0.10f, 0.65f, 0.85f), c2 = o3(0.95f, 0.90f, 0.20f),
+        c3 = o3(0.95f, 0.35f, 0.05f), c4 = o3(0.85f, 0.05f, 0.05f);
+    if (t < 0.25f) return omix3(c0, c1, t / 0.25f);
+    if (t < 0.5f) return omix3(c1, c2, (t - 0.25f) / 0.25f);
+    if (t < 0.75f) return omix3(c2, c3, (t - 0.5f) / 0.25f);
+    return omix3(c3, c4, (t - 0.75f) / 0.25f);
+}
+static ov3 oglow(float T) {
+    float t = oclamp((T - 700.0f) / 1000.0f, 0.0f, 1.0f);
+    return omul(omul(o3(1.0f, 0.22f + 0.6f * t, 0.04f + 0.45f * t * t), t), t);
+}
+static float ohash2(float px, float py) { return ofract(sinf(px * 12.9898f + py * 78.233f) * 43758.5453f); }
+static float ohash3(ov3 p) {
+    p = o3(ofract(p.x * 0.3183099f + 0.1f), ofract(p.y * 0.3183099f + 0.1f), ofract(p.z * 0.3183099f + 0.1f));
+    p = omul(p, 17.0f);
+    return ofract(p.x * p.y * p.z * (p.x + p.y + p.z));
+}
+static float onoise(ov3 x) {
+    ov3 i = o3(floorf(x.x), floorf(x.y), floorf(x.z));
+    ov3 f = o3(ofract(x.x), ofract(x.y), ofract(x.z));
+    f = o3(f.x * f.x * (3.0f - 2.0f * f.x), f.y * f.y * (3.0f - 2.0f * f.y), f.z * f.z * (3.0f - 2.0f * f.z));
+    float a = omix(omix(ohash3(i), ohash3(oadd(i, o3(1, 0, 0))), f.x),
+                   omix(ohash3(oadd(i, o3(0, 1, 0))), ohash3(oadd(i, o3(1, 1, 0))), f.x), f.y);
+    float b = omix(omix(ohash3(oadd(i, o3(0, 0, 1))), ohash3(oadd(i, o3(1, 0, 1))), f.x),
+                   omix(ohash3(oadd(i, o3(0, 1, 1))), ohash3(oadd(i, o3(1, 1, 1))), f.x), f.y);
+    return omix(a, b, f.z);
+}
+static float oflame_noise(ov3 p, float time) {
+    ov3 q = osub(omulv(p, o3(5.0f, 5.0f, 2.6f)), o3(0.0f, 0.0f, time * 3.2f));
+    return 0.55f * onoise(q) + 0.30f * onoise(oadd(omul(q, 2.1f), o3(0.0f, 0.0f, -time * 2.0f))) +
+           0.15f * onoise(omul(q, 4.3f));
+}
+static float osmoke_noise(ov3 p, float time) {
+    ov3 q = osub(omul(p, 1.6f), o3(0.0f, 0.0f, time * 0.35f));
+    ov3 w = o3(onoise(oadd(q, o3(5.2f, 1.3f, 0.0f))), onoise(oadd(q, o3(1.7f, 9.2f, 3.1f))),
+               onoise(oadd(q, o3(8.3f, 2.8f, 4.7f))));
+    q = oadd(q, osub(omul(w, 0.6f), o3(0.3f, 0.3f, 0.3f)));
+    float n = 0.5f * onoise(q) + 0.3f * onoise(oadd(omul(q, 2.03f), o3(1.7f, 1.7f, 1.7f))) +
+              0.2f * onoise(oadd(omul(q, 4.1f), o3(3.3f, 3.3f, 3.3f)));
+    return osmooth(0.2f, 0.8f, n);
+}
+static ov3 oflame_color(float k) {
+    return omix3(omix3(o3(0.9f, 0.18f, 0.02f), o3(1.0f, 0.5f, 0.08f), osmooth(0.0f, 0.4f, k)), o3(1.0f, 0.9f, 0.55f),
+                 osmooth(0.45f, 1.0f, k));
+}
+typedef struct { const float* vol; int nx, ny, nz; ov3 bmin, bmax; } OVol;
+static void osample(const OVol* G, ov3 p, float out[4]) {
+    ov3 u = o3((p.x - G->bmin.x) / (G->bmax.x - G->bmin.x), (p.y - G->bmin.y) / (G->bmax.y - G->bmin.y),
+               (p.z - G->bmin.z) / (G->bmax.z - G->bmin.z));
+    float x = u.x * G->nx - 0.5f, y = u.y * G->ny - 0.5f, z = u.z * G->nz - 0.5f;
+    float fx = floorf(x), fy = floorf(y), fz = floorf(z);
+    float ax = x - fx, ay = y - fy, az = z - fz;
+    int i0 = (int)fmaxf(fminf(fx, (float)(G->nx - 1)), 0.0f), i1 = (int)fmaxf(fminf(fx + 1.0f, (float)(G->nx - 1)), 0.0f);
+    int j0 = (int)fmaxf(fminf(fy, (float)(G->ny - 1)), 0.0f), j1 = (int)fmaxf(fminf(fy + 1.0f, (float)(G->ny - 1)), 0.0f);
+    int k0 = (int)fmaxf(fminf(fz, (float)(G->nz - 1)), 0.0f), k1 = (int)fmaxf(fminf(fz + 1.0f, (float)(G->nz - 1)), 0.0f);
+#define OAT(i, j, k) (G->vol + 4 * ((size_t)(i) + (size_t)G->nx * ((size_t)(j) + (size_t)G->ny * (size_t)(k))))
+    for (int q = 0; q < 4; ++q) {
+        float c00 = OAT(i0, j0, k0)[q] * (1.0f - ax) + OAT(i1, j0, k0)[q] * ax;
+        float c10 = OAT(i0, j1, k0)[q] * (1.0f - ax) + OAT(i1, j1, k0)[q] * ax;
+        float c01 = OAT(i0, j0, k1)[q] * (1.0f - ax) + OAT(i1, j0, k1)[q] * ax;
+        float c11 = OAT(i0, j1, k1)[q] * (1.0f - ax) + OAT(i1, j1, k1)[q] * ax;
+        float a = c00 * (1.0f - ay) + c10 * ay, b = c01 * (1.0f - ay) + c11 * ay;
+        out[q] = a * (1.0f - az) + b * az;
+    }
+#undef OAT
+}
+
+/* the temperature slice where the ray crosses uSliceZ */
+static void oslice(const OVol* G, const orc_vol_params* P, ov3 ro, ov3 rd, float tS, ov3* col, float* tr) {
+    float sv[4];
+    osample(G, oadd(ro, omul(rd, tS)), sv);
+    if (sv[2] > 150.0f) {
+        float tn = (sv[2] - P->t_min) / (P->t_max - P->t_min);
+        float sa = omix(0.12f, 0.88f, osmooth(0.0f, 0.2f, tn));
+        *col = oadd(*col, omul(oheatmap(tn), *tr * sa));
+        *tr *= 1.0f - sa;
+    }
+}
+
+void orc_vol_render(int nx, int ny, int nz, float dx, float ox, float oy, float oz, const float* vol,
+                    const orc_vol_params* P, const float* depth, float* rgb, int row0, int row1) {
+    OVol G = {vol, nx, ny, nz, o3(ox, oy, oz), o3(ox + nx * dx, oy + ny * dx, oz + nz * dx)};
+    const float* M = P->inv_vp;
+    for (int py = row0; py < row1; ++py)
+        for (int px = 0; px < P->width; ++px) {
+            float uvx = (px + 0.5f) / P->width, uvy = (py + 0.5f) / P->height;
+            float wa = uvx * 2.0f - 1.0f, wb = uvy * 2.0f - 1.0f;
+#define OWORLD(dd, out)                                                                   \
+    do {                                                                                  \
+        float c_ = (dd) * 2.0f - 1.0f;                                                    \
+        float X_ = M[0] * wa + M[4] * wb + M[8] * c_ + M[12], Y_ = M[1] * wa + M[5] * wb + M[9] * c_ + M[13]; \
+        float Z_ = M[2] * wa + M[6] * wb + M[10] * c_ + M[14], W_ = M[3] * wa + M[7] * wb + M[11] * c_ + M[15]; \
+        out = o3(X_ / W_, Y_ / W_, Z_ / W_);                                              \
+    } while (0)
+            ov3 base = o3(P->background[0], P->background[1], P->background[2]);
+            float d = depth ? depth[(size_t)py * P->width + px] : 1.0f;
+            ov3 ro = o3(P->eye[0], P->eye[1], P->eye[2]), far_, wd;
+            OWORLD(1.0f, far_);
+            ov3 rd = osub(far_, ro);
+            rd = omul(rd, 1.0f / sqrtf(odot(rd, rd)));
+            float tScene = 1e9f;
+            if (d < 1.0f) { OWORLD(d, wd); ov3 e = osub(wd, ro); tScene = sqrtf(odot(e, e)); }
+#undef OWORLD
+            ov3 bmax = o3(G.bmax.x, G.bmax.y, fminf(G.bmax.z, P->clip_z));
+            ov3 inv = o3(1.0f / rd.x, 1.0f / rd.y, 1.0f / rd.z);
+            ov3 ta = omulv(osub(G.bmin, ro), inv), tb = omulv(osub(bmax, ro), inv);
+            ov3 tmn = o3(fminf(ta.x, tb.x), fminf(ta.y, tb.y), fminf(ta.z, tb.z));
+            ov3 tmx = o3(fmaxf(ta.x, tb.x), fmaxf(ta.y, tb.y), fmaxf(ta.z, tb.z));
+            float t0 = fmaxf(fmaxf(fmaxf(tmn.x, tmn.y), tmn.z), 0.0f);
+            float t1 = fminf(fminf(tmx.x, tmx.y), tmx.z);
+            float tEnd = fminf(t1, tScene);
+            ov3 col = o3(0, 0, 0);
+            float tr = 1.0f;
+            float tS = (P->slice_z - ro.z) / rd.z;
+            int sliceHit = P->slice == 1 && tS > t0 && tS < tEnd && P->slice_z < bmax.z;
+            ov3 sun = o3(P->sun_dir[0], P->sun_dir[1], P->sun_dir[2]);
+            int sliceDone = !sliceHit;
+            if (t0 < tEnd) {
+                float ds = P->step;
+                float jit = ohash2(px + 0.5f, py + 0.5f);
+                int n = (int)fminf(600.0f, (tEnd - t0) / ds + 1.0f);
+                for (int i = 0; i < n; ++i) {
+                    float t = t0 + ((float)i + jit) * ds;
+                    if (t > tEnd) break;
+                    if (!sliceDone && t >= tS) {
+                        oslice(&G, P, ro, rd, tS, &col, &tr);
+                        sliceDone = 1;
+                    }
+                    if (P->smoke == 0 && P->fire == 0) continue;
+                    ov3 p = oadd(ro, omul(rd, t));
+                    float v[4];
+                    osample(&G, p, v);
+                    float soot = fmaxf(v[0], 0.0f), aero = fmaxf(v[1], 0.0f);
+                    float sigma0 = (8700.0f * soot + 3000.0f * aero) * P->smoke_scale;
+                    float sigma = sigma0, a = 0.0f;
+                    float lightFrac = aero / (soot * 3.0f + aero + 1e-12f);
+                    ov3 scat = o3(0, 0, 0);
+                    if (P->smoke == 1 && sigma0 > 0.02f) {
+                        float bill = osmoke_noise(p, P->time);
+                        sigma = sigma0 * omix(0.25f, 1.75f, bill);
+                        a = 1.0f - expf(-sigma * ds);
+                        float od = 0.0f;
+                        for (int sh = 1; sh <= 4; ++sh) {
+                            float sv2[4];
+                            osample(&G, oadd(p, omul(sun, 0.35f * (float)sh)), sv2);
+                            od += (8700.0f * fmaxf(sv2[0], 0.0f) + 3000.0f * fmaxf(sv2[1], 0.0f)) * P->smoke_scale * 0.35f;
+                        }
+                        float sunT = expf(-od);
+                        float g = 0.35f, ct = odot(rd, sun);
+                        float hg = (1.0f - g * g) / powf(1.0f + g * g - 2.0f * g * ct, 1.5f) * 0.25f;
+                        ov3 albedo = omix3(o3(0.10f, 0.095f, 0.09f), o3(0.86f, 0.84f, 0.78f), lightFrac);
+                        float amb = 0.45f + 0.25f * oclamp((p.z - G.bmin.z) * 0.15f, 0.0f, 1.0f);
+                        scat = omul(albedo, amb * omix(0.55f, 1.0f, sunT) + 1.6f * hg * sunT);
+                        scat = omul(scat, omix(0.85f, 1.1f, bill));
+                    }
+                    if (P->fire == 1) {
+                        float alb = omix(0.45f, 0.95f, lightFrac);
+                        float fl = 0.0f;
+                        for (int li = 0; li < P->n_lights; ++li) {
+                            ov3 dl = osub(o3(P->lights[li][0], P->lights[li][1], P->lights[li][2]), p);
+                            fl += P->lights[li][3] / (0.6f + odot(dl, dl));
+                        }
+                        scat = oadd(scat, omul(omul(omul(o3(1.0f, 0.45f, 0.15f), fl), alb), 0.9f));
+                    }
+                    ov3 emit = o3(0, 0, 0);
+                    if (P->fire == 1) {
+                        float q = v[3] / 1.0e6f;
+                        float hot = osmooth(1000.0f, 1600.0f, v[2]);
+                        float drive = oclamp(q * 0.9f, 0.0f, 3.0f) + hot * 0.9f;
+                        if (drive > 0.01f) {
+                            float nn = oflame_noise(p, P->time);
+                            float shape = osmooth(0.62f - 0.25f * oclamp(drive, 0.0f, 1.5f), 0.85f, nn + 0.15f * fminf(drive, 1.5f));
+                            float k = oclamp(0.25f * drive + 0.6f * nn * shape, 0.0f, 1.0f);
+                            emit = omul(omul(omul(oflame_color(k), shape), drive), 6.0f);
+                        }
+                        emit = oadd(emit, omul(omul(oglow(v[2]), oclamp(sigma * 0.6f, 0.0f, 1.0f)), 4.0f));
+                    }
+                    col = oadd(col, omul(oadd(omul(scat, a), omul(emit, ds)), tr));
+                    tr *= 1.0f - a;
+                    if (tr < 0.004f) break;
+                }
+                if (!sliceDone) oslice(&G, P, ro, rd, tS, &col, &tr);
+            }
+            float* o = rgb + 3 * ((size_t)py * P->width + px);
+            o[0] = base.x * tr + (1.0f - expf(-col.x * 1.1f));
+            o[1] = base.y * tr + (1.0f - expf(-col.y * 1.1f));
+            o[2] = base.z * tr + (1.0f - expf(-col.z * 1.1f));
+        }
+}

@@ -61,6 +61,27 @@ void orc_rad_trace(int nx, int ny, int nz, double dx, double ox, double oy, doub
                    const double* hrr, int nElem, const double* elem, int nWall, const double* wall,
                    const double* solidT, double* radAbs, double* radGas);
 
+/* The viewer's smoke and flame volume ray march (the VOL_FS fragment shader,
+ * src/render/renderer.cpp:119-283), restated in C with FP32 arithmetic: vol
+ * holds 4 floats per cell (soot density, aerosol density, T, heat release, as
+ * src/app/viewer.cpp:941-949 packs them); the parameters mirror the shader's
+ * uniforms (same layout as phx_vol_params); rgb gets width*height*3 floats,
+ * rows from the bottom. depth may be NULL (no scene). */
+typedef struct orc_vol_params {
+    int width, height;
+    float inv_vp[16];
+    float eye[3];
+    float step, clip_z, slice_z, t_min, t_max;
+    int smoke, slice, fire;
+    float time, smoke_scale;
+    float sun_dir[3];
+    int n_lights;
+    float lights[8][4];
+    float background[3];
+} orc_vol_params;
+void orc_vol_render(int nx, int ny, int nz, float dx, float ox, float oy, float oz, const float* vol,
+                    const orc_vol_params* p, const float* depth, float* rgb, int row0, int row1);
+
 #ifdef __cplusplus
 }
 #endif

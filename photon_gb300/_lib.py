@@ -26,7 +26,7 @@ STAGE_ID = {n: i for i, n in enumerate(STAGES)}
 SYMBOLS = ["phx_create", "phx_destroy", "phx_last_error", "phx_last_global_error", "phx_abi_version", "phx_add_burner",
            "phx_add_ignition", "phx_step", "phx_run", "phx_stage", "phx_precondition", "phx_get_field",
            "phx_set_field", "phx_field_count", "phx_get_stats", "phx_set_scalars", "phx_set_stats", "phx_device_bytes", "phx_sync",
-           "phx_time_steps", "phx_profile_step", "phx_last_step_launches", "phx_rad_trace", "phx_batch_rad_trace", "phx_rad_last_ms", "phx_select_device", "phx_alloc_host",
+           "phx_time_steps", "phx_profile_step", "phx_last_step_launches", "phx_rad_trace", "phx_batch_rad_trace", "phx_rad_last_ms", "phx_vol_render", "phx_batch_vol_render", "phx_vol_last_ms", "phx_select_device", "phx_alloc_host",
            "phx_free_host", "phx_create_batch", "phx_batch_add", "phx_batch_remove", "phx_batch_size",
            "phx_batch_scenario_bytes", "phx_batch_add_burner", "phx_batch_step", "phx_batch_get_field",
            "phx_batch_set_field", "phx_batch_field_count", "phx_batch_get_stats", "phx_batch_set_stats", "phx_gather_stats_noalloc",
@@ -78,6 +78,16 @@ def rad_walls(a) -> np.ndarray:
     r["axis"], r["face"] = a[:, 0].astype(np.int32), a[:, 1].astype(np.int32)
     r["t_lower"], r["t_upper"] = a[:, 2], a[:, 3]
     return r
+
+
+class PhxVolParams(ctypes.Structure):
+    """phx_vol_params (include/phx.h): the volume shader's uniforms."""
+    _fields_ = [("width", ctypes.c_int), ("height", ctypes.c_int), ("inv_vp", ctypes.c_float * 16),
+                ("eye", ctypes.c_float * 3), ("step", ctypes.c_float), ("clip_z", ctypes.c_float),
+                ("slice_z", ctypes.c_float), ("t_min", ctypes.c_float), ("t_max", ctypes.c_float),
+                ("smoke", ctypes.c_int), ("slice", ctypes.c_int), ("fire", ctypes.c_int), ("time", ctypes.c_float),
+                ("smoke_scale", ctypes.c_float), ("sun_dir", ctypes.c_float * 3), ("n_lights", ctypes.c_int),
+                ("lights", (ctypes.c_float * 4) * 8), ("background", ctypes.c_float * 3)]
 
 
 class PhxStats(ctypes.Structure):
@@ -173,6 +183,10 @@ def load():
     L.phx_batch_rad_trace.argtypes = [vp, i, vp, i, vp, i, vp, vp, vp]
     L.phx_rad_last_ms.restype = d
     L.phx_rad_last_ms.argtypes = [vp]
+    L.phx_vol_render.argtypes = [vp, ctypes.POINTER(PhxVolParams), vp, vp]
+    L.phx_batch_vol_render.argtypes = [vp, i, ctypes.POINTER(PhxVolParams), vp, vp]
+    L.phx_vol_last_ms.restype = d
+    L.phx_vol_last_ms.argtypes = [vp]
     L.phx_alloc_host.restype = vp
     L.phx_alloc_host.argtypes = [sz]
     L.phx_free_host.argtypes = [vp]

@@ -217,6 +217,14 @@ int phx_rad_trace(phx_ctx* c, const phx_rad_elem* elems, int n_elems, const phx_
 }
 double phx_rad_last_ms(const phx_ctx* c) { return c && c->impl ? c->impl->radLastMs() : 0.0; }
 
+int phx_batch_vol_render(phx_ctx* c, int s, const phx_vol_params* params, const float* depth, float* rgb) {
+    return guarded(c, [&](phx::CtxBase* x) { return x->volRender(s, params, depth, rgb); });
+}
+int phx_vol_render(phx_ctx* c, const phx_vol_params* params, const float* depth, float* rgb) {
+    return phx_batch_vol_render(c, 0, params, depth, rgb);
+}
+double phx_vol_last_ms(const phx_ctx* c) { return c && c->impl ? c->impl->volLastMs() : 0.0; }
+
 int phx_gather_stats_noalloc(phx_ctx* c, int scenario, phx_stats* out) {
     if (!out) return fail(c, PHX_ERR_INVALID, "null stats");
     return guarded(c, [&](phx::CtxBase* x) { return phx::gatherStatsNoAlloc(x, c->precision, scenario, out, x->err); });

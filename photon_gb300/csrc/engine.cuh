@@ -20,6 +20,7 @@
 #include "host_setup.h"
 #include "mixed_kernels.cuh"
 #include "radiation.cuh"
+#include "volume.cuh"
 #include "rowblock.cuh"
 
 namespace phx {
@@ -412,6 +413,7 @@ public:
     ~Ctx() override {
         if (st) cudaStreamSynchronize(st);
         rad.release();
+        volw.release();
         destroyGraph();
         sc.clear();
         if (tab) cudaFree(tab);
@@ -563,6 +565,78 @@ public:
         return checkDeviceError();
     }
     double radLastMs() const override { return rad.lastMs; }
+
+    // the viewer's volume ray march for scenario s (src/render/renderer.cpp:119-283)
+    struct VolWork {
+        float4* vol = nullptr;
+        size_t capVol = 0;
+        float* depth = nullptr;
+        float* rgb = nullptr;
+        size_t capPix = 0;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        double lastMs = 0;
+        void release() {
+            if (vol) cudaFree(vol);
+            if (depth) cudaFree(depth);
+            if (rgb) cudaFree(rgb);
+            if (e0) cudaEventDestroy(e0);
+            if (e1) cudaEventDestroy(e1);
+        }
+    } volw;
+
+    int volRender(int s, const phx_vol_params* p, const float* depth, float* rgb) override {
+        PHX_TRY(checkScn(s));
+        if (!p || !rgb || p->width <= 0 || p->height <= 0 || (size_t)p->width * p->height > (size_t)1 << 26 ||
+            p->n_lights < 0 || p->n_lights > 8 || !(p->step > 0)) {
+            err = "invalid volume render parameters";
+            return PHX_ERR_INVALID;
+        }
+        const Scenario<R>& S = *sc[s];
+        const size_t N = (size_t)S.geo.nx * S.geo.ny * S.geo.nz, npx = (size_t)p->width * p->height;
+        PHX_TRY(ensureTables());
+        PHX_TRY(initStream());
+        auto alloc = [&](auto*& ptr, size_t& cap, size_t n, size_t esz) -> int {
+            if (ptr && cap >= n) return PHX_OK;
+            if (ptr) { PHX_CK(cudaStreamSynchronize(st)); cudaFree(ptr); ptr = nullptr; cap = 0; }
+            void* q = nullptr;
+            if (cudaMalloc(&q, n * esz) != cudaSuccess) {
+                cudaGetLastError();
+                err = "out of device memory for the volume render";
+                return PHX_ERR_OOM;
+            }
+            ptr = static_cast<std::remove_reference_t<decltype(ptr)>>(q);
+            cap = n;
+            return PHX_OK;
+        };
+        PHX_TRY(alloc(volw.vol, volw.capVol, N, sizeof(float4)));
+        if (volw.capPix < npx || !volw.rgb) {
+            size_t c1 = volw.capPix, c2 = volw.capPix;
+            PHX_TRY(alloc(volw.rgb, c1, npx, 3 * sizeof(float)));
+            PHX_TRY(alloc(volw.depth, c2, npx, sizeof(float)));
+            volw.capPix = npx;
+        }
+        if (!volw.e0) { PHX_CK(cudaEventCreate(&volw.e0)); PHX_CK(cudaEventCreate(&volw.e1)); }
+        if (depth) PHX_CK(cudaMemcpyAsync(volw.depth, depth, npx * sizeof(float), cudaMemcpyHostToDevice, st));
+        VolGrid G;
+        G.vol = volw.vol;
+        G.nx = S.geo.nx; G.ny = S.geo.ny; G.nz = S.geo.nz;
+        const float dxf = (float)S.geo.dx;
+        G.bmin = v3((float)S.geo.ox, (float)S.geo.oy, (float)S.geo.oz);
+        G.bmax = v3((float)S.geo.ox + G.nx * dxf, (float)S.geo.oy + G.ny * dxf, (float)S.geo.oz + G.nz * dxf);
+        PHX_CK(cudaEventRecord(volw.e0, st));
+        k_vol_pack<R><<<(unsigned)((N + 255) / 256), 256, 0, st>>>(dS, s, volw.vol);
+        dim3 grid((p->width + 15) / 16, (p->height + 7) / 8);
+        k_vol_render<R><<<grid, 128, 0, st>>>(G, *p, depth ? volw.depth : nullptr, volw.rgb);
+        PHX_CK(cudaGetLastError());
+        PHX_CK(cudaEventRecord(volw.e1, st));
+        PHX_CK(cudaMemcpyAsync(rgb, volw.rgb, npx * 3 * sizeof(float), cudaMemcpyDeviceToHost, st));
+        PHX_CK(cudaStreamSynchronize(st));
+        float ms = 0;
+        PHX_CK(cudaEventElapsedTime(&ms, volw.e0, volw.e1));
+        volw.lastMs = ms;
+        return checkDeviceError();
+    }
+    double volLastMs() const override { return volw.lastMs; }
 
     int readTimes(double* out) override {
         const int n = nscn();

@@ -51,6 +51,8 @@ public:
     virtual int radTrace(int s, const phx_rad_elem* el, int nE, const phx_rad_wall* wl, int nW, const double* solidT,
                          double* radAbs, double* radGas) = 0;
     virtual double radLastMs() const = 0;
+    virtual int volRender(int s, const phx_vol_params* p, const float* depth, float* rgb) = 0;
+    virtual double volLastMs() const = 0;
     std::string err;
 };
 

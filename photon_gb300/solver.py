@@ -174,6 +174,22 @@ class Solver:
     def rad_last_ms(self) -> float:
         return float(self.L.phx_rad_last_ms(self.h))
 
+    def vol_render(self, params, depth=None) -> np.ndarray:
+        """The viewer's smoke and flame volume render of this context's fields
+        (src/render/renderer.cpp:119-283): params is a PhxVolParams
+        (photon_gb300.render.camera builds one); returns an (height, width, 3)
+        float image, rows from the bottom. vol_last_ms() is its device time."""
+        rgb = np.zeros((params.height, params.width, 3), np.float32)
+        d = None if depth is None else np.ascontiguousarray(depth, np.float32)
+        if d is not None and d.size != params.width * params.height:
+            raise PhxError(_lib.PHX_ERR_INVALID, "depth needs one value per pixel")
+        self._check(self.L.phx_vol_render(self.h, ctypes.byref(params), None if d is None else d.ctypes.data,
+                                          rgb.ctypes.data))
+        return rgb
+
+    def vol_last_ms(self) -> float:
+        return float(self.L.phx_vol_last_ms(self.h))
+
     def device_bytes(self) -> int:
         return int(self.L.phx_device_bytes(self.h))
 
