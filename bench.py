@@ -433,7 +433,7 @@ def measure_radiation(args, cpu_baseline: bool):
     sample of the elements as the CPU baseline."""
     from photon_gb300 import _lib, casegen
     from photon_gb300.solver import Solver
-    c = casegen.house_fine(1)
+    c = casegen.house_fine(1) if args.extras_case == "fine" else casegen.house_small(1)
     w = casegen.rad_workload(c)
     el, wl = _lib.rad_elements(w["elements"]), _lib.rad_walls(w["walls"])
     rays = int(32 * np.count_nonzero(el["sphere"])) + 16 * int(np.count_nonzero(el["sphere"] == 0))
@@ -477,7 +477,7 @@ def measure_volume(args, cpu_baseline: bool):
     C restatement of the shader on a band of rows as the CPU baseline."""
     from photon_gb300 import _lib, casegen, render
     from photon_gb300.solver import Solver
-    c = casegen.house_fine(1)
+    c = casegen.house_fine(1) if args.extras_case == "fine" else casegen.house_small(1)
     w = casegen.rad_workload(c)
     g = Solver(c, _lib.PREC_MIXED)
     gas = dict(w["gas"])
@@ -525,7 +525,11 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=8.0, help="request arrivals per second (Poisson)")
     ap.add_argument("--serve-scale", type=float, default=0.01, help="scale of the 30-300 s simulated durations")
     ap.add_argument("--no-serving", action="store_true")
-    ap.add_argument("--no-radiation", action="store_true")
+    ap.add_argument("--no-radiation", action="store_true", help="skip the radiation trace and volume render")
+    ap.add_argument("--extras-only", action="store_true",
+                    help="time only the radiation trace and the volume render (one JSON line)")
+    ap.add_argument("--extras-case", default="fine", choices=["fine", "small"],
+                    help="house for the trace and the render: 144x104x88 at 0.1 m, or 72x52x44 at 0.2 m")
     ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64"],
                     help="which paths to time (the line's value is the mixed path unless only fp64 runs)")
     args = ap.parse_args()
@@ -542,6 +546,11 @@ def main():
     L = _lib.load()
     if L.phx_select_device(local) != 0:
         raise SystemExit("cannot select device %d" % local)
+    if args.extras_only:
+        if rank == 0:
+            print(json.dumps({"radiation_trace": measure_radiation(args, not args.no_cpu_baseline),
+                              "volume_render": measure_volume(args, not args.no_cpu_baseline)}))
+        return 0
 
     mixed = measure(args, _lib.PREC_MIXED, L, world, clocks=True) if args.precision in ("both", "mixed") else None
     fp64 = measure(args, _lib.PREC_FP64, L, world, clocks=mixed is None) if args.precision in ("both", "fp64") else None

@@ -398,7 +398,8 @@ public:
     // radiation trace work space, grown on demand (traces are seconds of
     // simulated time apart)
     struct RadWork {
-        enum { EL, WL, WALLI, ABS, WALLOF, CELLS, FLAGS, SOLIDT, GAS, KC, NBUF };
+        enum { EL, WL, WALLI, ABS, WALLOF, CELLS, FLAGS, SOLIDT, GAS, KC, ELEMIS, RAYW, RAYVAL, RAYS, CNT, NBUF };
+        int marchCtas = 0;
         void* buf[NBUF] = {};
         size_t cap[NBUF] = {};
         cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -518,6 +519,18 @@ public:
         PHX_TRY(grow(RadWork::SOLIDT, N * sizeof(double)));
         PHX_TRY(grow(RadWork::GAS, N * sizeof(R)));
         PHX_TRY(grow(RadWork::KC, sizeof(RadConst<R>)));
+        PHX_TRY(grow(RadWork::ELEMIS, (size_t)nE * RAD_NB * sizeof(R)));
+        PHX_TRY(grow(RadWork::RAYW, (size_t)nE * RAD_DIRS * sizeof(R)));
+        PHX_TRY(grow(RadWork::RAYVAL, (size_t)nE * RAD_DIRS * sizeof(R)));
+        PHX_TRY(grow(RadWork::RAYS, (size_t)nE * RAD_DIRS * sizeof(int)));
+        PHX_TRY(grow(RadWork::CNT, 2 * sizeof(int)));
+        if (!rad.marchCtas) {
+            int dev = 0, sms = 0, per = 0;
+            PHX_CK(cudaGetDevice(&dev));
+            PHX_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            PHX_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rad_march<R>, 256, 0));
+            rad.marchCtas = std::max(1, sms * std::max(1, per));
+        }
         if (!rad.e0) {
             PHX_CK(cudaEventCreate(&rad.e0));
             PHX_CK(cudaEventCreate(&rad.e1));
@@ -532,19 +545,29 @@ public:
         double* dSolid = static_cast<double*>(rad.buf[RadWork::SOLIDT]);
         R* dGas = static_cast<R*>(rad.buf[RadWork::GAS]);
         RadConst<R>* dKc = static_cast<RadConst<R>*>(rad.buf[RadWork::KC]);
+        R* dElemIs = static_cast<R*>(rad.buf[RadWork::ELEMIS]);
+        R* dRayW = static_cast<R*>(rad.buf[RadWork::RAYW]);
+        R* dRayVal = static_cast<R*>(rad.buf[RadWork::RAYVAL]);
+        int* dRays = static_cast<int*>(rad.buf[RadWork::RAYS]);
+        int* dCnt = static_cast<int*>(rad.buf[RadWork::CNT]);
         if (nE) PHX_CK(cudaMemcpyAsync(dEl, el, nE * sizeof(phx_rad_elem), cudaMemcpyHostToDevice, st));
         if (nW) PHX_CK(cudaMemcpyAsync(dWl, wl, nW * sizeof(phx_rad_wall), cudaMemcpyHostToDevice, st));
         if (solidT) PHX_CK(cudaMemcpyAsync(dSolid, solidT, N * sizeof(double), cudaMemcpyHostToDevice, st));
         PHX_CK(cudaMemsetAsync(dWallOf, 0xff, nF * sizeof(int), st));
         PHX_CK(cudaMemsetAsync(dGas, 0, N * sizeof(R), st));
+        PHX_CK(cudaMemsetAsync(dCnt, 0, 2 * sizeof(int), st));
         PHX_CK(cudaEventRecord(rad.e0, st));
         k_rad_setup<R><<<1, 32, 0, st>>>(dKc);
         if (nW) k_rad_walls<R><<<(nW + 127) / 128, 128, 0, st>>>(dWl, nW, (int)NF[0], (int)NF[1], dWallOf, dWallI, dKc);
         k_rad_cells<R><<<(unsigned)((N + 255) / 256), 256, 0, st>>>(dS, s, solidT ? dSolid : nullptr, dCells, dFlags,
                                                                     dKc);
-        if (nE)
-            k_rad_trace<R><<<(nE + RAD_WARPS - 1) / RAD_WARPS, RAD_WARPS * 32, 0, st>>>(
-                dS, s, dEl, nE, dCells, dFlags, dWallOf, dWallI, dKc, dGas, dAbs);
+        if (nE) {
+            k_rad_elems<R><<<(nE + RAD_WARPS - 1) / RAD_WARPS, RAD_WARPS * 32, 0, st>>>(
+                dS, s, dEl, nE, dKc, dElemIs, dRayW, dRayVal, dRays, dCnt);
+            k_rad_march<R><<<rad.marchCtas, 256, 0, st>>>(dS, s, dEl, dCells, dFlags, dWallOf, dWallI, dKc, dElemIs,
+                                                          dRayW, dRayVal, dRays, dCnt, dGas);
+            k_rad_absorbed<R><<<(nE + 255) / 256, 256, 0, st>>>(dRayVal, nE, dAbs);
+        }
         PHX_CK(cudaGetLastError());
         PHX_CK(cudaEventRecord(rad.e1, st));
         if (nE) PHX_CK(cudaMemcpyAsync(radAbs, dAbs, nE * sizeof(double), cudaMemcpyDeviceToHost, st));

@@ -8,9 +8,13 @@
 // every band. Everything is relative to ambient, as in the reference.
 //
 // GB300 mapping:
-// * one warp per element, one lane per direction (the reference's 32
-//   directions are exactly one warp); the element's absorbed power is the
-//   lanes' contributions summed in direction order, as the reference sums them;
+// * a warp per element (lane = direction: the reference's 32 directions are
+//   one warp) computes the element's emission and weights and lists the
+//   directions it emits into; a persistent march kernel then hands rays to
+//   lanes as they free up, so lanes neither idle on directions an element
+//   does not emit into nor wait for the longest ray of their warp; each
+//   element's absorbed power is its rays' results summed in direction order,
+//   as the reference sums them;
 // * per-cell absorption coefficient and source function of the four bands are
 //   computed once per trace into one interleaved record per cell (32 B FP32,
 //   64 B FP64), so a ray step gathers one record;
@@ -182,39 +186,39 @@ __global__ void k_rad_cells(const Scn<R>* __restrict__ S, int s, const double* _
     flags[c] = fl ? 2 : 0;
 }
 
-// the march (:223-306): warp = element, lane = direction
+// Per element (one warp, lane = direction; :225-248): the element's own
+// emission in each band, the hemisphere normalisation summed in direction
+// order, and each direction's weight w (0 for a direction the element does
+// not emit into or an origin outside the grid). The directions with w > 0
+// are appended to the ray list (slot = 32 e + d); every slot's result is
+// cleared.
 template <class R>
 __global__ void __launch_bounds__(RAD_WARPS * 32)
-k_rad_trace(const Scn<R>* __restrict__ S, int s, const phx_rad_elem* __restrict__ els, int nE,
-            const RadCell<R>* __restrict__ cells, const uint8_t* __restrict__ flags, const int* __restrict__ wallOf,
-            const R* __restrict__ wallI, const RadConst<R>* __restrict__ kc, R* __restrict__ radGas,
-            double* __restrict__ radAbs) {
+k_rad_elems(const Scn<R>* __restrict__ S, int s, const phx_rad_elem* __restrict__ els, int nE,
+            const RadConst<R>* __restrict__ kc, R* __restrict__ elemIs, R* __restrict__ rayW,
+            R* __restrict__ rayVal, int* __restrict__ rays, int* __restrict__ counters) {
     const int lane = threadIdx.x & 31;
     const int e = blockIdx.x * RAD_WARPS + (threadIdx.x >> 5);
     if (e >= nE) return;   // warp-uniform
     const Scn<R>& g = S[s];
-    const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const int NX = g.NX, NY = g.NY;
-    const R dx = (R)g.dx;
     const R PI = RadPi<R>::v;
     const phx_rad_elem& el = els[e];
     const R eps = (R)el.emissivity, temp = (R)el.temperature, area = (R)el.area;
     const bool sphere = el.sphere != 0;
     const R n0 = (R)el.n[0], n1 = (R)el.n[1], n2 = (R)el.n[2];
     const R dW = kc->dW;
-
-    // own emission in each band, relative to ambient: lanes 0-2 evaluate the band edges
+    // own emission, relative to ambient: lanes 0-2 evaluate the band edges
     R up = 0;
     if (lane < 3) up = radPlanckBelow<R>(radEdge<R>(lane + 1) * temp);
     const R u0 = __shfl_sync(0xffffffffu, up, 0), u1 = __shfl_sync(0xffffffffu, up, 1),
             u2 = __shfl_sync(0xffffffffu, up, 2);
-    R Is[RAD_NB];
-    {
+    if (lane < RAD_NB) {
         const R f[RAD_NB] = {u0 - (R)0, u1 - u0, u2 - u1, (R)1 - u2};
-#pragma unroll
-        for (int q = 0; q < RAD_NB; ++q) { Is[q] = radPower<R>(*kc, f, temp, q); Is[q] *= eps / PI; }
+        R Is = radPower<R>(*kc, f, temp, lane);
+        Is *= eps / PI;
+        elemIs[(size_t)e * RAD_NB + lane] = Is;
     }
-    // hemisphere weights normalised so that sum(cos dW) = pi, summed in direction order
+    // hemisphere weights normalised so that sum(cos dW) = pi, in direction order
     R wsum = 0;
     if (!sphere) {
 #pragma unroll 4
@@ -224,7 +228,6 @@ k_rad_trace(const Scn<R>* __restrict__ S, int s, const phx_rad_elem* __restrict_
         }
     }
     const R norm = sphere ? (R)1 : (wsum > 0 ? PI / wsum : (R)0);
-
     const R dvx = kc->dir[lane][0], dvy = kc->dir[lane][1], dvz = kc->dir[lane][2];
     bool active = true;
     R w = 0;
@@ -234,36 +237,94 @@ k_rad_trace(const Scn<R>* __restrict__ S, int s, const phx_rad_elem* __restrict_
         if (cs <= 0) active = false;
         else w = cs * dW * norm * area;
     }
-    const R px = ((R)el.o[0] - (R)g.ox) / dx, py = ((R)el.o[1] - (R)g.oy) / dx, pz = ((R)el.o[2] - (R)g.oz) / dx;
-    int ci = (int)radFloor(px), cj = (int)radFloor(py), ck = (int)radFloor(pz);
-    if (ci < 0 || cj < 0 || ck < 0 || ci >= nx || cj >= ny || ck >= nz) active = false;
+    const R px = ((R)el.o[0] - (R)g.ox) / (R)g.dx, py = ((R)el.o[1] - (R)g.oy) / (R)g.dx,
+            pz = ((R)el.o[2] - (R)g.oz) / (R)g.dx;
+    const int ci = (int)radFloor(px), cj = (int)radFloor(py), ck = (int)radFloor(pz);
+    if (ci < 0 || cj < 0 || ck < 0 || ci >= g.nx || cj >= g.ny || ck >= g.nz) active = false;
+    const size_t slot = (size_t)e * RAD_DIRS + lane;
+    rayW[slot] = active ? w : (R)0;
+    rayVal[slot] = 0;
+    const unsigned mask = __ballot_sync(0xffffffffu, active);
+    int base = 0;
+    if (lane == 0 && mask) base = atomicAdd(counters, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (active) rays[base + __popc(mask & ((1u << lane) - 1u))] = (int)slot;
+}
 
-    R val = 0;
-    if (active) {
-        int sx, sy, sz;
-        R tMx, tMy, tMz, tDx, tDy, tDz;
-        if (dvx > (R)1e-9) { sx = 1; tMx = (ci + 1 - px) / dvx; tDx = 1 / dvx; }
-        else if (dvx < (R)-1e-9) { sx = -1; tMx = (px - ci) / -dvx; tDx = -1 / dvx; }
-        else { sx = 0; tMx = (R)1e30; tDx = (R)1e30; }
-        if (dvy > (R)1e-9) { sy = 1; tMy = (cj + 1 - py) / dvy; tDy = 1 / dvy; }
-        else if (dvy < (R)-1e-9) { sy = -1; tMy = (py - cj) / -dvy; tDy = -1 / dvy; }
-        else { sy = 0; tMy = (R)1e30; tDy = (R)1e30; }
-        if (dvz > (R)1e-9) { sz = 1; tMz = (ck + 1 - pz) / dvz; tDz = 1 / dvz; }
-        else if (dvz < (R)-1e-9) { sz = -1; tMz = (pz - ck) / -dvz; tDz = -1 / dvz; }
-        else { sz = 0; tMz = (R)1e30; tDz = (R)1e30; }
-        R t = 0;
-        R tau[RAD_NB] = {1, 1, 1, 1}, I[RAD_NB] = {0, 0, 0, 0}, Iend[RAD_NB] = {0, 0, 0, 0};
-        const R tEnd = (R)8.0 / dx;
-        int c = ci + nx * (cj + ny * ck);
-        const int skip = el.skip_own_cell ? c : -1;
-        for (;;) {
+// The march (:249-306), persistent: every lane takes the next ray of the list
+// as soon as its own ray ends (a warp-aggregated atomic hands out rays), so
+// lanes do not idle behind the longest ray of their warp. A ray's result
+// eps w It lands in its slot; gas cells gain by atomic adds.
+template <class R>
+__global__ void __launch_bounds__(256)
+k_rad_march(const Scn<R>* __restrict__ S, int s, const phx_rad_elem* __restrict__ els,
+            const RadCell<R>* __restrict__ cells, const uint8_t* __restrict__ flags, const int* __restrict__ wallOf,
+            const R* __restrict__ wallI, const RadConst<R>* __restrict__ kc, const R* __restrict__ elemIs,
+            const R* __restrict__ rayW, R* __restrict__ rayVal, const int* __restrict__ rays,
+            int* __restrict__ counters, R* __restrict__ radGas) {
+    const int lane = threadIdx.x & 31;
+    const Scn<R>& g = S[s];
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const int NX = g.NX, NY = g.NY;
+    const R dx = (R)g.dx;
+    const int nRays = counters[0];
+    const R tEnd = (R)8.0 / dx;
+    int slot = -1;        // ray in flight; -1 none, -2 the list is exhausted
+    int ci = 0, cj = 0, ck = 0, c = 0, skip = -1, sx = 0, sy = 0, sz = 0;
+    R tMx = 0, tMy = 0, tMz = 0, tDx = 0, tDy = 0, tDz = 0, t = 0, w = 0, eps = 0;
+    R tau[RAD_NB], I[RAD_NB], Is[RAD_NB];
+    for (;;) {
+        const bool need = slot == -1;
+        const unsigned mNeed = __ballot_sync(0xffffffffu, need);
+        if (mNeed) {
+            const int leader = __ffs(mNeed) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(counters + 1, __popc(mNeed));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (need) {
+                const int k = base + __popc(mNeed & ((1u << lane) - 1u));
+                if (k >= nRays) slot = -2;
+                else {
+                    slot = rays[k];
+                    const int e = slot >> 5, d = slot & 31;
+                    const phx_rad_elem& el = els[e];
+                    eps = (R)el.emissivity;
+                    w = rayW[slot];
+#pragma unroll
+                    for (int q = 0; q < RAD_NB; ++q) { Is[q] = elemIs[(size_t)e * RAD_NB + q]; tau[q] = 1; I[q] = 0; }
+                    const R dvx = kc->dir[d][0], dvy = kc->dir[d][1], dvz = kc->dir[d][2];
+                    const R px = ((R)el.o[0] - (R)g.ox) / dx, py = ((R)el.o[1] - (R)g.oy) / dx,
+                            pz = ((R)el.o[2] - (R)g.oz) / dx;
+                    ci = (int)radFloor(px); cj = (int)radFloor(py); ck = (int)radFloor(pz);
+                    if (dvx > (R)1e-9) { sx = 1; tMx = (ci + 1 - px) / dvx; tDx = 1 / dvx; }
+                    else if (dvx < (R)-1e-9) { sx = -1; tMx = (px - ci) / -dvx; tDx = -1 / dvx; }
+                    else { sx = 0; tMx = (R)1e30; tDx = (R)1e30; }
+                    if (dvy > (R)1e-9) { sy = 1; tMy = (cj + 1 - py) / dvy; tDy = 1 / dvy; }
+                    else if (dvy < (R)-1e-9) { sy = -1; tMy = (py - cj) / -dvy; tDy = -1 / dvy; }
+                    else { sy = 0; tMy = (R)1e30; tDy = (R)1e30; }
+                    if (dvz > (R)1e-9) { sz = 1; tMz = (ck + 1 - pz) / dvz; tDz = 1 / dvz; }
+                    else if (dvz < (R)-1e-9) { sz = -1; tMz = (pz - ck) / -dvz; tDz = -1 / dvz; }
+                    else { sz = 0; tMz = (R)1e30; tDz = (R)1e30; }
+                    t = 0;
+                    c = ci + nx * (cj + ny * ck);
+                    skip = el.skip_own_cell ? c : -1;
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, slot >= 0) == 0) break;   // every lane exhausted
+        if (slot < 0) continue;
+        // advance this lane's ray by up to 16 cells
+        bool ended = false;
+        R Iend[RAD_NB] = {0, 0, 0, 0};
+        for (int it = 0; it < 16; ++it) {
             const int a = tMx < tMy ? (tMx < tMz ? 0 : 2) : (tMy < tMz ? 1 : 2);
             const R tMa = a == 0 ? tMx : a == 1 ? tMy : tMz;
             const R tn = tEnd < tMa ? tEnd : tMa;
             const R ds = (tn - t) * dx;
-            if (ds > 0 && !(flags[c] & 1) && c != skip) {
+            const uint8_t fl = flags[c];
+            if (ds > 0 && !(fl & 1) && c != skip) {
                 const RadCell<R> cell = cells[c];
-                const bool flame = (flags[c] & 2) != 0;
+                const bool flame = (fl & 2) != 0;
                 R gsum = 0;
 #pragma unroll
                 for (int q = 0; q < RAD_NB; ++q) {
@@ -277,7 +338,10 @@ k_rad_trace(const Scn<R>* __restrict__ S, int s, const phx_rad_elem* __restrict_
                 atomicAdd(radGas + c, w * gsum);
             }
             t = tn;
-            if (t >= tEnd || (tau[0] < (R)1e-3 && tau[1] < (R)1e-3 && tau[2] < (R)1e-3 && tau[3] < (R)1e-3)) break;
+            if (t >= tEnd || (tau[0] < (R)1e-3 && tau[1] < (R)1e-3 && tau[2] < (R)1e-3 && tau[3] < (R)1e-3)) {
+                ended = true;
+                break;
+            }
             // the face crossed next: an intact wall ends the ray with its surface seen from c
             const int st = a == 0 ? sx : a == 1 ? sy : sz;
             const int upf = st > 0 ? 1 : 0;
@@ -288,31 +352,46 @@ k_rad_trace(const Scn<R>* __restrict__ S, int s, const phx_rad_elem* __restrict_
             if (wi >= 0) {
 #pragma unroll
                 for (int q = 0; q < RAD_NB; ++q) Iend[q] = wallI[8 * wi + (upf ? 0 : 4) + q];
+                ended = true;
                 break;
             }
-            if (a == 0) { ci += sx; if (ci < 0 || ci >= nx) break; }
-            else if (a == 1) { cj += sy; if (cj < 0 || cj >= ny) break; }
-            else { ck += sz; if (ck < 0 || ck >= nz) break; }
+            bool out;
+            if (a == 0) { ci += sx; out = ci < 0 || ci >= nx; }
+            else if (a == 1) { cj += sy; out = cj < 0 || cj >= ny; }
+            else { ck += sz; out = ck < 0 || ck >= nz; }
+            if (out) { ended = true; break; }
             const int nb = ci + nx * (cj + ny * ck);
             if (flags[nb] & 1) {
                 const RadCell<R> cell = cells[nb];
 #pragma unroll
                 for (int q = 0; q < RAD_NB; ++q) Iend[q] = cell.src[q];
+                ended = true;
                 break;
             }
             c = nb;
             if (a == 0) tMx += tDx; else if (a == 1) tMy += tDy; else tMz += tDz;
         }
-        R It = 0;
+        if (ended) {
+            R It = 0;
 #pragma unroll
-        for (int q = 0; q < RAD_NB; ++q) It += I[q] + tau[q] * Iend[q];
-        val = eps * w * It;
+            for (int q = 0; q < RAD_NB; ++q) It += I[q] + tau[q] * Iend[q];
+            rayVal[slot] = eps * w * It;
+            slot = -1;
+        }
     }
-    // absorbed power: the directions' contributions summed in direction order
+}
+
+// absorbed power of each element: its directions' results summed in direction
+// order (:305, directions it does not emit into hold 0)
+template <class R>
+__global__ void k_rad_absorbed(const R* __restrict__ rayVal, int nE, double* __restrict__ radAbs) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nE) return;
+    const R* v = rayVal + (size_t)e * RAD_DIRS;
     R acc = 0;
 #pragma unroll
-    for (int l = 0; l < 32; ++l) acc += __shfl_sync(0xffffffffu, val, l);
-    if (lane == 0) radAbs[e] = (double)acc;
+    for (int d = 0; d < RAD_DIRS; ++d) acc += v[d];
+    radAbs[e] = (double)acc;
 }
 
 }  // namespace phx
