@@ -625,8 +625,9 @@ __global__ void k_leak_finish(const Scn<R>* __restrict__ S, Dom dom) {
 // ---------------------------------------------------------------------------
 // Solver::project, right-hand side and warm-start residual
 // (src/sim/gasphase.cpp:528-549, 576-581), with the closed-zone divergence
-// shift of leakage (:495-498) applied to S first. With b64 set (mixed path)
-// the right-hand side is also stored in FP64 for the refinement loop.
+// shift of leakage (:495-498) applied to S first. The right-hand side is
+// stored in the arithmetic type (FP32 on the mixed path: the system the
+// refinement loop solves to 1e-8 is the one with this b).
 template <class R>
 __global__ void k_rhs(const Scn<R>* __restrict__ S, Dom dom) {
     using T = R;
