@@ -319,6 +319,15 @@ int phx_batch_vol_render(struct phx_ctx* ctx, int scenario, const phx_vol_params
 /* device time (ms, CUDA events) of the last render's kernels on this context */
 double phx_vol_last_ms(const struct phx_ctx* ctx);
 
+/* --- failure-path self-test ------------------------------------------------
+ * Every wait inside a kernel of this library is bounded; when one runs out the
+ * kernel records it in the context's device error word and returns, and the
+ * next synchronising call reports PHX_ERR_TIMEOUT and clears the word. This
+ * call exercises that path on purpose: one thread waits, for limit_ms (at most
+ * 1000), on an mbarrier that nothing arrives on. It returns PHX_ERR_TIMEOUT
+ * with a message; the context stays usable. No counterpart in the reference. */
+int phx_selftest_wait_timeout(struct phx_ctx* ctx, double limit_ms);
+
 /* --- process-level helpers ------------------------------------------------
  * select the CUDA device later contexts of this thread are created on */
 int phx_select_device(int device);

@@ -26,7 +26,7 @@ STAGE_ID = {n: i for i, n in enumerate(STAGES)}
 SYMBOLS = ["phx_create", "phx_destroy", "phx_last_error", "phx_last_global_error", "phx_abi_version", "phx_add_burner",
            "phx_add_ignition", "phx_step", "phx_run", "phx_stage", "phx_precondition", "phx_get_field",
            "phx_set_field", "phx_field_count", "phx_get_stats", "phx_set_scalars", "phx_set_stats", "phx_device_bytes", "phx_sync",
-           "phx_time_steps", "phx_profile_step", "phx_last_step_launches", "phx_rad_trace", "phx_batch_rad_trace", "phx_rad_last_ms", "phx_vol_render", "phx_batch_vol_render", "phx_vol_last_ms", "phx_select_device", "phx_alloc_host",
+           "phx_time_steps", "phx_profile_step", "phx_last_step_launches", "phx_rad_trace", "phx_batch_rad_trace", "phx_rad_last_ms", "phx_vol_render", "phx_batch_vol_render", "phx_vol_last_ms", "phx_selftest_wait_timeout", "phx_select_device", "phx_alloc_host",
            "phx_free_host", "phx_create_batch", "phx_batch_add", "phx_batch_remove", "phx_batch_size",
            "phx_batch_scenario_bytes", "phx_batch_add_burner", "phx_batch_step", "phx_batch_get_field",
            "phx_batch_set_field", "phx_batch_field_count", "phx_batch_get_stats", "phx_batch_set_stats", "phx_gather_stats_noalloc",
@@ -187,6 +187,7 @@ def load():
     L.phx_batch_vol_render.argtypes = [vp, i, ctypes.POINTER(PhxVolParams), vp, vp]
     L.phx_vol_last_ms.restype = d
     L.phx_vol_last_ms.argtypes = [vp]
+    L.phx_selftest_wait_timeout.argtypes = [vp, d]
     L.phx_alloc_host.restype = vp
     L.phx_alloc_host.argtypes = [sz]
     L.phx_free_host.argtypes = [vp]

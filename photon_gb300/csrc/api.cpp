@@ -225,6 +225,10 @@ int phx_vol_render(phx_ctx* c, const phx_vol_params* params, const float* depth,
 }
 double phx_vol_last_ms(const phx_ctx* c) { return c && c->impl ? c->impl->volLastMs() : 0.0; }
 
+int phx_selftest_wait_timeout(phx_ctx* c, double limit_ms) {
+    return guarded(c, [&](phx::CtxBase* x) { return x->selftestWait(limit_ms); });
+}
+
 int phx_gather_stats_noalloc(phx_ctx* c, int scenario, phx_stats* out) {
     if (!out) return fail(c, PHX_ERR_INVALID, "null stats");
     return guarded(c, [&](phx::CtxBase* x) { return phx::gatherStatsNoAlloc(x, c->precision, scenario, out, x->err); });

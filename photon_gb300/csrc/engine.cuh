@@ -589,6 +589,22 @@ public:
     }
     double radLastMs() const override { return rad.lastMs; }
 
+    // one bounded wait that nothing satisfies: the failure path a timed-out
+    // copy takes (error word, host report, context still usable)
+    int selftestWait(double limitMs) override {
+        if (!(limitMs > 0) || limitMs > 1000) { err = "self-test limit must be in (0, 1000] ms"; return PHX_ERR_INVALID; }
+        PHX_TRY(ensureTables());
+        PHX_TRY(initStream());
+        int dev = 0, khz = 0;
+        PHX_CK(cudaGetDevice(&dev));
+        PHX_CK(cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, dev));
+        const long long cycles = (long long)(limitMs * (double)std::max(khz, 1000000));
+        k_selftest_wait<R><<<1, 32, 0, st>>>(dErr, cycles);
+        PHX_CK(cudaGetLastError());
+        PHX_CK(cudaStreamSynchronize(st));
+        return checkDeviceError();
+    }
+
     // the viewer's volume ray march for scenario s (src/render/renderer.cpp:119-283)
     struct VolWork {
         float4* vol = nullptr;
@@ -1010,8 +1026,13 @@ public:
         PHX_CK(cudaMemcpyAsync(&w, dErr, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
         PHX_CK(cudaStreamSynchronize(st));
         if (w) {
-            err = "a staged shared-memory copy did not arrive within its time limit (device error word " + std::to_string(w) + ")";
-            return PHX_ERR_CUDA;
+            // report once and clear, so that the context stays usable
+            PHX_CK(cudaMemsetAsync(dErr, 0, sizeof(unsigned), st));
+            PHX_CK(cudaStreamSynchronize(st));
+            err = (w & 3u) ? "a staged shared-memory copy did not arrive within its time limit; the step's results are "
+                             "not valid (device error word " + std::to_string(w) + ")"
+                           : "a bounded device wait ran out (self-test, device error word " + std::to_string(w) + ")";
+            return PHX_ERR_TIMEOUT;
         }
         return PHX_OK;
     }
@@ -1157,11 +1178,13 @@ public:
         launchRB("k_cg_apply", cfgApply, k_cg_apply_rb<R>, S, adom[0][D_RB], (R* const*)dD, cfgApply.shape);
         launchA("k_cg_update", D_QUAD, TPB, k_cg_update<R>, S, adom[0][D_QUAD], (R* const*)dD);
         if (kMixed) {
+            if (anyClosed) launchA("k_mx_zone_center", D_CZ, TPB, k_mx_zone_center<R>, S, adom[0][D_CZ], 0);
             launchA("k_mx_update", D_CELLS, TPB, k_mx_update<R>, S, adom[1][D_CELLS], 1);
             launchA("k_mx_res64", D_CELLS, TPB, k_mx_res64<R>, S, adom[1][D_CELLS], 1);
             launchA("k_mx_zone_proj", D_CZ, TPB, k_mx_zone_proj<R>, S, adom[1][D_CZ], 1);
         }
         vcycle(1);
+        if (kMixed && anyClosed) launchA("k_mx_zone_center", D_CZ, TPB, k_mx_zone_center<R>, S, adom[0][D_CZ], 1);
     }
     // zone mean removal and velocity correction (:629-676)
     void projectEpilogue() {
@@ -1181,6 +1204,7 @@ public:
         launchA("k_mx_res64", D_CELLS, TPB, k_mx_res64<R>, S, adom[0][D_CELLS], 0);
         launchA("k_mx_zone_proj", D_CZ, TPB, k_mx_zone_proj<R>, S, adom[0][D_CZ], 0);
         vcycle(0);
+        if (anyClosed) launchA("k_mx_zone_center", D_CZ, TPB, k_mx_zone_center<R>, S, adom[0][D_CZ], 1);
     }
     void mixedEpilogue() {
         launch("k_mx_final", D_CELLS, TPB, k_mx_final<R>, dS, dom[D_CELLS]);

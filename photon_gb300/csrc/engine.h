@@ -52,6 +52,7 @@ public:
                          double* radAbs, double* radGas) = 0;
     virtual double radLastMs() const = 0;
     virtual int volRender(int s, const phx_vol_params* p, const float* depth, float* rgb) = 0;
+    virtual int selftestWait(double limitMs) = 0;
     virtual double volLastMs() const = 0;
     std::string err;
 };

@@ -103,6 +103,40 @@ __global__ void k_mx_zone_proj(const Scn<R>* __restrict__ S, ADom dom, int inLoo
     }
 }
 
+// Closed zones, every CG iteration (mixed path): the FP32 matrix's diagonal is
+// not exactly the sum of its off-diagonals, so the recursive residual r and
+// the preconditioned residual z pick up a constant per closed zone (the null
+// space of the zone's operator) that the FP32 iteration cannot remove. Their
+// mean over each closed zone is subtracted (which 0: r after its update,
+// 1: z after the V-cycle; FP64 sums, one CTA per closed zone).
+template <class R>
+__global__ void k_mx_zone_center(const Scn<R>* __restrict__ S, ADom dom, int which) {
+    __shared__ int sst_[MAX_BATCH + 1];
+    for (int i_ = threadIdx.x; i_ <= dom.nscn; i_ += blockDim.x) sst_[i_] = dom.start[i_];
+    __syncthreads();
+    const int tot_ = sst_[dom.nscn];
+    for (int b_ = blockIdx.x; b_ < tot_; b_ += gridDim.x) {
+        int s_, tile_;
+        locateShared(sst_, dom.nscn, b_, s_, tile_);
+        const Scn<R>& g = S[s_];
+        __shared__ double sh[32];
+        __shared__ double meanSh;
+        R* const a = which == 0 ? g.r : g.z;
+        const int e0 = g.closedStart[tile_], e1 = g.closedStart[tile_ + 1];
+        double acc = 0;
+        for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) acc += (double)a[g.closedCells[e]];
+        const double sum = blockSum(acc, sh);
+        if (threadIdx.x == 0) meanSh = e1 > e0 ? sum / (double)(e1 - e0) : 0.0;
+        __syncthreads();
+        const double mean = meanSh;
+        for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+            const int c = g.closedCells[e];
+            if (g.diag[c] > 0) a[c] = (R)((double)a[c] - mean);
+        }
+        __syncthreads();
+    }
+}
+
 // p64 += e: fold the FP32 iterate into the FP64 pressure
 template <class R>
 __global__ void k_mx_update(const Scn<R>* __restrict__ S, ADom dom, int inLoop) {

@@ -251,6 +251,10 @@ __device__ void closeCgIteration(const Scn<R>& g, int phase, double tot) {
             sv[SV_PREL] = rel;
             converged = !(res > g.tol) || (g.relTol > 0 && rel <= g.relTol) || !(r64 > 0);
             sv[SV_R64MAX] = 0;
+            // closed zones: the replaced residual is no longer conjugate to the
+            // search direction of the singular zone operators; restart the
+            // FP32 CG from it (d = z)
+            if (phase != 0 && g.nClosed > 0) sv[SV_BETA] = 0;
         }
         const bool stop = converged || it >= g.maxIters || !(sv[SV_RZ] > 0);
         const double rrec = sv[SV_RMAX];

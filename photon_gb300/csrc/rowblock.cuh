@@ -84,6 +84,25 @@ __device__ __forceinline__ bool mbarWaitBounded(uint64_t* b, unsigned parity, un
     return true;
 }
 
+// Self-test of the failure path of a bounded wait: one thread waits, with a
+// limit of `limitCycles`, on an mbarrier that nothing arrives on. The wait
+// runs out, the kernel records bit 4 in the context's error word and
+// returns; no copy is in flight and nothing else waits on it. R is the
+// engine's precision (one instance per engine).
+template <class R>
+__global__ void k_selftest_wait(unsigned* errWord, long long limitCycles) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x != 0) return;
+    mbarInit(&bar, 1);
+    fenceBarrierInit();
+    const long long t0 = clock64();
+    bool arrived = false;
+    while (!(arrived = mbarTryWait(&bar, 0))) {
+        if (clock64() - t0 > limitCycles) break;
+        __nanosleep(1000);
+    }
+    if (!arrived) atomicOr(errWord, 4u);
+}
 
 // One staged array of a plane slot: rows [rowLo, rowLo + rows) of plane k of
 // an array with `pitch` elements of `esz` bytes per row and `plane` elements

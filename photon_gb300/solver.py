@@ -190,6 +190,11 @@ class Solver:
     def vol_last_ms(self) -> float:
         return float(self.L.phx_vol_last_ms(self.h))
 
+    def selftest_wait_timeout(self, limit_ms: float = 20.0):
+        """Make one bounded device wait run out (phx_selftest_wait_timeout);
+        raises PhxError with PHX_ERR_TIMEOUT, after which the context is usable."""
+        self._check(self.L.phx_selftest_wait_timeout(self.h, float(limit_ms)))
+
     def device_bytes(self) -> int:
         return int(self.L.phx_device_bytes(self.h))
 

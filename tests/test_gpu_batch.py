@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from photon_gb300 import _lib, casegen
-from photon_gb300.solver import Batch, Solver
+from photon_gb300.solver import Batch, PhxError, Solver
 
 from gpu_util import STATE
 
@@ -79,3 +79,23 @@ def test_batch_equals_alone_with_many_tiles_per_cta(precision, monkeypatch):
             assert np.array_equal(a, b), (precision, s, f, float(np.max(np.abs(a - b))))
         assert B.stats(s)["pressure_iters"] == g.stats()["pressure_iters"]
         assert B.stats(s)["pressure_rel_residual"] <= 1e-8
+
+
+@pytest.mark.parametrize("precision", [_lib.PREC_FP64, _lib.PREC_MIXED])
+def test_bounded_wait_timeout_is_reported_and_context_stays_usable(precision):
+    """One bounded device wait runs out on purpose (an mbarrier nothing arrives
+    on, 20 ms limit): the call reports PHX_ERR_TIMEOUT, the error word is
+    cleared, and the same context then steps exactly like a fresh one."""
+    c = cases()[0]
+    g, ref = Solver(c, precision), Solver(c, precision)
+    g.step(0.02)
+    ref.step(0.02)
+    with pytest.raises(PhxError) as e:
+        g.selftest_wait_timeout(20.0)
+    assert e.value.code == _lib.PHX_ERR_TIMEOUT
+    assert "ran out" in str(e.value)
+    g.sync()                                   # the word was cleared: no error left
+    for _ in range(3):
+        assert g.step(0.02) == ref.step(0.02)
+    for f in STATE:
+        assert np.array_equal(g.get(f), ref.get(f)), f

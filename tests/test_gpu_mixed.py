@@ -13,6 +13,7 @@ from photon_gb300 import _lib, casegen
 from photon_gb300.solver import Solver
 
 from gpu_util import STATE, rel_l2
+from test_gpu_parity import leaky_rooms
 
 pytestmark = pytest.mark.gpu
 
@@ -31,6 +32,7 @@ CASES = {
     "room": lambda: rel_case(casegen.tiny_room(12, 10, 9, 0.2, 60e3)),
     "sealed": lambda: rel_case(casegen.tiny_room(10, 8, 8, 0.2, 40e3, doorway=False)),
     "house": lambda: rel_case(casegen.house(24, 20, 14, 0.2, 3)),
+    "leaky": lambda: rel_case(leaky_rooms()),
 }
 
 
@@ -44,6 +46,7 @@ def test_mixed_step_matches_oracle_from_identical_state(name):
     for f in STATE:
         g.set(f, o.get(f))
     g.set("lit", o.get("lit"))
+    g.set("zoneP", o.get("zoneP"))
     sc = o.scalars()
     g.set_scalars(sc["time"], sc["maxVel"], sc["maxNu"], sc["maxDiv"])
     for s in range(3):
@@ -60,6 +63,7 @@ def test_mixed_step_matches_oracle_from_identical_state(name):
         for f in STATE:
             g.set(f, o.get(f))
         g.set("lit", o.get("lit"))
+        g.set("zoneP", o.get("zoneP"))
         sc = o.scalars()
         g.set_scalars(sc["time"], sc["maxVel"], sc["maxNu"], sc["maxDiv"])
 
