@@ -201,6 +201,7 @@ struct Scenario {
         s.hrr = carve<R>(base, off, N); s.massSrc = carve<R>(base, off, N);
         s.lit = carve<uint8_t>(base, off, N); s.lit2 = carve<uint8_t>(base, off, N); s.pilot = carve<uint8_t>(base, off, N);
         for (int q = 0; q < 9; ++q) s.tmp[q] = carve<R>(base, off, N);
+        s.adv = kMixed ? nullptr : carve<double>(base, off, (size_t)ADV_REC * (NX + NY + NZ));
         s.b = carve<R>(base, off, N); s.r = carve<R>(base, off, N); s.z = carve<R>(base, off, N);
         dbuf[0] = carve<R>(base, off, N); dbuf[1] = carve<R>(base, off, N);
         s.d = dbuf[0];
@@ -1233,6 +1234,11 @@ public:
         return PHX_OK;
     }
     void stAdvect() {
+        if (!kMixed) {
+            launch("k_adv_faces", D_FX, TPB, k_adv_faces<R>, (const Scn<R>*)dS, dom[D_FX], 0);
+            launch("k_adv_faces", D_FY, TPB, k_adv_faces<R>, (const Scn<R>*)dS, dom[D_FY], 1);
+            launch("k_adv_faces", D_FZ, TPB, k_adv_faces<R>, (const Scn<R>*)dS, dom[D_FZ], 2);
+        }
         launch("k_advect", D_CELLS, TPB, k_advect<R>, (const Scn<R>*)dS, dom[D_CELLS]);
         swapBoth(4);
     }

@@ -43,6 +43,10 @@ constexpr double K_BURNER_SOOT = 0.01;
 constexpr double K_GAMMA = K_CP / (K_CP - K_RS);
 
 constexpr int NSC = 10;          // transported scalars: T Yo Yf Ys Ya Yp Yc Yw Yco Yai
+// per-face transport record: upwind density, the 10 limited face values, and
+// the diffusion terms of the 9 species for the momentum-free and the mass form
+constexpr int ADV_RUP = 0, ADV_FACE = 1, ADV_DQ = ADV_FACE + NSC, ADV_MQ = ADV_DQ + NSC - 1,
+              ADV_REC = ADV_MQ + NSC - 1;
 constexpr int MAX_SRC = 16;      // burners + ignitions per scenario
 constexpr int MAX_LEVELS = 12;   // multigrid levels (the reference's cap)
 constexpr int TPB = 256;         // threads per CTA of the cell/face kernels
@@ -127,6 +131,8 @@ struct Scn {
     R *p, *S, *nu, *Pb, *Q, *Qr, *hrr, *massSrc;
     uint8_t *lit, *lit2, *pilot;
     R* tmp[9];                   // turbulence: cell-centre velocities and filter passes
+    double* adv;                 // FP64 path: per-face transport records (ADV_REC arrays over the
+                                 // NX + NY + NZ faces, x faces first), k_adv_faces -> k_advect
     // pressure solve
     R *b, *r, *z, *d, *q;
     double* p64;                 // mixed path: FP64 pressure; the FP32 iterate p holds the part not yet folded in

@@ -795,6 +795,82 @@ __device__ __forceinline__ float superbeeTimes(float num, float den) {
     return fminf(0.f, fminf(fmaxf(2.f * num, den), fmaxf(num, 2.f * den)));
 }
 
+// FP64 path: the quantities of one interior face between two gas cells that
+// both cells' transport reads -- the upwind density, each scalar's
+// Superbee-limited face value and the species' diffusion terms -- evaluated
+// once per face, from the lower cell's side, with the cell kernel's
+// expressions. The upper cell's diffusion terms are their exact negations
+// ((a - b) = -(b - a) in IEEE arithmetic; products and quotients keep the
+// sign), its face values the same upwind expressions, its Dd and rfd the same
+// sums in the other order (IEEE addition commutes). At zero flux the cells
+// use their own values (multiplied by zero). Halves the FP64 divisions of the
+// transport.
+template <class R>
+__global__ void k_adv_faces(const Scn<R>* __restrict__ S, Dom dom, int axis) {
+    using T = R;
+    PHX_PROLOGUE(dom);
+    const int f = tile_ * TPB + threadIdx.x;
+    const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
+    const int nfa = axis == 0 ? g.NX : axis == 1 ? g.NY : g.NZ;
+    if (!g.adv || f >= nfa) return;
+    int i, j, k, id, dim, st;
+    if (axis == 0) { i = f % (nx + 1); j = (f / (nx + 1)) % ny; k = f / ((nx + 1) * ny); id = i; dim = nx; st = 1; }
+    else if (axis == 1) { i = f % nx; j = (f / nx) % (ny + 1); k = f / (nx * (ny + 1)); id = j; dim = ny; st = nx; }
+    else { i = f % nx; j = (f / nx) % ny; k = f / sxy; id = k; dim = nz; st = sxy; }
+    if (id < 1 || id > dim - 1) return;   // domain faces: one cell, evaluated inline
+    const int U = i + nx * (j + ny * k), L = U - st;
+    const T fo = axis == 0 ? g.fx[f] : axis == 1 ? g.fy[f] : g.fz[f];
+    if (!(fo > T(0)) || g.blocked[L] || g.blocked[U]) return;
+    const T un = fo * (axis == 0 ? g.u[f] : axis == 1 ? g.v[f] : g.w[f]);
+    int opp = id - 2 >= 0 ? L - st : -1, nb2 = id + 1 < dim ? U + st : -1;
+    if (opp >= 0 && g.blocked[opp]) opp = -2;
+    if (nb2 >= 0 && g.blocked[nb2]) nb2 = -2;
+    const int NF = g.NX + g.NY + g.NZ;
+    const int fg = (axis == 0 ? 0 : axis == 1 ? g.NX : g.NX + g.NY) + f;
+    double* rec = g.adv + fg;
+    const T dx = (T)g.dx;
+    // upwind density (the temperature part of :700-717)
+    {
+        const R* Tf = g.sc[0];
+        const T tn = Tf[U], tc = Tf[L];
+        T tface;
+        if (un > T(0)) {
+            T tu2 = opp >= 0 ? Tf[opp] : (opp == -1 ? T(K_T0) : tc);
+            T den = tn - tc;
+            tface = tc + (fabs(den) > T(1e-6) ? T(0.5) * superbee((tc - tu2) / den) * den : T(0));
+        } else {
+            T tu2 = nb2 >= 0 ? Tf[nb2] : (nb2 == -1 ? T(K_T0) : tn);
+            T den = tc - tn;
+            tface = tn + (fabs(den) > T(1e-6) ? T(0.5) * superbee((tn - tu2) / den) * den : T(0));
+        }
+        T pu = un > T(0) ? g.Pb[L] : g.Pb[U];
+        rec[(size_t)ADV_RUP * NF] = (double)(pu / (T(K_RS) * mx(tface, T(K_T_MIN))));
+    }
+    const T Dd = T(0.5) * (g.nu[L] + g.nu[U]) / T(K_SC_T) + T(2.0e-5);
+    const T rfd = T(0.5) * (rhoOf(g, L) + rhoOf(g, U));
+    const T amb[NSC] = {T(K_T0), T(K_YO2_AMB), T(0), T(0), T(0), T(0), T(K_YCO2_AMB), T(K_YH2O_AMB), T(0), T(0)};
+    for (int q = 0; q < NSC; ++q) {
+        const R* F = g.sc[q];
+        const T fc = F[L], fn = F[U];
+        T face = fc;
+        if (un > T(0)) {
+            T fu2 = opp >= 0 ? F[opp] : (opp == -1 ? amb[q] : fc);
+            T den = fn - fc;
+            if (fabs(den) > T(1e-12)) face += T(0.5) * superbee((fc - fu2) / den) * den;
+        } else if (un < T(0)) {
+            T fu2 = nb2 >= 0 ? F[nb2] : (nb2 == -1 ? amb[q] : fn);
+            T den = fc - fn;
+            face = fn;
+            if (fabs(den) > T(1e-12)) face += T(0.5) * superbee((fn - fu2) / den) * den;
+        }
+        rec[(size_t)(ADV_FACE + q) * NF] = (double)face;
+        if (q > 0) {
+            rec[(size_t)(ADV_DQ + q - 1) * NF] = (double)(fo * Dd * (fn - fc) / dx);
+            rec[(size_t)(ADV_MQ + q - 1) * NF] = (double)(fo * rfd * Dd * (fn - fc) / dx);
+        }
+    }
+}
+
 template <class R>
 __global__ void k_advect(const Scn<R>* __restrict__ S, Dom dom) {
     using T = R;
@@ -838,12 +914,21 @@ __global__ void k_advect(const Scn<R>* __restrict__ S, Dom dom) {
     const R* Tf = g.sc[0];
     const T nuc = g.nu[c];
     const T rc = rhoOf(g, c);
+    // FP64 path: interior faces between gas cells come from k_adv_faces
+    const double* adv = kF32 ? nullptr : g.adv;
+    const int NF = g.NX + g.NY + g.NZ;
+    const int fgl[6] = {fa0, fa1, g.NX + fb0, g.NX + fb1, g.NX + g.NY + fc0, g.NX + g.NY + fc1};
     T rUp[6], Dd[6], rfd[6], mden = rc;
     for (int d = 0; d < 6; ++d) {
         rUp[d] = 0;
         Dd[d] = 0;
         rfd[d] = 0;
         if (fo[d] <= T(0) || nb[d] == -2) continue;
+        if (adv && nb[d] >= 0) {
+            rUp[d] = (T)adv[(size_t)ADV_RUP * NF + fgl[d]];
+            mden -= s * rUp[d] * un[d];
+            continue;
+        }
         T tn = nb[d] >= 0 ? Tf[nb[d]] : T(K_T0), tc = Tf[c], tface;
         if (un[d] > T(0)) {
             T tu2 = opp[d] >= 0 ? Tf[opp[d]] : (opp[d] == -1 ? T(K_T0) : tc);
@@ -883,6 +968,19 @@ __global__ void k_advect(const Scn<R>* __restrict__ S, Dom dom) {
             lo = mn(lo, fn);
             hi = mx(hi, fn);
             T flux = un[d];
+            if (adv && nb[d] >= 0) {
+                const T face = flux != T(0) ? (T)adv[(size_t)(ADV_FACE + q) * NF + fgl[d]] : fc;
+                acc -= flux * (face - fc);
+                macc -= rUp[d] * flux * face;
+                if (q > 0) {
+                    T dq = (T)adv[(size_t)(ADV_DQ + q - 1) * NF + fgl[d]];
+                    T mq = (T)adv[(size_t)(ADV_MQ + q - 1) * NF + fgl[d]];
+                    if (!(d & 1)) { dq = -dq; mq = -mq; }   // the cell is the face's upper cell
+                    acc += dq;
+                    macc += mq;
+                }
+                continue;
+            }
             T face = fc;
             if (flux > T(0)) {
                 T fu2 = opp[d] >= 0 ? F[opp[d]] : (opp[d] == -1 ? amb[q] : fc);
