@@ -13,6 +13,7 @@
 // caller, exactly as the discretizer would leave it.
 #include "scene/materials.h"
 #include "scene/scene.h"
+#include "sim/devices.h"
 #include "sim/solver.h"
 
 #include <chrono>
@@ -373,6 +374,15 @@ void ref_rad_trace(void* h, double* radAbs, double* radGas) {
     s.traceRadiation();
     for (size_t e = 0; e < s.radAbs_.size(); ++e) radAbs[e] = s.radAbs_[e];
     for (int c = 0; c < s.N; ++c) radGas[c] = s.radGas_[c];
+}
+
+// photon::sampleDevice (src/sim/devices.h:61-96) of the harness's solver:
+// kind is the DeviceKind's position in its enum
+double ref_sample_device(void* h, int kind, double x, double y, double z, double z0, double z1) {
+    Device d;
+    d.kind = (DeviceKind)kind;
+    d.x = (float)x; d.y = (float)y; d.z = (float)z; d.z0 = (float)z0; d.z1 = (float)z1;
+    return sampleDevice(*((Ctx*)h)->s, d);
 }
 
 // Solver::saveState / Solver::loadState (src/sim/state.cpp:62-195); 0 on success

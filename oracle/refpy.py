@@ -68,6 +68,8 @@ def load(bits: int = 64):
     L.ref_phase_ms.argtypes = [vp, i]
     L.ref_set_stats.argtypes = [vp, ctypes.c_void_p]
     L.ref_rad_counts.argtypes = [vp, ctypes.c_void_p]
+    L.ref_sample_device.restype = d
+    L.ref_sample_device.argtypes = [vp, i, d, d, d, d, d]
     L.ref_rad_export.argtypes = [vp, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     L.ref_rad_trace.argtypes = [vp, ctypes.c_void_p, ctypes.c_void_p]
     L.ref_compute_zones.argtypes = [vp]
@@ -215,6 +217,14 @@ class RefSolver:
         gas = np.zeros(n, np.float64)
         self.L.ref_rad_trace(self.h, _ptr(ab), _ptr(gas))
         return ab, gas
+
+    # photon::DeviceKind (src/sim/devices.h:11)
+    DEVICE_KINDS = ("Temperature", "VelU", "VelV", "VelW", "LayerHeight", "UpperTemp", "LowerTemp", "O2", "CO2",
+                    "CO", "Soot", "Pressure")
+
+    def sample_device(self, kind: str, x: float, y: float, z: float, z0: float = 0.0, z1: float = 0.0) -> float:
+        """photon::sampleDevice on this solver (src/sim/devices.h:61-96)."""
+        return self.L.ref_sample_device(self.h, self.DEVICE_KINDS.index(kind), x, y, z, z0, z1)
 
     def compute_zones(self):
         self.L.ref_compute_zones(self.h)

@@ -126,3 +126,28 @@ def test_gpu_refuses_state_of_other_zones(tmp_path):
     g = Solver(_cases()["room"])
     with pytest.raises(PhxError):
         g.import_state(sealed)
+
+
+@pytest.mark.gpu
+def test_reference_devices_read_gpu_state():
+    """The reference's own device probes (photon::sampleDevice,
+    src/sim/devices.h) on a host solver holding the GPU's exported state read
+    what they read on the reference's own run of the same case (FP64 builds,
+    8 steps): thermocouples, velocities, gas fractions, soot, pressure and the
+    two-zone layer reduction."""
+    c = _cases()["room"]
+    g = Solver(c)
+    r = refpy.RefSolver(c, 64, 2)
+    for _ in range(8):
+        g.step(0.02)
+        r.step(0.02)
+    host = refpy.RefSolver(c, 64, 2)
+    host.compute_zones()
+    g.export_state(host)
+    x, y = c.ox + 0.45 * c.nx * c.dx, c.oy + 0.5 * c.ny * c.dx
+    probes = [(k, x, y, z, 0.0, 0.0) for k in ("Temperature", "VelU", "VelV", "VelW", "O2", "CO2", "CO", "Soot",
+                                                "Pressure") for z in (0.3, 0.9, 1.5)]
+    probes += [(k, x, y, 0.0, 0.0, c.nz * c.dx) for k in ("LayerHeight", "UpperTemp", "LowerTemp")]
+    for kind, px, py, pz, z0, z1 in probes:
+        a, b = host.sample_device(kind, px, py, pz, z0, z1), r.sample_device(kind, px, py, pz, z0, z1)
+        assert abs(a - b) <= 1e-7 * max(1.0, abs(b)), (kind, pz, a, b)
