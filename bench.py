@@ -248,11 +248,12 @@ def run_reference(args, rank, world):
     v = cells * args.steps / el
     desc = "%d steps of %d of the %d scenarios (%d cells) after %d spin-up and %d warm-up steps" % (
         args.steps, len(sample), len(cases), cells, args.spinup, args.warmup)
-    line = {"metric": METRIC, "value": v, "unit": "cell-updates/s", "n_gpus": 0, "steps": args.steps,
+    line = {"metric": METRIC, "value": v, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded house generator)",
             "config": {"workload": args.workload, "scenarios_sampled": len(sample), "cells": cells,
-                       "pressure_stop": "absolute 1e-8 1/s", "threads": threads, "spinup_steps": args.spinup},
+                       "pressure_stop": "absolute 1e-8 1/s", "threads": threads, "spinup_steps": args.spinup,
+                       "hardware": "host CPU cores of rank 0 (the reference has no GPU path)"},
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": "reference",
                              "sample": desc},
