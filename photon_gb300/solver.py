@@ -300,10 +300,36 @@ class Batch:
         self._check(self.L.phx_batch_get_field(self.h, s, fid, _ptr(a), a.nbytes))
         return a
 
+    def set(self, s: int, name: str, arr):
+        dt = np.uint8 if name == "lit" else np.int32 if name == "zone" else np.float64
+        a = np.ascontiguousarray(arr, dtype=dt)
+        self._check(self.L.phx_batch_set_field(self.h, s, FIELD_ID[name], _ptr(a), a.nbytes))
+
     def stats(self, s: int) -> dict:
         st = PhxStats()
         self._check(self.L.phx_batch_get_stats(self.h, s, ctypes.byref(st)))
         return {k: getattr(st, k) for k, _ in PhxStats._fields_}
+
+    def rad_trace(self, s: int, elements, walls, solid_t=None, gas: bool = True):
+        """Solver.rad_trace for scenario s of the batch (phx_batch_rad_trace)."""
+        el, wl = _lib.rad_elements(elements), _lib.rad_walls(walls)
+        n = len(self.get(s, "T"))
+        st = None if solid_t is None else np.ascontiguousarray(solid_t, np.float64)
+        ab = np.zeros(len(el), np.float64)
+        g = np.zeros(n, np.float64) if gas else None
+        self._check(self.L.phx_batch_rad_trace(self.h, s, el.ctypes.data if len(el) else None, len(el),
+                                               wl.ctypes.data if len(wl) else None, len(wl),
+                                               None if st is None else st.ctypes.data, ab.ctypes.data,
+                                               None if g is None else g.ctypes.data))
+        return ab, g
+
+    def vol_render(self, s: int, params, depth=None) -> np.ndarray:
+        """Solver.vol_render for scenario s of the batch (phx_batch_vol_render)."""
+        rgb = np.zeros((params.height, params.width, 3), np.float32)
+        d = None if depth is None else np.ascontiguousarray(depth, np.float32)
+        self._check(self.L.phx_batch_vol_render(self.h, s, ctypes.byref(params), None if d is None else d.ctypes.data,
+                                                rgb.ctypes.data))
+        return rgb
 
     def device_bytes(self) -> int:
         return int(self.L.phx_device_bytes(self.h))

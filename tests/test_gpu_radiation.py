@@ -113,3 +113,27 @@ def test_trace_rejects_bad_walls():
     bad[0, 0], bad[0, 1] = 3, 0
     with pytest.raises(PhxError, match="out of range"):
         g.rad_trace(fx["elements"][:4], bad, None)
+
+
+def test_trace_and_render_of_a_batch_scenario():
+    """phx_batch_rad_trace / phx_batch_vol_render on scenario 1 of a batch
+    equal the single-context calls on the same case and fields."""
+    from photon_gb300 import render
+    from photon_gb300.solver import Batch
+    c0, c1 = casegen.tiny_room(12, 10, 9, 0.2, 60e3), casegen.house_small(2)
+    w = casegen.rad_workload(c1)
+    B = Batch([c0, c1], _lib.PREC_FP64)
+    g = Solver(c1, _lib.PREC_FP64)
+    gas = dict(w["gas"])
+    gas["Ys"] = gas["Ys"] * 0.01
+    for f, a in gas.items():
+        B.set(1, f, a)
+        g.set(f, a)
+    ab_b, gas_b = B.rad_trace(1, w["elements"], w["walls"], w["solidT"])
+    ab_g, gas_g = g.rad_trace(w["elements"], w["walls"], w["solidT"])
+    np.testing.assert_array_equal(ab_b, ab_g)                 # absorbed powers are summed in a fixed order
+    assert rel_l2(gas_b, gas_g) <= 1e-13                      # gas cells gain by atomic adds
+    cx, cy = c1.ox + c1.nx * c1.dx / 2, c1.oy + c1.ny * c1.dx / 2
+    p = render.camera(c1, eye=(cx - 14, cy - 16, 9.0), target=(cx, cy, 2.0), width=96, height=54,
+                      lights=render.fire_lights(c1, gas["hrr"]))
+    np.testing.assert_array_equal(B.vol_render(1, p), g.vol_render(p))
