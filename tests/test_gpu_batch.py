@@ -99,4 +99,3 @@ def test_bounded_wait_timeout_is_reported_and_context_stays_usable(precision):
         assert g.step(0.02) == ref.step(0.02)
     for f in STATE:
         assert np.array_equal(g.get(f), ref.get(f)), f
-
