@@ -872,7 +872,7 @@ __global__ void k_adv_faces(const Scn<R>* __restrict__ S, Dom dom, int axis) {
 }
 
 template <class R>
-__global__ void k_advect(const Scn<R>* __restrict__ S, Dom dom) {
+__global__ void __launch_bounds__(TPB, 2) k_advect(const Scn<R>* __restrict__ S, Dom dom) {
     using T = R;
     PHX_PROLOGUE(dom);
     int c = tile_ * TPB + threadIdx.x;
