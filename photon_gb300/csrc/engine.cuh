@@ -1111,7 +1111,14 @@ public:
             for (int a = 0; a < 3; ++a) launch("k_turb_filter", D_CELLS, TPB, k_turb_filter<R>, S, dom[D_CELLS], q, a);
         launch("k_turb_nu", D_CELLS, TPB, k_turb_nu<R>, S, dom[D_CELLS]);
     }
-    void stHeat() { launch("k_heat", D_CELLS, TPB, k_heat<R>, (const Scn<R>*)dS, dom[D_CELLS]); }
+    void stHeat() {
+        if (!kMixed) {   // FP64: each interior face's conductive flux once
+            launch("k_heat_faces", D_FX, TPB, k_heat_faces<R>, (const Scn<R>*)dS, dom[D_FX], 0);
+            launch("k_heat_faces", D_FY, TPB, k_heat_faces<R>, (const Scn<R>*)dS, dom[D_FY], 1);
+            launch("k_heat_faces", D_FZ, TPB, k_heat_faces<R>, (const Scn<R>*)dS, dom[D_FZ], 2);
+        }
+        launch("k_heat", D_CELLS, TPB, k_heat<R>, (const Scn<R>*)dS, dom[D_CELLS]);
+    }
     void stEnergy() { launch("k_energy", D_CELLS, TPB, k_energy<R>, (const Scn<R>*)dS, dom[D_CELLS]); }
     void stMomentum() {
         const Scn<R>* S = dS;

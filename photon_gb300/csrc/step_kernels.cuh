@@ -295,6 +295,37 @@ __global__ void k_turb_nu(const Scn<R>* __restrict__ S, Dom dom) {
 
 // ---------------------------------------------------------------------------
 // Solver::heatDiffusion (src/sim/gasphase.cpp:221-248)
+// FP64 path: the conductive flux of every interior face between two gas cells,
+// fo kf dx (T_upper - T_lower), once per face into the transport's record
+// scratch (free at this point of the step). kf is symmetric in the two cells
+// (the sums commute in IEEE arithmetic), and the lower cell's term is the
+// exact negation of the upper cell's, so k_heat's sums are unchanged.
+template <class R>
+__global__ void k_heat_faces(const Scn<R>* __restrict__ S, Dom dom, int axis) {
+    using T = R;
+    PHX_PROLOGUE(dom);
+    const int f = tile_ * TPB + threadIdx.x;
+    const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
+    const int nfa = axis == 0 ? g.NX : axis == 1 ? g.NY : g.NZ;
+    if (!g.adv || f >= nfa) return;
+    int i, j, k, id, dim, st;
+    if (axis == 0) { i = f % (nx + 1); j = (f / (nx + 1)) % ny; k = f / ((nx + 1) * ny); id = i; dim = nx; st = 1; }
+    else if (axis == 1) { i = f % nx; j = (f / nx) % (ny + 1); k = f / (nx * (ny + 1)); id = j; dim = ny; st = nx; }
+    else { i = f % nx; j = (f / nx) % ny; k = f / sxy; id = k; dim = nz; st = sxy; }
+    if (id < 1 || id > dim - 1) return;
+    const int U = i + nx * (j + ny * k), L = U - st;
+    const T fo = axis == 0 ? g.fx[f] : axis == 1 ? g.fy[f] : g.fz[f];
+    if (fo <= T(0) || g.blocked[L] || g.blocked[U]) return;
+    const R* Tf = g.sc[0];
+    const T dx = (T)g.dx;
+    // from the lower cell's side, as k_heat evaluates it (src/sim/gasphase.cpp:230-243)
+    const T Tc = Tf[L], Tn = Tf[U], nuc = g.nu[L], nun = g.nu[U];
+    const T rc = rhoOf(g, L), rn = rhoOf(g, U);
+    const T Tface = T(0.5) * (Tc + Tn);
+    const T kf = T(0.5) * (rc + rn) * T(K_CP) * T(0.5) * (nuc + nun) / T(K_PR_T) + T(0.0258) * pow(Tface / T(293.15), T(0.8));
+    g.adv[(axis == 0 ? 0 : axis == 1 ? g.NX : g.NX + g.NY) + f] = (double)(fo * kf * dx * (Tn - Tc));
+}
+
 template <class R>
 __global__ void k_heat(const Scn<R>* __restrict__ S, Dom dom) {
     using T = R;
@@ -311,10 +342,17 @@ __global__ void k_heat(const Scn<R>* __restrict__ S, Dom dom) {
     const T dx = (T)g.dx;
     const T Tc = Tf[c], nuc = g.nu[c];
     T rc = rhoOf(g, c), q = 0;
+    const double* hf = std::is_same<T, float>::value ? nullptr : g.adv;   // FP64: fluxes from k_heat_faces
+    const int fgl[6] = {fx0, fx0 + 1, g.NX + fy0, g.NX + fy0 + nx, g.NX + g.NY + c, g.NX + g.NY + c + sxy};
     for (int d = 0; d < 6; ++d) {
         if (fo[d] <= T(0)) continue;
         int n = nb[d];
         if (n >= 0 && g.blocked[n]) continue;
+        if (hf && n >= 0) {
+            const T F = (T)hf[fgl[d]];
+            q += (d & 1) ? F : -F;   // the cell is the face's lower cell for d odd
+            continue;
+        }
         T Tn = n >= 0 ? Tf[n] : T(K_T0);
         T nun = n >= 0 ? g.nu[n] : nuc;
         T rn = n >= 0 ? rhoOf(g, n) : T(K_P0) / (T(K_RS) * T(K_T0));
