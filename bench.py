@@ -146,7 +146,10 @@ class ClockSampler:
 
     def __init__(self, gpu_index: int):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "bench_clocks_%d.csv" % os.getpid())
+        # raw samples: PHX_CLOCKS_DIR if set, else the system temporary directory
+        import tempfile
+        self.path = os.path.join(os.environ.get("PHX_CLOCKS_DIR", tempfile.gettempdir()),
+                                 "bench_clocks_%d.csv" % os.getpid())
         self.gpu = gpu_index
 
     def __enter__(self):
