@@ -207,6 +207,7 @@ struct Scenario {
         s.d = dbuf[0];
         s.q = carve<R>(base, off, N);
         s.p64 = kMixed ? carve<double>(base, off, N) : nullptr;
+        s.p64prev = kMixed ? carve<double>(base, off, N) : nullptr;
         s.nLevels = nl;
         for (int l = 0; l < nl; ++l) {
             const MgLevel& L = MG.lv[l];
@@ -278,6 +279,7 @@ struct Scenario {
         s.nClosed = (int)Z.closed.size();
         s.mixed = kMixed ? 1 : 0;
         s.replaceEvery = REPLACE_EVERY;
+        s.extrap = std::getenv("PHX_NO_EXTRAP") == nullptr;   // mixed path: extrapolated initial guess
         s.fp16Scratch = kMixed && std::getenv("PHX_FP16_SCRATCH") != nullptr;
         s.tj = rowBlockRows<R>(geo.nx, geo.ny);
         s.njb = (geo.ny + s.tj - 1) / s.tj;
@@ -1208,6 +1210,7 @@ public:
         const Scn<R>* S = dS;
         launch("k_reset", D_ONE, 32, k_reset<R>, S, dom[D_ONE], 0);
         rebuildActive();
+        launch("k_mx_extrap", D_CELLS, TPB, k_mx_extrap<R>, S, dom[D_CELLS]);
         launch("k_rhs", D_CELLS, TPB, k_rhs<R>, S, dom[D_CELLS]);
         launchA("k_mx_res64", D_CELLS, TPB, k_mx_res64<R>, S, adom[0][D_CELLS], 0);
         launchA("k_mx_zone_proj", D_CZ, TPB, k_mx_zone_proj<R>, S, adom[0][D_CZ], 0);
@@ -1506,7 +1509,12 @@ public:
         Scenario<R>& S = *sc[s];
         if (t == 0) {
             const double* d = (const double*)host;
-            if (kMixed && f == PHX_FIELD_P) PHX_TRY(S.putRaw(st, S.h.p64, d, n));
+            if (kMixed && f == PHX_FIELD_P) {
+                PHX_TRY(S.putRaw(st, S.h.p64, d, n));
+                const double zero = 0;   // the previous step's pressure no longer applies
+                PHX_CK(cudaMemcpyAsync(S.h.sv + SV_HAVEPREV, &zero, sizeof(double), cudaMemcpyHostToDevice, st));
+                PHX_CK(cudaStreamSynchronize(st));
+            }
             return S.put(st, (R*)p, std::vector<double>(d, d + n));
         }
         PHX_CK(cudaMemcpyAsync(p, host, bytes, cudaMemcpyHostToDevice, st));

@@ -137,6 +137,22 @@ __global__ void k_mx_zone_center(const Scn<R>* __restrict__ S, ADom dom, int whi
     }
 }
 
+// start of a mixed solve: the initial guess 2 p(n) - p(n-1) when the previous
+// step's pressure is known (a linear extrapolation in time), and p(n) kept
+// as the next step's p(n-1). The solve stops on the same residual test, so
+// only the iteration count depends on the guess.
+template <class R>
+__global__ void k_mx_extrap(const Scn<R>* __restrict__ S, Dom dom) {
+    int s_, tile_;
+    locate(dom, blockIdx.x, s_, tile_);
+    const Scn<R>& g = S[s_];
+    const int c = tile_ * TPB + threadIdx.x;
+    if (c >= g.N || !g.p64prev) return;
+    const double cur = g.p64[c];
+    if (g.extrap && g.sv[SV_HAVEPREV] != 0 && g.diag[c] > 0) g.p64[c] = 2.0 * cur - g.p64prev[c];
+    g.p64prev[c] = cur;
+}
+
 // p64 += e: fold the FP32 iterate into the FP64 pressure
 template <class R>
 __global__ void k_mx_update(const Scn<R>* __restrict__ S, ADom dom, int inLoop) {
@@ -169,6 +185,7 @@ __global__ void k_mx_final(const Scn<R>* __restrict__ S, Dom dom) {
     if (g.diag[c] > 0) v += (double)g.p[c];
     g.p64[c] = v;
     g.p[c] = (R)v;
+    if (c == 0) g.sv[SV_HAVEPREV] = 1;
 }
 
 // simulated time of every scenario into one array (one read-back per batch)

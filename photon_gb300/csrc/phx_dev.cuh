@@ -60,6 +60,7 @@ enum Slot {
     SV_INV, SV_ACTIVE,
     // mixed path: FP64 refinement loop around the FP32 inner CG
     SV_R64MAX, SV_R0MAX, SV_OUTER, SV_ODONE, SV_ITTOT, SV_REPL,
+    SV_HAVEPREV,                 // mixed path: p64prev holds the previous step's pressure
     SV_SRC_MF = 32,              // MAX_SRC injection amounts of this step (-1 = inactive)
     SV_COUNT = 64
 };
@@ -138,6 +139,8 @@ struct Scn {
     double* p64;                 // mixed path: FP64 pressure; the FP32 iterate p holds the part not yet folded in
     int mixed;                   // mixed path: FP32 CG with FP64 residual replacement
     int replaceEvery;            // mixed path: iterations between FP64 residual replacements
+    int extrap;                  // mixed path: start the solve from 2 p(n) - p(n-1) (PHX_NO_EXTRAP=1: from p(n))
+    double* p64prev;             // mixed path: the previous step's pressure (FP64)
     int fp16Scratch;             // mixed path: Jacobi scratch rounded to FP16 (an accuracy study; off by default)
     int nLevels;
     Level<R> lv[MAX_LEVELS];
