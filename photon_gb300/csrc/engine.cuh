@@ -979,8 +979,10 @@ public:
         ++launches;
     }
 
-    // persistent grid over the active tiles of domain d (solve kernels)
-    static constexpr int PERSIST_CTAS = 152 * 8;
+    // persistent grid over the active tiles of domain d (solve kernels): 16 CTAs of 256
+    // threads per SM of GB300 measured best on the 64-scenario batch (8: 274.5, 12: 278.5,
+    // 16: 279.0, 32: 278.2 M cell-updates/s; a CTA per tile: 268.7)
+    static constexpr int PERSIST_CTAS = 152 * 16;
     int persistCtas = PERSIST_CTAS;   // PHX_PERSIST_CTAS caps it (tests: many tiles per CTA)
     template <class K, class... A>
     void launchA(const char* name, int d, int threads, K kern, A... args) {
