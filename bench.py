@@ -516,6 +516,53 @@ def measure_volume(args, cpu_baseline: bool):
     return out
 
 
+def precision_study(args):
+    """The precision form's outputs on the seeded house at 10 cm (144x104x88 =
+    1.32 M cells): the per-step pressure error of the mixed path against the
+    FP64 path stepped from the same state (sampled along the FP64 run), the
+    mixed solve's divergence residual on every step, and the layer-averaged
+    temperature profile of the two runs after args.study_seconds simulated.
+    The FP64 GPU path is the FP64 run here (it tracks the oracle within 1e-9
+    per step)."""
+    from photon_gb300 import _lib, casegen
+    from photon_gb300.solver import Solver
+    c = casegen.house_fine(1)
+    c.profile.tol = 0.0
+    c.profile.rel_tol = REL_TOL
+    dt_max = c.profile.dtMax
+    f64, mx, probe = Solver(c, _lib.PREC_FP64), Solver(c, _lib.PREC_MIXED), Solver(c, _lib.PREC_MIXED)
+    rel = lambda a, b: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+    p_err, n64 = [], 0
+    while f64.stats()["time"] < args.study_seconds:
+        if n64 % args.study_every == args.study_every // 2:
+            f64.export_state(probe)           # identical state, then one step each
+            probe.step(dt_max)
+            f64.step(dt_max)
+            p_err.append(rel(probe.get("p"), f64.get("p")))
+        else:
+            f64.step(dt_max)
+        n64 += 1
+    rres, nmx = [], 0
+    while mx.stats()["time"] < args.study_seconds:
+        mx.step(dt_max)
+        rres.append(mx.stats()["pressure_rel_residual"])
+        nmx += 1
+    gas = c.blocked.reshape(c.nz, c.ny, c.nx) == 0
+    def layers(g):
+        T = g.get("T").reshape(c.nz, c.ny, c.nx)
+        return np.array([T[k][gas[k]].mean() if gas[k].any() else np.nan for k in range(c.nz)])
+    lf, lm = layers(f64), layers(mx)
+    ok = ~np.isnan(lf)
+    lerr = np.abs(lm[ok] - lf[ok]) / lf[ok]
+    return {"workload": "house %dx%dx%d at %.1f m (%d cells), seed 1" % (c.nx, c.ny, c.nz, c.dx, c.N),
+            "simulated_s": args.study_seconds, "steps": {"fp64": n64, "mixed": nmx},
+            "pressure_rel_l2_one_step_from_fp64_state": {"samples": len(p_err), "max": max(p_err),
+                                                         "median": float(np.median(p_err))},
+            "mixed_rel_residual": {"max": max(rres), "steps_above_1e-8": int(sum(r > REL_TOL for r in rres))},
+            "layer_T_rel_err": {"max": float(lerr.max()), "mean": float(lerr.mean())},
+            "layer_T_K": {"fp64": [round(float(v), 2) for v in lf[ok]], "mixed": [round(float(v), 2) for v in lm[ok]]}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -532,6 +579,10 @@ def main():
     ap.add_argument("--no-radiation", action="store_true", help="skip the radiation trace and volume render")
     ap.add_argument("--extras-only", action="store_true",
                     help="time only the radiation trace and the volume render (one JSON line)")
+    ap.add_argument("--precision-study", action="store_true",
+                    help="the precision form's error outputs on the 1.32 M-cell house (one JSON line)")
+    ap.add_argument("--study-seconds", type=float, default=60.0)
+    ap.add_argument("--study-every", type=int, default=200, help="FP64 steps between pressure-error samples")
     ap.add_argument("--extras-case", default="fine", choices=["fine", "small"],
                     help="house for the trace and the render: 144x104x88 at 0.1 m, or 72x52x44 at 0.2 m")
     ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64"],
@@ -550,6 +601,10 @@ def main():
     L = _lib.load()
     if L.phx_select_device(local) != 0:
         raise SystemExit("cannot select device %d" % local)
+    if args.precision_study:
+        if rank == 0:
+            print(json.dumps(precision_study(args)))
+        return 0
     if args.extras_only:
         if rank == 0:
             print(json.dumps({"radiation_trace": measure_radiation(args, not args.no_cpu_baseline),
