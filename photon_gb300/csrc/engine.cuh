@@ -1251,7 +1251,7 @@ public:
             launch("k_adv_faces", D_FY, TPB, k_adv_faces<R>, (const Scn<R>*)dS, dom[D_FY], 1);
             launch("k_adv_faces", D_FZ, TPB, k_adv_faces<R>, (const Scn<R>*)dS, dom[D_FZ], 2);
         }
-        launch("k_advect", D_CELLS, TPB, k_advect<R>, (const Scn<R>*)dS, dom[D_CELLS]);
+        launch("k_advect", D_CELLS, TPB, kMixed ? k_advect<R> : k_advect_2cta<R>, (const Scn<R>*)dS, dom[D_CELLS]);
         swapBoth(4);
     }
     void stEnd() {
