@@ -42,7 +42,8 @@ enum {
 /* precision of a context */
 enum {
     PHX_PREC_FP64 = 0,   /* every field and every operation in FP64 */
-    PHX_PREC_MIXED = 1   /* FP32 fields and stencils, FP16 smoother scratch, FP64 dots/refinement/global sums */
+    PHX_PREC_MIXED = 1   /* FP32 fields, stencils and smoother scratch; FP64 dots, residual
+                            refinement, closed-zone mean removal and global sums */
 };
 
 /* Grid and settings of one scenario. Mirrors what Solver::build leaves in the
