@@ -66,21 +66,12 @@ __global__ void k_stats_noalloc(const Scn<R>* __restrict__ gp, double* __restric
     __shared__ double sh[32];
     __shared__ int amLast;
     const int tile = blockIdx.x, ntiles = gridDim.x;
-    const int c = tile * NA_TPB + threadIdx.x;
-    const double V = g.dx * g.dx * g.dx;
-    double h = 0, fd = 0, mt = 0, nb = 0;
-    if (c < g.N && !g.blocked[c]) {
-        const double hr = g.hrr[c];
-        fd = (double)g.sc[2][c] * gasDensity(g, c) * V;
-        h = hr * V;
-        mt = g.sc[0][c];
-        nb = hr > 0 ? 1.0 : 0.0;
-    }
-    blockMaxTo(w + NA_MAXT, mt);
-    const double nbs = blockSum(nb, sh);
-    if (threadIdx.x == 0 && nbs > 0) atomicAdd(w + NA_BURN, nbs);
-    const double fs = blockSum(fd, sh);
-    const double hs = blockSum(h, sh);
+    const StatsTerms<R> st = statsTerms(g, tile * NA_TPB + threadIdx.x);
+    blockMaxTo(w + NA_MAXT, st.t);
+    const int nbs = __syncthreads_count(st.burning);
+    if (threadIdx.x == 0 && nbs > 0) atomicAdd(w + NA_BURN, (double)nbs);
+    const double fs = blockSum(st.fd, sh);
+    const double hs = blockSum(st.h, sh);
     if (threadIdx.x == 0) {
         w[NA_HEAD + tile] = hs;
         w[NA_HEAD + NA_MAX_TILES + tile] = fs;

@@ -277,7 +277,7 @@ __global__ void k_turb_nu(const Scn<R>* __restrict__ S, Dom dom) {
     using T = R;
     PHX_PROLOGUE(dom);
     int c = tile_ * TPB + threadIdx.x;
-    double m = 0;
+    T m = 0;   // the max is taken in the arithmetic type: no FP64 instruction per cell on the mixed path
     if (c < g.N) {
         if (g.blocked[c]) g.nu[c] = 0;
         else {
@@ -287,7 +287,7 @@ __global__ void k_turb_nu(const Scn<R>* __restrict__ S, Dom dom) {
             T ks = T(0.5) * (du * du + dv * dv + dw * dw);
             T nu = mn(T(1), T(K_C_NU) * (T)g.dx * sqrt(ks) + T(1.5e-5) * pow(g.sc[0][c] / T(293.15), T(1.7)));
             g.nu[c] = nu;
-            m = (double)nu;
+            m = nu;
         }
     }
     blockMaxTo(g.sv + SV_MAXNU, m);
@@ -369,7 +369,7 @@ __global__ void k_energy(const Scn<R>* __restrict__ S, Dom dom) {
     using T = R;
     PHX_PROLOGUE(dom);
     int c = tile_ * TPB + threadIdx.x;
-    double md = 0;
+    T md = 0;
     if (c < g.N) {
         if (g.blocked[c]) g.S[c] = 0;
         else {
@@ -385,7 +385,7 @@ __global__ void k_energy(const Scn<R>* __restrict__ S, Dom dom) {
             g.sc[0][c] = Tn;
             T Sv = clampd(D, -T(K_D_MAX), T(K_D_MAX));
             g.S[c] = Sv;
-            md = fabs((double)Sv);
+            md = fabs(Sv);
         }
     }
     blockMaxTo(g.sv + SV_MAXDIV, md);
@@ -671,7 +671,7 @@ __global__ void k_rhs(const Scn<R>* __restrict__ S, Dom dom) {
     using T = R;
     PHX_PROLOGUE(dom);
     int c = tile_ * TPB + threadIdx.x;
-    double bm = 0, rm = 0;
+    T bm = 0, rm = 0;
     if (c < g.N) {
         if (g.blocked[c]) {
             g.b[c] = 0;
@@ -716,10 +716,10 @@ __global__ void k_rhs(const Scn<R>* __restrict__ S, Dom dom) {
                 if (k > 0) s -= A4 * x[c - sxy];
                 if (k < nz - 1) s -= A5 * x[c + sxy];
                 r = b - s;
-                bm = fabs((double)b);
+                bm = fabs(b);
             }
             g.r[c] = r;
-            rm = fabs((double)r);
+            rm = fabs(r);
         }
     }
     blockMaxTo(g.sv + SV_BMAX, bm);
@@ -771,7 +771,7 @@ __global__ void k_velcorr(const Scn<R>* __restrict__ S, Dom dom, int comp) {
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     const int dX = nx + (comp == 0), dY = ny + (comp == 1), dZ = nz + (comp == 2);
     int f = tile_ * TPB + threadIdx.x;
-    double vm = 0;
+    T vm = 0;
     if (f < dX * dY * dZ) {
         const int i = f % dX, j = (f / dX) % dY, k = f / (dX * dY);
         R* vel = comp == 0 ? g.u : comp == 1 ? g.v : g.w;
@@ -809,7 +809,7 @@ __global__ void k_velcorr(const Scn<R>* __restrict__ S, Dom dom, int comp) {
                     vel[f] = un;
                 }
             }
-            vm = fabs((double)un) * (double)fof;
+            vm = fabs(un) * fof;   // in the arithmetic type, as the reference's float build
         }
     }
     blockMaxTo(g.sv + SV_MAXVEL, vm);
@@ -1092,24 +1092,47 @@ __global__ void k_zone_pb(const Scn<R>* __restrict__ S, Dom dom) {
     g.Pb[c] = (R)g.zoneP[g.zone[c]];
 }
 
+// gatherStats' terms of cell c (src/sim/solver.cpp:889-894): heat release
+// hrr V, fuel mass Yf rho V, temperature, burning flag; zero for blocked cells
+// and c >= N. FP64 path: in FP64. Mixed path: the FP32 terms of the
+// reference's float build (its gasDensity and hrr V are float), carried as
+// double-float pairs into the sums, so that no FP64 instruction runs per cell.
+template <class R>
+struct StatsTerms {
+    decltype(dotTerm(R(0), R(0))) h{}, fd{};   // double, or F2 on the mixed path
+    R t = 0;
+    int burning = 0;
+};
+template <class R>
+__device__ __forceinline__ StatsTerms<R> statsTerms(const Scn<R>& g, int c) {
+    StatsTerms<R> o;
+    if (c >= g.N || g.blocked[c]) return o;
+    const R hr = g.hrr[c];
+    if constexpr (sizeof(R) == 4) {
+        const float dxf = (float)g.dx, V = dxf * dxf * dxf;
+        const float rho = g.Pb[c] / ((float)K_RS * g.sc[0][c]);
+        o.h = F2{hr * V, 0.f};
+        o.fd = F2{g.sc[2][c] * rho * V, 0.f};
+    } else {
+        const double V = g.dx * g.dx * g.dx;
+        o.fd = g.sc[2][c] * gasDensity(g, c) * V;
+        o.h = hr * V;
+    }
+    o.t = g.sc[0][c];
+    o.burning = hr > 0;
+    return o;
+}
+
 template <class R>
 __global__ void k_stats(const Scn<R>* __restrict__ S, Dom dom) {
     PHX_PROLOGUE(dom);
     __shared__ double shA[32];
-    int c = tile_ * TPB + threadIdx.x;
-    const double V = g.dx * g.dx * g.dx;
-    double h = 0, fd = 0, mt = 0, nb = 0;
-    if (c < g.N && !g.blocked[c]) {
-        double hr = g.hrr[c];
-        fd = (double)g.sc[2][c] * gasDensity(g, c) * V;
-        h = hr * V;
-        mt = g.sc[0][c];
-        nb = hr > 0 ? 1.0 : 0.0;
-    }
-    blockMaxTo(g.sv + SV_MAXGAST, mt);
-    double nbs = blockSum(nb, shA);
-    if (threadIdx.x == 0 && nbs > 0) atomicAdd(g.sv + SV_BURNING, nbs);
-    double fs = blockSum(fd, shA);
+    const StatsTerms<R> st = statsTerms(g, tile_ * TPB + threadIdx.x);
+    const auto h = st.h;
+    blockMaxTo(g.sv + SV_MAXGAST, st.t);
+    const int nbs = __syncthreads_count(st.burning);
+    if (threadIdx.x == 0 && nbs > 0) atomicAdd(g.sv + SV_BURNING, (double)nbs);
+    double fs = blockSum(st.fd, shA);
     int nt = ntilesOf(dom, s_);
     double tot;
     // two partial slots; the last CTA of the first closes both
