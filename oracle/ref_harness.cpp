@@ -16,7 +16,9 @@
 #include "sim/devices.h"
 #include "sim/solver.h"
 
+#include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -169,6 +171,21 @@ void ref_set_profile(void* h, double cfl, double dtMax, int maxIters, double tol
     Solver& s = *((Ctx*)h)->s;
     s.profile.cfl = (float)cfl; s.profile.dtMax = (float)dtMax;
     s.profile.pressureMaxIters = maxIters; s.profile.pressureTol = (float)tol;
+}
+
+// the CG stop of the next steps: Solver::profile.pressureTol, 1/s (the
+// reference's only stop test, src/sim/gasphase.cpp:604-605)
+void ref_set_pressure_tol(void* h, double tol) {
+    ((Ctx*)h)->s->profile.pressureTol = (float)tol;
+}
+
+// max |b| of the last projection's right-hand side (src/sim/gasphase.cpp:528-549),
+// in the solver's units: 1/s times dx^2 / dt
+double ref_rhs_max_abs(void* h) {
+    const Solver& s = *((Ctx*)h)->s;
+    float m = 0;
+    for (float v : s.rhs_) m = std::max(m, std::fabs(v));
+    return m;
 }
 
 void ref_set_switches(void* h, int radiationOn, int adiabatic) {

@@ -45,6 +45,9 @@ def load(bits: int = 64):
     L.ref_grid_info.argtypes = [vp, ctypes.c_void_p, ctypes.c_void_p]
     L.ref_set_profile.argtypes = [vp, d, d, i, d]
     L.ref_set_switches.argtypes = [vp, i, i]
+    L.ref_set_pressure_tol.argtypes = [vp, d]
+    L.ref_rhs_max_abs.restype = d
+    L.ref_rhs_max_abs.argtypes = [vp]
     L.ref_set_wind.argtypes = [vp, d, d, d]
     L.ref_mark_geometry_dirty.argtypes = [vp]
     L.ref_add_burner.argtypes = [vp, d, d, d, d, d, d, d, d, d]
@@ -160,6 +163,25 @@ class RefSolver:
 
     def step(self, dtMax: float) -> float:
         return self.L.ref_step(self.h, dtMax)
+
+    def set_pressure_tol(self, tol: float):
+        self.L.ref_set_pressure_tol(self.h, tol)
+
+    def rhs_max_abs(self) -> float:
+        return self.L.ref_rhs_max_abs(self.h)
+
+    def step_relative(self, dtMax: float, rel_tol: float) -> float:
+        """One step, then the CG stop of the next step set to rel_tol times
+        this step's max|b| in 1/s. The reference has only an absolute stop,
+        max|r| dt/dx^2 <= pressureTol (src/sim/gasphase.cpp:594-605); with
+        this it stops at about max|r| <= rel_tol max|b|, the GPU path's
+        relative stop, with b taken one step behind (1e-8 1/s after a step
+        whose b was zero)."""
+        dt = self.step(dtMax)
+        dx = self.grid()[1][0]
+        bmax = self.rhs_max_abs()
+        self.set_pressure_tol(rel_tol * bmax * dt / (dx * dx) if bmax > 0 else 1e-8)
+        return dt
 
     def stage(self, name: str, dt: float = 0.0):
         if self.L.ref_stage(self.h, name.encode(), dt) != 0:
