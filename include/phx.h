@@ -210,20 +210,27 @@ int phx_server_get_field(phx_server* server, int request_id, int field, void* ho
 int phx_server_release(phx_server* server, int request_id);
 int phx_server_counts(phx_server* server, int* queued, int* running, size_t* used_bytes, long long* cell_updates);
 
-/* gatherStats' sums of one scenario's current fields (src/sim/solver.cpp:884-915),
- * recomputed without allocating device memory. No counterpart in the reference
- * (its stats live in host memory). For callers that must not allocate at the
- * time of the call: a watchdog or monitoring thread sampling a running batch
- * whose device memory is committed to admitted scenarios under an HBM budget,
- * or a real-time stepping loop where an allocation's implicit device
- * synchronisation would stall the stepping stream.
- * Fills hrr, fuel_in_domain, max_gas_t and burning_cells (the values
+/* The statistics gatherStats reports (heat-release rate, fuel mass in the
+ * domain, hottest gas temperature, burning cells) of one scenario's current
+ * fields, recomputed without allocating device memory. No counterpart in the
+ * reference (its stats live in host memory). For callers that must not
+ * allocate at the time of the call: a serving process whose device memory is
+ * committed to admitted scenarios under an HBM budget (an allocation could
+ * fail or overrun the budget), or a real-time stepping loop where an
+ * allocation's implicit device synchronisation would stall the stepping
+ * stream. Fills hrr, fuel_in_domain, max_gas_t and burning_cells (the values
  * phx_batch_get_stats reports after the step's gatherStats, when the fields
  * have not changed since) and zeroes the other members; the context's own
  * stats are not modified. Limits and rules:
  *  - the scenario has at most 4,194,304 cells (PHX_ERR_INVALID beyond);
  *  - the context has been stepped since its last membership change
  *    (PHX_ERR_STATE otherwise: building its tables would allocate);
+ *  - like every call on a context, it must not overlap another call on the
+ *    same context (one host thread at a time): it reads the context's
+ *    tables and enqueues work on the context's stream. While that stream is
+ *    being captured into a graph it returns PHX_ERR_STATE;
+ *  - it runs on the context's device, whichever device the calling thread
+ *    has selected, and restores the caller's device before returning;
  *  - the first call on a device does a one-time set-up (it looks up the
  *    address of the function's device scratch); make it before any stream
  *    capture begins;
@@ -253,6 +260,11 @@ int phx_batch_set_field(struct phx_ctx* ctx, int scenario, int field, const void
 size_t phx_batch_field_count(const struct phx_ctx* ctx, int scenario, int field);
 int phx_batch_get_stats(struct phx_ctx* ctx, int scenario, phx_stats* out);
 int phx_batch_set_stats(struct phx_ctx* ctx, int scenario, const phx_stats* in);
+/* The pressure multigrid hierarchy Solver::buildPressureLevels built for a
+ * scenario (src/sim/pressure_mg.cpp:28-191): *levels gets the number of
+ * levels and rows[0..cap) the unknowns of the first cap levels (level 0 is
+ * the grid's cells). For tests and tuning; rows may be NULL. */
+int phx_batch_mg_info(struct phx_ctx* ctx, int scenario, int* levels, int* rows, int cap);
 
 /* --- radiation trace -------------------------------------------------------
  * Replaces Solver::traceRadiation (src/sim/radiation.cpp:181-319): rays from

@@ -432,6 +432,7 @@ public:
 
     int initStream() {
         if (st) return PHX_OK;
+        PHX_CK(cudaGetDevice(&device));
         PHX_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
         PHX_CK(cudaMallocHost(&hPin, 8192 * sizeof(double)));
         for (auto& e : ev) PHX_CK(cudaEventCreate(&e));
@@ -1584,6 +1585,13 @@ public:
         *descriptor = dS + s;
         *cells = sc[s]->geo.N();
         *stream = (void*)st;
+        return PHX_OK;
+    }
+    int mgInfo(int s, int* levels, int* rows, int cap) override {
+        PHX_TRY(checkScn(s));
+        const Multigrid& M = sc[s]->MG;
+        if (levels) *levels = (int)M.lv.size();
+        for (int l = 0; rows && l < cap && l < (int)M.lv.size(); ++l) rows[l] = M.lv[l].n;
         return PHX_OK;
     }
     int lastLaunches() const override {

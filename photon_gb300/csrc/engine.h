@@ -38,6 +38,11 @@ public:
     // device view of scenario s for kernels outside the engine: its descriptor
     // in device memory, its cell count and the context's stream (as void*)
     virtual int deviceView(int s, const void** descriptor, int* cells, void** stream) = 0;
+    // the CUDA device the context's stream and memory live on (-1 before the first scenario)
+    int device = -1;
+    // multigrid hierarchy of scenario s: the number of levels, and the unknowns
+    // of levels 0..min(levels, cap)-1 into rows
+    virtual int mgInfo(int s, int* levels, int* rows, int cap) = 0;
     // two-phase admission for the serving loop: host set-up of a scenario
     // (validation, zones, multigrid; no device work) with its device bytes,
     // then its allocation and upload into the batch. prepare() may run on

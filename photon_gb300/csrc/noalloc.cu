@@ -38,16 +38,13 @@ static __device__ __align__(256) double g_naScratch[NA_WORDS];
 std::mutex g_naMutex;
 double* g_naPtr[NA_MAX_DEVICES] = {};
 
-// address of the scratch on the current device, taken once per device
-int scratchOnCurrentDevice(double** out, std::string& err) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) { err = std::string("cudaGetDevice: ") + cudaGetErrorString(e); return PHX_ERR_CUDA; }
+// address of the scratch on device dev (the current device), taken once per device
+int scratchOnDevice(int dev, double** out, std::string& err) {
     if (dev < 0 || dev >= NA_MAX_DEVICES) { err = "device index out of range for the no-allocation scratch"; return PHX_ERR_CUDA; }
     std::lock_guard<std::mutex> lock(g_naMutex);
     if (!g_naPtr[dev]) {
         void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_naScratch);
+        cudaError_t e = cudaGetSymbolAddress(&p, g_naScratch);
         if (e != cudaSuccess || !p) {
             err = std::string("cudaGetSymbolAddress of the no-allocation scratch: ") + cudaGetErrorString(e);
             return PHX_ERR_CUDA;
@@ -58,7 +55,27 @@ int scratchOnCurrentDevice(double** out, std::string& err) {
     return PHX_OK;
 }
 
-// k_stats' sums (src/sim/solver.cpp:884-915) over one scenario, with the same
+// makes the context's device current for the duration of a call and restores
+// the caller's device afterwards
+struct DeviceGuard {
+    int prev = -1;
+    bool switched = false;
+    int enter(int dev, std::string& err) {
+        cudaError_t e = cudaGetDevice(&prev);
+        if (e != cudaSuccess) { err = std::string("cudaGetDevice: ") + cudaGetErrorString(e); return PHX_ERR_CUDA; }
+        if (prev != dev) {
+            e = cudaSetDevice(dev);
+            if (e != cudaSuccess) { err = std::string("cudaSetDevice: ") + cudaGetErrorString(e); return PHX_ERR_CUDA; }
+            switched = true;
+        }
+        return PHX_OK;
+    }
+    ~DeviceGuard() {
+        if (switched) cudaSetDevice(prev);
+    }
+};
+
+// k_stats' sums over one scenario, with the same
 // CTA tiling and the same fixed-order reductions, into the scratch w
 template <class R>
 __global__ void k_stats_noalloc(const Scn<R>* __restrict__ gp, double* __restrict__ w) {
@@ -110,11 +127,29 @@ int gatherStatsNoAlloc(CtxBase* ctx, int precision, int scenario, phx_stats* out
               " partial sums)";
         return PHX_ERR_INVALID;
     }
-    double* w = nullptr;
-    r = scratchOnCurrentDevice(&w, err);
-    if (r != PHX_OK) return r;
+    std::memset(out, 0, sizeof(*out));
+    if (cells <= 0) {   // nothing to sum: gatherStats' initial values
+        out->max_gas_t = K_T0;
+        return PHX_OK;
+    }
     cudaStream_t st = static_cast<cudaStream_t>(streamV);
-    cudaError_t e = cudaMemsetAsync(w, 0, NA_HEAD * sizeof(double), st);
+    // work enqueued here while another thread captures the context's stream
+    // would land in (or break) that capture: refuse instead
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(st, &cs);
+    if (e != cudaSuccess) { err = std::string("cudaStreamIsCapturing: ") + cudaGetErrorString(e); return PHX_ERR_CUDA; }
+    if (cs != cudaStreamCaptureStatusNone) {
+        err = "the context's stream is being captured into a graph; call phx_gather_stats_noalloc between other "
+              "calls on this context, not during one";
+        return PHX_ERR_STATE;
+    }
+    DeviceGuard guard;
+    r = guard.enter(ctx->device, err);
+    if (r != PHX_OK) return r;
+    double* w = nullptr;
+    r = scratchOnDevice(ctx->device, &w, err);
+    if (r != PHX_OK) return r;
+    e = cudaMemsetAsync(w, 0, NA_HEAD * sizeof(double), st);
     if (e != cudaSuccess) { err = std::string("cudaMemsetAsync: ") + cudaGetErrorString(e); return PHX_ERR_CUDA; }
     const int ntiles = (cells + NA_TPB - 1) / NA_TPB;
     if (precision == PHX_PREC_FP64)
@@ -127,7 +162,6 @@ int gatherStatsNoAlloc(CtxBase* ctx, int precision, int scenario, phx_stats* out
     e = cudaMemcpyAsync(head, w, sizeof(head), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) { err = std::string("reading the no-allocation scratch: ") + cudaGetErrorString(e); return PHX_ERR_CUDA; }
-    std::memset(out, 0, sizeof(*out));
     out->hrr = head[NA_HRR];
     out->fuel_in_domain = head[NA_FUEL];
     out->max_gas_t = head[NA_MAXT] > K_T0 ? head[NA_MAXT] : K_T0;   // gatherStats starts its max at T0

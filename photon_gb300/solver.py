@@ -48,6 +48,16 @@ STAT_KEYS = ("time", "max_vel", "max_nu", "max_div", "hrr", "max_gas_t", "burnin
              "fuel_burned", "fuel_in_domain")
 
 
+def _mg_rows(L, h, s):
+    """unknowns per multigrid level of scenario s (phx_batch_mg_info)"""
+    nl = ctypes.c_int()
+    rows = (ctypes.c_int * 16)()
+    r = L.phx_batch_mg_info(h, s, ctypes.byref(nl), ctypes.cast(rows, ctypes.c_void_p), 16)
+    if r != 0:
+        raise PhxError(r, L.phx_last_error(h).decode())
+    return [rows[l] for l in range(min(nl.value, 16))]
+
+
 class Solver:
     def __init__(self, case, precision: int = _lib.PREC_FP64, add_burners: bool = True):
         self.L = _lib.load()
@@ -195,6 +205,10 @@ class Solver:
         raises PhxError with PHX_ERR_TIMEOUT, after which the context is usable."""
         self._check(self.L.phx_selftest_wait_timeout(self.h, float(limit_ms)))
 
+    def mg_levels(self) -> list:
+        """unknowns of each level of the pressure multigrid"""
+        return _mg_rows(self.L, self.h, 0)
+
     def device_bytes(self) -> int:
         return int(self.L.phx_device_bytes(self.h))
 
@@ -268,6 +282,10 @@ class Batch:
 
     def __len__(self):
         return self.L.phx_batch_size(self.h)
+
+    def mg_levels(self, s: int) -> list:
+        """unknowns of each level of scenario s's pressure multigrid"""
+        return _mg_rows(self.L, self.h, s)
 
     def scenario_bytes(self, s: int) -> int:
         return int(self.L.phx_batch_scenario_bytes(self.h, s))

@@ -8,6 +8,11 @@
 // src/sim/state.cpp:62-121) into a second GPU solver, checks that the fields
 // arrive unchanged, steps both solvers 10 more steps and prints the largest
 // relative difference of their temperature and velocity fields.
+//
+// With "dump <prefix>" as the second and third arguments it writes, after the
+// 40 steps, the adapter's host vectors (float, as photon::Solver holds them)
+// to <prefix>_<field>.f32 and the same fields read through the C ABI in
+// double to <prefix>_<field>.f64, for a comparison with the oracle.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -69,9 +74,34 @@ static double maxRel(const std::vector<float>& a, const std::vector<float>& b) {
     return den > 0 ? num / den : num;
 }
 
+template <class T>
+static bool writeRaw(const std::string& path, const std::vector<T>& v) {
+    FILE* f = std::fopen(path.c_str(), "wb");
+    if (!f) return false;
+    const size_t n = std::fwrite(v.data(), sizeof(T), v.size(), f);
+    std::fclose(f);
+    return n == v.size();
+}
+
+// the fields of the comparison: adapter vector, C-ABI field id, name
+static bool dumpFields(photon_gpu::Solver& s, const std::string& prefix) {
+    s.sync();
+    struct F { const std::vector<float>* v; int id; const char* name; };
+    const F fs[] = {{&s.u, PHX_FIELD_U, "u"}, {&s.v, PHX_FIELD_V, "v"}, {&s.w, PHX_FIELD_W, "w"},
+                    {&s.p, PHX_FIELD_P, "p"}, {&s.T, PHX_FIELD_T, "T"}, {&s.Yo, PHX_FIELD_YO, "Yo"},
+                    {&s.Yf, PHX_FIELD_YF, "Yf"}, {&s.Ys, PHX_FIELD_YS, "Ys"}, {&s.nu, PHX_FIELD_NU, "nu"}};
+    for (const F& f : fs) {
+        std::vector<double> d(phx_field_count(s.handle(), f.id));
+        if (phx_get_field(s.handle(), f.id, d.data(), d.size() * sizeof(double)) != PHX_OK) return false;
+        if (!writeRaw(prefix + "_" + f.name + ".f32", *f.v) || !writeRaw(prefix + "_" + f.name + ".f64", d)) return false;
+    }
+    return true;
+}
+
 int main(int argc, char** argv) {
     const bool mixed = argc > 1 && std::string(argv[1]) == "mixed";
     const bool ckpt = argc > 2 && std::string(argv[2]) == "checkpoint";
+    const bool dump = argc > 3 && std::string(argv[2]) == "dump";
     photon_gpu::Solver s;
     if (!setupRoom(s, mixed)) return 1;
     float t = 0;
@@ -81,6 +111,7 @@ int main(int argc, char** argv) {
     for (float v : s.T) maxT = std::fmax(maxT, v);
     std::printf("time %.6f hrr %.3f maxT %.3f iters %d fuelIn %.9f maxVel %.6f cells %zu", t, s.stats.hrr, maxT,
                 s.pressureIters, s.stats.fuelIn, s.maxVel, s.T.size());
+    if (dump && !dumpFields(s, argv[3])) { std::printf("\ndump failed\n"); return 1; }
     if (ckpt) {
         HostState h;
         h.nx = s.nx; h.ny = s.ny; h.nz = s.nz; h.dx = s.dx;

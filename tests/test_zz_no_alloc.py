@@ -45,6 +45,12 @@ def test_noalloc_stats_match_step_stats_twice(precision):
             assert _close(st.fuel_in_domain, ref["fuel_in_domain"]), (st.fuel_in_domain, ref["fuel_in_domain"])
             assert _close(st.max_gas_t, ref["max_gas_t"]), (st.max_gas_t, ref["max_gas_t"])
             assert st.burning_cells == ref["burning_cells"]
+            # the members the call does not compute are zero
+            for name in ("time", "dt", "max_vel", "max_nu", "max_div", "pressure_iters", "pressure_residual",
+                         "pressure_rel_residual", "fuel_in", "fuel_burned", "zones", "leak_faces"):
+                assert getattr(st, name) == 0, name
+        # the context's own stats are left as the step gathered them
+        assert B.stats(s) == ref
     B.close()
 
 
