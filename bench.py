@@ -7,13 +7,19 @@ pressure solve run to a relative residual of 1e-8 (max|r| <= 1e-8 max|b|).
 value = cell-updates/s (cells x steps / device seconds) with all state resident
 in HBM, timed with CUDA events on the solver's stream, L2 flushed before each
 step when the working set fits in L2. e2e = the same metric through the C ABI
-per step: phx_step from the host, then the temperature field and the stats read
-back into pinned host memory. cpu_baseline = the reference's own FP32 solver
-(oracle/_ref) on the host cores, on a bounded sample of the same workload.
+per step: phx_batch_step with every scenario's dtMax copied from pinned host
+memory, then every scenario's stats (phx_stats: time, dt, heat-release rate,
+CG iterations, residual, ...) read back to the host. cpu_baseline = the
+reference's own FP32 solver (oracle/_ref) on the host cores, on a bounded
+sample of the same workload. plain_c1 / plain_c2: the plain FP64 method on the
+36x24x24 single room and the 72x52x44 house, each with the reference's FP32
+and FP64 CPU builds timed on the same grid.
 
 --impl reference times the reference's own CPU step (oracle/_ref) on the same
-workload with all host threads. With --gpus N > 1 (torchrun) the work is
-replicated: every rank steps its own copy, no collective on the data path.
+workload: every scenario of the batch, stepped by one reference solver thread
+each, as many scenarios at a time as the host has threads. With --gpus N > 1
+(torchrun) the work is replicated: every rank steps its own copy, no
+collective on the data path.
 """
 from __future__ import annotations
 
@@ -223,43 +229,91 @@ def cpu_reference_rate(case, steps: int, warm: int, threads: int, bits: int = 32
     return case.N * n / el, kind, threads, n, el
 
 
+def cpu_model() -> str:
+    """the host CPU's model name (lscpu, else /proc/cpuinfo)"""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        info = open("/proc/cpuinfo").read()
+        for line in info.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+        imp = [l.split(":")[1].strip() for l in info.splitlines() if l.startswith("CPU implementer")]
+        part = [l.split(":")[1].strip() for l in info.splitlines() if l.startswith("CPU part")]
+        if imp and part:
+            return "Arm implementer %s part %s" % (imp[0], part[0])
+    except Exception:
+        pass
+    return "unknown"
+
+
+def balance(sizes, workers):
+    """scenario indices per worker, largest first onto the least-loaded worker"""
+    load = [0] * workers
+    out = [[] for _ in range(workers)]
+    for i in sorted(range(len(sizes)), key=lambda i: -sizes[i]):
+        w = min(range(workers), key=lambda k: load[k])
+        out[w].append(i)
+        load[w] += sizes[i]
+    return [o for o in out if o]
+
+
 def run_reference(args, rank, world):
-    """The reference's own FP32 CPU step on the workload (a sample of every
-    eighth scenario for the batch), all host threads, spun up like our arm."""
+    """The reference's own FP32 CPU step on every scenario of the workload,
+    spun up like our arm. The scenarios are independent: each gets its own
+    reference solver with one thread, and as many run at a time as the host
+    has threads (measured faster than one scenario at a time with a thread per
+    core, which leaves cores idle in the solver's serial parts)."""
     if rank != 0:
         return 0
+    import threading
     cases = make_workloads(args.workload)
-    sample = cases[::8] if len(cases) > 8 else cases
     threads = os.cpu_count() or 1
     from oracle import refpy
     if not refpy.available(32):
         print(json.dumps({"impl": "reference", "unavailable": "reference CPU build (oracle/_ref) is not present"}))
         return 0
     solvers = []
-    for c in sample:
+    for c in cases:
         # the reference has only an absolute CG stop: step_relative sets it before each step to
         # REL_TOL times the previous step's max|b|, the relative stop of our arm (1e-8 1/s for the
         # first step)
         c.profile.tol = 1e-8
-        solvers.append((c, refpy.RefSolver(c, 32, threads)))
-    for _ in range(args.spinup + args.warmup):
-        for c, s in solvers:
-            s.step_relative(c.profile.dtMax, REL_TOL)
+        solvers.append(refpy.RefSolver(c, 32, 1))
+    groups = balance([c.N for c in cases], threads)
+
+    def phase(nsteps):
+        def work(idx):
+            for _ in range(nsteps):
+                for k in idx:
+                    solvers[k].step_relative(cases[k].profile.dtMax, REL_TOL)
+        ths = [threading.Thread(target=work, args=(g,)) for g in groups]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+
+    phase(args.spinup + args.warmup)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        for c, s in solvers:
-            s.step_relative(c.profile.dtMax, REL_TOL)
+    phase(args.steps)
     el = time.perf_counter() - t0
-    cells = sum(c.N for c in sample)
+    cells = sum(c.N for c in cases)
     v = cells * args.steps / el
-    desc = "%d steps of %d of the %d scenarios (%d cells) after %d spin-up and %d warm-up steps" % (
-        args.steps, len(sample), len(cases), cells, args.spinup, args.warmup)
+    desc = ("%d steps of all %d scenarios (%d cells) after %d spin-up and %d warm-up steps; one reference solver "
+            "thread per scenario, %d scenarios at a time" % (args.steps, len(cases), cells, args.spinup,
+                                                               args.warmup, len(groups)))
     line = {"metric": METRIC, "value": v, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded house generator)",
-            "config": {"workload": args.workload, "scenarios_sampled": len(sample), "cells": cells,
+            "config": {"workload": args.workload, "scenarios": len(cases), "cells": cells,
                        "pressure_stop": "relative 1e-8: the reference's absolute stop set each step to 1e-8 max|b| of its "
                                         "previous step", "threads": threads, "spinup_steps": args.spinup,
+                       "cpu_model": cpu_model(),
                        "hardware": "host CPU cores of rank 0 (the reference has no GPU path)"},
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": "reference",
@@ -267,6 +321,63 @@ def run_reference(args, rank, world):
             "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
+
+
+def step_bytes_model(k: float, w: int) -> float:
+    """Algorithmic bytes per cell-update of one plain step with k CG
+    iterations: every pass of the reference's step reads each input array once
+    and writes each output once (153 + 61 k words of width w, 24 + 25 (k + 1)
+    bytes of masks and maps)."""
+    return (153 + 61 * k) * w + 24 + 25 * (k + 1)
+
+
+def measure_plain(args, name: str):
+    """The plain method on one grid: the FP64 GPU step (and the mixed one) timed
+    with CUDA events after the same spin-up as the batch, with its roofline by
+    the step's byte model, beside the reference's CPU builds on the same grid:
+    FP32 with every host thread and with the default hardware threads - 2
+    (Solver(), src/sim/solver.cpp:41), and the FP64 build."""
+    from photon_gb300 import _lib
+    from photon_gb300.solver import Batch
+    out = {"workload": name}
+    peak, peak_kind = measured_peak()
+    for pname, prec, w in (("fp64", _lib.PREC_FP64, 8), ("mixed", _lib.PREC_MIXED, 4)):
+        c = make_workload(name)
+        g = Batch([c], prec)
+        dtMax = c.profile.dtMax
+        g.run(args.spinup + max(3, args.warmup), dtMax)
+        flush = g.device_bytes() < (200 << 20)
+        g.sync()
+        ms, iters = [], []
+        for _ in range(args.steps):
+            t, _n = g.time_steps(1, dtMax, flush_l2=flush)
+            ms.append(t)
+            iters.append(g.stats(0)["pressure_iters"])
+        value = c.N * args.steps / (sum(ms) / 1e3)
+        k = float(np.mean(iters))
+        achieved = step_bytes_model(k, w) * value / 1e9
+        out[pname] = {"value": value, "unit": "cell-updates/s", "ms_per_step": sum(ms) / len(ms),
+                      "cg_iters_mean": k, "cells": c.N,
+                      "max_rel_residual_last_step": g.stats(0)["pressure_rel_residual"],
+                      "roofline": {"bound": "hbm", "model": "step bytes per cell-update (153 + 61 k) w + 24 + 25 (k + 1)",
+                                   "bytes_per_cell_update": step_bytes_model(k, w), "achieved": achieved,
+                                   "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind},
+                      "l2": "flushed before each step" if flush else "inputs larger than L2"}
+        g.close()
+    if not args.no_cpu_baseline:
+        nproc = os.cpu_count() or 1
+        cpu = {"cores": nproc, "cpu_model": cpu_model()}
+        for key, bits, thr in (("ref32_all_threads", 32, nproc), ("ref32_default_threads", 32, max(1, nproc - 2)),
+                               ("ref64_all_threads", 64, nproc)):
+            c = make_workload(name)
+            c.profile.tol = 1e-8
+            v, kind, t_used, nst, el = cpu_reference_rate(c, steps=20, warm=2, threads=thr, bits=bits,
+                                                          budget_s=args.cpu_budget, spinup=args.spinup)
+            cpu[key] = {"value": v, "unit": "cell-updates/s", "threads": t_used, "kind": kind,
+                        "sample": "%d steps after %d spin-up and 2 warm-up steps (%.1f s)" % (nst, args.spinup, el)}
+        out["cpu_baseline"] = cpu
+        out["fp64_over_ref32_all_threads"] = out["fp64"]["value"] / cpu["ref32_all_threads"]["value"]
+    return out
 
 
 def measure(args, precision, L, world, clocks: bool):
@@ -306,7 +417,7 @@ def measure(args, precision, L, world, clocks: bool):
     iters = [g.stats(s)["pressure_iters"] for s in range(len(cases))]
     rels = [g.stats(s)["pressure_rel_residual"] for s in range(len(cases))]
     # e2e through the C ABI: per step, the dtMax of every scenario goes down
-    # from pinned memory and every scenario's stats come back
+    # from pinned memory and every scenario's stats (phx_stats) come back
     n = len(cases)
     h2d = L.phx_alloc_host(8 * n)
     dtm = (ctypes.c_double * n).from_address(h2d)
@@ -523,28 +634,37 @@ def measure_volume(args, cpu_baseline: bool):
 def precision_study(args):
     """The precision form's outputs on the seeded house at 10 cm (144x104x88 =
     1.32 M cells): the per-step pressure error of the mixed path against the
-    FP64 path stepped from the same state (sampled along the FP64 run), the
-    mixed solve's divergence residual on every step, and the layer-averaged
-    temperature profile of the two runs after args.study_seconds simulated.
-    The FP64 GPU path is the FP64 run here (it tracks the oracle within 1e-9
-    per step)."""
+    converged FP64 answer (an FP64 step from the same state with the pressure
+    solved to a relative residual of 1e-12), sampled along an FP64 run; the
+    same for the FP64 path at the 1e-8 stop; the mixed solve's divergence
+    residual on every step; and the layer-averaged temperature profile of the
+    mixed and FP64 runs after args.study_seconds simulated. The FP64 GPU path
+    tracks the oracle within 1e-9 per step at these grid sizes."""
     from photon_gb300 import _lib, casegen
     from photon_gb300.solver import Solver
-    c = casegen.house_fine(1)
-    c.profile.tol = 0.0
-    c.profile.rel_tol = REL_TOL
+
+    def case(rel):
+        c = casegen.house_fine(1)
+        c.profile.tol = 0.0
+        c.profile.rel_tol = rel
+        return c
+    c = case(REL_TOL)
     dt_max = c.profile.dtMax
-    f64, mx, probe = Solver(c, _lib.PREC_FP64), Solver(c, _lib.PREC_MIXED), Solver(c, _lib.PREC_MIXED)
+    f64, mx = Solver(c, _lib.PREC_FP64), Solver(c, _lib.PREC_MIXED)
+    probe, probe64, conv = Solver(c, _lib.PREC_MIXED), Solver(c, _lib.PREC_FP64), Solver(case(1e-12), _lib.PREC_FP64)
     rel = lambda a, b: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
-    p_err, n64 = [], 0
+    p_err, p_err64, n64 = [], [], 0
     while f64.stats()["time"] < args.study_seconds:
         if n64 % args.study_every == args.study_every // 2:
-            f64.export_state(probe)           # identical state, then one step each
+            for dst in (probe, probe64, conv):   # identical state, then one step each
+                f64.export_state(dst)
             probe.step(dt_max)
-            f64.step(dt_max)
-            p_err.append(rel(probe.get("p"), f64.get("p")))
-        else:
-            f64.step(dt_max)
+            probe64.step(dt_max)
+            conv.step(dt_max)
+            pc = conv.get("p")
+            p_err.append(rel(probe.get("p"), pc))
+            p_err64.append(rel(probe64.get("p"), pc))
+        f64.step(dt_max)
         n64 += 1
     rres, nmx = [], 0
     while mx.stats()["time"] < args.study_seconds:
@@ -560,8 +680,11 @@ def precision_study(args):
     lerr = np.abs(lm[ok] - lf[ok]) / lf[ok]
     return {"workload": "house %dx%dx%d at %.1f m (%d cells), seed 1" % (c.nx, c.ny, c.nz, c.dx, c.N),
             "simulated_s": args.study_seconds, "steps": {"fp64": n64, "mixed": nmx},
-            "pressure_rel_l2_one_step_from_fp64_state": {"samples": len(p_err), "max": max(p_err),
-                                                         "median": float(np.median(p_err))},
+            "pressure_rel_l2_vs_converged": {
+                "reference": "FP64 step from the same state, pressure solved to a relative residual of 1e-12",
+                "samples": len(p_err), "mixed_max": max(p_err), "mixed_median": float(np.median(p_err)),
+                "fp64_at_1e-8_max": max(p_err64), "fp64_at_1e-8_median": float(np.median(p_err64)),
+                "mixed_all": [float("%.3e" % e) for e in p_err]},
             "mixed_rel_residual": {"max": max(rres), "steps_above_1e-8": int(sum(r > REL_TOL for r in rres))},
             "layer_T_rel_err": {"max": float(lerr.max()), "mean": float(lerr.mean())},
             "layer_T_K": {"fp64": [round(float(v), 2) for v in lf[ok]], "mixed": [round(float(v), 2) for v in lm[ok]]}}
@@ -575,6 +698,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batch64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=8.0, help="seconds of timed CPU steps per CPU baseline")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 lines on the 36x24x24 room and the "
+                                                           "72x52x44 house")
     ap.add_argument("--spinup", type=int, default=SPINUP_STEPS, help="untimed steps before warm-up")
     ap.add_argument("--serve-requests", type=int, default=32)
     ap.add_argument("--serve-rate", type=float, default=8.0, help="request arrivals per second (Poisson)")
@@ -630,6 +756,11 @@ def main():
         if args.precision in ("both", "fp64"):
             serving["fp64"] = measure_serving(args, _lib.PREC_FP64)
 
+    plain = {}
+    if rank == 0 and not args.no_plain:
+        plain["plain_c1"] = measure_plain(args, "single_room_36x24x24")
+        plain["plain_c2"] = measure_plain(args, "house_72x52x44")
+
     radiation = volume = None
     if rank == 0 and not args.no_radiation:
         radiation = measure_radiation(args, not args.no_cpu_baseline)
@@ -671,6 +802,7 @@ def main():
                          "kernels": [{"name": p[0], "launches": p[1], "ms": round(p[2], 4)} for p in
                                      sorted(fp64["prof"], key=lambda p: -p[2])[:10]]},
                 "mixed_over_fp64": mixed["value"] / fp64["value"],
+                **plain,
                 "gpu_launches": mixed["launches"],
                 "roofline": mixed["roofline"],
                 "cpu_baseline": cpu,

@@ -22,6 +22,7 @@
 #include "radiation.cuh"
 #include "volume.cuh"
 #include "rowblock.cuh"
+#include "level0.cuh"
 
 namespace phx {
 
@@ -175,6 +176,7 @@ struct Scenario {
         s.ly = geo.anyLeak ? carve<uint8_t>(base, off, NY) : nullptr;
         s.lz = geo.anyLeak ? carve<uint8_t>(base, off, NZ) : nullptr;
         s.diag = carve<R>(base, off, N);
+        s.code0 = kMixed ? carve<unsigned char>(base, off, N) : nullptr;
         s.zone = carve<int>(base, off, N);
         const int nZ = (int)Z.zoneP.size(), nC = (int)Z.closed.size();
         s.zoneOpen = carve<uint8_t>(base, off, nZ + 1);
@@ -288,6 +290,10 @@ struct Scenario {
         PHX_TRY(put(st, s.ax, geo.ax)); PHX_TRY(put(st, s.ay, geo.ay)); PHX_TRY(put(st, s.az, geo.az));
         PHX_TRY(put(st, s.a0x, MG.a0x)); PHX_TRY(put(st, s.a0y, MG.a0y)); PHX_TRY(put(st, s.a0z, MG.a0z));
         PHX_TRY(put(st, s.diag, MG.lv[0].diag));
+        if (kMixed) {
+            const std::vector<unsigned char> cd = levelZeroCodes();
+            PHX_TRY(putRaw(st, s.code0, cd.data(), cd.size()));
+        }
         PHX_TRY(putRaw(st, s.zone, Z.zone.data(), N));
         PHX_TRY(putRaw(st, s.zoneOpen, Z.zoneOpen.data(), Z.zoneOpen.size()));
         PHX_TRY(putRaw(st, s.closedZone, Z.closed.data(), Z.closed.size()));
@@ -304,7 +310,7 @@ struct Scenario {
         PHX_TRY(putRaw(st, s.leakZStart, leakZStart.data(), leakZStart.size()));
         PHX_TRY(putRaw(st, s.leakZList, leakZList.data(), leakZList.size()));
         // initial state (src/sim/discretize.cpp:28-31)
-        const double amb[NSC] = {K_T0, K_YO2_AMB, 0, 0, 0, 0, K_YCO2_AMB, K_YH2O_AMB, 0, 0};
+        const double amb[NSC] = {tStoredFromKd<R>(K_T0), K_YO2_AMB, 0, 0, 0, 0, K_YCO2_AMB, K_YH2O_AMB, 0, 0};
         for (int q = 0; q < NSC; ++q) {
             PHX_TRY(put(st, s.sc[q], std::vector<double>(N, amb[q])));
             PHX_TRY(put(st, s.sc2[q], std::vector<double>(N, amb[q])));
@@ -327,6 +333,36 @@ struct Scenario {
             if (D.dense) PHX_TRY(put(st, D.dense, L.dense));
         }
         return PHX_OK;
+    }
+
+    // The level-0 coefficient code of every cell (level0.cuh): bits 0-5 for the
+    // x-, x+, y-, y+, z-, z+ faces whose coefficient is exactly 1 (an interior
+    // face couples the cell to its neighbour; an open domain-boundary face adds
+    // to the diagonal only); bit 6 when the cell needs the arrays (a
+    // coefficient other than 0 or 1, or a diagonal other than the count of its
+    // bits).
+    std::vector<unsigned char> levelZeroCodes() const {
+        const int nx = geo.nx, ny = geo.ny, nz = geo.nz;
+        std::vector<unsigned char> cd(geo.N(), 0);
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) {
+                    const int c = geo.cell(i, j, k);
+                    const double a[6] = {MG.a0x[geo.xface(i, j, k)], MG.a0x[geo.xface(i + 1, j, k)],
+                                         MG.a0y[geo.yface(i, j, k)], MG.a0y[geo.yface(i, j + 1, k)],
+                                         MG.a0z[geo.zface(i, j, k)], MG.a0z[geo.zface(i, j, k + 1)]};
+                    unsigned bits = 0;
+                    bool general = false;
+                    for (int f = 0; f < 6; ++f) {
+                        if (a[f] == 1.0) bits |= 1u << f;
+                        else if (a[f] != 0.0) general = true;   // a fraction
+                    }
+                    int cnt = 0;
+                    for (int f = 0; f < 6; ++f) cnt += (bits >> f) & 1u;
+                    if (MG.lv[0].diag[c] != (double)cnt) general = true;
+                    cd[c] = general ? CODE_GENERAL : (unsigned char)bits;
+                }
+        return cd;
     }
 
     // CTAs of each domain of this scenario
@@ -388,6 +424,12 @@ public:
         RbShape shape{0, 0, 0};
     };
     RbCfg cfgApply, cfgGs[3], cfgRes;
+    // mixed path: the coded-coefficient level-0 kernels (level0.cuh) and their launch shape;
+    // PHX_L0_ROWBLOCK=1 runs the mixed path's level 0 on the row-block kernels instead
+    const bool l0Requested = kMixed && std::getenv("PHX_L0_ROWBLOCK") == nullptr;
+    bool useL0 = false;
+    L0Shape l0shape{0, 0};
+    int l0grid[5] = {0, 0, 0, 0, 0};
     ADom adom[2][D_COUNT];
     double* hPin = nullptr;      // pinned scratch for read-backs
     Dom dom[D_COUNT];
@@ -784,7 +826,68 @@ public:
         PHX_CK(cudaMemcpyAsync(dAllTotal, &allTotal, sizeof(int), cudaMemcpyHostToDevice, st));
         PHX_CK(cudaStreamSynchronize(st));
         if (n > 0) PHX_TRY(tuneRowBlocks(shp));
+        useL0 = false;
+        if (n > 0 && l0Requested) PHX_TRY(setupL0());
         return PHX_OK;
+    }
+
+    // launch shape of the level-0 kernels of the mixed path: the ring planes of
+    // the batch's widest tile, a persistent grid of as many CTAs as fit on the SMs
+    int setupL0() {
+        l0shape = L0Shape{0, 0};
+        for (auto& S : sc) {
+            const int tj = rowBlockRows<R>(S->geo.nx, S->geo.ny);
+            l0shape.plane = std::max(l0shape.plane, (tj + 2) * S->geo.nx);
+            l0shape.own = std::max(l0shape.own, tj * S->geo.nx);
+        }
+        if (l0shape.plane > L0_MAX_PLANE) return PHX_OK;   // rows too long for the prefetch registers
+        int dev = 0, sms = 0;
+        PHX_CK(cudaGetDevice(&dev));
+        PHX_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        auto one = [&](auto kern, int mode) -> int {
+            const size_t smem = l0Smem(l0shape, mode);
+            if (smem > RB_SM_SMEM - RB_STATIC_SMEM) {
+                err = "the batch's widest grids need more shared memory than a CTA has (level-0 kernels)";
+                return PHX_ERR_UNSUPPORTED;
+            }
+            PHX_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            int occ = 0;
+            PHX_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, L0_THREADS, smem));
+            l0grid[mode] = std::min(sms * std::max(occ, 1), persistCtas);
+            return PHX_OK;
+        };
+        PHX_TRY(one(k_l0<L0_APPLY>, L0_APPLY));
+        PHX_TRY(one(k_l0<L0_PRE>, L0_PRE));
+        PHX_TRY(one(k_l0<L0_RES>, L0_RES));
+        PHX_TRY(one(k_l0<L0_BLACK>, L0_BLACK));
+        PHX_TRY(one(k_l0<L0_RED>, L0_RED));
+        useL0 = true;
+        return PHX_OK;
+    }
+
+    // a level-0 pass of the mixed path over the active row-block tiles
+    template <int MODE>
+    void launchL0(const char* name, int phase) {
+        if constexpr (kMixed) {
+            if (dom[D_RB].total <= 0) return;
+            const int grid = std::min(dom[D_RB].total, l0grid[MODE]);
+            const size_t smem = l0Smem(l0shape, MODE);
+            const Scn<float>* S = reinterpret_cast<const Scn<float>*>(dS);
+            float* const* D = reinterpret_cast<float* const*>(dD);
+            if (prof) {
+                if (evNext + 2 > (int)evPool.size()) {
+                    for (int i = 0; i < 64; ++i) { cudaEvent_t e; cudaEventCreate(&e); evPool.push_back(e); }
+                }
+                cudaEventRecord(evPool[evNext], st);
+                k_l0<MODE><<<grid, L0_THREADS, smem, st>>>(S, adom[0][D_RB], D, l0shape, phase);
+                cudaEventRecord(evPool[evNext + 1], st);
+                evUse.push_back({name, evNext});
+                evNext += 2;
+            } else {
+                k_l0<MODE><<<grid, L0_THREADS, smem, st>>>(S, adom[0][D_RB], D, l0shape, phase);
+            }
+            ++launches;
+        }
     }
 
     // ---- launch shapes of the row-block kernels -----------------------------------------
@@ -1147,11 +1250,16 @@ public:
     // it, 2: a bare V-cycle
     void vcycle(int phase) {
         const Scn<R>* S = dS;
-        launchRB("k_gs_pre", cfgGs[GS_PRE], k_gs_rb<R, GS_PRE>, S, adom[0][D_RB], cfgGs[GS_PRE].shape, phase);
-        launchRB("k_res_restrict", cfgRes, k_res_rb<R>, S, adom[0][D_RB], cfgRes.shape);
+        if (useL0) {
+            launchL0<L0_PRE>("k_gs_pre", phase);
+            launchL0<L0_RES>("k_res_restrict", phase);
+        } else {
+            launchRB("k_gs_pre", cfgGs[GS_PRE], k_gs_rb<R, GS_PRE>, S, adom[0][D_RB], cfgGs[GS_PRE].shape, phase);
+            launchRB("k_res_restrict", cfgRes, k_res_rb<R>, S, adom[0][D_RB], cfgRes.shape);
+        }
         // down: level 1's first Jacobi sweep; then per level its second sweep and
         // its residual restricted to level l+1 with l+1's first sweep
-        launchA("k_jacobi", D_LV0 + 1, TPB, k_jacobi<R>, S, adom[0][D_LV0 + 1], 1, 0);
+        if (!useL0) launchA("k_jacobi", D_LV0 + 1, TPB, k_jacobi<R>, S, adom[0][D_LV0 + 1], 1, 0);
         for (int l = 1; l < maxLevels - 1; ++l) {
             launchA("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, adom[0][D_LV0 + l], l, 1);
             launchA("k_res_restrict_jac0", D_RS0 + l, TPB, k_res_restrict_jac0<R>, S, adom[0][D_RS0 + l], l);
@@ -1162,8 +1270,13 @@ public:
             launchA("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, adom[0][D_LV0 + l], l, 2);
             launchA("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, adom[0][D_LV0 + l], l, 1);
         }
-        launchRB("k_gs_black", cfgGs[GS_BLACK], k_gs_rb<R, GS_BLACK>, S, adom[0][D_RB], cfgGs[GS_BLACK].shape, phase);
-        launchRB("k_gs_red_dot", cfgGs[GS_RED], k_gs_rb<R, GS_RED>, S, adom[0][D_RB], cfgGs[GS_RED].shape, phase);
+        if (useL0) {
+            launchL0<L0_BLACK>("k_gs_black", phase);
+            launchL0<L0_RED>("k_gs_red_dot", phase);
+        } else {
+            launchRB("k_gs_black", cfgGs[GS_BLACK], k_gs_rb<R, GS_BLACK>, S, adom[0][D_RB], cfgGs[GS_BLACK].shape, phase);
+            launchRB("k_gs_red_dot", cfgGs[GS_RED], k_gs_rb<R, GS_RED>, S, adom[0][D_RB], cfgGs[GS_RED].shape, phase);
+        }
     }
     // all scenarios' flag in slot `slot` set?
     int readAll(int slot, bool& all) {
@@ -1188,7 +1301,8 @@ public:
     // so its first red half sweep runs after that.
     void cgIteration() {
         const Scn<R>* S = dS;
-        launchRB("k_cg_apply", cfgApply, k_cg_apply_rb<R>, S, adom[0][D_RB], (R* const*)dD, cfgApply.shape);
+        if (useL0) launchL0<L0_APPLY>("k_cg_apply", 1);
+        else launchRB("k_cg_apply", cfgApply, k_cg_apply_rb<R>, S, adom[0][D_RB], (R* const*)dD, cfgApply.shape);
         launchA("k_cg_update", D_QUAD, TPB, k_cg_update<R>, S, adom[0][D_QUAD], (R* const*)dD);
         if (kMixed) {
             if (anyClosed) launchA("k_mx_zone_center", D_CZ, TPB, k_mx_zone_center<R>, S, adom[0][D_CZ], 0);
@@ -1496,7 +1610,12 @@ public:
             PHX_CK(cudaStreamSynchronize(st));
             return PHX_OK;
         }
-        if (t == 0) return getReal((const R*)p, n, (double*)host);
+        if (t == 0) {
+            PHX_TRY(getReal((const R*)p, n, (double*)host));
+            if (tempIsOffset<R>() && f == PHX_FIELD_T)   // the stored offset back to kelvin, in FP64
+                for (size_t i = 0; i < n; ++i) ((double*)host)[i] = tKFromStoredd<R>(((double*)host)[i]);
+            return PHX_OK;
+        }
         PHX_CK(cudaMemcpyAsync(host, p, bytes, cudaMemcpyDeviceToHost, st));
         PHX_CK(cudaStreamSynchronize(st));
         return PHX_OK;
@@ -1518,7 +1637,10 @@ public:
                 PHX_CK(cudaMemcpyAsync(S.h.sv + SV_HAVEPREV, &zero, sizeof(double), cudaMemcpyHostToDevice, st));
                 PHX_CK(cudaStreamSynchronize(st));
             }
-            return S.put(st, (R*)p, std::vector<double>(d, d + n));
+            std::vector<double> v(d, d + n);
+            if (tempIsOffset<R>() && f == PHX_FIELD_T)   // kelvin to the stored offset, in FP64
+                for (auto& x : v) x = tStoredFromKd<R>(x);
+            return S.put(st, (R*)p, v);
         }
         PHX_CK(cudaMemcpyAsync(p, host, bytes, cudaMemcpyHostToDevice, st));
         PHX_CK(cudaStreamSynchronize(st));

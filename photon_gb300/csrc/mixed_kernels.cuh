@@ -37,19 +37,32 @@ __global__ void k_mx_res64(const Scn<R>* __restrict__ S, ADom dom, int inLoop) {
     const int c = tile_ * TPB + threadIdx.x;
     double rm = 0;
     if (c < g.N) {
-        const double dg = g.diag[c];
+        // a coded cell (level0.cuh) has coefficients of exactly 0 or 1 and
+        // needs no FP64 multiply per neighbour; the others read the arrays
+        const unsigned cd = g.code0 ? g.code0[c] : 64u;
+        const bool coded = !(cd & 64u);
+        const double dg = coded ? (double)__popc(cd & 63u) : (double)g.diag[c];
         double r = 0;
         if (dg > 0) {
             const int i = c % nx, j = (c / nx) % ny, k = c / sxy;
-            const int fx0 = i + (nx + 1) * (j + ny * k), fy0 = i + nx * (j + (ny + 1) * k);
             const double* x = g.p64;
             double s = dg * x[c];
-            if (i > 0) s -= (double)g.a0x[fx0] * x[c - 1];
-            if (i < nx - 1) s -= (double)g.a0x[fx0 + 1] * x[c + 1];
-            if (j > 0) s -= (double)g.a0y[fy0] * x[c - nx];
-            if (j < ny - 1) s -= (double)g.a0y[fy0 + nx] * x[c + nx];
-            if (k > 0) s -= (double)g.a0z[c] * x[c - sxy];
-            if (k < nz - 1) s -= (double)g.a0z[c + sxy] * x[c + sxy];
+            if (coded) {
+                if ((cd & 1u) && i > 0) s -= x[c - 1];
+                if ((cd & 2u) && i < nx - 1) s -= x[c + 1];
+                if ((cd & 4u) && j > 0) s -= x[c - nx];
+                if ((cd & 8u) && j < ny - 1) s -= x[c + nx];
+                if ((cd & 16u) && k > 0) s -= x[c - sxy];
+                if ((cd & 32u) && k < nz - 1) s -= x[c + sxy];
+            } else {
+                const int fx0 = i + (nx + 1) * (j + ny * k), fy0 = i + nx * (j + (ny + 1) * k);
+                if (i > 0) s -= (double)g.a0x[fx0] * x[c - 1];
+                if (i < nx - 1) s -= (double)g.a0x[fx0 + 1] * x[c + 1];
+                if (j > 0) s -= (double)g.a0y[fy0] * x[c - nx];
+                if (j < ny - 1) s -= (double)g.a0y[fy0 + nx] * x[c + nx];
+                if (k > 0) s -= (double)g.a0z[c] * x[c - sxy];
+                if (k < nz - 1) s -= (double)g.a0z[c + sxy] * x[c + sxy];
+            }
             r = (double)g.b[c] - s;
         }
         g.r[c] = (R)r;

@@ -43,6 +43,33 @@ constexpr double K_BURNER_SOOT = 0.01;
 constexpr double K_GAMMA = K_CP / (K_CP - K_RS);
 
 constexpr int NSC = 10;          // transported scalars: T Yo Yf Ys Ya Yp Yc Yw Yco Yai
+
+// Temperature storage. The FP64 path stores the temperature itself. The mixed
+// path stores its offset from the ambient T0 (theta = T - 293.15 K, converted
+// in FP64 at the host boundary): ambient cells hold exactly 0 and a cell a
+// fraction of a kelvin above ambient keeps FP32's relative precision on that
+// fraction. With T itself in FP32 (ulp about 3e-5 K near 293 K), the rounding
+// of near-ambient cells drives buoyancy and baroclinic noise that the
+// projection turns into pressure errors of up to 3e-5 relative in a
+// quiescent house (the reference's own float build shows the same).
+// Differences of temperatures are differences of offsets; the absolute
+// temperature (densities, viscosity, conductivity, ignition, radiation)
+// is tAbs(stored).
+template <class R>
+__host__ __device__ __forceinline__ constexpr bool tempIsOffset() { return sizeof(R) == 4; }
+template <class R>
+__host__ __device__ __forceinline__ R tAbs(R stored) {
+    if constexpr (sizeof(R) == 4) return R(K_T0) + stored;
+    else return stored;
+}
+// the stored value of the ambient temperature
+template <class R>
+__host__ __device__ __forceinline__ constexpr R tAmbient() { return sizeof(R) == 4 ? R(0) : R(K_T0); }
+// conversions between a temperature in K and the stored value, in FP64
+template <class R>
+__host__ __device__ __forceinline__ constexpr double tStoredFromKd(double t) { return sizeof(R) == 4 ? t - K_T0 : t; }
+template <class R>
+__host__ __device__ __forceinline__ constexpr double tKFromStoredd(double s) { return sizeof(R) == 4 ? K_T0 + s : s; }
 // per-face transport record: upwind density, the 10 limited face values, and
 // the diffusion terms of the 9 species for the momentum-free and the mass form
 constexpr int ADV_RUP = 0, ADV_FACE = 1, ADV_DQ = ADV_FACE + NSC, ADV_MQ = ADV_DQ + NSC - 1,
@@ -108,6 +135,7 @@ struct Scn {
     const R *a0x, *a0y, *a0z;    // the same with wind-inflow boundary faces closed (multigrid level 0)
     const uint8_t *lx, *ly, *lz; // crack faces (null when there are none)
     const R* diag;               // level-0 diagonal
+    const unsigned char* code0;  // mixed path: level-0 coefficient code per cell (level0.cuh)
     const int* zone;
     const uint8_t* zoneOpen;
     int nZones, nClosed;

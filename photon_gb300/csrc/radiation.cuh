@@ -160,7 +160,7 @@ __global__ void k_rad_cells(const Scn<R>* __restrict__ S, int s, const double* _
         flags[c] = 1;
         return;
     }
-    const R T = g.sc[0][c], Ys = g.sc[3][c], Yc = g.sc[6][c], Yw = g.sc[7][c], Pb = g.Pb[c], hrr = g.hrr[c];
+    const R T = tAbs(g.sc[0][c]), Ys = g.sc[3][c], Yc = g.sc[6][c], Yw = g.sc[7][c], Pb = g.Pb[c], hrr = g.hrr[c];
     const R rho = Pb / ((R)K_RS * T);
     const R fv = rho * Ys / (R)1800.0;
     const R pg = (Yw * (R)28.96 / (R)18.02 + Yc * (R)28.96 / (R)44.01) * Pb / (R)K_P0;

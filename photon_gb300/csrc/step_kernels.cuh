@@ -20,7 +20,8 @@ namespace phx {
 
 template <class R>
 __device__ __forceinline__ double gasDensity(const Scn<R>& g, int c) {
-    return (double)g.Pb[c] / (K_RS * (double)g.sc[0][c]);
+    const double t = tempIsOffset<R>() ? K_T0 + (double)g.sc[0][c] : (double)g.sc[0][c];
+    return (double)g.Pb[c] / (K_RS * t);
 }
 
 // ---------------------------------------------------------------------------
@@ -123,7 +124,7 @@ __global__ void k_begin(const Scn<R>* __restrict__ S, Dom dom, int computeDt, do
 // gas density P / (R T) of a cell in the arithmetic type
 template <class R>
 __device__ __forceinline__ R rhoOf(const Scn<R>& g, int c) {
-    return g.Pb[c] / (R(K_RS) * g.sc[0][c]);
+    return g.Pb[c] / (R(K_RS) * tAbs(g.sc[0][c]));
 }
 
 // Per-step clears (src/sim/solver.cpp:231-233), injectIgnitions + injectBurners
@@ -145,7 +146,7 @@ __global__ void k_combust(const Scn<R>* __restrict__ S, Dom dom) {
     if (!g.blocked[c]) {
         const int i = c % nx, j = (c / nx) % ny, k = c / sz;
         R* const* Y = g.sc;
-        T Tc = Y[0][c];
+        T Tc = tAbs(Y[0][c]);
         T yf = Y[2][c];
         bool member = false;
         for (int q = 0; q < g.nsrc; ++q) {
@@ -285,7 +286,7 @@ __global__ void k_turb_nu(const Scn<R>* __restrict__ S, Dom dom) {
             T dv = g.tmp[1][c] - g.tmp[4][c];
             T dw = g.tmp[2][c] - g.tmp[5][c];
             T ks = T(0.5) * (du * du + dv * dv + dw * dw);
-            T nu = mn(T(1), T(K_C_NU) * (T)g.dx * sqrt(ks) + T(1.5e-5) * pow(g.sc[0][c] / T(293.15), T(1.7)));
+            T nu = mn(T(1), T(K_C_NU) * (T)g.dx * sqrt(ks) + T(1.5e-5) * pow(tAbs(g.sc[0][c]) / T(293.15), T(1.7)));
             g.nu[c] = nu;
             m = nu;
         }
@@ -353,10 +354,10 @@ __global__ void k_heat(const Scn<R>* __restrict__ S, Dom dom) {
             q += (d & 1) ? F : -F;   // the cell is the face's lower cell for d odd
             continue;
         }
-        T Tn = n >= 0 ? Tf[n] : T(K_T0);
+        T Tn = n >= 0 ? Tf[n] : tAmbient<T>();
         T nun = n >= 0 ? g.nu[n] : nuc;
         T rn = n >= 0 ? rhoOf(g, n) : T(K_P0) / (T(K_RS) * T(K_T0));
-        T Tface = T(0.5) * (Tc + Tn);
+        T Tface = tAbs(T(0.5) * (Tc + Tn));
         T kf = T(0.5) * (rc + rn) * T(K_CP) * T(0.5) * (nuc + nun) / T(K_PR_T) + T(0.0258) * pow(Tface / T(293.15), T(0.8));
         q += fo[d] * kf * dx * (Tn - Tc);
     }
@@ -376,13 +377,15 @@ __global__ void k_energy(const Scn<R>* __restrict__ S, Dom dom) {
             const T dt = (T)g.sv[SV_DT];
             const T dx = (T)g.dx;
             const T V = dx * dx * dx;
-            const T Tc = g.sc[0][c], Q = g.Q[c], Pb = g.Pb[c];
+            const T Ts = g.sc[0][c], Q = g.Q[c], Pb = g.Pb[c];
+            const T Tc = tAbs(Ts);
             T rho = Pb / (T(K_RS) * Tc);
             T m = rho * V;
-            T Tn = clampd(Tc + Q / (m * T(K_CP)), T(K_T_MIN), T(K_T_MAX));
-            T rhoN = Pb / (T(K_RS) * Tn);
+            // the clamp to [T_MIN, T_MAX] on the stored value (the offset on the mixed path)
+            T Tns = clampd(Ts + Q / (m * T(K_CP)), T(tStoredFromKd<T>(K_T_MIN)), T(tStoredFromKd<T>(K_T_MAX)));
+            T rhoN = Pb / (T(K_RS) * tAbs(Tns));
             T D = Q / (m * T(K_CP) * Tc * dt) + g.massSrc[c] / (rhoN * V * dt);
-            g.sc[0][c] = Tn;
+            g.sc[0][c] = Tns;
             T Sv = clampd(D, -T(K_D_MAX), T(K_D_MAX));
             g.S[c] = Sv;
             md = fabs(Sv);
@@ -490,12 +493,25 @@ __global__ void k_momentum(const Scn<R>* __restrict__ S, Dom dom, int comp) {
     T rf = T(0.5) * (ra + rb);
     T nuf = T(0.5) * (g.nu[ca] + g.nu[cb]);
     acc += nuf * lap;
-    if (comp == 2) {
-        T r0 = T(0.5) * (g.Pb[ca] + g.Pb[cb]) / (T(K_RS) * T(K_T0));
-        acc += T(K_G) * (r0 - rf) / rf;
+    T pt;
+    if constexpr (tempIsOffset<T>()) {
+        // The same terms from the temperature offsets th = T - T0, free of the
+        // cancellation of two near-equal FP32 densities:
+        //   r0 - rf = 0.5 (Pa / (R T0) - ra + Pb / (R T0) - rb) = 0.5 (ra th_a + rb th_b) / T0
+        //   1 / rb - 1 / ra = R (Tb / Pb - Ta / Pa) = R (T0 (1 / Pb - 1 / Pa) + th_b / Pb - th_a / Pa)
+        const T tha = g.sc[0][ca], thb = g.sc[0][cb];
+        if (comp == 2) acc += T(K_G) * (T(0.5) * (ra * tha + rb * thb) / T(K_T0)) / rf;
+        pt = rf * T(0.5) * (g.p[ca] + g.p[cb]);
+        const T ipa = T(1) / g.Pb[ca], ipb = T(1) / g.Pb[cb];
+        acc += pt * (T(K_RS) * (T(K_T0) * (ipb - ipa) + (thb * ipb - tha * ipa))) * idx;
+    } else {
+        if (comp == 2) {
+            T r0 = T(0.5) * (g.Pb[ca] + g.Pb[cb]) / (T(K_RS) * T(K_T0));
+            acc += T(K_G) * (r0 - rf) / rf;
+        }
+        pt = rf * T(0.5) * (g.p[ca] + g.p[cb]);
+        acc += pt * (T(1) / rb - T(1) / ra) * idx;
     }
-    T pt = rf * T(0.5) * (g.p[ca] + g.p[cb]);
-    acc += pt * (T(1) / rb - T(1) / ra) * idx;
     out[f] = clampd(v0 + (T)g.sv[SV_DT] * acc, -T(K_VMAX), T(K_VMAX));
 }
 
@@ -923,7 +939,7 @@ __device__ __forceinline__ void advectCells(const Scn<R>* __restrict__ S, const 
     // expressions: the limiter as superbeeTimes, 1/dx and 1/mden multiplied.
     // The FP64 path keeps the reference's operations one for one.
     constexpr bool kF32 = std::is_same<T, float>::value;
-    const T amb[NSC] = {T(K_T0), T(K_YO2_AMB), T(0), T(0), T(0), T(0), T(K_YCO2_AMB), T(K_YH2O_AMB), T(0), T(0)};
+    const T amb[NSC] = {tAmbient<T>(), T(K_YO2_AMB), T(0), T(0), T(0), T(0), T(K_YCO2_AMB), T(K_YH2O_AMB), T(0), T(0)};
     const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
     const int i = c % nx, j = (c / nx) % ny, k = c / sxy;
     const T dx = (T)g.dx;
@@ -967,20 +983,20 @@ __device__ __forceinline__ void advectCells(const Scn<R>* __restrict__ S, const 
             mden -= s * rUp[d] * un[d];
             continue;
         }
-        T tn = nb[d] >= 0 ? Tf[nb[d]] : T(K_T0), tc = Tf[c], tface;
+        T tn = nb[d] >= 0 ? Tf[nb[d]] : tAmbient<T>(), tc = Tf[c], tface;
         if (un[d] > T(0)) {
-            T tu2 = opp[d] >= 0 ? Tf[opp[d]] : (opp[d] == -1 ? T(K_T0) : tc);
+            T tu2 = opp[d] >= 0 ? Tf[opp[d]] : (opp[d] == -1 ? tAmbient<T>() : tc);
             T den = tn - tc;
             if constexpr (kF32) tface = tc + (fabs(den) > T(1e-6) ? T(0.5) * superbeeTimes(tc - tu2, den) : T(0));
             else tface = tc + (fabs(den) > T(1e-6) ? T(0.5) * superbee((tc - tu2) / den) * den : T(0));
         } else {
-            T tu2 = nb2[d] >= 0 ? Tf[nb2[d]] : (nb2[d] == -1 ? T(K_T0) : tn);
+            T tu2 = nb2[d] >= 0 ? Tf[nb2[d]] : (nb2[d] == -1 ? tAmbient<T>() : tn);
             T den = tc - tn;
             if constexpr (kF32) tface = tn + (fabs(den) > T(1e-6) ? T(0.5) * superbeeTimes(tn - tu2, den) : T(0));
             else tface = tn + (fabs(den) > T(1e-6) ? T(0.5) * superbee((tn - tu2) / den) * den : T(0));
         }
         T pu = un[d] > T(0) ? g.Pb[c] : (nb[d] >= 0 ? g.Pb[nb[d]] : T(K_P0));
-        rUp[d] = pu / (T(K_RS) * mx(tface, T(K_T_MIN)));
+        rUp[d] = pu / (T(K_RS) * mx(tAbs(tface), T(K_T_MIN)));
         mden -= s * rUp[d] * un[d];
         // species diffusion coefficient and face density: the same for every species
         T nun = nb[d] >= 0 ? g.nu[nb[d]] : nuc;
@@ -1110,7 +1126,7 @@ __device__ __forceinline__ StatsTerms<R> statsTerms(const Scn<R>& g, int c) {
     const R hr = g.hrr[c];
     if constexpr (sizeof(R) == 4) {
         const float dxf = (float)g.dx, V = dxf * dxf * dxf;
-        const float rho = g.Pb[c] / ((float)K_RS * g.sc[0][c]);
+        const float rho = g.Pb[c] / ((float)K_RS * tAbs(g.sc[0][c]));
         o.h = F2{hr * V, 0.f};
         o.fd = F2{g.sc[2][c] * rho * V, 0.f};
     } else {
@@ -1118,7 +1134,7 @@ __device__ __forceinline__ StatsTerms<R> statsTerms(const Scn<R>& g, int c) {
         o.fd = g.sc[2][c] * gasDensity(g, c) * V;
         o.h = hr * V;
     }
-    o.t = g.sc[0][c];
+    o.t = tAbs(g.sc[0][c]);
     o.burning = hr > 0;
     return o;
 }

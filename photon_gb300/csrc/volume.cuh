@@ -107,7 +107,7 @@ __global__ void k_vol_pack(const Scn<R>* __restrict__ S, int s, float4* __restri
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= g.N) return;
     if (g.blocked[c]) { vol[c] = make_float4(0, 0, 0, 0); return; }
-    const float T = (float)g.sc[0][c];
+    const float T = (float)tAbs(g.sc[0][c]);
     const float rho = (float)g.Pb[c] / (287.0f * T);
     vol[c] = make_float4((float)g.sc[3][c] * rho, (float)g.sc[4][c] * rho, T, (float)g.hrr[c]);
 }

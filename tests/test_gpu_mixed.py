@@ -4,7 +4,10 @@ inside an FP64 refinement loop) against the FP64 oracle.
 Tolerances, from the benchmark spec's target: pressure within 1e-5 relative (L2) of
 the FP64 oracle per step from identical inputs, with the pressure solve at a
 relative residual of at most 1e-8 (max|r| <= 1e-8 max|b|, checked in FP64).
-Velocities and scalars carry FP32 rounding: 1e-5 relative per step."""
+Velocities and scalars carry FP32 rounding: 1e-5 relative per step. Every
+step starts from the oracle's state, so the bars are the same on every step.
+The oracle solves its pressure to a relative residual of 1e-12 (the converged
+answer), so the error measured is the mixed step's own."""
 import numpy as np
 import pytest
 
@@ -21,11 +24,16 @@ P_TOL = 1e-5
 FIELD_TOL = 1e-5
 
 
-def rel_case(c):
+def rel_case(c, rel=1e-8):
     c.profile.tol = 0.0
-    c.profile.rel_tol = 1e-8
+    c.profile.rel_tol = rel
     c.profile.maxIters = 400
     return c
+
+
+def converged(make):
+    """the same case with the oracle's pressure solve run to 1e-12"""
+    return rel_case(make(), 1e-12)
 
 
 CASES = {
@@ -36,36 +44,100 @@ CASES = {
 }
 
 
-@pytest.mark.parametrize("name", list(CASES))
-def test_mixed_step_matches_oracle_from_identical_state(name):
-    c = CASES[name]()
-    o = OracleSolver(c)
-    for _ in range(10):
-        o.step(0.02)
-    g = Solver(c, _lib.PREC_MIXED)
+def load_state(o, g):
     for f in STATE:
         g.set(f, o.get(f))
     g.set("lit", o.get("lit"))
     g.set("zoneP", o.get("zoneP"))
     sc = o.scalars()
     g.set_scalars(sc["time"], sc["maxVel"], sc["maxNu"], sc["maxDiv"])
-    for s in range(3):
+
+
+def mixed_steps_vs_oracle(c_gpu, c_oracle, spin, nsteps):
+    o = OracleSolver(c_oracle)
+    for _ in range(spin):
+        o.step(0.02)
+    g = Solver(c_gpu, _lib.PREC_MIXED)
+    load_state(o, g)
+    worst = 0.0
+    for s in range(nsteps):
         dto, dtg = o.step(0.02), g.step(0.02)
         assert abs(dto - dtg) <= 1e-5 * dto
         st = g.stats()
         assert st["pressure_rel_residual"] <= 1e-8, st
         e = rel_l2(g.get("p"), o.get("p"))
-        assert e <= P_TOL * (s + 1), ("p", s, e)
+        worst = max(worst, e)
+        assert e <= P_TOL, ("p", s, e)
         for f in ("u", "v", "w", "T", "Yo", "Yf"):
             ef = rel_l2(g.get(f), o.get(f))
-            assert ef <= FIELD_TOL * (s + 1), (f, s, ef)
+            assert ef <= FIELD_TOL, (f, s, ef)
         # start the next step from the oracle's state again
-        for f in STATE:
-            g.set(f, o.get(f))
-        g.set("lit", o.get("lit"))
-        g.set("zoneP", o.get("zoneP"))
-        sc = o.scalars()
-        g.set_scalars(sc["time"], sc["maxVel"], sc["maxNu"], sc["maxDiv"])
+        load_state(o, g)
+    return worst
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_mixed_step_matches_oracle_from_identical_state(name):
+    mixed_steps_vs_oracle(CASES[name](), converged(CASES[name]), 10, 3)
+
+
+def _batch_extreme(which):
+    cs = casegen.batch_scenarios(64)
+    return min(cs, key=lambda c: c.N) if which == "min" else max(cs, key=lambda c: c.N)
+
+
+CONFIG_CASES = {
+    "house_40x32x24": (lambda: casegen.house(40, 32, 24, 0.2, 5), 40, 2),
+    "batch_smallest": (lambda: _batch_extreme("min"), 30, 2),
+    "batch_largest": (lambda: _batch_extreme("max"), 20, 2),
+}
+
+
+@pytest.mark.parametrize("name", list(CONFIG_CASES))
+def test_mixed_step_matches_converged_oracle_at_config_size(name):
+    """Scenarios of the batch workload and a 30 k-cell house (three and four
+    multigrid levels): the 1e-5 pressure bar against the converged FP64
+    answer."""
+    make, spin, n = CONFIG_CASES[name]
+    mixed_steps_vs_oracle(rel_case(make()), converged(make), spin, n)
+
+
+@pytest.mark.parametrize("name,make,spin", [("single_room_36x24x24", casegen.single_room, 60),
+                                            ("house_72x52x44", lambda: casegen.house_small(1), 30)])
+def test_mixed_pressure_at_least_as_close_as_reference_float_build(name, make, spin):
+    """The 36x24x24 room and the 72x52x44 house early in the fire, when the air
+    is nearly at rest: the pressure of one mixed step from the oracle's state,
+    against the converged FP64 answer, is no further from it than the
+    reference's own FP32 build stepped from the same state (both stop at a
+    relative residual of 1e-8). FP32 storage of the velocities bounds both
+    near 1e-5 here: the divergence of a field at rest is the difference of
+    nearly equal face fluxes."""
+    from oracle import refpy
+    if not refpy.available(32):
+        pytest.skip("reference FP32 build not present")
+    o = OracleSolver(converged(make))
+    for _ in range(spin):
+        o.step(0.02)
+    state = {f: o.get(f) for f in STATE}
+    lit, sc = o.get("lit"), o.scalars()
+    g = Solver(rel_case(make()), _lib.PREC_MIXED)
+    load_state(o, g)
+    c32 = make()
+    c32.profile.tol = 1e-8
+    c32.profile.maxIters = 400
+    r = refpy.RefSolver(c32, 32, 4)
+    for f in STATE:
+        r.set(f, state[f])
+    r.set("lit", lit)
+    r.set_scalars(sc["time"], sc["maxVel"], sc["maxNu"], sc["maxDiv"])
+    o.step(0.02)
+    g.step(0.02)
+    r.step(0.02)
+    p = o.get("p")
+    e_mixed, e_ref = rel_l2(g.get("p"), p), rel_l2(r.get("p"), p)
+    assert g.stats()["pressure_rel_residual"] <= 1e-8
+    assert e_mixed <= e_ref, (e_mixed, e_ref)
+    assert e_mixed <= 5e-5, e_mixed
 
 
 def test_mixed_relative_residual_reached_every_step():
