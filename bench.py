@@ -94,16 +94,19 @@ def make_workload(name: str):
 # Algorithmic bytes per unit of each kernel's domain for storage width w
 # (8 for FP64 fields, 4 for the mixed path): each input array read once and
 # each output written once per launch; uint8 masks count 1 B, int32 maps 4 B.
+# The mixed path's level-0 kernels read one coefficient-code byte per cell in
+# place of the diagonal and the three coefficient arrays.
 def kernel_bytes(name: str, w: int):
+    coded = w == 4
     table = {
         "k_advect": 18 * w + 1 + 10 * w,        # 10 scalars + u,v,w + fx,fy,fz + Pb,nu + blocked -> 10 scalars
         "k_momentum": 9 * w,                    # vel, 2 other components, fo, Pb, T, nu, p -> vel' (per face)
-        "k_gs_pre": 6 * w,                      # r, diag, 3 coefficients -> z
-        "k_gs_black": 6.5 * w + 4,              # r, diag, z, 3 coefficients, agg -> z (black)
-        "k_gs_red_dot": 6.5 * w,                # r, diag, z, 3 coefficients -> z (red), r.z
-        "k_cg_apply": 8 * w,                    # z, d, diag, 3 coefficients -> d, q
+        "k_gs_pre": 2 * w + 1 if coded else 6 * w,                 # r, code (diag, 3 coefficients) -> z
+        "k_gs_black": 3 * w + 4 + 1 if coded else 6.5 * w + 4,     # r, z, agg, code -> z (black)
+        "k_gs_red_dot": 3 * w + 1 if coded else 6.5 * w,           # r, z, code -> z (red), r.z
+        "k_cg_apply": 4 * w + 1 if coded else 8 * w,               # z, d, code -> d, q
         "k_cg_update": 7 * w,                   # p, d, r, q, diag -> p, r
-        "k_res_restrict": 6 * w + 4,            # r, z, diag, 3 coefficients, agg
+        "k_res_restrict": 2 * w + 4 + 1 if coded else 6 * w + 4,   # r, z, agg, code -> level-1 b
         "k_rhs": 13 * w + 1,
         "k_heat": 8 * w + 1,
         "k_energy": 6 * w + 1,
@@ -113,7 +116,7 @@ def kernel_bytes(name: str, w: int):
         "k_turb_nu": 5 * w + 1,
         "k_velcorr": 5 * w,
         "k_stats": 4 * w + 1,
-        "k_mx_res64": 8 + 5 * w + 4,            # p64, b, diag, coefficients -> r, e
+        "k_mx_res64": 8 + 3 * w + 1,            # p64, b, code -> r, e
         "k_mx_update": 8 + 8 + 2 * w,
     }
     return table.get(name)

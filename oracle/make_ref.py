@@ -14,8 +14,8 @@ Both builds also map ``private`` to ``public`` in the prelude so the harness can
 fill geometry and call single stages. The reference sources are copied into
 oracle/_ref/src32 and oracle/_ref/src64 (git-ignored build copies, never
 committed) so the libraries can be rebuilt on a machine without the reference
-checkout. Only this script reads the reference checkout; set PHX_REFERENCE to
-point elsewhere.
+checkout. Only this script reads the reference checkout: PHX_REFERENCE, or a
+directory named "reference" beside this repository.
 
 Usage: python oracle/make_ref.py [--jobs N]
 """
@@ -31,7 +31,8 @@ from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REF = os.environ.get("PHX_REFERENCE", "/root/reference")
+# the reference checkout: PHX_REFERENCE, else a directory named "reference" beside this repository
+REF = os.environ.get("PHX_REFERENCE", os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 
 # the solver and the scene/material loaders it links against
 SOURCES = [

@@ -40,7 +40,9 @@ namespace phx {
 constexpr int DENSE_MAX = 4096;
 
 enum DomId {
-    D_ONE = 0, D_CELLS, D_FX, D_FY, D_FZ, D_BX, D_BY, D_BZ, D_CZ, D_CC, D_CO_DENSE, D_CO_SERIAL, D_RB, D_QUAD, D_LEAK,
+    D_ONE = 0, D_CELLS, D_FX, D_FY, D_FZ, D_BX, D_BY, D_BZ, D_CZ, D_CC, D_CO_DENSE, D_CO_SERIAL, D_CO_CTA, D_RB, D_QUAD, D_LEAK,
+    D_L0,                        // level-0 tiles of the mixed path: 2x2x2 blocks (level0.cuh)
+    D_L0R,                       // the same, several blocks per thread (the passes with a dot product)
     D_LV0,                       // D_LV0 + l: rows of level l when l is not the coarsest (1 <= l < 12)
     D_RS0 = D_LV0 + MAX_LEVELS,  // D_RS0 + l: rows of level l+1 for restriction from level l >= 1
     D_COUNT = D_RS0 + MAX_LEVELS
@@ -65,6 +67,7 @@ struct Scenario {
     GridGeom geo;
     double cfl = 0.5, dtMaxP = 0.02, tol = 0.002, relTol = 0;
     int maxIters = 400, radiationOn = 1;
+    int coarseStop = MG_COARSE_STOP_REF;   // multigrid coarsening stop (the V-cycle schedule)
     Zones Z;
     Multigrid MG;
     std::vector<double> Pb0;
@@ -114,7 +117,9 @@ struct Scenario {
         // set-up on the host: zones, multigrid
         Pb0.assign(NN, 101325.0);
         Z = computeZones(geo, Pb0);
-        MG = buildMultigrid(geo, DENSE_MAX);
+        if (kMixed)
+            if (const char* e = std::getenv("PHX_MG_STOP")) coarseStop = std::max(16, std::atoi(e));
+        MG = buildMultigrid(geo, DENSE_MAX, coarseStop);
         buildLeakFaces();
         return PHX_OK;
     }
@@ -165,7 +170,11 @@ struct Scenario {
     size_t layout(char* base) {
         const int N = geo.N(), NX = geo.NX(), NY = geo.NY(), NZ = geo.NZ();
         const int nl = (int)MG.lv.size();
-        const int partStride = (N + TPB - 1) / TPB + 1;
+        // one reduction partial per CTA of the widest reduction domain (cells,
+        // row-block tiles, level-0 tiles)
+        int tl[D_COUNT];
+        tiles(tl);
+        const int partStride = std::max(tl[D_CELLS], std::max(tl[D_RB], tl[D_L0])) + 1;
         size_t off = 0;
         Scn<R>& s = h;
         s.blocked = carve<uint8_t>(base, off, N);
@@ -273,6 +282,10 @@ struct Scenario {
         Scn<R>& s = h;
         PHX_CK(cudaMemsetAsync(arena, 0, arenaBytes, st));
         s.nx = geo.nx; s.ny = geo.ny; s.nz = geo.nz; s.N = N; s.NX = geo.NX(); s.NY = geo.NY(); s.NZ = geo.NZ();
+        s.dvA[0] = makeDivU(geo.nx); s.dvB[0] = makeDivU(geo.nx * geo.ny); s.dY[0] = geo.ny;
+        s.dvA[1] = makeDivU(geo.nx + 1); s.dvB[1] = makeDivU((geo.nx + 1) * geo.ny); s.dY[1] = geo.ny;
+        s.dvA[2] = makeDivU(geo.nx); s.dvB[2] = makeDivU(geo.nx * (geo.ny + 1)); s.dY[2] = geo.ny + 1;
+        s.dvL0[0] = makeDivU((geo.nx + 1) >> 1); s.dvL0[1] = makeDivU(((geo.nx + 1) >> 1) * ((geo.ny + 1) >> 1));
         s.dx = geo.dx; s.ox = geo.ox; s.oy = geo.oy; s.oz = geo.oz;
         s.cfl = cfl; s.dtMaxP = dtMaxP; s.tol = tol; s.relTol = relTol; s.maxIters = maxIters; s.radiationOn = radiationOn;
         double th = geo.windFromDeg * 3.14159265 / 180.0;
@@ -336,11 +349,11 @@ struct Scenario {
     }
 
     // The level-0 coefficient code of every cell (level0.cuh): bits 0-5 for the
-    // x-, x+, y-, y+, z-, z+ faces whose coefficient is exactly 1 (an interior
-    // face couples the cell to its neighbour; an open domain-boundary face adds
-    // to the diagonal only); bit 6 when the cell needs the arrays (a
-    // coefficient other than 0 or 1, or a diagonal other than the count of its
-    // bits).
+    // interior x-, x+, y-, y+, z-, z+ faces whose coefficient is exactly 1 (they
+    // couple the cell to its neighbour), bit 7 for one open domain-boundary
+    // face with coefficient 1 (it adds to the diagonal only), bit 6 when the
+    // cell needs the arrays (a coefficient other than 0 or 1, two or more open
+    // boundary faces, or a diagonal other than the count of its bits).
     std::vector<unsigned char> levelZeroCodes() const {
         const int nx = geo.nx, ny = geo.ny, nz = geo.nz;
         std::vector<unsigned char> cd(geo.N(), 0);
@@ -351,18 +364,33 @@ struct Scenario {
                     const double a[6] = {MG.a0x[geo.xface(i, j, k)], MG.a0x[geo.xface(i + 1, j, k)],
                                          MG.a0y[geo.yface(i, j, k)], MG.a0y[geo.yface(i, j + 1, k)],
                                          MG.a0z[geo.zface(i, j, k)], MG.a0z[geo.zface(i, j, k + 1)]};
+                    const bool inner[6] = {i > 0, i < nx - 1, j > 0, j < ny - 1, k > 0, k < nz - 1};
                     unsigned bits = 0;
+                    int boundary = 0;
                     bool general = false;
                     for (int f = 0; f < 6; ++f) {
-                        if (a[f] == 1.0) bits |= 1u << f;
-                        else if (a[f] != 0.0) general = true;   // a fraction
+                        if (a[f] == 1.0) {
+                            if (inner[f]) bits |= 1u << f;
+                            else ++boundary;
+                        } else if (a[f] != 0.0) {
+                            general = true;   // a fraction
+                        }
                     }
-                    int cnt = 0;
+                    if (boundary > 1) general = true;
+                    int cnt = boundary;
                     for (int f = 0; f < 6; ++f) cnt += (bits >> f) & 1u;
                     if (MG.lv[0].diag[c] != (double)cnt) general = true;
-                    cd[c] = general ? CODE_GENERAL : (unsigned char)bits;
+                    cd[c] = general ? CODE_GENERAL : (unsigned char)(bits | (boundary ? CODE_BOUNDARY : 0u));
                 }
         return cd;
+    }
+
+    // levels 2 and coarser in one CTA (k_coarse_cta): mixed path, three or more
+    // levels, a coarsest level small enough for one CTA's dense product
+    bool ctaCoarse() const {
+        const int nl = (int)MG.lv.size();
+        return kMixed && nl >= 3 && !MG.lv[nl - 1].dense.empty() && MG.lv[nl - 1].n <= CTA_COARSE_DENSE_MAX &&
+               std::getenv("PHX_NO_CTA_COARSE") == nullptr;
     }
 
     // CTAs of each domain of this scenario
@@ -373,6 +401,8 @@ struct Scenario {
         t[D_ONE] = 1;
         t[D_CELLS] = cdiv(N, TPB);
         t[D_RB] = cdiv(ny, rowBlockRows<R>(nx, ny)) * cdiv(nz, RB_KZ);      // row blocks x plane blocks
+        t[D_L0] = kMixed ? l0Tiles(nx, ny, nz, 1) : 0;
+        t[D_L0R] = kMixed ? l0Tiles(nx, ny, nz, l0Bpt(L0_RED)) : 0;
         t[D_QUAD] = cdiv(N, TPB * CG_QUAD);                                 // 4 cells per thread
         t[D_LEAK] = cdiv((long long)leak.size() / 4, TPB);
         t[D_FX] = cdiv(geo.NX(), TPB);
@@ -385,11 +415,14 @@ struct Scenario {
         t[D_CC] = cdiv((long long)Z.closedCells.size(), TPB);
         const int nl = (int)MG.lv.size();
         const MgLevel& Lc = MG.lv[nl - 1];
-        t[D_CO_DENSE] = Lc.dense.empty() ? 0 : cdiv(Lc.n, TPB / 32);
+        const bool cta = ctaCoarse();
+        t[D_CO_DENSE] = Lc.dense.empty() || cta ? 0 : cdiv(Lc.n, TPB / 32);
         t[D_CO_SERIAL] = Lc.dense.empty() ? 1 : 0;
+        t[D_CO_CTA] = cta ? 1 : 0;
         for (int l = 1; l < MAX_LEVELS; ++l) {
-            t[D_LV0 + l] = (l < nl - 1) ? cdiv(MG.lv[l].n, TPB) : 0;
-            t[D_RS0 + l] = (l + 1 <= nl - 1) ? cdiv(MG.lv[l + 1].n, TPB / RRJ_LANES) : 0;   // 8 lanes per unknown
+            const bool batch = !cta || l < 2;   // levels 2 and coarser run in k_coarse_cta
+            t[D_LV0 + l] = (l < nl - 1 && batch) ? cdiv(MG.lv[l].n, TPB) : 0;
+            t[D_RS0 + l] = (l + 1 <= nl - 1 && batch) ? cdiv(MG.lv[l + 1].n, TPB / RRJ_LANES) : 0;   // 8 lanes per unknown
         }
     }
 };
@@ -415,6 +448,8 @@ public:
     int* dAStart = nullptr;      // [2][D_COUNT][cap + 1] active-tile prefixes (solving / replacing)
     int* dATotal = nullptr;      // [2][D_COUNT]
     unsigned* dErr = nullptr;    // error word of the device side (bounded waits that ran out)
+    unsigned* ownTab = nullptr;  // CTA -> (scenario, tile) of every domain (Dom::owner)
+    size_t ownCap = 0;
     double* dTimes = nullptr;    // simulated time of each scenario (read-back staging)
     int* dAllTotal = nullptr;    // the row-block tile total of the batch (every tile active), for tuning runs
     // launch shape of a row-block kernel: dynamic shared memory, persistent grid, slot strides
@@ -428,8 +463,8 @@ public:
     // PHX_L0_ROWBLOCK=1 runs the mixed path's level 0 on the row-block kernels instead
     const bool l0Requested = kMixed && std::getenv("PHX_L0_ROWBLOCK") == nullptr;
     bool useL0 = false;
-    L0Shape l0shape{0, 0};
     int l0grid[5] = {0, 0, 0, 0, 0};
+    int ctaCoarseGrid = 152 * 2;   // CTAs of k_coarse_cta: two per SM
     ADom adom[2][D_COUNT];
     double* hPin = nullptr;      // pinned scratch for read-backs
     Dom dom[D_COUNT];
@@ -463,6 +498,7 @@ public:
         destroyGraph();
         sc.clear();
         if (tab) cudaFree(tab);
+        if (ownTab) cudaFree(ownTab);
         if (hPin) cudaFreeHost(hPin);
         if (flushBuf) cudaFree(flushBuf);
         for (auto e : evPool) cudaEventDestroy(e);
@@ -798,10 +834,38 @@ public:
             S.h.errWord = dErr;
             shp.add(S.geo.nx, S.geo.ny);
         }
+        // per domain, the scenario and tile of every CTA (packed 11 + 20 bits)
+        size_t ownTotal = 0;
+        bool packable = true;
+        for (int d = 0; d < D_COUNT; ++d) {
+            ownTotal += (size_t)starts[(size_t)d * (n + 1) + n];
+            for (int s = 0; s < n; ++s) packable &= tilesAll[(size_t)d * cap + s] < (1 << 20);
+        }
+        std::vector<unsigned> own;
+        if (packable && n <= 2048) {
+            own.reserve(ownTotal);
+            for (int d = 0; d < D_COUNT; ++d)
+                for (int s = 0; s < n; ++s)
+                    for (int t = 0; t < tilesAll[(size_t)d * cap + s]; ++t) own.push_back(((unsigned)s << 20) | (unsigned)t);
+            if (own.size() > ownCap) {
+                if (ownTab) { PHX_CK(cudaStreamSynchronize(st)); cudaFree(ownTab); ownTab = nullptr; ownCap = 0; }
+                if (cudaMalloc(&ownTab, own.size() * sizeof(unsigned)) != cudaSuccess) {
+                    ownTab = nullptr;
+                    err = "device allocation of the CTA owner tables failed";
+                    return PHX_ERR_OOM;
+                }
+                ownCap = own.size();
+            }
+            if (!own.empty())
+                PHX_CK(cudaMemcpyAsync(ownTab, own.data(), own.size() * sizeof(unsigned), cudaMemcpyHostToDevice, st));
+        }
+        size_t ownOff = 0;
         for (int d = 0; d < D_COUNT; ++d) {
             dom[d].start = dDomStart + (size_t)d * (n + 1);
             dom[d].nscn = n;
             dom[d].total = starts[(size_t)d * (n + 1) + n];
+            dom[d].owner = own.empty() ? nullptr : ownTab + ownOff;
+            ownOff += (size_t)dom[d].total;
         }
         for (int k = 0; k < 2; ++k)
             for (int d = 0; d < D_COUNT; ++d) {
@@ -831,29 +895,16 @@ public:
         return PHX_OK;
     }
 
-    // launch shape of the level-0 kernels of the mixed path: the ring planes of
-    // the batch's widest tile, a persistent grid of as many CTAs as fit on the SMs
+    // launch shape of the level-0 kernels of the mixed path: a persistent grid
+    // of as many CTAs as fit on the SMs
     int setupL0() {
-        l0shape = L0Shape{0, 0};
-        for (auto& S : sc) {
-            const int tj = rowBlockRows<R>(S->geo.nx, S->geo.ny);
-            l0shape.plane = std::max(l0shape.plane, (tj + 2) * S->geo.nx);
-            l0shape.own = std::max(l0shape.own, tj * S->geo.nx);
-        }
-        if (l0shape.plane > L0_MAX_PLANE) return PHX_OK;   // rows too long for the prefetch registers
         int dev = 0, sms = 0;
         PHX_CK(cudaGetDevice(&dev));
         PHX_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         auto one = [&](auto kern, int mode) -> int {
-            const size_t smem = l0Smem(l0shape, mode);
-            if (smem > RB_SM_SMEM - RB_STATIC_SMEM) {
-                err = "the batch's widest grids need more shared memory than a CTA has (level-0 kernels)";
-                return PHX_ERR_UNSUPPORTED;
-            }
-            PHX_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             int occ = 0;
-            PHX_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, L0_THREADS, smem));
-            l0grid[mode] = std::min(sms * std::max(occ, 1), persistCtas);
+            PHX_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, L0_THREADS, 0));
+            l0grid[mode] = std::min(sms * std::max(occ, 1), persistCtas * TPB / L0_THREADS);
             return PHX_OK;
         };
         PHX_TRY(one(k_l0<L0_APPLY>, L0_APPLY));
@@ -865,13 +916,13 @@ public:
         return PHX_OK;
     }
 
-    // a level-0 pass of the mixed path over the active row-block tiles
+    // a level-0 pass of the mixed path over the active level-0 tiles
     template <int MODE>
     void launchL0(const char* name, int phase) {
         if constexpr (kMixed) {
-            if (dom[D_RB].total <= 0) return;
-            const int grid = std::min(dom[D_RB].total, l0grid[MODE]);
-            const size_t smem = l0Smem(l0shape, MODE);
+            constexpr int d = l0Bpt(MODE) > 1 ? D_L0R : D_L0;
+            if (dom[d].total <= 0) return;
+            const int grid = std::min(dom[d].total, l0grid[MODE]);
             const Scn<float>* S = reinterpret_cast<const Scn<float>*>(dS);
             float* const* D = reinterpret_cast<float* const*>(dD);
             if (prof) {
@@ -879,12 +930,12 @@ public:
                     for (int i = 0; i < 64; ++i) { cudaEvent_t e; cudaEventCreate(&e); evPool.push_back(e); }
                 }
                 cudaEventRecord(evPool[evNext], st);
-                k_l0<MODE><<<grid, L0_THREADS, smem, st>>>(S, adom[0][D_RB], D, l0shape, phase);
+                k_l0<MODE><<<grid, L0_THREADS, 0, st>>>(S, adom[0][d], D, phase);
                 cudaEventRecord(evPool[evNext + 1], st);
                 evUse.push_back({name, evNext});
                 evNext += 2;
             } else {
-                k_l0<MODE><<<grid, L0_THREADS, smem, st>>>(S, adom[0][D_RB], D, l0shape, phase);
+                k_l0<MODE><<<grid, L0_THREADS, 0, st>>>(S, adom[0][d], D, phase);
             }
             ++launches;
         }
@@ -1157,7 +1208,7 @@ public:
         // the domains of the solve's persistent kernels (kind 0: solving, kind 1: replacing)
         int n = 0;
         auto add = [&](int kind, int d) { if (n < 32) t.list[n++] = (short)(kind * D_COUNT + d); };
-        add(0, D_CELLS); add(0, D_CZ); add(0, D_RB); add(0, D_QUAD); add(0, D_CO_DENSE); add(0, D_CO_SERIAL);
+        add(0, D_CELLS); add(0, D_CZ); add(0, D_RB); add(0, D_L0); add(0, D_L0R); add(0, D_QUAD); add(0, D_CO_DENSE); add(0, D_CO_SERIAL); add(0, D_CO_CTA);
         for (int l = 1; l < maxLevels - 1 && l < MAX_LEVELS; ++l) { add(0, D_LV0 + l); add(0, D_RS0 + l); }
         add(1, D_CELLS); add(1, D_CZ);
         t.nlist = n;
@@ -1263,6 +1314,22 @@ public:
         for (int l = 1; l < maxLevels - 1; ++l) {
             launchA("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, adom[0][D_LV0 + l], l, 1);
             launchA("k_res_restrict_jac0", D_RS0 + l, TPB, k_res_restrict_jac0<R>, S, adom[0][D_RS0 + l], l);
+        }
+        if (dom[D_CO_CTA].total > 0) {
+            const int grid = std::min(dom[D_CO_CTA].total, ctaCoarseGrid);
+            if (prof) {
+                if (evNext + 2 > (int)evPool.size()) {
+                    for (int i = 0; i < 64; ++i) { cudaEvent_t e; cudaEventCreate(&e); evPool.push_back(e); }
+                }
+                cudaEventRecord(evPool[evNext], st);
+                k_coarse_cta<R><<<grid, CTA_COARSE_THREADS, 0, st>>>(S, adom[0][D_CO_CTA]);
+                cudaEventRecord(evPool[evNext + 1], st);
+                evUse.push_back({"k_coarse_cta", evNext});
+                evNext += 2;
+            } else {
+                k_coarse_cta<R><<<grid, CTA_COARSE_THREADS, 0, st>>>(S, adom[0][D_CO_CTA]);
+            }
+            ++launches;
         }
         launchA("k_coarse_dense", D_CO_DENSE, TPB, k_coarse_dense<R>, S, adom[0][D_CO_DENSE]);
         launchA("k_coarse_serial", D_CO_SERIAL, 32, k_coarse_serial<R>, S, adom[0][D_CO_SERIAL]);

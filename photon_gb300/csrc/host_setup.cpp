@@ -144,7 +144,7 @@ void gsSweep(const MgLevel& L, const double* b, double* x, bool forward) {
 }
 }  // namespace
 
-Multigrid buildMultigrid(const GridGeom& g, int denseMax) {
+Multigrid buildMultigrid(const GridGeom& g, int denseMax, int coarseStop) {
     Multigrid M;
     const int nx = g.nx, ny = g.ny, nz = g.nz, n0 = g.N(), sxy = nx * ny;
     M.a0x = g.ax;
@@ -236,7 +236,7 @@ Multigrid buildMultigrid(const GridGeom& g, int denseMax) {
         M.lv.push_back(std::move(C));
     }
     // coarser levels: connected pieces of 2x2x2 groups of block coordinates
-    while (M.lv.back().n > 2000 && M.lv.size() < 12) {
+    while (M.lv.back().n > coarseStop && M.lv.size() < 12) {
         MgLevel& F = M.lv.back();
         UnionFind uf(F.n);
         for (int I = 0; I < F.n; ++I)

@@ -61,8 +61,11 @@ struct Multigrid {
 // Solver::buildPressureLevels (src/sim/pressure_mg.cpp:28-191), plus the
 // children lists of each aggregation and, when the coarsest level has at most
 // denseMax unknowns, the dense operator of its 20 forward + backward
-// Gauss-Seidel sweeps from x = 0 (pressure_mg.cpp:258-266, 279).
-Multigrid buildMultigrid(const GridGeom& g, int denseMax);
+// Gauss-Seidel sweeps from x = 0 (pressure_mg.cpp:258-266, 279). Levels are
+// added while the last one has more than coarseStop unknowns: 2000 is the
+// reference's schedule (:141); a smaller stop gives a deeper hierarchy.
+constexpr int MG_COARSE_STOP_REF = 2000;
+Multigrid buildMultigrid(const GridGeom& g, int denseMax, int coarseStop = MG_COARSE_STOP_REF);
 
 // Solver::addBurner cell selection (src/sim/gasphase.cpp:72-90): the gas cells
 // whose centres lie in the rectangle at height z + dx/2, or the centre cell.

@@ -41,19 +41,20 @@ __global__ void k_mx_res64(const Scn<R>* __restrict__ S, ADom dom, int inLoop) {
         // needs no FP64 multiply per neighbour; the others read the arrays
         const unsigned cd = g.code0 ? g.code0[c] : 64u;
         const bool coded = !(cd & 64u);
-        const double dg = coded ? (double)__popc(cd & 63u) : (double)g.diag[c];
+        const double dg = coded ? (double)(__popc(cd & 63u) + (cd >> 7)) : (double)g.diag[c];
         double r = 0;
         if (dg > 0) {
-            const int i = c % nx, j = (c / nx) % ny, k = c / sxy;
+            int i, j, k;
+            ijkOf(g, 0, c, i, j, k);
             const double* x = g.p64;
             double s = dg * x[c];
             if (coded) {
-                if ((cd & 1u) && i > 0) s -= x[c - 1];
-                if ((cd & 2u) && i < nx - 1) s -= x[c + 1];
-                if ((cd & 4u) && j > 0) s -= x[c - nx];
-                if ((cd & 8u) && j < ny - 1) s -= x[c + nx];
-                if ((cd & 16u) && k > 0) s -= x[c - sxy];
-                if ((cd & 32u) && k < nz - 1) s -= x[c + sxy];
+                if (cd & 1u) s -= x[c - 1];
+                if (cd & 2u) s -= x[c + 1];
+                if (cd & 4u) s -= x[c - nx];
+                if (cd & 8u) s -= x[c + nx];
+                if (cd & 16u) s -= x[c - sxy];
+                if (cd & 32u) s -= x[c + sxy];
             } else {
                 const int fx0 = i + (nx + 1) * (j + ny * k), fy0 = i + nx * (j + (ny + 1) * k);
                 if (i > 0) s -= (double)g.a0x[fx0] * x[c - 1];

@@ -105,6 +105,23 @@ struct Src {
     double power;                // ignition power (W)
 };
 
+// division by a grid dimension d as a multiply-high: q = floor(x m / 2^64)
+// with m = ceil(2^64 / d) is exact for every 32-bit x (the error x (m - 2^64 / d)
+// / 2^64 stays below 1 / d)
+struct DivU {
+    unsigned long long m;
+    unsigned d;
+};
+inline DivU makeDivU(unsigned d) {
+    DivU v;
+    v.d = d;
+    v.m = d <= 1 ? 0ull : (~0ull / d) + 1ull;
+    return v;
+}
+__device__ __forceinline__ unsigned divU(unsigned x, const DivU& v) {
+    return v.d <= 1 ? x : (unsigned)__umul64hi((unsigned long long)x, v.m);
+}
+
 template <class R>
 struct Level {
     int n;                       // unknowns
@@ -120,6 +137,11 @@ struct Level {
 template <class R>
 struct Scn {
     int nx, ny, nz, N, NX, NY, NZ;
+    // index recovery of the three layouts (kind 0: cells and z-faces, 1: x-faces, 2: y-faces):
+    // row length dvA, plane size dvB, rows per plane dY
+    DivU dvA[3], dvB[3];
+    int dY[3];
+    DivU dvL0[2];                // 2x2x2 blocks of the mixed path's level-0 kernels: blocks per row, per plane
     double dx, ox, oy, oz;
     double cfl, dtMaxP, tol, relTol;
     const double* dtMaxArg;      // this step's dtMax argument (one slot per scenario of the batch)
@@ -187,6 +209,7 @@ struct Dom {
     const int* start;            // [nscn + 1] prefix of CTAs per scenario
     int nscn;
     int total;                   // CTAs of the launch
+    const unsigned* owner;       // [total] scenario << 20 | tile of each CTA (null: search the prefix)
 };
 
 // the same over the scenarios still active in a solve: the prefix and the
@@ -220,6 +243,12 @@ __device__ __forceinline__ void locate(const ADom& d, int b, int& s, int& tile) 
 }
 
 __device__ __forceinline__ void locate(const Dom& d, int b, int& s, int& tile) {
+    if (d.owner) {   // one load instead of a search through the prefix
+        const unsigned v = __ldg(d.owner + b);
+        s = (int)(v >> 20);
+        tile = (int)(v & 0xFFFFFu);
+        return;
+    }
     int lo = 0, hi = d.nscn - 1;
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;

@@ -64,10 +64,9 @@ __device__ __forceinline__ R scratchRound(const Scn<R>& g, R v) {
 // mode 0: from x = 0, into y; mode 1: y -> x; mode 2: x plus the coarser
 // level's x prolongated (:290-297), into y.
 template <class R>
-__device__ __forceinline__ void jacobiTile(const Scn<R>& g, int tile, int l, int mode) {
+__device__ __forceinline__ void jacobiRow(const Scn<R>& g, int I, int l, int mode) {
     using T = R;
     const Level<R>& L = g.lv[l];
-    const int I = tile * TPB + threadIdx.x;
     if (I >= L.n) return;
     R* out = mode == 1 ? L.x : L.y;
     const T dg = L.diag[I];
@@ -91,6 +90,10 @@ __device__ __forceinline__ void jacobiTile(const Scn<R>& g, int tile, int l, int
     const T v = (T(1) - om) * X(I) + om * s / dg;
     out[I] = mode == 1 ? v : scratchRound(g, v);
 }
+template <class R>
+__device__ __forceinline__ void jacobiTile(const Scn<R>& g, int tile, int l, int mode) {
+    jacobiRow(g, tile * TPB + (int)threadIdx.x, l, mode);
+}
 
 // residual of level l fused with its restriction to level l+1 and the first
 // (from-zero) Jacobi sweep of level l+1 (pressure_mg.cpp:248-257, 285-286,
@@ -101,11 +104,11 @@ __device__ __forceinline__ void jacobiTile(const Scn<R>& g, int tile, int l, int
 // is the coarsest. Every thread of the tile takes part (warp shuffles).
 constexpr int RRJ_LANES = 8;
 template <class R>
-__device__ __forceinline__ void resRestrictJac0Tile(const Scn<R>& g, int tile, int l) {
+__device__ __forceinline__ void resRestrictJac0Group(const Scn<R>& g, int jBase, int l) {
     using T = R;
     const Level<R>& L = g.lv[l];
     const Level<R>& C = g.lv[l + 1];
-    const int J = tile * (TPB / RRJ_LANES) + (threadIdx.x / RRJ_LANES);
+    const int J = jBase + (threadIdx.x / RRJ_LANES);
     const int c = threadIdx.x % RRJ_LANES;
     const int groupLane0 = threadIdx.x & 31 & ~(RRJ_LANES - 1);
     int nch = 0, e0 = 0;
@@ -141,15 +144,19 @@ __device__ __forceinline__ void resRestrictJac0Tile(const Scn<R>& g, int tile, i
         }
     }
 }
+template <class R>
+__device__ __forceinline__ void resRestrictJac0Tile(const Scn<R>& g, int tile, int l) {
+    resRestrictJac0Group(g, tile * (TPB / RRJ_LANES), l);
+}
 
 // coarsest level: x = M b with the dense operator of the reference's 20
 // forward + backward Gauss-Seidel sweeps (pressure_mg.cpp:258-266, 279).
 // One warp per row.
 template <class R>
-__device__ __forceinline__ void coarseDenseTile(const Scn<R>& g, int tile) {
+__device__ __forceinline__ void coarseDenseRows(const Scn<R>& g, int rowBase) {
     using T = R;
     const Level<R>& L = g.lv[g.nLevels - 1];
-    const int row = tile * (TPB / 32) + (threadIdx.x >> 5);
+    const int row = rowBase + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (row >= L.n) return;
     const R* M = L.dense + (size_t)row * L.n;
@@ -157,6 +164,50 @@ __device__ __forceinline__ void coarseDenseTile(const Scn<R>& g, int tile) {
     for (int j = lane; j < L.n; j += 32) acc += M[j] * L.b[j];
     acc = warpSum(acc);
     if (lane == 0) L.x[row] = acc;
+}
+template <class R>
+__device__ __forceinline__ void coarseDenseTile(const Scn<R>& g, int tile) {
+    coarseDenseRows(g, tile * (TPB / 32));
+}
+
+// The levels from 2 down to the coarsest and back up again, for one scenario
+// in one CTA of CTA_COARSE_THREADS threads, with a barrier between passes
+// instead of a launch per pass: level l's second Jacobi sweep, its residual
+// restricted to level l+1 with l+1's first sweep, ..., the coarsest level's
+// dense operator, then per level the prolongated sweep and the last sweep.
+// Each pass computes what the per-level launches compute, row for row. For
+// scenarios with three or more levels whose coarsest level is small enough
+// for one CTA's dense product (the mixed path's deeper hierarchy).
+constexpr int CTA_COARSE_THREADS = 1024;
+constexpr int CTA_COARSE_DENSE_MAX = 640;
+template <class R>
+__global__ void __launch_bounds__(CTA_COARSE_THREADS) k_coarse_cta(const Scn<R>* __restrict__ S, ADom dom) {
+    __shared__ int sst_[MAX_BATCH + 1];
+    for (int i = threadIdx.x; i <= dom.nscn; i += blockDim.x) sst_[i] = dom.start[i];
+    __syncthreads();
+    const int tot = sst_[dom.nscn];
+    for (int b = blockIdx.x; b < tot; b += gridDim.x) {
+        int s, tile;
+        locateShared(sst_, dom.nscn, b, s, tile);
+        const Scn<R>& g = S[s];
+        if (g.sv[SV_DONE] != 0) continue;
+        const int nl = g.nLevels;
+        for (int l = 2; l < nl - 1; ++l) {
+            for (int I = threadIdx.x; I < g.lv[l].n; I += CTA_COARSE_THREADS) jacobiRow(g, I, l, 1);
+            __syncthreads();
+            const int nJ = g.lv[l + 1].n;
+            for (int jb = 0; jb < nJ; jb += CTA_COARSE_THREADS / RRJ_LANES) resRestrictJac0Group(g, jb, l);
+            __syncthreads();
+        }
+        for (int rb = 0; rb < g.lv[nl - 1].n; rb += CTA_COARSE_THREADS / 32) coarseDenseRows(g, rb);
+        __syncthreads();
+        for (int l = nl - 2; l >= 2; --l) {
+            for (int I = threadIdx.x; I < g.lv[l].n; I += CTA_COARSE_THREADS) jacobiRow(g, I, l, 2);
+            __syncthreads();
+            for (int I = threadIdx.x; I < g.lv[l].n; I += CTA_COARSE_THREADS) jacobiRow(g, I, l, 1);
+            __syncthreads();
+        }
+    }
 }
 
 // coarsest level solved as the reference does it: 20 forward + backward

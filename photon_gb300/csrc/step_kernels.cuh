@@ -18,6 +18,17 @@ namespace phx {
     locate(dom, blockIdx.x, s_, tile_);   \
     const Scn<R>& g = S[s_];
 
+// (i, j, k) of element f of a layout: kind 0 cells and z-faces, 1 x-faces, 2 y-faces
+template <class R>
+__device__ __forceinline__ void ijkOf(const Scn<R>& g, int kind, int f, int& i, int& j, int& k) {
+    const unsigned q = divU((unsigned)f, g.dvA[kind]);
+    k = (int)divU((unsigned)f, g.dvB[kind]);
+    i = f - (int)(q * g.dvA[kind].d);
+    j = (int)q - k * g.dY[kind];
+}
+// the layout kind of the faces normal to axis a
+__device__ __forceinline__ int faceKind(int a) { return a == 0 ? 1 : a == 1 ? 2 : 0; }
+
 template <class R>
 __device__ __forceinline__ double gasDensity(const Scn<R>& g, int c) {
     const double t = tempIsOffset<R>() ? K_T0 + (double)g.sc[0][c] : (double)g.sc[0][c];
@@ -144,7 +155,8 @@ __global__ void k_combust(const Scn<R>* __restrict__ S, Dom dom) {
     T Qc = 0, Qrc = 0, hrrc = 0, ms = 0;
     uint8_t pil = 0, litn = 0;
     if (!g.blocked[c]) {
-        const int i = c % nx, j = (c / nx) % ny, k = c / sz;
+        int i, j, k;
+        ijkOf(g, 0, c, i, j, k);
         R* const* Y = g.sc;
         T Tc = tAbs(Y[0][c]);
         T yf = Y[2][c];
@@ -246,7 +258,8 @@ __global__ void k_turb_center(const Scn<R>* __restrict__ S, Dom dom) {
     R *uc = g.tmp[0], *vc = g.tmp[1], *wc = g.tmp[2];
     if (g.blocked[c]) { uc[c] = vc[c] = wc[c] = 0; return; }
     const int nx = g.nx, ny = g.ny;
-    const int i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
+    int i, j, k;
+    ijkOf(g, 0, c, i, j, k);
     int fx0 = i + (nx + 1) * (j + ny * k);
     int fy0 = i + nx * (j + (ny + 1) * k);
     uc[c] = T(0.5) * (g.u[fx0] + g.u[fx0 + 1]);
@@ -264,7 +277,8 @@ __global__ void k_turb_filter(const Scn<R>* __restrict__ S, Dom dom, int q, int 
     R* out = axis == 1 ? g.tmp[6 + q] : g.tmp[3 + q];
     if (g.blocked[c]) { out[c] = 0; return; }
     const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const int i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
+    int i, j, k;
+    ijkOf(g, 0, c, i, j, k);
     const int id = axis == 0 ? i : axis == 1 ? j : k, n = axis == 0 ? nx : axis == 1 ? ny : nz;
     const int st = axis == 0 ? 1 : axis == 1 ? nx : nx * ny;
     T self = in[c];
@@ -310,9 +324,10 @@ __global__ void k_heat_faces(const Scn<R>* __restrict__ S, Dom dom, int axis) {
     const int nfa = axis == 0 ? g.NX : axis == 1 ? g.NY : g.NZ;
     if (!g.adv || f >= nfa) return;
     int i, j, k, id, dim, st;
-    if (axis == 0) { i = f % (nx + 1); j = (f / (nx + 1)) % ny; k = f / ((nx + 1) * ny); id = i; dim = nx; st = 1; }
-    else if (axis == 1) { i = f % nx; j = (f / nx) % (ny + 1); k = f / (nx * (ny + 1)); id = j; dim = ny; st = nx; }
-    else { i = f % nx; j = (f / nx) % ny; k = f / sxy; id = k; dim = nz; st = sxy; }
+    ijkOf(g, faceKind(axis), f, i, j, k);
+    if (axis == 0) { id = i; dim = nx; st = 1; }
+    else if (axis == 1) { id = j; dim = ny; st = nx; }
+    else { id = k; dim = nz; st = sxy; }
     if (id < 1 || id > dim - 1) return;
     const int U = i + nx * (j + ny * k), L = U - st;
     const T fo = axis == 0 ? g.fx[f] : axis == 1 ? g.fy[f] : g.fz[f];
@@ -334,7 +349,8 @@ __global__ void k_heat(const Scn<R>* __restrict__ S, Dom dom) {
     int c = tile_ * TPB + threadIdx.x;
     if (c >= g.N || g.blocked[c]) return;
     const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
-    const int i = c % nx, j = (c / nx) % ny, k = c / sxy;
+    int i, j, k;
+    ijkOf(g, 0, c, i, j, k);
     const int fx0 = i + (nx + 1) * (j + ny * k), fy0 = i + nx * (j + (ny + 1) * k);
     const T fo[6] = {g.fx[fx0], g.fx[fx0 + 1], g.fy[fy0], g.fy[fy0 + nx], g.fz[c], g.fz[c + sxy]};
     const int nb[6] = {i > 0 ? c - 1 : -1, i < nx - 1 ? c + 1 : -1, j > 0 ? c - nx : -1, j < ny - 1 ? c + nx : -1,
@@ -415,7 +431,8 @@ __global__ void k_momentum(const Scn<R>* __restrict__ S, Dom dom, int comp) {
     R* out = comp == 0 ? g.u2 : comp == 1 ? g.v2 : g.w2;
     if (fo[f] <= T(0)) { out[f] = 0; return; }
     if (lk && lk[f]) { out[f] = vel[f]; return; }   // set by leakage()
-    const int i = f % dX, j = (f / dX) % dY, k = f / (dX * dY);
+    int i, j, k;
+    ijkOf(g, faceKind(comp), f, i, j, k);
     const int id[3] = {i, j, k};
     const int ncell[3] = {nx, ny, nz};
     const int st[3] = {1, dX, dX * dY};
@@ -695,7 +712,8 @@ __global__ void k_rhs(const Scn<R>* __restrict__ S, Dom dom) {
             g.r[c] = 0;
         } else {
             const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
-            const int i = c % nx, j = (c / nx) % ny, k = c / sxy;
+            int i, j, k;
+            ijkOf(g, 0, c, i, j, k);
             const T dt = (T)g.sv[SV_DT];
             const T dx = (T)g.dx;
             const T inv = dx * dx / dt;
@@ -789,7 +807,8 @@ __global__ void k_velcorr(const Scn<R>* __restrict__ S, Dom dom, int comp) {
     int f = tile_ * TPB + threadIdx.x;
     T vm = 0;
     if (f < dX * dY * dZ) {
-        const int i = f % dX, j = (f / dX) % dY, k = f / (dX * dY);
+        int i, j, k;
+        ijkOf(g, faceKind(comp), f, i, j, k);
         R* vel = comp == 0 ? g.u : comp == 1 ? g.v : g.w;
         const R* fo = comp == 0 ? g.fx : comp == 1 ? g.fy : g.fz;
         const R* am = comp == 0 ? g.ax : comp == 1 ? g.ay : g.az;
@@ -868,9 +887,10 @@ __global__ void k_adv_faces(const Scn<R>* __restrict__ S, Dom dom, int axis) {
     const int nfa = axis == 0 ? g.NX : axis == 1 ? g.NY : g.NZ;
     if (!g.adv || f >= nfa) return;
     int i, j, k, id, dim, st;
-    if (axis == 0) { i = f % (nx + 1); j = (f / (nx + 1)) % ny; k = f / ((nx + 1) * ny); id = i; dim = nx; st = 1; }
-    else if (axis == 1) { i = f % nx; j = (f / nx) % (ny + 1); k = f / (nx * (ny + 1)); id = j; dim = ny; st = nx; }
-    else { i = f % nx; j = (f / nx) % ny; k = f / sxy; id = k; dim = nz; st = sxy; }
+    ijkOf(g, faceKind(axis), f, i, j, k);
+    if (axis == 0) { id = i; dim = nx; st = 1; }
+    else if (axis == 1) { id = j; dim = ny; st = nx; }
+    else { id = k; dim = nz; st = sxy; }
     if (id < 1 || id > dim - 1) return;   // domain faces: one cell, evaluated inline
     const int U = i + nx * (j + ny * k), L = U - st;
     const T fo = axis == 0 ? g.fx[f] : axis == 1 ? g.fy[f] : g.fz[f];
@@ -941,7 +961,8 @@ __device__ __forceinline__ void advectCells(const Scn<R>* __restrict__ S, const 
     constexpr bool kF32 = std::is_same<T, float>::value;
     const T amb[NSC] = {tAmbient<T>(), T(K_YO2_AMB), T(0), T(0), T(0), T(0), T(K_YCO2_AMB), T(K_YH2O_AMB), T(0), T(0)};
     const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
-    const int i = c % nx, j = (c / nx) % ny, k = c / sxy;
+    int i, j, k;
+    ijkOf(g, 0, c, i, j, k);
     const T dx = (T)g.dx;
     const T invDx = T(1) / dx;
     const T dt = (T)g.sv[SV_DT];

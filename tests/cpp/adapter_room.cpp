@@ -13,6 +13,10 @@
 // 40 steps, the adapter's host vectors (float, as photon::Solver holds them)
 // to <prefix>_<field>.f32 and the same fields read through the C ABI in
 // double to <prefix>_<field>.f64, for a comparison with the oracle.
+//
+// With "case <prefix>" it runs photon_gpu::runCase for 2 s with rows every
+// 0.5 s and a checkpoint every 1 s (the host's saveState writes the time and
+// the temperature field), and prints the row times.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -20,6 +24,7 @@
 #include <string>
 #include <vector>
 
+#include "photon_gpu/case_loop.hpp"
 #include "photon_gpu/solver.hpp"
 
 // the members of photon::Solver a checkpoint's gas phase consists of
@@ -34,6 +39,15 @@ struct HostState {
         int burningCells = 0;
         double fuelIn = 0, fuelBurned = 0, fuelInDomain = 0;
     } stats;
+    // a stand-in for Solver::saveState: the time and the temperature field
+    bool saveState(const std::string& path, std::string& err) const {
+        FILE* f = std::fopen(path.c_str(), "wb");
+        if (!f) { err = "cannot open " + path; return false; }
+        std::fwrite(&time, sizeof(time), 1, f);
+        std::fwrite(T.data(), sizeof(float), T.size(), f);
+        std::fclose(f);
+        return true;
+    }
 };
 
 static bool setupRoom(photon_gpu::Solver& s, bool mixed) {
@@ -102,6 +116,23 @@ int main(int argc, char** argv) {
     const bool mixed = argc > 1 && std::string(argv[1]) == "mixed";
     const bool ckpt = argc > 2 && std::string(argv[2]) == "checkpoint";
     const bool dump = argc > 3 && std::string(argv[2]) == "dump";
+    const bool caseRun = argc > 3 && std::string(argv[2]) == "case";
+    if (caseRun) {
+        photon_gpu::Solver c;
+        if (!setupRoom(c, mixed)) return 1;
+        HostState h;
+        h.nx = c.nx; h.ny = c.ny; h.nz = c.nz; h.dx = c.dx;
+        photon_gpu::CaseSchedule sc;
+        sc.duration = 2.0f;
+        sc.outputInterval = 0.5f;
+        sc.checkpoint = 1.0f;
+        sc.prefix = argv[3];
+        const long steps = photon_gpu::runCase(c, h, sc, false, [&](HostState& host) {
+            std::printf("row %.7f\n", (double)host.time);
+        });
+        std::printf("steps %ld\n", steps);
+        return 0;
+    }
     photon_gpu::Solver s;
     if (!setupRoom(s, mixed)) return 1;
     float t = 0;

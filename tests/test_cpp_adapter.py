@@ -100,3 +100,20 @@ def test_adapter_checkpoint_round_trip(mode):
     assert int(vals["ckpt_same"]) == 1
     assert float(vals["ckpt_dtime"]) < 1e-5
     assert float(vals["ckpt_maxrel"]) < 1e-3
+
+
+@pytest.mark.gpu
+def test_adapter_case_loop_lands_on_output_times():
+    """photon_gpu::runCase (include/photon_gpu/case_loop.hpp): rows at 0, 0.5,
+    1, 1.5 and 2 s exactly (in the float time of photon::Solver), and one
+    checkpoint at 1 s and one at 2 s, written by the host's saveState."""
+    exe = compile_adapter()
+    with tempfile.TemporaryDirectory() as d:
+        prefix = os.path.join(d, "room")
+        out = subprocess.run([exe, "fp64", "case", prefix], capture_output=True, text=True, timeout=300)
+        assert out.returncode == 0, out.stdout + out.stderr
+        times = [float(l.split()[1]) for l in out.stdout.splitlines() if l.startswith("row ")]
+        assert len(times) == 5, out.stdout
+        for t, want in zip(times, (0.0, 0.5, 1.0, 1.5, 2.0)):
+            assert abs(t - want) <= 1e-6, (t, want)
+        assert sorted(os.listdir(d)) == ["room_1s.state", "room_2s.state"]
