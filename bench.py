@@ -395,6 +395,13 @@ def measure(args, precision, L, world, clocks: bool):
     dtMax = cases[0].profile.dtMax
     if args.spinup > 0:
         g.run(args.spinup, dtMax)
+    vcycle = None
+    if precision == _lib.PREC_MIXED and not args.no_tune:
+        # the V-cycle schedule per size bucket, tuned on the developed batch (state restored)
+        t0 = time.perf_counter()
+        stops = g.tune_vcycle(3, dtMax)
+        vcycle = {"coarsening_stop_per_bucket": stops, "tuning_s": round(time.perf_counter() - t0, 2),
+                  "buckets": "bucket b: [20000 * 2^b, 20000 * 2^(b+1)) cells"}
     g.run(max(3, args.warmup), dtMax)
     # a working set that fits in L2 is flushed before every timed step
     flush = g.device_bytes() < (200 << 20)
@@ -470,7 +477,7 @@ def measure(args, precision, L, world, clocks: bool):
     return {"cases": cases, "cells": cells, "value": value, "t_s": t_s, "iters": iters, "rels": rels,
             "launches": launches, "roofline": roof, "clk": clk, "prof": prof, "e2e": e2e_value,
             "h2d": 8 * n, "d2h": n * ctypes.sizeof(_lib.PhxStats) + 8 * n, "flush": flush,
-            "p50_ms": pct(0.5), "p99_ms": pct(0.99)}
+            "p50_ms": pct(0.5), "p99_ms": pct(0.99), "vcycle": vcycle}
 
 
 def measure_serving(args, precision):
@@ -701,6 +708,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batch64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="keep the reference's V-cycle schedule (no autotuning)")
     ap.add_argument("--cpu-budget", type=float, default=8.0, help="seconds of timed CPU steps per CPU baseline")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 lines on the 36x24x24 room and the "
                                                            "72x52x44 house")
@@ -791,6 +799,7 @@ def main():
                            "pressure_stop": "relative 1e-8 (max|r| <= 1e-8 max|b|, FP64)",
                            "l2": "flushed before each step" if mixed["flush"] else "inputs larger than L2",
                            "spinup_steps": args.spinup,
+                           "vcycle_schedule": mixed.get("vcycle"),
                            "cg_iters_last_step": {"min": min(mixed["iters"]), "max": max(mixed["iters"])},
                            "max_rel_residual_last_step": max(mixed["rels"]),
                            "parallelism": "replicas" if world > 1 else "single GPU, batched"},

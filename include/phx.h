@@ -265,6 +265,21 @@ int phx_batch_set_stats(struct phx_ctx* ctx, int scenario, const phx_stats* in);
  * levels and rows[0..cap) the unknowns of the first cap levels (level 0 is
  * the grid's cells). For tests and tuning; rows may be NULL. */
 int phx_batch_mg_info(struct phx_ctx* ctx, int scenario, int* levels, int* rows, int cap);
+/* V-cycle schedule autotuner of the mixed path. No counterpart in the
+ * reference, whose schedule is fixed (levels are added while the coarsest has
+ * more than 2000 unknowns, src/sim/pressure_mg.cpp:141). Scenarios fall in
+ * size buckets: bucket b holds scenarios of [20000 * 2^b, 20000 * 2^(b+1))
+ * cells (bucket 0 also the smaller ones, bucket 7 also the larger ones). For
+ * each bucket present in the batch, each candidate coarsening stop (2000,
+ * 1000, 500 unknowns) is applied to the bucket's scenarios and the batch is
+ * stepped `steps` times (1-50, timed with CUDA events, after one untimed step)
+ * from the same saved state at dt_max; every candidate solves to the same
+ * relative residual, and the fastest is kept. The choice is recorded process-
+ * wide, so scenarios created later with a size in that bucket use it; the
+ * batch's state is restored when the call returns. stops_out[0..cap) gets the
+ * chosen stop of every bucket (2000 where none was tuned). On an FP64 context
+ * the call changes nothing (the FP64 path keeps the reference's schedule). */
+int phx_batch_tune_vcycle(struct phx_ctx* ctx, int steps, double dt_max, int* stops_out, int cap);
 
 /* --- radiation trace -------------------------------------------------------
  * Replaces Solver::traceRadiation (src/sim/radiation.cpp:181-319): rays from

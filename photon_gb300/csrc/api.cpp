@@ -179,6 +179,11 @@ int phx_batch_set_stats(phx_ctx* c, int s, const phx_stats* in) {
 }
 int phx_set_stats(phx_ctx* c, const phx_stats* in) { return phx_batch_set_stats(c, 0, in); }
 
+int phx_batch_tune_vcycle(phx_ctx* c, int steps, double dt_max, int* stops_out, int cap) {
+    if (cap < 0) return fail(c, PHX_ERR_INVALID, "negative capacity");
+    return guarded(c, [&](phx::CtxBase* x) { return x->tuneVcycle(steps, dt_max, stops_out, cap); });
+}
+
 int phx_batch_mg_info(phx_ctx* c, int s, int* levels, int* rows, int cap) {
     if (cap < 0) return fail(c, PHX_ERR_INVALID, "negative capacity");
     return guarded(c, [&](phx::CtxBase* x) { return x->mgInfo(s, levels, rows, cap); });

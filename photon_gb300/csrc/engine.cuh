@@ -12,6 +12,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -40,7 +41,7 @@ namespace phx {
 constexpr int DENSE_MAX = 4096;
 
 enum DomId {
-    D_ONE = 0, D_CELLS, D_FX, D_FY, D_FZ, D_BX, D_BY, D_BZ, D_CZ, D_CC, D_CO_DENSE, D_CO_SERIAL, D_CO_CTA, D_RB, D_QUAD, D_LEAK,
+    D_ONE = 0, D_CELLS, D_FX, D_FY, D_FZ, D_BX, D_BY, D_BZ, D_CZ, D_CC, D_CO_DENSE, D_CO_SERIAL, D_RB, D_QUAD, D_LEAK,
     D_L0,                        // level-0 tiles of the mixed path: 2x2x2 blocks (level0.cuh)
     D_L0R,                       // the same, several blocks per thread (the passes with a dot product)
     D_LV0,                       // D_LV0 + l: rows of level l when l is not the coarsest (1 <= l < 12)
@@ -61,6 +62,27 @@ static T* carve(char*& base, size_t& off, size_t n) {
 // residual by the FP64 residual b - A p64
 constexpr int REPLACE_EVERY = 10;
 
+// V-cycle schedules of the mixed path, per bucket of scenario size: bucket b
+// holds scenarios of [20000 * 2^b, 20000 * 2^(b+1)) cells (bucket 0 also the
+// smaller ones, the last one the larger ones). A bucket's entry is the
+// multigrid coarsening stop the autotuner chose (0: not tuned, the
+// reference's 2000). Process-wide, so scenarios admitted later (serving,
+// batch_add) are built with the tuned schedule of their size.
+constexpr int VC_BUCKETS = 8;
+inline int vcycleBucket(long long cells) {
+    int b = 0;
+    long long e = 40000;
+    while (cells >= e && b < VC_BUCKETS - 1) { e *= 2; ++b; }
+    return b;
+}
+inline std::mutex& vcycleMutex() { static std::mutex m; return m; }
+inline int* vcycleTable() { static int t[VC_BUCKETS] = {0}; return t; }
+inline int vcycleStopFor(long long cells) {
+    std::lock_guard<std::mutex> lock(vcycleMutex());
+    const int v = vcycleTable()[vcycleBucket(cells)];
+    return v > 0 ? v : MG_COARSE_STOP_REF;
+}
+
 template <class R>
 struct Scenario {
     static constexpr bool kMixed = std::is_same<R, float>::value;
@@ -72,14 +94,17 @@ struct Scenario {
     Multigrid MG;
     std::vector<double> Pb0;
     std::vector<Src> ignitions, burners;
-    char* arena = nullptr;
-    size_t arenaBytes = 0;
+    char* arena = nullptr;       // fields, geometry, solve vectors, scalars
+    char* mgArena = nullptr;     // the multigrid levels (replaced when the V-cycle schedule changes)
+    size_t arenaBytes = 0;       // both arenas
+    size_t mainBytes = 0, mgBytes = 0;
     Scn<R> h{};                  // host copy of the device descriptor
     R* dbuf[2] = {nullptr, nullptr};
     std::string err;
 
     ~Scenario() {
         if (arena) cudaFree(arena);
+        if (mgArena) cudaFree(mgArena);
     }
 
     int setup(const phx_grid* g) {
@@ -117,8 +142,7 @@ struct Scenario {
         // set-up on the host: zones, multigrid
         Pb0.assign(NN, 101325.0);
         Z = computeZones(geo, Pb0);
-        if (kMixed)
-            if (const char* e = std::getenv("PHX_MG_STOP")) coarseStop = std::max(16, std::atoi(e));
+        if (kMixed) coarseStop = vcycleStopFor(NN);   // the tuned schedule of the scenario's size, if any
         MG = buildMultigrid(geo, DENSE_MAX, coarseStop);
         buildLeakFaces();
         return PHX_OK;
@@ -166,8 +190,13 @@ struct Scenario {
         }
     }
 
-    // device bytes the scenario will take (the arena layout without memory)
+    // device bytes the scenario will take (both arenas' layouts without memory)
     size_t layout(char* base) {
+        if (base) return layoutMain(base) + layoutLevels(mgArena);
+        return layoutMain(nullptr) + layoutLevels(nullptr);
+    }
+
+    size_t layoutMain(char* base) {
         const int N = geo.N(), NX = geo.NX(), NY = geo.NY(), NZ = geo.NZ();
         const int nl = (int)MG.lv.size();
         // one reduction partial per CTA of the widest reduction domain (cells,
@@ -219,16 +248,31 @@ struct Scenario {
         s.q = carve<R>(base, off, N);
         s.p64 = kMixed ? carve<double>(base, off, N) : nullptr;
         s.p64prev = kMixed ? carve<double>(base, off, N) : nullptr;
+        Level<R>& L0 = s.lv[0];
+        L0.diag = s.diag;
+        L0.x = s.z; L0.y = nullptr; L0.b = s.r;
+        L0.rowStart = nullptr; L0.col = nullptr; L0.val = nullptr;
+        L0.childStart = nullptr; L0.child = nullptr;
+        s.sv = carve<double>(base, off, SV_COUNT);
+        s.part = carve<double>(base, off, (size_t)PS_COUNT * partStride);
+        s.partStride = partStride;
+        s.cnt = carve<unsigned>(base, off, PS_COUNT + 4);
+        return off + 256;
+    }
+
+    // the levels' arrays in their own arena: level 0's aggregation map, and per
+    // coarser level its CSR rows, diagonal, iterate and scratch, child lists and,
+    // at the coarsest level, the dense operator
+    size_t layoutLevels(char* base) {
+        const int nl = (int)MG.lv.size();
+        size_t off = 0;
+        Scn<R>& s = h;
         s.nLevels = nl;
         for (int l = 0; l < nl; ++l) {
             const MgLevel& L = MG.lv[l];
             Level<R>& D = s.lv[l];
             D.n = L.n;
-            if (l == 0) {
-                D.diag = s.diag;
-                D.x = s.z; D.y = nullptr; D.b = s.r;
-                D.rowStart = nullptr; D.col = nullptr; D.val = nullptr;
-            } else {
+            if (l > 0) {
                 D.rowStart = carve<int>(base, off, L.rowStart.size());
                 D.col = carve<int>(base, off, L.col.size() + 1);
                 D.val = carve<R>(base, off, L.val.size() + 1);
@@ -240,22 +284,51 @@ struct Scenario {
             D.child = (l == 0 || L.child.empty()) ? nullptr : carve<int>(base, off, L.child.size() + 1);
             D.dense = L.dense.empty() ? nullptr : carve<R>(base, off, L.dense.size());
         }
-        s.sv = carve<double>(base, off, SV_COUNT);
-        s.part = carve<double>(base, off, (size_t)PS_COUNT * partStride);
-        s.partStride = partStride;
-        s.cnt = carve<unsigned>(base, off, PS_COUNT + 4);
         return off + 256;
     }
 
     int allocate() {
-        arenaBytes = layout(nullptr);
-        cudaError_t e = cudaMalloc(&arena, arenaBytes);
+        mainBytes = layoutMain(nullptr);
+        mgBytes = layoutLevels(nullptr);
+        arenaBytes = mainBytes + mgBytes;
+        cudaError_t e = cudaMalloc(&arena, mainBytes);
+        if (e == cudaSuccess) e = cudaMalloc(&mgArena, mgBytes);
         if (e != cudaSuccess) {
+            cudaGetLastError();
+            if (arena) cudaFree(arena);
             arena = nullptr;
+            mgArena = nullptr;
             err = std::string("device allocation of ") + std::to_string(arenaBytes) + " bytes failed: " + cudaGetErrorString(e);
             return PHX_ERR_OOM;
         }
-        layout(arena);
+        layoutMain(arena);
+        layoutLevels(mgArena);
+        return PHX_OK;
+    }
+
+    // Replace the multigrid hierarchy by one built with another coarsening stop
+    // (the V-cycle schedule): a new levels arena, uploaded; the fields and the
+    // solve's state in the main arena are untouched. The caller rebuilds the
+    // batch tables (the level domains change).
+    int rebuildLevels(cudaStream_t st, int stop) {
+        if (stop == coarseStop && mgArena) return PHX_OK;
+        Multigrid M = buildMultigrid(geo, DENSE_MAX, stop);
+        PHX_CK(cudaStreamSynchronize(st));
+        char* old = mgArena;
+        MG = std::move(M);
+        coarseStop = stop;
+        mgBytes = layoutLevels(nullptr);
+        char* fresh = nullptr;
+        if (cudaMalloc(&fresh, mgBytes) != cudaSuccess) {
+            cudaGetLastError();
+            err = "device allocation of the multigrid levels failed";
+            return PHX_ERR_OOM;
+        }
+        mgArena = fresh;
+        arenaBytes = mainBytes + mgBytes;
+        layoutLevels(mgArena);
+        PHX_TRY(uploadLevels(st));
+        if (old) cudaFree(old);
         return PHX_OK;
     }
 
@@ -280,7 +353,7 @@ struct Scenario {
     int upload(cudaStream_t st) {
         const int N = geo.N();
         Scn<R>& s = h;
-        PHX_CK(cudaMemsetAsync(arena, 0, arenaBytes, st));
+        PHX_CK(cudaMemsetAsync(arena, 0, mainBytes, st));
         s.nx = geo.nx; s.ny = geo.ny; s.nz = geo.nz; s.N = N; s.NX = geo.NX(); s.NY = geo.NY(); s.NZ = geo.NZ();
         s.dvA[0] = makeDivU(geo.nx); s.dvB[0] = makeDivU(geo.nx * geo.ny); s.dY[0] = geo.ny;
         s.dvA[1] = makeDivU(geo.nx + 1); s.dvB[1] = makeDivU((geo.nx + 1) * geo.ny); s.dY[1] = geo.ny;
@@ -296,6 +369,7 @@ struct Scenario {
         s.replaceEvery = REPLACE_EVERY;
         s.extrap = std::getenv("PHX_NO_EXTRAP") == nullptr;   // mixed path: extrapolated initial guess
         s.fp16Scratch = kMixed && std::getenv("PHX_FP16_SCRATCH") != nullptr;
+        s.fp16Z0 = kMixed && std::getenv("PHX_FP16_Z0") != nullptr;
         s.tj = rowBlockRows<R>(geo.nx, geo.ny);
         s.njb = (geo.ny + s.tj - 1) / s.tj;
         PHX_TRY(putRaw(st, s.blocked, geo.blocked.data(), N));
@@ -329,6 +403,12 @@ struct Scenario {
             PHX_TRY(put(st, s.sc2[q], std::vector<double>(N, amb[q])));
         }
         PHX_TRY(put(st, s.Pb, Pb0));
+        return uploadLevels(st);
+    }
+
+    int uploadLevels(cudaStream_t st) {
+        Scn<R>& s = h;
+        PHX_CK(cudaMemsetAsync(mgArena, 0, mgBytes, st));
         for (int l = 1; l < (int)MG.lv.size(); ++l) {
             const MgLevel& L = MG.lv[l];
             Level<R>& D = s.lv[l];
@@ -385,14 +465,6 @@ struct Scenario {
         return cd;
     }
 
-    // levels 2 and coarser in one CTA (k_coarse_cta): mixed path, three or more
-    // levels, a coarsest level small enough for one CTA's dense product
-    bool ctaCoarse() const {
-        const int nl = (int)MG.lv.size();
-        return kMixed && nl >= 3 && !MG.lv[nl - 1].dense.empty() && MG.lv[nl - 1].n <= CTA_COARSE_DENSE_MAX &&
-               std::getenv("PHX_NO_CTA_COARSE") == nullptr;
-    }
-
     // CTAs of each domain of this scenario
     void tiles(int* t) const {
         const int N = geo.N(), nx = geo.nx, ny = geo.ny, nz = geo.nz;
@@ -415,14 +487,11 @@ struct Scenario {
         t[D_CC] = cdiv((long long)Z.closedCells.size(), TPB);
         const int nl = (int)MG.lv.size();
         const MgLevel& Lc = MG.lv[nl - 1];
-        const bool cta = ctaCoarse();
-        t[D_CO_DENSE] = Lc.dense.empty() || cta ? 0 : cdiv(Lc.n, TPB / 32);
+        t[D_CO_DENSE] = Lc.dense.empty() ? 0 : cdiv(Lc.n, TPB / 32);
         t[D_CO_SERIAL] = Lc.dense.empty() ? 1 : 0;
-        t[D_CO_CTA] = cta ? 1 : 0;
         for (int l = 1; l < MAX_LEVELS; ++l) {
-            const bool batch = !cta || l < 2;   // levels 2 and coarser run in k_coarse_cta
-            t[D_LV0 + l] = (l < nl - 1 && batch) ? cdiv(MG.lv[l].n, TPB) : 0;
-            t[D_RS0 + l] = (l + 1 <= nl - 1 && batch) ? cdiv(MG.lv[l + 1].n, TPB / RRJ_LANES) : 0;   // 8 lanes per unknown
+            t[D_LV0 + l] = (l < nl - 1) ? cdiv(MG.lv[l].n, TPB) : 0;
+            t[D_RS0 + l] = (l + 1 <= nl - 1) ? cdiv(MG.lv[l + 1].n, TPB / RRJ_LANES) : 0;   // 8 lanes per unknown
         }
     }
 };
@@ -462,9 +531,9 @@ public:
     // mixed path: the coded-coefficient level-0 kernels (level0.cuh) and their launch shape;
     // PHX_L0_ROWBLOCK=1 runs the mixed path's level 0 on the row-block kernels instead
     const bool l0Requested = kMixed && std::getenv("PHX_L0_ROWBLOCK") == nullptr;
+    const bool splitApply = std::getenv("PHX_FUSED_APPLY") == nullptr;   // d = z + beta d in its own pass
     bool useL0 = false;
-    int l0grid[5] = {0, 0, 0, 0, 0};
-    int ctaCoarseGrid = 152 * 2;   // CTAs of k_coarse_cta: two per SM
+    int l0grid[6] = {0, 0, 0, 0, 0, 0};
     ADom adom[2][D_COUNT];
     double* hPin = nullptr;      // pinned scratch for read-backs
     Dom dom[D_COUNT];
@@ -673,6 +742,104 @@ public:
 
     // one bounded wait that nothing satisfies: the failure path a timed-out
     // copy takes (error word, host report, context still usable)
+    // ---- V-cycle schedule autotuner ----------------------------------------------
+    // For each size bucket present in the batch (largest total first), every
+    // candidate coarsening stop is applied to the bucket's scenarios and the
+    // whole batch is stepped from the same saved state: one untimed step (the
+    // step graph is rebuilt), then `steps` steps timed with CUDA events. Every
+    // candidate solves to the same relative residual, so the fastest one
+    // delivers the most cell-updates per second at equal residual; it is kept
+    // and recorded in the process-wide table. The batch's state is restored at
+    // the end. The FP64 path keeps the reference's schedule (its parity with
+    // the reference needs the reference's V-cycle).
+    int tuneVcycle(int steps, double dtMax, int* out, int cap) override {
+        if (steps < 1 || steps > 50 || !(dtMax > 0)) { err = "invalid tuning arguments"; return PHX_ERR_INVALID; }
+        auto report = [&]() {
+            std::lock_guard<std::mutex> lock(vcycleMutex());
+            for (int b = 0; b < cap && b < VC_BUCKETS && out; ++b) {
+                const int v = vcycleTable()[b];
+                out[b] = v > 0 ? v : MG_COARSE_STOP_REF;
+            }
+        };
+        if (!kMixed || nscn() == 0) { report(); return PHX_OK; }
+        PHX_TRY(ensureTables());
+        PHX_CK(cudaStreamSynchronize(st));
+        // the batch's state: every scenario's main arena (fields, solve vectors, scalars)
+        size_t snapBytes = 0;
+        for (auto& S : sc) snapBytes += S->mainBytes;
+        char* snap = nullptr;
+        if (cudaMalloc(&snap, snapBytes) != cudaSuccess) {
+            cudaGetLastError();
+            err = "device allocation of the tuner's state copy failed";
+            return PHX_ERR_OOM;
+        }
+        auto copyState = [&](bool save) -> int {
+            size_t o = 0;
+            for (auto& S : sc) {
+                if (save) PHX_CK(cudaMemcpyAsync(snap + o, S->arena, S->mainBytes, cudaMemcpyDeviceToDevice, st));
+                else PHX_CK(cudaMemcpyAsync(S->arena, snap + o, S->mainBytes, cudaMemcpyDeviceToDevice, st));
+                o += S->mainBytes;
+            }
+            return PHX_OK;
+        };
+        // host descriptors: the swap state of the double buffers is part of the state
+        std::vector<Scn<R>> hostSaved;
+        for (auto& S : sc) hostSaved.push_back(S->h);
+        auto restoreHost = [&]() {
+            for (int i = 0; i < nscn(); ++i) {
+                Scn<R>& h = sc[i]->h;
+                const Scn<R>& o = hostSaved[i];
+                h.u = o.u; h.v = o.v; h.w = o.w; h.u2 = o.u2; h.v2 = o.v2; h.w2 = o.w2;
+                h.lit = o.lit; h.lit2 = o.lit2;
+                for (int q = 0; q < NSC; ++q) { h.sc[q] = o.sc[q]; h.sc2[q] = o.sc2[q]; }
+            }
+        };
+        int r = copyState(true);
+        std::vector<long long> bucketCells(VC_BUCKETS, 0);
+        for (auto& S : sc) bucketCells[vcycleBucket(S->geo.N())] += S->geo.N();
+        std::vector<int> order;
+        for (int b = 0; b < VC_BUCKETS; ++b) if (bucketCells[b] > 0) order.push_back(b);
+        std::sort(order.begin(), order.end(), [&](int a, int b) { return bucketCells[a] > bucketCells[b]; });
+        const int cands[] = {MG_COARSE_STOP_REF, 1000, 500};
+        auto trial = [&](double* ms) -> int {
+            PHX_TRY(copyState(false));
+            restoreHost();
+            tablesDirty = true;
+            PHX_TRY(step(1, dtMax, nullptr, nullptr));
+            double t = 0;
+            int nl = 0;
+            PHX_TRY(timeSteps(steps, dtMax, 0, &t, &nl));
+            *ms = t;
+            return PHX_OK;
+        };
+        for (int b : order) {
+            if (r != PHX_OK) break;
+            int best = MG_COARSE_STOP_REF;
+            double bestMs = 1e300;
+            for (int c : cands) {
+                for (auto& S : sc)
+                    if (vcycleBucket(S->geo.N()) == b && (r = S->rebuildLevels(st, c)) != PHX_OK) { err = S->err; break; }
+                if (r != PHX_OK) break;
+                double ms = 0;
+                if ((r = trial(&ms)) != PHX_OK) break;
+                if (ms < bestMs) { bestMs = ms; best = c; }
+            }
+            if (r != PHX_OK) break;
+            for (auto& S : sc)
+                if (vcycleBucket(S->geo.N()) == b && (r = S->rebuildLevels(st, best)) != PHX_OK) { err = S->err; break; }
+            std::lock_guard<std::mutex> lock(vcycleMutex());
+            vcycleTable()[b] = best;
+        }
+        if (r == PHX_OK) r = copyState(false);
+        restoreHost();
+        tablesDirty = true;
+        cudaStreamSynchronize(st);
+        cudaFree(snap);
+        if (r != PHX_OK) return r;
+        report();
+        return checkDeviceError();
+    }
+
     int selftestWait(double limitMs) override {
         if (!(limitMs > 0) || limitMs > 1000) { err = "self-test limit must be in (0, 1000] ms"; return PHX_ERR_INVALID; }
         PHX_TRY(ensureTables());
@@ -912,6 +1079,7 @@ public:
         PHX_TRY(one(k_l0<L0_RES>, L0_RES));
         PHX_TRY(one(k_l0<L0_BLACK>, L0_BLACK));
         PHX_TRY(one(k_l0<L0_RED>, L0_RED));
+        PHX_TRY(one(k_l0<L0_APPLYD>, L0_APPLYD));
         useL0 = true;
         return PHX_OK;
     }
@@ -1208,7 +1376,7 @@ public:
         // the domains of the solve's persistent kernels (kind 0: solving, kind 1: replacing)
         int n = 0;
         auto add = [&](int kind, int d) { if (n < 32) t.list[n++] = (short)(kind * D_COUNT + d); };
-        add(0, D_CELLS); add(0, D_CZ); add(0, D_RB); add(0, D_L0); add(0, D_L0R); add(0, D_QUAD); add(0, D_CO_DENSE); add(0, D_CO_SERIAL); add(0, D_CO_CTA);
+        add(0, D_CELLS); add(0, D_CZ); add(0, D_RB); add(0, D_L0); add(0, D_L0R); add(0, D_QUAD); add(0, D_CO_DENSE); add(0, D_CO_SERIAL);
         for (int l = 1; l < maxLevels - 1 && l < MAX_LEVELS; ++l) { add(0, D_LV0 + l); add(0, D_RS0 + l); }
         add(1, D_CELLS); add(1, D_CZ);
         t.nlist = n;
@@ -1266,8 +1434,9 @@ public:
     void stTurbulence() {
         const Scn<R>* S = dS;
         launch("k_turb_center", D_CELLS, TPB, k_turb_center<R>, S, dom[D_CELLS]);
-        for (int q = 0; q < 3; ++q)
-            for (int a = 0; a < 3; ++a) launch("k_turb_filter", D_CELLS, TPB, k_turb_filter<R>, S, dom[D_CELLS], q, a);
+        launch("k_turb_filter", D_CELLS, TPB, k_turb_filter<R, 0>, S, dom[D_CELLS]);
+        launch("k_turb_filter", D_CELLS, TPB, k_turb_filter<R, 1>, S, dom[D_CELLS]);
+        launch("k_turb_filter", D_CELLS, TPB, k_turb_filter<R, 2>, S, dom[D_CELLS]);
         launch("k_turb_nu", D_CELLS, TPB, k_turb_nu<R>, S, dom[D_CELLS]);
     }
     void stHeat() {
@@ -1281,9 +1450,9 @@ public:
     void stEnergy() { launch("k_energy", D_CELLS, TPB, k_energy<R>, (const Scn<R>*)dS, dom[D_CELLS]); }
     void stMomentum() {
         const Scn<R>* S = dS;
-        launch("k_momentum", D_FX, TPB, k_momentum<R>, S, dom[D_FX], 0);
-        launch("k_momentum", D_FY, TPB, k_momentum<R>, S, dom[D_FY], 1);
-        launch("k_momentum", D_FZ, TPB, k_momentum<R>, S, dom[D_FZ], 2);
+        launch("k_momentum", D_FX, TPB, k_momentum<R, 0>, S, dom[D_FX]);
+        launch("k_momentum", D_FY, TPB, k_momentum<R, 1>, S, dom[D_FY]);
+        launch("k_momentum", D_FZ, TPB, k_momentum<R, 2>, S, dom[D_FZ]);
         launch("k_mom_bnd", D_BX, TPB, k_mom_bnd<R>, S, dom[D_BX], 0);
         launch("k_mom_bnd", D_BY, TPB, k_mom_bnd<R>, S, dom[D_BY], 1);
         launch("k_mom_bnd", D_BZ, TPB, k_mom_bnd<R>, S, dom[D_BZ], 2);
@@ -1314,22 +1483,6 @@ public:
         for (int l = 1; l < maxLevels - 1; ++l) {
             launchA("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, adom[0][D_LV0 + l], l, 1);
             launchA("k_res_restrict_jac0", D_RS0 + l, TPB, k_res_restrict_jac0<R>, S, adom[0][D_RS0 + l], l);
-        }
-        if (dom[D_CO_CTA].total > 0) {
-            const int grid = std::min(dom[D_CO_CTA].total, ctaCoarseGrid);
-            if (prof) {
-                if (evNext + 2 > (int)evPool.size()) {
-                    for (int i = 0; i < 64; ++i) { cudaEvent_t e; cudaEventCreate(&e); evPool.push_back(e); }
-                }
-                cudaEventRecord(evPool[evNext], st);
-                k_coarse_cta<R><<<grid, CTA_COARSE_THREADS, 0, st>>>(S, adom[0][D_CO_CTA]);
-                cudaEventRecord(evPool[evNext + 1], st);
-                evUse.push_back({"k_coarse_cta", evNext});
-                evNext += 2;
-            } else {
-                k_coarse_cta<R><<<grid, CTA_COARSE_THREADS, 0, st>>>(S, adom[0][D_CO_CTA]);
-            }
-            ++launches;
         }
         launchA("k_coarse_dense", D_CO_DENSE, TPB, k_coarse_dense<R>, S, adom[0][D_CO_DENSE]);
         launchA("k_coarse_serial", D_CO_SERIAL, 32, k_coarse_serial<R>, S, adom[0][D_CO_SERIAL]);
@@ -1368,7 +1521,11 @@ public:
     // so its first red half sweep runs after that.
     void cgIteration() {
         const Scn<R>* S = dS;
-        if (useL0) launchL0<L0_APPLY>("k_cg_apply", 1);
+        if (useL0 && splitApply) {
+            launchA("k_l0_dupdate", D_QUAD, TPB, k_l0_dupdate<0>, reinterpret_cast<const Scn<float>*>(S), adom[0][D_QUAD],
+                    reinterpret_cast<float* const*>(dD));
+            launchL0<L0_APPLYD>("k_cg_apply", 1);
+        } else if (useL0) launchL0<L0_APPLY>("k_cg_apply", 1);
         else launchRB("k_cg_apply", cfgApply, k_cg_apply_rb<R>, S, adom[0][D_RB], (R* const*)dD, cfgApply.shape);
         launchA("k_cg_update", D_QUAD, TPB, k_cg_update<R>, S, adom[0][D_QUAD], (R* const*)dD);
         if (kMixed) {

@@ -58,6 +58,10 @@ public:
     virtual double radLastMs() const = 0;
     virtual int volRender(int s, const phx_vol_params* p, const float* depth, float* rgb) = 0;
     virtual int selftestWait(double limitMs) = 0;
+    // V-cycle schedule autotuner (mixed path): per scenario-size bucket, the
+    // multigrid coarsening stop that steps the batch fastest at the solve's
+    // relative residual; out[b] gets bucket b's stop
+    virtual int tuneVcycle(int steps, double dtMax, int* out, int cap) = 0;
     virtual double volLastMs() const = 0;
     std::string err;
 };

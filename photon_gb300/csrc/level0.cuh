@@ -39,7 +39,7 @@ constexpr unsigned char CODE_BOUNDARY = 128;
 
 constexpr int L0_THREADS = 128;
 
-enum { L0_APPLY = 0, L0_PRE, L0_RES, L0_BLACK, L0_RED };
+enum { L0_APPLY = 0, L0_PRE, L0_RES, L0_BLACK, L0_RED, L0_APPLYD };
 
 // 2x2x2 blocks per thread: one for the sweeps and the residual; several for
 // the passes with a dot product, whose per-tile reduction they amortise
@@ -114,6 +114,12 @@ __device__ __forceinline__ float l0Sum(float sacc, unsigned cd, const L0Coef& a,
     return sacc;
 }
 
+// the level-0 smoother's output as stored: FP32, or rounded to FP16 when the
+// context studies FP16 storage of the smoother scratch (PHX_FP16_Z0)
+__device__ __forceinline__ float z0Store(const Scn<float>& g, float v) {
+    return g.fp16Z0 ? __half2float(__float2half_rn(v)) : v;
+}
+
 // whether a cell reads its neighbour across face f (0..5): a set bit of a
 // coded cell, an interior face of a general cell
 __device__ __forceinline__ bool l0Reads(unsigned cd, int f, bool interior) {
@@ -167,12 +173,15 @@ __global__ void __launch_bounds__(L0_THREADS, (MODE == L0_PRE || MODE == L0_BLAC
         const unsigned char* __restrict__ cf = g.code0;
         const int* __restrict__ af = g.lv[0].agg;
         const float* __restrict__ dprev = (MODE == L0_APPLY && it > 0) ? dbuf[2 * s + (it & 1)] : nullptr;
+        const float* __restrict__ dcur = MODE == L0_APPLYD ? dbuf[2 * s + ((it + 1) & 1)] : nullptr;
         const float* __restrict__ xc = MODE == L0_BLACK ? g.lv[1].x : nullptr;
         // the stencil value of cell c (red: i + j + k even)
         auto value = [&](int c, bool red) -> float {
             if constexpr (MODE == L0_APPLY) {
                 const float zv = zf[c];
                 return dprev ? zv + beta * dprev[c] : zv;
+            } else if constexpr (MODE == L0_APPLYD) {
+                return dcur[c];                                       // d, formed by k_l0_dupdate
             } else if constexpr (MODE == L0_PRE) {
                 const float rv = rf[c];
                 if (!red) return rv;                                  // black: its right-hand side
@@ -221,7 +230,7 @@ __global__ void __launch_bounds__(L0_THREADS, (MODE == L0_PRE || MODE == L0_BLAC
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
             const bool red = (((u & 1) + ((u >> 1) & 1) + (u >> 2)) & 1) == 0;
-            const bool reads = MODE == L0_APPLY || MODE == L0_RES ||
+            const bool reads = MODE == L0_APPLY || MODE == L0_APPLYD || MODE == L0_RES ||
                                (MODE == L0_RED ? red : !red);   // the colour this pass updates
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
@@ -253,26 +262,26 @@ __global__ void __launch_bounds__(L0_THREADS, (MODE == L0_PRE || MODE == L0_BLAC
             n.yp = dj ? NB[u][1] : X[u + 2];
             n.zm = dk ? X[u - 4] : NB[u][2];
             n.zp = dk ? NB[u][2] : X[u + 4];
-            if constexpr (MODE == L0_APPLY) {
-                dbuf[2 * s + ((it + 1) & 1)][c] = X[u];
+            if constexpr (MODE == L0_APPLY || MODE == L0_APPLYD) {
+                if constexpr (MODE == L0_APPLY) dbuf[2 * s + ((it + 1) & 1)][c] = X[u];
                 if (dg <= 0.f) { g.q[c] = 0.f; continue; }
                 const float sacc = l0Sum<-1>(dg * X[u], code, gen, n, i, j, k, nx, ny, nz);
                 g.q[c] = sacc;
                 dot = accAdd(dot, dotTerm(sacc, X[u]));
             } else if constexpr (MODE == L0_PRE) {
-                if (red) { g.z[c] = X[u]; continue; }
+                if (red) { g.z[c] = z0Store(g, X[u]); continue; }
                 float zc = 0.f;
-                if (dg > 0.f) zc = gsDiv(l0Sum<1>(X[u], code, gen, n, i, j, k, nx, ny, nz), dg);
+                if (dg > 0.f) zc = z0Store(g, gsDiv(l0Sum<1>(X[u], code, gen, n, i, j, k, nx, ny, nz), dg));
                 g.z[c] = zc;
             } else if constexpr (MODE == L0_BLACK) {
                 if (red) continue;
                 float zc = 0.f;
-                if (dg > 0.f) zc = gsDiv(l0Sum<1>(X[u], code, gen, n, i, j, k, nx, ny, nz), dg);
+                if (dg > 0.f) zc = z0Store(g, gsDiv(l0Sum<1>(X[u], code, gen, n, i, j, k, nx, ny, nz), dg));
                 g.z[c] = zc;
             } else if constexpr (MODE == L0_RED) {
                 if (red) {
                     float zc = 0.f;
-                    if (dg > 0.f) zc = gsDiv(l0Sum<1>(X[u], code, gen, n, i, j, k, nx, ny, nz), dg);
+                    if (dg > 0.f) zc = z0Store(g, gsDiv(l0Sum<1>(X[u], code, gen, n, i, j, k, nx, ny, nz), dg));
                     g.z[c] = zc;
                     dot = accAdd(dot, dotTerm(X[u], zc));
                 } else {
@@ -312,13 +321,14 @@ __global__ void __launch_bounds__(L0_THREADS, (MODE == L0_PRE || MODE == L0_BLAC
             }
         }
         }   // blocks of the thread
-        if constexpr (MODE == L0_APPLY || MODE == L0_RED) {
+        if constexpr (MODE == L0_APPLY || MODE == L0_APPLYD || MODE == L0_RED) {
             if (MODE == L0_RED && phase == 2) continue;
             const int nt = sst_[s + 1] - sst_[s];
             // fixed-order CTA sum, then the last CTA of the scenario sums the CTA partials
             const double v = blockSum(dot, shd);
-            double* part = g.part + (size_t)(MODE == L0_APPLY ? PS_DQ : PS_RZ) * g.partStride;
-            unsigned* cnt = g.cnt + (MODE == L0_APPLY ? PS_DQ : PS_RZ);
+            constexpr int slot = MODE == L0_RED ? PS_RZ : PS_DQ;
+            double* part = g.part + (size_t)slot * g.partStride;
+            unsigned* cnt = g.cnt + slot;
             if (threadIdx.x == 0) {
                 part[tile] = v;
                 __threadfence();
@@ -333,7 +343,7 @@ __global__ void __launch_bounds__(L0_THREADS, (MODE == L0_PRE || MODE == L0_BLAC
                 const double total = blockSum(acc, shd);
                 if (threadIdx.x == 0) {
                     *cnt = 0;
-                    if constexpr (MODE == L0_APPLY) {
+                    if constexpr (MODE != L0_RED) {
                         g.sv[SV_DQ] = total;
                         if (total <= 0) g.sv[SV_DONE] = 1;
                         else g.sv[SV_ALPHA] = g.sv[SV_RZ] / total;
@@ -342,6 +352,38 @@ __global__ void __launch_bounds__(L0_THREADS, (MODE == L0_PRE || MODE == L0_BLAC
                     }
                 }
             }
+        }
+    }
+}
+
+// d = z + beta d (src/sim/gasphase.cpp:620-622; d = z on the first iteration)
+// ahead of q = A d (L0_APPLYD), four cells per thread, over the active scenarios
+template <int UNUSED = 0>
+__global__ void __launch_bounds__(256) k_l0_dupdate(const Scn<float>* __restrict__ S, ADom dom, float* const* dbuf) {
+    __shared__ int sst_[MAX_BATCH + 1];
+    for (int i = threadIdx.x; i <= dom.nscn; i += blockDim.x) sst_[i] = dom.start[i];
+    __syncthreads();
+    const int tot = sst_[dom.nscn];
+    for (int b = blockIdx.x; b < tot; b += gridDim.x) {
+        int s, tile;
+        locateShared(sst_, dom.nscn, b, s, tile);
+        const Scn<float>& g = S[s];
+        const int it = (int)g.sv[SV_IT];
+        const float beta = (float)g.sv[SV_BETA];
+        const float* __restrict__ dp = it > 0 ? dbuf[2 * s + (it & 1)] : nullptr;
+        float* __restrict__ dn = dbuf[2 * s + ((it + 1) & 1)];
+        const float* __restrict__ z = g.z;
+        const int c0 = (tile * 256 + (int)threadIdx.x) * 4;
+        if (c0 + 4 <= g.N) {   // a tile is 1024 cells: quads start on 16-byte boundaries
+            float4 zv = *reinterpret_cast<const float4*>(z + c0);
+            if (dp) {
+                const float4 pv = *reinterpret_cast<const float4*>(dp + c0);
+                zv.x = zv.x + beta * pv.x; zv.y = zv.y + beta * pv.y;
+                zv.z = zv.z + beta * pv.z; zv.w = zv.w + beta * pv.w;
+            }
+            *reinterpret_cast<float4*>(dn + c0) = zv;
+        } else {
+            for (int c = c0; c < g.N; ++c) dn[c] = dp ? z[c] + beta * dp[c] : z[c];
         }
     }
 }

@@ -192,6 +192,7 @@ struct Scn {
     int extrap;                  // mixed path: start the solve from 2 p(n) - p(n-1) (PHX_NO_EXTRAP=1: from p(n))
     double* p64prev;             // mixed path: the previous step's pressure (FP64)
     int fp16Scratch;             // mixed path: Jacobi scratch rounded to FP16 (an accuracy study; off by default)
+    int fp16Z0;                  // mixed path: level-0 smoother output z rounded to FP16 (an accuracy study; off by default)
     int nLevels;
     Level<R> lv[MAX_LEVELS];
     // row-block tiles of the level-0 pressure kernels: tj rows x RB_KZ planes, njb blocks along y

@@ -170,46 +170,6 @@ __device__ __forceinline__ void coarseDenseTile(const Scn<R>& g, int tile) {
     coarseDenseRows(g, tile * (TPB / 32));
 }
 
-// The levels from 2 down to the coarsest and back up again, for one scenario
-// in one CTA of CTA_COARSE_THREADS threads, with a barrier between passes
-// instead of a launch per pass: level l's second Jacobi sweep, its residual
-// restricted to level l+1 with l+1's first sweep, ..., the coarsest level's
-// dense operator, then per level the prolongated sweep and the last sweep.
-// Each pass computes what the per-level launches compute, row for row. For
-// scenarios with three or more levels whose coarsest level is small enough
-// for one CTA's dense product (the mixed path's deeper hierarchy).
-constexpr int CTA_COARSE_THREADS = 1024;
-constexpr int CTA_COARSE_DENSE_MAX = 640;
-template <class R>
-__global__ void __launch_bounds__(CTA_COARSE_THREADS) k_coarse_cta(const Scn<R>* __restrict__ S, ADom dom) {
-    __shared__ int sst_[MAX_BATCH + 1];
-    for (int i = threadIdx.x; i <= dom.nscn; i += blockDim.x) sst_[i] = dom.start[i];
-    __syncthreads();
-    const int tot = sst_[dom.nscn];
-    for (int b = blockIdx.x; b < tot; b += gridDim.x) {
-        int s, tile;
-        locateShared(sst_, dom.nscn, b, s, tile);
-        const Scn<R>& g = S[s];
-        if (g.sv[SV_DONE] != 0) continue;
-        const int nl = g.nLevels;
-        for (int l = 2; l < nl - 1; ++l) {
-            for (int I = threadIdx.x; I < g.lv[l].n; I += CTA_COARSE_THREADS) jacobiRow(g, I, l, 1);
-            __syncthreads();
-            const int nJ = g.lv[l + 1].n;
-            for (int jb = 0; jb < nJ; jb += CTA_COARSE_THREADS / RRJ_LANES) resRestrictJac0Group(g, jb, l);
-            __syncthreads();
-        }
-        for (int rb = 0; rb < g.lv[nl - 1].n; rb += CTA_COARSE_THREADS / 32) coarseDenseRows(g, rb);
-        __syncthreads();
-        for (int l = nl - 2; l >= 2; --l) {
-            for (int I = threadIdx.x; I < g.lv[l].n; I += CTA_COARSE_THREADS) jacobiRow(g, I, l, 2);
-            __syncthreads();
-            for (int I = threadIdx.x; I < g.lv[l].n; I += CTA_COARSE_THREADS) jacobiRow(g, I, l, 1);
-            __syncthreads();
-        }
-    }
-}
-
 // coarsest level solved as the reference does it: 20 forward + backward
 // sweeps, serially in one thread (used when the level is too large for a dense
 // operator)

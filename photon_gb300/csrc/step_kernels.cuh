@@ -29,6 +29,13 @@ __device__ __forceinline__ void ijkOf(const Scn<R>& g, int kind, int f, int& i, 
 // the layout kind of the faces normal to axis a
 __device__ __forceinline__ int faceKind(int a) { return a == 0 ? 1 : a == 1 ? 2 : 0; }
 
+// ambient value of transported scalar q (the value outside the domain):
+// T (stored), O2, CO2 and H2O; zero for the others
+template <class T>
+__device__ __forceinline__ T ambOf(int q) {
+    return q == 0 ? tAmbient<T>() : q == 1 ? T(K_YO2_AMB) : q == 6 ? T(K_YCO2_AMB) : q == 7 ? T(K_YH2O_AMB) : T(0);
+}
+
 template <class R>
 __device__ __forceinline__ double gasDensity(const Scn<R>& g, int c) {
     const double t = tempIsOffset<R>() ? K_T0 + (double)g.sc[0][c] : (double)g.sc[0][c];
@@ -267,24 +274,35 @@ __global__ void k_turb_center(const Scn<R>* __restrict__ S, Dom dom) {
     wc[c] = T(0.5) * (g.w[c] + g.w[c + nx * ny]);
 }
 
-template <class R>
-__global__ void k_turb_filter(const Scn<R>* __restrict__ S, Dom dom, int q, int axis) {
+// one pass of the test filter along AXIS for the three velocity components
+// (the reference filters each component x -> y -> z; the components are
+// independent, so one launch per axis covers all three)
+template <class R, int AXIS>
+__global__ void k_turb_filter(const Scn<R>* __restrict__ S, Dom dom) {
     using T = R;
     PHX_PROLOGUE(dom);
     int c = tile_ * TPB + threadIdx.x;
     if (c >= g.N) return;
-    const R* in = axis == 0 ? g.tmp[q] : axis == 1 ? g.tmp[3 + q] : g.tmp[6 + q];
-    R* out = axis == 1 ? g.tmp[6 + q] : g.tmp[3 + q];
-    if (g.blocked[c]) { out[c] = 0; return; }
+    if (g.blocked[c]) {
+#pragma unroll
+        for (int q = 0; q < 3; ++q) (AXIS == 1 ? g.tmp[6 + q] : g.tmp[3 + q])[c] = 0;
+        return;
+    }
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     int i, j, k;
     ijkOf(g, 0, c, i, j, k);
-    const int id = axis == 0 ? i : axis == 1 ? j : k, n = axis == 0 ? nx : axis == 1 ? ny : nz;
-    const int st = axis == 0 ? 1 : axis == 1 ? nx : nx * ny;
-    T self = in[c];
-    T lo = id > 0 && !g.blocked[c - st] ? in[c - st] : self;
-    T hi = id < n - 1 && !g.blocked[c + st] ? in[c + st] : self;
-    out[c] = T(0.25) * lo + T(0.5) * self + T(0.25) * hi;
+    const int id = AXIS == 0 ? i : AXIS == 1 ? j : k, n = AXIS == 0 ? nx : AXIS == 1 ? ny : nz;
+    const int st = AXIS == 0 ? 1 : AXIS == 1 ? nx : nx * ny;
+    const bool hasLo = id > 0 && !g.blocked[c - st], hasHi = id < n - 1 && !g.blocked[c + st];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const R* in = AXIS == 0 ? g.tmp[q] : AXIS == 1 ? g.tmp[3 + q] : g.tmp[6 + q];
+        R* out = AXIS == 1 ? g.tmp[6 + q] : g.tmp[3 + q];
+        T self = in[c];
+        T lo = hasLo ? in[c - st] : self;
+        T hi = hasHi ? in[c + st] : self;
+        out[c] = T(0.25) * lo + T(0.5) * self + T(0.25) * hi;
+    }
 }
 
 template <class R>
@@ -416,9 +434,10 @@ __global__ void k_energy(const Scn<R>* __restrict__ S, Dom dom) {
 template <class T>
 __device__ __forceinline__ T vanLeer(T a, T b) { return a * b > T(0) ? T(2) * a * b / (a + b) : T(0); }
 
-template <class R>
-__global__ void k_momentum(const Scn<R>* __restrict__ S, Dom dom, int comp) {
+template <class R, int COMP>
+__global__ void k_momentum(const Scn<R>* __restrict__ S, Dom dom) {
     using T = R;
+    constexpr int comp = COMP;   // the face component: compile-time, so the per-axis arrays stay in registers
     PHX_PROLOGUE(dom);
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     const int dX = nx + (comp == 0), dY = ny + (comp == 1), dZ = nz + (comp == 2);
@@ -922,17 +941,16 @@ __global__ void k_adv_faces(const Scn<R>* __restrict__ S, Dom dom, int axis) {
     }
     const T Dd = T(0.5) * (g.nu[L] + g.nu[U]) / T(K_SC_T) + T(2.0e-5);
     const T rfd = T(0.5) * (rhoOf(g, L) + rhoOf(g, U));
-    const T amb[NSC] = {T(K_T0), T(K_YO2_AMB), T(0), T(0), T(0), T(0), T(K_YCO2_AMB), T(K_YH2O_AMB), T(0), T(0)};
     for (int q = 0; q < NSC; ++q) {
         const R* F = g.sc[q];
         const T fc = F[L], fn = F[U];
         T face = fc;
         if (un > T(0)) {
-            T fu2 = opp >= 0 ? F[opp] : (opp == -1 ? amb[q] : fc);
+            T fu2 = opp >= 0 ? F[opp] : (opp == -1 ? ambOf<T>(q) : fc);
             T den = fn - fc;
             if (fabs(den) > T(1e-12)) face += T(0.5) * superbee((fc - fu2) / den) * den;
         } else if (un < T(0)) {
-            T fu2 = nb2 >= 0 ? F[nb2] : (nb2 == -1 ? amb[q] : fn);
+            T fu2 = nb2 >= 0 ? F[nb2] : (nb2 == -1 ? ambOf<T>(q) : fn);
             T den = fc - fn;
             face = fn;
             if (fabs(den) > T(1e-12)) face += T(0.5) * superbee((fn - fu2) / den) * den;
@@ -959,7 +977,6 @@ __device__ __forceinline__ void advectCells(const Scn<R>* __restrict__ S, const 
     // expressions: the limiter as superbeeTimes, 1/dx and 1/mden multiplied.
     // The FP64 path keeps the reference's operations one for one.
     constexpr bool kF32 = std::is_same<T, float>::value;
-    const T amb[NSC] = {tAmbient<T>(), T(K_YO2_AMB), T(0), T(0), T(0), T(0), T(K_YCO2_AMB), T(K_YH2O_AMB), T(0), T(0)};
     const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
     int i, j, k;
     ijkOf(g, 0, c, i, j, k);
@@ -1039,7 +1056,7 @@ __device__ __forceinline__ void advectCells(const Scn<R>* __restrict__ S, const 
         T lo = fc, hi = fc, acc = 0, macc = 0;
         for (int d = 0; d < 6; ++d) {
             if (fo[d] <= T(0) || nb[d] == -2) continue;
-            T fn = nb[d] >= 0 ? F[nb[d]] : amb[q];
+            T fn = nb[d] >= 0 ? F[nb[d]] : ambOf<T>(q);
             lo = mn(lo, fn);
             hi = mx(hi, fn);
             T flux = un[d];
@@ -1058,7 +1075,7 @@ __device__ __forceinline__ void advectCells(const Scn<R>* __restrict__ S, const 
             }
             T face = fc;
             if (flux > T(0)) {
-                T fu2 = opp[d] >= 0 ? F[opp[d]] : (opp[d] == -1 ? amb[q] : fc);
+                T fu2 = opp[d] >= 0 ? F[opp[d]] : (opp[d] == -1 ? ambOf<T>(q) : fc);
                 T den = fn - fc;
                 if constexpr (kF32) {
                     if (fabs(den) > T(1e-12)) face += T(0.5) * superbeeTimes(fc - fu2, den);
@@ -1066,7 +1083,7 @@ __device__ __forceinline__ void advectCells(const Scn<R>* __restrict__ S, const 
                     if (fabs(den) > T(1e-12)) face += T(0.5) * superbee((fc - fu2) / den) * den;
                 }
             } else if (flux < T(0)) {
-                T fu2 = nb2[d] >= 0 ? F[nb2[d]] : (nb2[d] == -1 ? amb[q] : fn);
+                T fu2 = nb2[d] >= 0 ? F[nb2[d]] : (nb2[d] == -1 ? ambOf<T>(q) : fn);
                 T den = fc - fn;
                 face = fn;
                 if constexpr (kF32) {

@@ -287,6 +287,12 @@ class Batch:
         """unknowns of each level of scenario s's pressure multigrid"""
         return _mg_rows(self.L, self.h, s)
 
+    def tune_vcycle(self, steps: int = 3, dtMax: float = 0.02) -> list:
+        """phx_batch_tune_vcycle: the coarsening stop chosen per size bucket"""
+        out = (ctypes.c_int * 8)()
+        self._check(self.L.phx_batch_tune_vcycle(self.h, steps, dtMax, ctypes.cast(out, ctypes.c_void_p), 8))
+        return list(out)
+
     def scenario_bytes(self, s: int) -> int:
         return int(self.L.phx_batch_scenario_bytes(self.h, s))
 
