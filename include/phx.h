@@ -265,6 +265,12 @@ int phx_batch_set_stats(struct phx_ctx* ctx, int scenario, const phx_stats* in);
  * levels and rows[0..cap) the unknowns of the first cap levels (level 0 is
  * the grid's cells). For tests and tuning; rows may be NULL. */
 int phx_batch_mg_info(struct phx_ctx* ctx, int scenario, int* levels, int* rows, int cap);
+/* Stored off-diagonal entries of each level's CSR rows in the same hierarchy
+ * (the reference's PressureLevel rowStart/col/val arrays,
+ * src/sim/pressure_mg.cpp:100-184): nnz[0..cap) for the first cap levels;
+ * level 0, the structured grid, has no CSR rows and gets 0. For the
+ * benchmark's byte model of the coarse-level kernels. */
+int phx_batch_mg_nnz(struct phx_ctx* ctx, int scenario, int* nnz, int cap);
 /* V-cycle schedule autotuner of the mixed path. No counterpart in the
  * reference, whose schedule is fixed (levels are added while the coarsest has
  * more than 2000 unknowns, src/sim/pressure_mg.cpp:141). Scenarios fall in

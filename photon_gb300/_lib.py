@@ -29,7 +29,7 @@ SYMBOLS = ["phx_create", "phx_destroy", "phx_last_error", "phx_last_global_error
            "phx_time_steps", "phx_profile_step", "phx_last_step_launches", "phx_rad_trace", "phx_batch_rad_trace", "phx_rad_last_ms", "phx_vol_render", "phx_batch_vol_render", "phx_vol_last_ms", "phx_selftest_wait_timeout", "phx_select_device", "phx_alloc_host",
            "phx_free_host", "phx_create_batch", "phx_batch_add", "phx_batch_remove", "phx_batch_size",
            "phx_batch_scenario_bytes", "phx_batch_add_burner", "phx_batch_step", "phx_batch_get_field",
-           "phx_batch_set_field", "phx_batch_field_count", "phx_batch_get_stats", "phx_batch_set_stats", "phx_batch_mg_info", "phx_batch_tune_vcycle", "phx_gather_stats_noalloc",
+           "phx_batch_set_field", "phx_batch_field_count", "phx_batch_get_stats", "phx_batch_set_stats", "phx_batch_mg_info", "phx_batch_mg_nnz", "phx_batch_tune_vcycle", "phx_gather_stats_noalloc",
            "phx_server_create", "phx_server_destroy", "phx_server_last_error", "phx_server_submit", "phx_server_step",
            "phx_server_poll", "phx_server_get_field", "phx_server_release", "phx_server_counts"]
 
@@ -180,6 +180,7 @@ def load():
     L.phx_batch_get_stats.argtypes = [vp, i, ctypes.POINTER(PhxStats)]
     L.phx_batch_set_stats.argtypes = [vp, i, ctypes.POINTER(PhxStats)]
     L.phx_batch_mg_info.argtypes = [vp, i, ctypes.POINTER(i), vp, i]
+    L.phx_batch_mg_nnz.argtypes = [vp, i, vp, i]
     L.phx_batch_tune_vcycle.argtypes = [vp, i, d, vp, i]
     L.phx_rad_trace.argtypes = [vp, vp, i, vp, i, vp, vp, vp]
     L.phx_batch_rad_trace.argtypes = [vp, i, vp, i, vp, i, vp, vp, vp]

@@ -189,6 +189,11 @@ int phx_batch_mg_info(phx_ctx* c, int s, int* levels, int* rows, int cap) {
     return guarded(c, [&](phx::CtxBase* x) { return x->mgInfo(s, levels, rows, cap); });
 }
 
+int phx_batch_mg_nnz(phx_ctx* c, int s, int* nnz, int cap) {
+    if (cap < 0) return fail(c, PHX_ERR_INVALID, "negative capacity");
+    return guarded(c, [&](phx::CtxBase* x) { return x->mgNnz(s, nnz, cap); });
+}
+
 int phx_get_field(phx_ctx* c, int field, void* host, size_t bytes) { return phx_batch_get_field(c, 0, field, host, bytes); }
 int phx_set_field(phx_ctx* c, int field, const void* host, size_t bytes) { return phx_batch_set_field(c, 0, field, host, bytes); }
 size_t phx_field_count(const phx_ctx* c, int field) { return phx_batch_field_count(c, 0, field); }

@@ -214,7 +214,7 @@ struct Scenario {
         s.ly = geo.anyLeak ? carve<uint8_t>(base, off, NY) : nullptr;
         s.lz = geo.anyLeak ? carve<uint8_t>(base, off, NZ) : nullptr;
         s.diag = carve<R>(base, off, N);
-        s.code0 = kMixed ? carve<unsigned char>(base, off, N) : nullptr;
+        s.code0 = carve<unsigned char>(base, off, N);
         s.zone = carve<int>(base, off, N);
         const int nZ = (int)Z.zoneP.size(), nC = (int)Z.closed.size();
         s.zoneOpen = carve<uint8_t>(base, off, nZ + 1);
@@ -360,6 +360,11 @@ struct Scenario {
         s.dvA[2] = makeDivU(geo.nx); s.dvB[2] = makeDivU(geo.nx * (geo.ny + 1)); s.dY[2] = geo.ny + 1;
         s.dvL0[0] = makeDivU((geo.nx + 1) >> 1); s.dvL0[1] = makeDivU(((geo.nx + 1) >> 1) * ((geo.ny + 1) >> 1));
         s.dx = geo.dx; s.ox = geo.ox; s.oy = geo.oy; s.oz = geo.oz;
+        {   // IEEE divisions in R: the values of the kernels' R(1) / dx
+            const R dxr = (R)geo.dx;
+            s.rdx = R(1) / dxr;
+            s.rdx2 = R(1) / (dxr * dxr);
+        }
         s.cfl = cfl; s.dtMaxP = dtMaxP; s.tol = tol; s.relTol = relTol; s.maxIters = maxIters; s.radiationOn = radiationOn;
         double th = geo.windFromDeg * 3.14159265 / 180.0;
         s.windSpeed = geo.windSpeed; s.windSin = std::sin(th); s.windCos = std::cos(th); s.windExp = geo.windExp;
@@ -377,7 +382,7 @@ struct Scenario {
         PHX_TRY(put(st, s.ax, geo.ax)); PHX_TRY(put(st, s.ay, geo.ay)); PHX_TRY(put(st, s.az, geo.az));
         PHX_TRY(put(st, s.a0x, MG.a0x)); PHX_TRY(put(st, s.a0y, MG.a0y)); PHX_TRY(put(st, s.a0z, MG.a0z));
         PHX_TRY(put(st, s.diag, MG.lv[0].diag));
-        if (kMixed) {
+        {
             const std::vector<unsigned char> cd = levelZeroCodes();
             PHX_TRY(putRaw(st, s.code0, cd.data(), cd.size()));
         }
@@ -473,8 +478,8 @@ struct Scenario {
         t[D_ONE] = 1;
         t[D_CELLS] = cdiv(N, TPB);
         t[D_RB] = cdiv(ny, rowBlockRows<R>(nx, ny)) * cdiv(nz, RB_KZ);      // row blocks x plane blocks
-        t[D_L0] = kMixed ? l0Tiles(nx, ny, nz, 1) : 0;
-        t[D_L0R] = kMixed ? l0Tiles(nx, ny, nz, l0Bpt(L0_RED)) : 0;
+        t[D_L0] = l0Tiles(nx, ny, nz, 1);
+        t[D_L0R] = l0Tiles(nx, ny, nz, l0Bpt(L0_RED));
         t[D_QUAD] = cdiv(N, TPB * CG_QUAD);                                 // 4 cells per thread
         t[D_LEAK] = cdiv((long long)leak.size() / 4, TPB);
         t[D_FX] = cdiv(geo.NX(), TPB);
@@ -512,7 +517,7 @@ public:
     R** dD = nullptr;            // CG direction buffers, 2 per scenario
     int* dDomStart = nullptr;    // D_COUNT x (cap + 1)
     double* dDtMax = nullptr;    // per-scenario dtMax of the step
-    int* dLoop = nullptr;        // loop counters of the graph's while nodes
+    int* dLoop = nullptr;        // [0] iterations of the graph's CG while node, [1] runs of its replacement node
     int* dTiles = nullptr;       // [D_COUNT][cap] tiles of each scenario per domain
     int* dAStart = nullptr;      // [2][D_COUNT][cap + 1] active-tile prefixes (solving / replacing)
     int* dATotal = nullptr;      // [2][D_COUNT]
@@ -528,12 +533,12 @@ public:
         RbShape shape{0, 0, 0};
     };
     RbCfg cfgApply, cfgGs[3], cfgRes;
-    // mixed path: the coded-coefficient level-0 kernels (level0.cuh) and their launch shape;
-    // PHX_L0_ROWBLOCK=1 runs the mixed path's level 0 on the row-block kernels instead
-    const bool l0Requested = kMixed && std::getenv("PHX_L0_ROWBLOCK") == nullptr;
-    const bool splitApply = std::getenv("PHX_FUSED_APPLY") == nullptr;   // d = z + beta d in its own pass
+    // the coded-coefficient level-0 kernels (level0.cuh) and their launch shape;
+    // PHX_L0_ROWBLOCK=1 runs level 0 on the row-block kernels instead
+    const bool l0Requested = std::getenv("PHX_L0_ROWBLOCK") == nullptr;
     bool useL0 = false;
-    int l0grid[6] = {0, 0, 0, 0, 0, 0};
+    bool l0RedWide = false;            // the red sweep with L0_RED_WIDE blocks per thread
+    int l0grid[L0_MODES + 1] = {};     // per pass; [L0_MODES]: the wide red sweep
     ADom adom[2][D_COUNT];
     double* hPin = nullptr;      // pinned scratch for read-backs
     Dom dom[D_COUNT];
@@ -1062,8 +1067,8 @@ public:
         return PHX_OK;
     }
 
-    // launch shape of the level-0 kernels of the mixed path: a persistent grid
-    // of as many CTAs as fit on the SMs
+    // launch shape of the level-0 kernels: a persistent grid of as many CTAs
+    // as fit on the SMs
     int setupL0() {
         int dev = 0, sms = 0;
         PHX_CK(cudaGetDevice(&dev));
@@ -1074,36 +1079,48 @@ public:
             l0grid[mode] = std::min(sms * std::max(occ, 1), persistCtas * TPB / L0_THREADS);
             return PHX_OK;
         };
-        PHX_TRY(one(k_l0<L0_APPLY>, L0_APPLY));
-        PHX_TRY(one(k_l0<L0_PRE>, L0_PRE));
-        PHX_TRY(one(k_l0<L0_RES>, L0_RES));
-        PHX_TRY(one(k_l0<L0_BLACK>, L0_BLACK));
-        PHX_TRY(one(k_l0<L0_RED>, L0_RED));
-        PHX_TRY(one(k_l0<L0_APPLYD>, L0_APPLYD));
+        PHX_TRY(one(k_l0<R, L0_APPLY, 1>, L0_APPLY));
+        PHX_TRY(one(k_l0<R, L0_PRE, 1>, L0_PRE));
+        PHX_TRY(one(k_l0<R, L0_RES, 1>, L0_RES));
+        PHX_TRY(one(k_l0<R, L0_BLACK, 1>, L0_BLACK));
+        PHX_TRY(one(k_l0<R, L0_RED, 1>, L0_RED));
+        PHX_TRY(one(k_l0<R, L0_RED, L0_RED_WIDE>, L0_MODES));
+        // several blocks per thread only where the batch's wide tiles still fill
+        // every CTA slot of the GPU twice
+        l0RedWide = dom[D_L0R].total >= 2 * l0grid[L0_MODES];
         useL0 = true;
         return PHX_OK;
     }
 
-    // a level-0 pass of the mixed path over the active level-0 tiles
+    // a level-0 pass over the active level-0 tiles
     template <int MODE>
     void launchL0(const char* name, int phase) {
-        if constexpr (kMixed) {
-            constexpr int d = l0Bpt(MODE) > 1 ? D_L0R : D_L0;
+        if constexpr (MODE == L0_RED) {
+            if (l0RedWide) {
+                launchL0k<MODE, L0_RED_WIDE>(name, phase, D_L0R, l0grid[L0_MODES]);
+                return;
+            }
+        }
+        launchL0k<MODE, 1>(name, phase, D_L0, l0grid[MODE]);
+    }
+    template <int MODE, int BPT>
+    void launchL0k(const char* name, int phase, int d, int gridCap) {
+        {
             if (dom[d].total <= 0) return;
-            const int grid = std::min(dom[d].total, l0grid[MODE]);
-            const Scn<float>* S = reinterpret_cast<const Scn<float>*>(dS);
-            float* const* D = reinterpret_cast<float* const*>(dD);
+            const int grid = std::min(dom[d].total, gridCap);
+            const Scn<R>* S = dS;
+            R* const* D = (R* const*)dD;
             if (prof) {
                 if (evNext + 2 > (int)evPool.size()) {
                     for (int i = 0; i < 64; ++i) { cudaEvent_t e; cudaEventCreate(&e); evPool.push_back(e); }
                 }
                 cudaEventRecord(evPool[evNext], st);
-                k_l0<MODE><<<grid, L0_THREADS, 0, st>>>(S, adom[0][d], D, phase);
+                k_l0<R, MODE, BPT><<<grid, L0_THREADS, 0, st>>>(S, adom[0][d], D, phase);
                 cudaEventRecord(evPool[evNext + 1], st);
                 evUse.push_back({name, evNext});
                 evNext += 2;
             } else {
-                k_l0<MODE><<<grid, L0_THREADS, 0, st>>>(S, adom[0][d], D, phase);
+                k_l0<R, MODE, BPT><<<grid, L0_THREADS, 0, st>>>(S, adom[0][d], D, phase);
             }
             ++launches;
         }
@@ -1519,23 +1536,35 @@ public:
     // one CG iteration (src/sim/gasphase.cpp:605-625). The mixed path can
     // replace the recursive residual by the FP64 one before preconditioning,
     // so its first red half sweep runs after that.
-    void cgIteration() {
+    // The CG iteration in three parts: q = A d and the update; the mixed path's
+    // residual replacement (in the step graph, a conditional node that runs it
+    // only on iterations where some scenario replaces); the preconditioner.
+    void cgIterUpdate(cudaGraphConditionalHandle repl, int setCond) {
         const Scn<R>* S = dS;
-        if (useL0 && splitApply) {
-            launchA("k_l0_dupdate", D_QUAD, TPB, k_l0_dupdate<0>, reinterpret_cast<const Scn<float>*>(S), adom[0][D_QUAD],
-                    reinterpret_cast<float* const*>(dD));
-            launchL0<L0_APPLYD>("k_cg_apply", 1);
-        } else if (useL0) launchL0<L0_APPLY>("k_cg_apply", 1);
-        else launchRB("k_cg_apply", cfgApply, k_cg_apply_rb<R>, S, adom[0][D_RB], (R* const*)dD, cfgApply.shape);
-        launchA("k_cg_update", D_QUAD, TPB, k_cg_update<R>, S, adom[0][D_QUAD], (R* const*)dD);
-        if (kMixed) {
-            if (anyClosed) launchA("k_mx_zone_center", D_CZ, TPB, k_mx_zone_center<R>, S, adom[0][D_CZ], 0);
-            launchA("k_mx_update", D_CELLS, TPB, k_mx_update<R>, S, adom[1][D_CELLS], 1);
-            launchA("k_mx_res64", D_CELLS, TPB, k_mx_res64<R>, S, adom[1][D_CELLS], 1);
-            launchA("k_mx_zone_proj", D_CZ, TPB, k_mx_zone_proj<R>, S, adom[1][D_CZ], 1);
-        }
+        if (useL0) {
+            launchA("k_l0_dupdate", D_QUAD, TPB, k_l0_dupdate<R>, S, adom[0][D_QUAD], (R* const*)dD);
+            launchL0<L0_APPLY>("k_cg_apply", 1);
+        } else launchRB("k_cg_apply", cfgApply, k_cg_apply_rb<R>, S, adom[0][D_RB], (R* const*)dD, cfgApply.shape);
+        launchA("k_cg_update", D_QUAD, TPB, k_cg_update<R>, S, adom[0][D_QUAD], (R* const*)dD, repl,
+                (const int*)adom[1][D_CELLS].total, dLoop + 1, setCond);
+        if (kMixed && anyClosed) launchA("k_mx_zone_center", D_CZ, TPB, k_mx_zone_center<R>, S, adom[0][D_CZ], 0);
+    }
+    void cgIterReplace() {
+        const Scn<R>* S = dS;
+        launchA("k_mx_update", D_CELLS, TPB, k_mx_update<R>, S, adom[1][D_CELLS], 1);
+        launchA("k_mx_res64", D_CELLS, TPB, k_mx_res64<R>, S, adom[1][D_CELLS], 1);
+        launchA("k_mx_zone_proj", D_CZ, TPB, k_mx_zone_proj<R>, S, adom[1][D_CZ], 1);
+    }
+    void cgIterPrecondition() {
+        const Scn<R>* S = dS;
         vcycle(1);
         if (kMixed && anyClosed) launchA("k_mx_zone_center", D_CZ, TPB, k_mx_zone_center<R>, S, adom[0][D_CZ], 1);
+    }
+    // one CG iteration (src/sim/gasphase.cpp:605-625), launched kernel by kernel
+    void cgIteration() {
+        cgIterUpdate(cudaGraphConditionalHandle{}, 0);
+        if (kMixed) cgIterReplace();
+        cgIterPrecondition();
     }
     // zone mean removal and velocity correction (:629-676)
     void projectEpilogue() {
@@ -1610,7 +1639,7 @@ public:
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     cudaGraphConditionalHandle cgHandle{};
-    int outerKernels = 0, bodyKernels = 0;
+    int outerKernels = 0, bodyKernels = 0, replKernels = 0;
     // the step runs as one CUDA graph; PHX_NO_GRAPH=1 launches the same kernels
     // one by one (kernels inside conditional graphs cannot be profiled by ncu)
     bool useGraph = std::getenv("PHX_NO_GRAPH") == nullptr;
@@ -1622,9 +1651,10 @@ public:
         graph = nullptr;
     }
 
-    // add a while node after the current capture position of st (which captures
-    // into graph g); capture continues after it
-    int addWhile(cudaGraph_t g, cudaGraphConditionalHandle handle, cudaGraph_t* body) {
+    // add a conditional node (while or if) after the current capture position of
+    // st (which captures into graph g); capture continues after it
+    int addConditional(cudaGraph_t g, cudaGraphConditionalHandle handle, cudaGraphConditionalNodeType type,
+                       cudaGraph_t* body) {
         cudaStreamCaptureStatus cs;
         const cudaGraphNode_t* deps = nullptr;
         size_t ndeps = 0;
@@ -1632,7 +1662,7 @@ public:
         cudaGraphNodeParams cp = {};
         cp.type = cudaGraphNodeTypeConditional;
         cp.conditional.handle = handle;
-        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.type = type;
         cp.conditional.size = 1;
         cudaGraphNode_t cond;
         PHX_CK(cudaGraphAddNode(&cond, g, deps, nullptr, ndeps, &cp));
@@ -1660,12 +1690,12 @@ public:
         stLeakage();
         if (kMixed) mixedPrelude();
         else projectPrelude();
-        cudaMemsetAsync(dLoop, 0, sizeof(int), st);
+        cudaMemsetAsync(dLoop, 0, 2 * sizeof(int), st);
         const int capIt = maxItersAll() + 2;
         k_cg_cond<R><<<1, 256, 0, st>>>(dS, n, cgHandle, dLoop, capIt, activeTables(), 1);
         ++launches;
         cudaGraph_t body = nullptr;
-        PHX_TRY(addWhile(graph, cgHandle, &body));
+        PHX_TRY(addConditional(graph, cgHandle, cudaGraphCondTypeWhile, &body));
         if (kMixed) mixedEpilogue();
         projectEpilogue();
         stAdvect();
@@ -1673,13 +1703,28 @@ public:
         cudaGraph_t outGraph = nullptr;
         PHX_CK(cudaStreamEndCapture(st, &outGraph));
         outerKernels = launches;
+        // the loop body; the mixed path's residual replacement is a conditional
+        // node of it, set by k_cg_update on each iteration
+        cudaGraphConditionalHandle replHandle{};
+        cudaGraph_t replBody = nullptr;
+        if (kMixed) PHX_CK(cudaGraphConditionalHandleCreate(&replHandle, body, 0, 0));
         PHX_CK(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
         launches = 0;
-        cgIteration();
+        cgIterUpdate(replHandle, kMixed ? 1 : 0);
+        if (kMixed) PHX_TRY(addConditional(body, replHandle, cudaGraphCondTypeIf, &replBody));
+        cgIterPrecondition();
         k_cg_cond<R><<<1, 256, 0, st>>>(dS, n, cgHandle, dLoop, capIt, activeTables(), 1);
         ++launches;
         PHX_CK(cudaStreamEndCapture(st, &body));
         bodyKernels = launches;
+        replKernels = 0;
+        if (kMixed) {
+            PHX_CK(cudaStreamBeginCaptureToGraph(st, replBody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+            launches = 0;
+            cgIterReplace();
+            PHX_CK(cudaStreamEndCapture(st, &replBody));
+            replKernels = launches;
+        }
         for (int s = 0; s < n; ++s) sc[s]->h = saved[s];
         PHX_CK(cudaGraphInstantiate(&gexec, graph, 0));
         return checkLaunch();
@@ -1695,10 +1740,10 @@ public:
 
     // kernels the last graph step ran: the outer nodes plus the loop body per iteration
     int graphLaunchCount(int* out) {
-        int lc = 0;
-        PHX_CK(cudaMemcpyAsync(&lc, dLoop, sizeof(int), cudaMemcpyDeviceToHost, st));
+        int lc[2] = {0, 0};
+        PHX_CK(cudaMemcpyAsync(lc, dLoop, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
         PHX_CK(cudaStreamSynchronize(st));
-        *out = outerKernels + bodyKernels * std::max(0, lc - 1);
+        *out = outerKernels + bodyKernels * std::max(0, lc[0] - 1) + replKernels * lc[1];
         return PHX_OK;
     }
 
@@ -1938,6 +1983,13 @@ public:
         const Multigrid& M = sc[s]->MG;
         if (levels) *levels = (int)M.lv.size();
         for (int l = 0; rows && l < cap && l < (int)M.lv.size(); ++l) rows[l] = M.lv[l].n;
+        return PHX_OK;
+    }
+    int mgNnz(int s, int* nnz, int cap) override {
+        PHX_TRY(checkScn(s));
+        const Multigrid& M = sc[s]->MG;
+        for (int l = 0; nnz && l < cap && l < (int)M.lv.size(); ++l)
+            nnz[l] = M.lv[l].rowStart.empty() ? 0 : M.lv[l].rowStart.back();
         return PHX_OK;
     }
     int lastLaunches() const override {

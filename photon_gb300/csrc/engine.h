@@ -43,6 +43,8 @@ public:
     // multigrid hierarchy of scenario s: the number of levels, and the unknowns
     // of levels 0..min(levels, cap)-1 into rows
     virtual int mgInfo(int s, int* levels, int* rows, int cap) = 0;
+    // stored off-diagonal entries of each level's CSR rows (0 for level 0)
+    virtual int mgNnz(int s, int* nnz, int cap) = 0;
     // two-phase admission for the serving loop: host set-up of a scenario
     // (validation, zones, multigrid; no device work) with its device bytes,
     // then its allocation and upload into the batch. prepare() may run on

@@ -1,6 +1,7 @@
-// Level-0 pressure kernels of the mixed path: the 7-point structured grid of
-// the multigrid V-cycle and of q = A d, with the matrix coefficients coded in
-// one byte per cell.
+// Level-0 pressure kernels: the 7-point structured grid of the multigrid
+// V-cycle and of q = A d, with the matrix coefficients coded in one byte per
+// cell. Both precisions run them (R = double: the FP64 path; R = float: the
+// mixed path).
 //
 // Coefficient codes. On the grids Photon discretizes, the level-0 matrix
 // coefficients (a0x, a0y, a0z: open fractions of a cell's six faces) are 0 or
@@ -13,9 +14,9 @@
 // that count gets bit 6 ("general") and its coefficients are read from the
 // arrays as before. The host builds and checks every code. Multiplying by a
 // coefficient of 1 is exact and adding a zero term changes nothing, so a
-// coded cell computes what the array form computes, in the same order. A pass
-// then streams 1 byte per cell of matrix data instead of 16 (four FP32
-// arrays).
+// coded cell computes what the array form computes, in the same order (the
+// FP64 path's sums keep the reference's order and rounding). A pass then
+// streams 1 byte per cell of matrix data instead of four coefficient arrays.
 //
 // Blocks of 2x2x2 cells. A thread owns one 2x2x2 block (the blocks level 1
 // aggregates) and computes its eight cells: it loads the block's values once,
@@ -28,6 +29,8 @@
 // (i + j + k even) are cells 0, 3, 5 and 6 of every block (cell u = di + 2 dj
 // + 4 dk), so a sweep loads only the neighbours of the colour it reads.
 #pragma once
+#include <type_traits>
+
 #include "rowblock.cuh"
 
 namespace phx {
@@ -39,11 +42,15 @@ constexpr unsigned char CODE_BOUNDARY = 128;
 
 constexpr int L0_THREADS = 128;
 
-enum { L0_APPLY = 0, L0_PRE, L0_RES, L0_BLACK, L0_RED, L0_APPLYD };
+// passes of k_l0; q = A d reads the d that k_l0_dupdate formed
+enum { L0_APPLY = 0, L0_PRE, L0_RES, L0_BLACK, L0_RED, L0_MODES };
 
-// 2x2x2 blocks per thread: one for the sweeps and the residual; several for
-// the passes with a dot product, whose per-tile reduction they amortise
-__host__ __device__ constexpr int l0Bpt(int mode) { return mode == L0_RED ? 4 : 1; }
+// 2x2x2 blocks per thread: one for the sweeps, the residual and q = A d;
+// four for the red sweep of a batch that fills the GPU several times over,
+// whose per-tile r.z reduction they amortise (a small grid keeps one, so
+// that its few tiles spread over more CTAs)
+constexpr int L0_RED_WIDE = 4;
+__host__ __device__ constexpr int l0Bpt(int mode) { return mode == L0_RED ? L0_RED_WIDE : 1; }
 
 // tiles of a scenario: L0_THREADS x bpt 2x2x2 blocks each
 __host__ __device__ inline int l0Tiles(int nx, int ny, int nz, int bpt) {
@@ -53,18 +60,21 @@ __host__ __device__ inline int l0Tiles(int nx, int ny, int nz, int bpt) {
 }
 
 // diagonal of a coded cell
-__device__ __forceinline__ float codeDiag(unsigned cd) { return (float)(__popc(cd & 63u) + (cd >> 7)); }
+template <class T>
+__device__ __forceinline__ T codeDiag(unsigned cd) { return (T)(__popc(cd & 63u) + (cd >> 7)); }
 
 // the general-cell form of the stencil: coefficients and diagonal from the arrays
+template <class R>
 struct L0Coef {
-    float dg, xm, xp, ym, yp, zm, zp;
+    R dg, xm, xp, ym, yp, zm, zp;
 };
-__device__ __forceinline__ L0Coef l0General(const Scn<float>& g, int i, int j, int k) {
+template <class R>
+__device__ __forceinline__ L0Coef<R> l0General(const Scn<R>& g, int i, int j, int k) {
     const int nx = g.nx, ny = g.ny;
     const long long c = (long long)k * nx * ny + (long long)j * nx + i;
     const long long fx = i + (long long)(nx + 1) * (j + (long long)ny * k);
     const long long fy = i + (long long)nx * (j + (long long)(ny + 1) * k);
-    L0Coef o;
+    L0Coef<R> o;
     o.dg = g.diag[c];
     o.xm = g.a0x[fx];
     o.xp = g.a0x[fx + 1];
@@ -76,17 +86,18 @@ __device__ __forceinline__ L0Coef l0General(const Scn<float>& g, int i, int j, i
 }
 
 // neighbour values of one cell in the reference's term order
+template <class R>
 struct L0Nb {
-    float xm, xp, ym, yp, zm, zp;
+    R xm, xp, ym, yp, zm, zp;
 };
 
 // sacc plus (SIGN > 0) or minus (SIGN < 0) the neighbour terms in the order
 // x-, x+, y-, y+, z-, z+: for a coded cell every set bit adds its neighbour
 // (coefficient 1); a general cell multiplies by the arrays' coefficients its
 // interior neighbours
-template <int SIGN>
-__device__ __forceinline__ float l0Sum(float sacc, unsigned cd, const L0Coef& a, const L0Nb& n, int i, int j, int k,
-                                       int nx, int ny, int nz) {
+template <int SIGN, class R>
+__device__ __forceinline__ R l0Sum(R sacc, unsigned cd, const L0Coef<R>& a, const L0Nb<R>& n, int i, int j, int k,
+                                   int nx, int ny, int nz) {
     if (!(cd & CODE_GENERAL)) {
         if (cd & 1u) sacc = SIGN > 0 ? sacc + n.xm : sacc - n.xm;
         if (cd & 2u) sacc = SIGN > 0 ? sacc + n.xp : sacc - n.xp;
@@ -114,10 +125,15 @@ __device__ __forceinline__ float l0Sum(float sacc, unsigned cd, const L0Coef& a,
     return sacc;
 }
 
-// the level-0 smoother's output as stored: FP32, or rounded to FP16 when the
-// context studies FP16 storage of the smoother scratch (PHX_FP16_Z0)
-__device__ __forceinline__ float z0Store(const Scn<float>& g, float v) {
-    return g.fp16Z0 ? __half2float(__float2half_rn(v)) : v;
+// the level-0 smoother's output as stored: as computed, or (mixed path)
+// rounded to FP16 when the context studies FP16 storage of the smoother
+// scratch (PHX_FP16_Z0)
+template <class R>
+__device__ __forceinline__ R z0Store(const Scn<R>& g, R v) {
+    if constexpr (sizeof(R) == 4) {
+        if (g.fp16Z0) return __half2float(__float2half_rn(v));
+    }
+    return v;
 }
 
 // whether a cell reads its neighbour across face f (0..5): a set bit of a
@@ -126,9 +142,24 @@ __device__ __forceinline__ bool l0Reads(unsigned cd, int f, bool interior) {
     return (cd & CODE_GENERAL) ? interior : ((cd >> f) & 1u) != 0;
 }
 
-// One pass over the active tiles of a batch. MODE selects the pass:
-//   L0_APPLY  q = A d with d = z + beta d (src/sim/gasphase.cpp:551-570,
-//             620-622), d.q (:606-608); alpha in the last CTA of a scenario
+// CTAs per SM the compiler budgets registers for (FP32): the most that keep
+// each pass free of spills or nearly so -- eight for the pre-smoothing pair
+// and the black sweep (64 registers), six for q = A d and the red sweep (80),
+// five for the residual with its restriction (96). The FP64 passes keep the
+// compiler's own choice.
+template <class R, int MODE>
+struct L0MinCtas {
+    static constexpr int value = sizeof(R) == 8 ? 1
+                                 : (MODE == L0_PRE || MODE == L0_BLACK) ? 8
+                                 : (MODE == L0_APPLY || MODE == L0_RED) ? 6
+                                 : 5;
+};
+
+// One pass over the active tiles of a batch; a thread computes BPT 2x2x2
+// blocks. MODE selects the pass:
+//   L0_APPLY  q = A d (src/sim/gasphase.cpp:551-570) of the d that
+//             k_l0_dupdate formed, d.q (:606-608); alpha in the last CTA of a
+//             scenario
 //   L0_PRE    pre-smoothing pair from x = 0 (gsColor, pressure_mg.cpp:195-216):
 //             red = r / diag, black from its red neighbours; writes z
 //   L0_RES    residual (residualGrid, :217-235) restricted to level 1
@@ -138,9 +169,11 @@ __device__ __forceinline__ bool l0Reads(unsigned cd, int f, bool interior) {
 //             are z + x1[agg]; writes the black cells of z
 //   L0_RED    red sweep with r.z (dotRZ, gasphase.cpp:582-588); the last CTA
 //             of a scenario closes the CG iteration (phase 2: a bare V-cycle)
-template <int MODE>
-__global__ void __launch_bounds__(L0_THREADS, (MODE == L0_PRE || MODE == L0_BLACK) ? 8 : MODE == L0_RED ? 6 : 1) k_l0(const Scn<float>* __restrict__ S, ADom dom, float* const* dbuf,
-                                                   int phase) {
+template <class R, int MODE, int BPT>
+__global__ void __launch_bounds__(L0_THREADS, (L0MinCtas<R, MODE>::value)) k_l0(const Scn<R>* __restrict__ S, ADom dom,
+                                                                                 R* const* dbuf, int phase) {
+    using T = R;
+    using Acc = decltype(dotTerm(T(0), T(0)));
     __shared__ int sst_[MAX_BATCH + 1];
     __shared__ double shd[32];
     __shared__ int amLastS;
@@ -150,13 +183,11 @@ __global__ void __launch_bounds__(L0_THREADS, (MODE == L0_PRE || MODE == L0_BLAC
     for (int b = blockIdx.x; b < tot; b += gridDim.x) {
         int s, tile;
         locateShared(sst_, dom.nscn, b, s, tile);
-        const Scn<float>& g = S[s];
+        const Scn<R>& g = S[s];
         const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
         const int hx = g.dvL0[0].d, hxy = g.dvL0[1].d;
         const int nblk = hxy * ((nz + 1) >> 1);
-        constexpr int BPT = l0Bpt(MODE);
-        using Acc = F2;
-        Acc dot{0.f, 0.f};
+        Acc dot{};
 #pragma unroll 1
         for (int ub = 0; ub < BPT; ++ub) {
         const int q = (tile * BPT + ub) * L0_THREADS + (int)threadIdx.x;
@@ -167,32 +198,27 @@ __global__ void __launch_bounds__(L0_THREADS, (MODE == L0_PRE || MODE == L0_BLAC
         const int bx = rem - by * hx;
         const int i0 = 2 * bx, j0 = 2 * by, k0 = 2 * bz;
         const int it = (int)g.sv[SV_IT];
-        const float beta = (float)g.sv[SV_BETA];
-        const float* __restrict__ zf = g.z;
-        const float* __restrict__ rf = g.r;
+        const T* __restrict__ zf = g.z;
+        const T* __restrict__ rf = g.r;
         const unsigned char* __restrict__ cf = g.code0;
         const int* __restrict__ af = g.lv[0].agg;
-        const float* __restrict__ dprev = (MODE == L0_APPLY && it > 0) ? dbuf[2 * s + (it & 1)] : nullptr;
-        const float* __restrict__ dcur = MODE == L0_APPLYD ? dbuf[2 * s + ((it + 1) & 1)] : nullptr;
-        const float* __restrict__ xc = MODE == L0_BLACK ? g.lv[1].x : nullptr;
+        const T* __restrict__ dcur = MODE == L0_APPLY ? dbuf[2 * s + ((it + 1) & 1)] : nullptr;
+        const T* __restrict__ xc = MODE == L0_BLACK ? g.lv[1].x : nullptr;
         // the stencil value of cell c (red: i + j + k even)
-        auto value = [&](int c, bool red) -> float {
+        auto value = [&](int c, bool red) -> T {
             if constexpr (MODE == L0_APPLY) {
-                const float zv = zf[c];
-                return dprev ? zv + beta * dprev[c] : zv;
-            } else if constexpr (MODE == L0_APPLYD) {
                 return dcur[c];                                       // d, formed by k_l0_dupdate
             } else if constexpr (MODE == L0_PRE) {
-                const float rv = rf[c];
+                const T rv = rf[c];
                 if (!red) return rv;                                  // black: its right-hand side
                 const unsigned cd = cf[c];
-                const float dg = (cd & CODE_GENERAL) ? g.diag[c] : codeDiag(cd);
-                return dg <= 0.f ? 0.f : gsDiv(rv, dg);               // red: after the first half sweep
+                const T dg = (cd & CODE_GENERAL) ? g.diag[c] : codeDiag<T>(cd);
+                return dg <= T(0) ? T(0) : gsDiv(rv, dg);             // red: after the first half sweep
             } else if constexpr (MODE == L0_BLACK) {
                 if (!red) return rf[c];
                 const int a = af[c];
-                const float zv = zf[c];
-                return a >= 0 ? (float)(zv + xc[a]) : zv;             // red: z plus the prolongated correction
+                const T zv = zf[c];
+                return a >= 0 ? (T)(zv + xc[a]) : zv;                 // red: z plus the prolongated correction
             } else if constexpr (MODE == L0_RED) {
                 return red ? rf[c] : zf[c];                           // black: its new z
             } else {
@@ -206,7 +232,7 @@ __global__ void __launch_bounds__(L0_THREADS, (MODE == L0_PRE || MODE == L0_BLAC
         bool on[8];
         int cc[8];
         unsigned cd[8];
-        float X[8], R[8], NB[8][3];
+        T X[8], Rv[8], NB[8][3];
         int A[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
@@ -215,14 +241,14 @@ __global__ void __launch_bounds__(L0_THREADS, (MODE == L0_PRE || MODE == L0_BLAC
             cc[u] = (i0 + di) + nx * (j0 + dj) + sxy * (k0 + dk);
             const bool red = ((di + dj + dk) & 1) == 0;
             cd[u] = 0;
-            X[u] = 0.f;
-            R[u] = 0.f;
+            X[u] = T(0);
+            Rv[u] = T(0);
             A[u] = -1;
             if (!on[u]) continue;
             cd[u] = cf[cc[u]];
             X[u] = value(cc[u], red);
-            if constexpr (MODE == L0_RED) { if (!red) R[u] = rf[cc[u]]; }
-            if constexpr (MODE == L0_RES) { R[u] = rf[cc[u]]; A[u] = af[cc[u]]; }
+            if constexpr (MODE == L0_RED) { if (!red) Rv[u] = rf[cc[u]]; }
+            if constexpr (MODE == L0_RES) { Rv[u] = rf[cc[u]]; A[u] = af[cc[u]]; }
         }
         // each cell's neighbour outside the block along each axis, where the cell
         // reads it (the sweeps read only the other colour's neighbours of the
@@ -230,11 +256,11 @@ __global__ void __launch_bounds__(L0_THREADS, (MODE == L0_PRE || MODE == L0_BLAC
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
             const bool red = (((u & 1) + ((u >> 1) & 1) + (u >> 2)) & 1) == 0;
-            const bool reads = MODE == L0_APPLY || MODE == L0_APPLYD || MODE == L0_RES ||
+            const bool reads = MODE == L0_APPLY || MODE == L0_RES ||
                                (MODE == L0_RED ? red : !red);   // the colour this pass updates
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                NB[u][a] = 0.f;
+                NB[u][a] = T(0);
                 const int bit = (u >> a) & 1;                    // 0: the outside neighbour is below, 1: above
                 const int f = 2 * a + bit;
                 const bool interior = bit ? org[a] + 2 < dimv[a] : org[a] > 0;
@@ -242,62 +268,61 @@ __global__ void __launch_bounds__(L0_THREADS, (MODE == L0_PRE || MODE == L0_BLAC
                     NB[u][a] = value(bit ? cc[u] + st[a] : cc[u] - st[a], !red);
             }
         }
-        float resv[8];
+        T resv[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
-            resv[u] = 0.f;
+            resv[u] = T(0);
             if (!on[u]) continue;
             const int di = u & 1, dj = (u >> 1) & 1, dk = u >> 2;
             const int i = i0 + di, j = j0 + dj, k = k0 + dk;
             const int c = cc[u];
             const bool red = ((di + dj + dk) & 1) == 0;
             const unsigned code = cd[u];
-            L0Coef gen{};
+            L0Coef<T> gen{};
             if (code & CODE_GENERAL) gen = l0General(g, i, j, k);
-            const float dg = (code & CODE_GENERAL) ? gen.dg : codeDiag(code);
-            L0Nb n;
+            const T dg = (code & CODE_GENERAL) ? gen.dg : codeDiag<T>(code);
+            L0Nb<T> n;
             n.xm = di ? X[u - 1] : NB[u][0];
             n.xp = di ? NB[u][0] : X[u + 1];
             n.ym = dj ? X[u - 2] : NB[u][1];
             n.yp = dj ? NB[u][1] : X[u + 2];
             n.zm = dk ? X[u - 4] : NB[u][2];
             n.zp = dk ? NB[u][2] : X[u + 4];
-            if constexpr (MODE == L0_APPLY || MODE == L0_APPLYD) {
-                if constexpr (MODE == L0_APPLY) dbuf[2 * s + ((it + 1) & 1)][c] = X[u];
-                if (dg <= 0.f) { g.q[c] = 0.f; continue; }
-                const float sacc = l0Sum<-1>(dg * X[u], code, gen, n, i, j, k, nx, ny, nz);
+            if constexpr (MODE == L0_APPLY) {
+                if (dg <= T(0)) { g.q[c] = T(0); continue; }
+                const T sacc = l0Sum<-1>(dg * X[u], code, gen, n, i, j, k, nx, ny, nz);
                 g.q[c] = sacc;
                 dot = accAdd(dot, dotTerm(sacc, X[u]));
             } else if constexpr (MODE == L0_PRE) {
                 if (red) { g.z[c] = z0Store(g, X[u]); continue; }
-                float zc = 0.f;
-                if (dg > 0.f) zc = z0Store(g, gsDiv(l0Sum<1>(X[u], code, gen, n, i, j, k, nx, ny, nz), dg));
+                T zc = T(0);
+                if (dg > T(0)) zc = z0Store(g, gsDiv(l0Sum<1>(X[u], code, gen, n, i, j, k, nx, ny, nz), dg));
                 g.z[c] = zc;
             } else if constexpr (MODE == L0_BLACK) {
                 if (red) continue;
-                float zc = 0.f;
-                if (dg > 0.f) zc = z0Store(g, gsDiv(l0Sum<1>(X[u], code, gen, n, i, j, k, nx, ny, nz), dg));
+                T zc = T(0);
+                if (dg > T(0)) zc = z0Store(g, gsDiv(l0Sum<1>(X[u], code, gen, n, i, j, k, nx, ny, nz), dg));
                 g.z[c] = zc;
             } else if constexpr (MODE == L0_RED) {
                 if (red) {
-                    float zc = 0.f;
-                    if (dg > 0.f) zc = z0Store(g, gsDiv(l0Sum<1>(X[u], code, gen, n, i, j, k, nx, ny, nz), dg));
+                    T zc = T(0);
+                    if (dg > T(0)) zc = z0Store(g, gsDiv(l0Sum<1>(X[u], code, gen, n, i, j, k, nx, ny, nz), dg));
                     g.z[c] = zc;
                     dot = accAdd(dot, dotTerm(X[u], zc));
                 } else {
-                    dot = accAdd(dot, dotTerm(R[u], X[u]));
+                    dot = accAdd(dot, dotTerm(Rv[u], X[u]));
                 }
             } else {   // L0_RES
-                if (A[u] >= 0) resv[u] = l0Sum<1>(R[u] - dg * X[u], code, gen, n, i, j, k, nx, ny, nz);
+                if (A[u] >= 0) resv[u] = l0Sum<1>(Rv[u] - dg * X[u], code, gen, n, i, j, k, nx, ny, nz);
             }
         }
         if constexpr (MODE == L0_RES) {
             // each level-1 aggregate lies in one 2x2x2 block: its cells are summed in
             // ascending cell order (i, then j, then k), the order of the reference's scatter
             if (live) {
-                float* const cb = g.lv[1].b;
-                float* const y1 = g.nLevels > 2 ? g.lv[1].y : nullptr;
-                const float* const d1 = g.lv[1].diag;
+                T* const cb = g.lv[1].b;
+                T* const y1 = g.nLevels > 2 ? g.lv[1].y : nullptr;
+                const T* const d1 = g.lv[1].diag;
 #pragma unroll
                 for (int m = 0; m < 8; ++m) {
                     const int a = on[m] ? A[m] : -1;
@@ -305,7 +330,7 @@ __global__ void __launch_bounds__(L0_THREADS, (MODE == L0_PRE || MODE == L0_BLAC
 #pragma unroll
                     for (int p = 0; p < m; ++p) first = first && !(on[p] && A[p] == a);
                     if (!first) continue;
-                    float acc = 0.f;
+                    T acc = T(0);
 #pragma unroll
                     for (int p = m; p < 8; ++p)
                         if (on[p] && A[p] == a) acc = acc + resv[p];
@@ -313,15 +338,15 @@ __global__ void __launch_bounds__(L0_THREADS, (MODE == L0_PRE || MODE == L0_BLAC
                     // level 1's first damped Jacobi sweep from x = 0 (jacobi,
                     // pressure_mg.cpp:237-247), unless level 1 is the coarsest
                     if (y1) {
-                        const float dc = d1[a];
-                        const float om = (float)OMEGA;
-                        y1[a] = dc <= 0.f ? 0.f : scratchRound(g, (1.f - om) * 0.f + om * acc / dc);
+                        const T dc = d1[a];
+                        const T om = T(OMEGA);
+                        y1[a] = dc <= T(0) ? T(0) : scratchRound(g, (T(1) - om) * T(0) + om * acc / dc);
                     }
                 }
             }
         }
         }   // blocks of the thread
-        if constexpr (MODE == L0_APPLY || MODE == L0_APPLYD || MODE == L0_RED) {
+        if constexpr (MODE == L0_APPLY || MODE == L0_RED) {
             if (MODE == L0_RED && phase == 2) continue;
             const int nt = sst_[s + 1] - sst_[s];
             // fixed-order CTA sum, then the last CTA of the scenario sums the CTA partials
@@ -343,7 +368,7 @@ __global__ void __launch_bounds__(L0_THREADS, (MODE == L0_PRE || MODE == L0_BLAC
                 const double total = blockSum(acc, shd);
                 if (threadIdx.x == 0) {
                     *cnt = 0;
-                    if constexpr (MODE != L0_RED) {
+                    if constexpr (MODE == L0_APPLY) {
                         g.sv[SV_DQ] = total;
                         if (total <= 0) g.sv[SV_DONE] = 1;
                         else g.sv[SV_ALPHA] = g.sv[SV_RZ] / total;
@@ -357,9 +382,11 @@ __global__ void __launch_bounds__(L0_THREADS, (MODE == L0_PRE || MODE == L0_BLAC
 }
 
 // d = z + beta d (src/sim/gasphase.cpp:620-622; d = z on the first iteration)
-// ahead of q = A d (L0_APPLYD), four cells per thread, over the active scenarios
-template <int UNUSED = 0>
-__global__ void __launch_bounds__(256) k_l0_dupdate(const Scn<float>* __restrict__ S, ADom dom, float* const* dbuf) {
+// ahead of q = A d, four cells per thread over the tiles of k_cg_update (1024
+// cells: every tile starts on a 16-byte boundary of a float array and a
+// 32-byte boundary of a double array)
+template <class R>
+__global__ void __launch_bounds__(256) k_l0_dupdate(const Scn<R>* __restrict__ S, ADom dom, R* const* dbuf) {
     __shared__ int sst_[MAX_BATCH + 1];
     for (int i = threadIdx.x; i <= dom.nscn; i += blockDim.x) sst_[i] = dom.start[i];
     __syncthreads();
@@ -367,23 +394,35 @@ __global__ void __launch_bounds__(256) k_l0_dupdate(const Scn<float>* __restrict
     for (int b = blockIdx.x; b < tot; b += gridDim.x) {
         int s, tile;
         locateShared(sst_, dom.nscn, b, s, tile);
-        const Scn<float>& g = S[s];
+        const Scn<R>& g = S[s];
         const int it = (int)g.sv[SV_IT];
-        const float beta = (float)g.sv[SV_BETA];
-        const float* __restrict__ dp = it > 0 ? dbuf[2 * s + (it & 1)] : nullptr;
-        float* __restrict__ dn = dbuf[2 * s + ((it + 1) & 1)];
-        const float* __restrict__ z = g.z;
+        const R beta = (R)g.sv[SV_BETA];
+        const R* __restrict__ dp = it > 0 ? dbuf[2 * s + (it & 1)] : nullptr;
+        R* __restrict__ dn = dbuf[2 * s + ((it + 1) & 1)];
+        const R* __restrict__ z = g.z;
         const int c0 = (tile * 256 + (int)threadIdx.x) * 4;
-        if (c0 + 4 <= g.N) {   // a tile is 1024 cells: quads start on 16-byte boundaries
-            float4 zv = *reinterpret_cast<const float4*>(z + c0);
-            if (dp) {
-                const float4 pv = *reinterpret_cast<const float4*>(dp + c0);
-                zv.x = zv.x + beta * pv.x; zv.y = zv.y + beta * pv.y;
-                zv.z = zv.z + beta * pv.z; zv.w = zv.w + beta * pv.w;
+        if (c0 + 4 <= g.N) {
+            // d = z where there is no previous d; one 16-byte access per array and
+            // thread (float), two (double)
+            constexpr int NV = sizeof(R) == 4 ? 1 : 2;
+            using V = typename std::conditional<sizeof(R) == 4, float4, double2>::type;
+            constexpr int W = 4 / NV;   // cells per vector
+#pragma unroll
+            for (int h = 0; h < NV; ++h) {
+                V zv = *reinterpret_cast<const V*>(z + c0 + W * h);
+                if (dp) {
+                    const V pv = *reinterpret_cast<const V*>(dp + c0 + W * h);
+                    zv.x = zv.x + beta * pv.x;
+                    zv.y = zv.y + beta * pv.y;
+                    if constexpr (W == 4) {
+                        zv.z = zv.z + beta * pv.z;
+                        zv.w = zv.w + beta * pv.w;
+                    }
+                }
+                *reinterpret_cast<V*>(dn + c0 + W * h) = zv;
             }
-            *reinterpret_cast<float4*>(dn + c0) = zv;
         } else {
-            for (int c = c0; c < g.N; ++c) dn[c] = dp ? z[c] + beta * dp[c] : z[c];
+            for (int c = c0; c < g.N; ++c) dn[c] = dp ? (R)(z[c] + beta * dp[c]) : z[c];
         }
     }
 }

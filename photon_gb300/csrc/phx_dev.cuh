@@ -151,6 +151,7 @@ struct Scn {
     int nsrc;
     Src src[MAX_SRC];
     // geometry
+    R rdx, rdx2;                 // 1 / dx and 1 / (dx dx), each one division in R
     const uint8_t* blocked;
     const R *fx, *fy, *fz;       // face open fractions
     const R *ax, *ay, *az;       // pressure-matrix coefficients (ax_, ay_, az_)

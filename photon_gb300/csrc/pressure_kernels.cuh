@@ -56,9 +56,11 @@ __device__ __forceinline__ R scratchRound(const Scn<R>& g, R v) {
 // ---- coarse levels ------------------------------------------------------------------
 // Each coarse-level pass is a per-tile device function run by a persistent
 // kernel over the active tiles; a tile function returns early where the tile
-// ends. (Running all coarse passes as phases of one cooperative kernel with
-// grid barriers was measured slower on the 64-scenario batch: the barriers
-// cost more than the launches they save inside the step graph.)
+// ends. (Two ways of saving the passes' launches were measured slower: all
+// coarse passes as phases of one cooperative kernel with grid barriers, and a
+// scenario's small levels on one thread-block cluster per scenario with
+// cluster barriers between the passes. A launch over the whole GPU hides the
+// dependent loads of a pass's rows better than either.)
 
 // damped Jacobi sweep on a coarse level (jacobi, pressure_mg.cpp:237-247).
 // mode 0: from x = 0, into y; mode 1: y -> x; mode 2: x plus the coarser
@@ -294,9 +296,20 @@ __device__ __forceinline__ void cgUpdateCell(R* p, R* r, const R* d, const R* q,
     rm = mx(rm, (R)fabs(rv));
 }
 
+// In the step graph (setCond != 0) the kernel also sets the condition of the
+// loop body's conditional node that runs the mixed path's residual
+// replacement: on while any scenario replaces its residual this iteration
+// (its active-tile total replTotal, built at the end of the previous
+// iteration, is not zero), counting the runs in *replRuns.
 template <class R>
-__global__ void k_cg_update(const Scn<R>* __restrict__ S, ADom dom, R* const* dbuf) {
+__global__ void k_cg_update(const Scn<R>* __restrict__ S, ADom dom, R* const* dbuf, cudaGraphConditionalHandle repl,
+                            const int* replTotal, int* replRuns, int setCond) {
     using T = R;
+    if (setCond && blockIdx.x == 0 && threadIdx.x == 0) {
+        const bool run = *replTotal > 0;
+        if (run) ++*replRuns;
+        cudaGraphSetConditional(repl, run ? 1u : 0u);
+    }
     PHX_TILES_BEGIN(dom)
     const int c0 = (tile_ * TPB + threadIdx.x) * CG_QUAD;
     T rm = 0;

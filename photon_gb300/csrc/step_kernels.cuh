@@ -293,15 +293,24 @@ __global__ void k_turb_filter(const Scn<R>* __restrict__ S, Dom dom) {
     ijkOf(g, 0, c, i, j, k);
     const int id = AXIS == 0 ? i : AXIS == 1 ? j : k, n = AXIS == 0 ? nx : AXIS == 1 ? ny : nz;
     const int st = AXIS == 0 ? 1 : AXIS == 1 ? nx : nx * ny;
-    const bool hasLo = id > 0 && !g.blocked[c - st], hasHi = id < n - 1 && !g.blocked[c + st];
+    // neighbours at clamped indices, loaded together with their solid flags and
+    // used through selects
+    const int cLo = id > 0 ? c - st : c, cHi = id < n - 1 ? c + st : c;
+    const bool hasLo = id > 0 && !g.blocked[cLo], hasHi = id < n - 1 && !g.blocked[cHi];
+    T self[3], lov[3], hiv[3];
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
         const R* in = AXIS == 0 ? g.tmp[q] : AXIS == 1 ? g.tmp[3 + q] : g.tmp[6 + q];
+        self[q] = in[c];
+        lov[q] = in[cLo];
+        hiv[q] = in[cHi];
+    }
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
         R* out = AXIS == 1 ? g.tmp[6 + q] : g.tmp[3 + q];
-        T self = in[c];
-        T lo = hasLo ? in[c - st] : self;
-        T hi = hasHi ? in[c + st] : self;
-        out[c] = T(0.25) * lo + T(0.5) * self + T(0.25) * hi;
+        const T lo = hasLo ? lov[q] : self[q];
+        const T hi = hasHi ? hiv[q] : self[q];
+        out[c] = T(0.25) * lo + T(0.5) * self[q] + T(0.25) * hi;
     }
 }
 
@@ -486,42 +495,37 @@ __global__ void k_momentum(const Scn<R>* __restrict__ S, Dom dom) {
         }
         adv[a] = T(0.25) * s;
     }
-    const T dx = (T)g.dx;
-    const T idx = T(1) / dx, idx2 = T(1) / (dx * dx);
+    const T idx = g.rdx, idx2 = g.rdx2;   // 1 / dx and 1 / (dx dx) in R, from the host
     T acc = 0, lap = 0;
+#pragma unroll
     for (int a = 0; a < 3; ++a) {
-        T m1, p1, m2, p2;
         // free slip across closed faces: neighbour along a, then the second
-        // neighbour only through two open faces
-        {
-            int ni = id[a] - 1, gg = f - st[a];
-            m1 = (ni < 0) ? v0 : (fo[gg] > T(0) && !(lk && lk[gg]) ? vel[gg] : v0);
-            ni = id[a] + 1;
-            gg = f + st[a];
-            p1 = (ni >= dim[a]) ? v0 : (fo[gg] > T(0) && !(lk && lk[gg]) ? vel[gg] : v0);
+        // neighbour only through two open faces. Every load is issued up front
+        // (indices clamped into the face grid, used only through the selects
+        // below), so a face's loads are in flight together.
+        const bool hm1 = id[a] >= 1, hp1 = id[a] + 1 < dim[a], hm2 = id[a] >= 2, hp2 = id[a] + 2 < dim[a];
+        const int im1 = hm1 ? f - st[a] : f, ip1 = hp1 ? f + st[a] : f;
+        const int im2 = hm2 ? f - 2 * st[a] : f, ip2 = hp2 ? f + 2 * st[a] : f;
+        const T om1 = fo[im1], op1 = fo[ip1], om2 = fo[im2], op2 = fo[ip2];
+        const T vm1 = vel[im1], vp1 = vel[ip1], vm2 = vel[im2], vp2 = vel[ip2];
+        bool cm1 = false, cp1 = false, cm2 = false, cp2 = false;   // crack faces
+        if (lk) {
+            cm1 = lk[im1] != 0;
+            cp1 = lk[ip1] != 0;
+            cm2 = lk[im2] != 0;
+            cp2 = lk[ip2] != 0;
         }
-        {
-            int ni = id[a] - 2;
-            if (ni < 0) m2 = m1;
-            else {
-                int gg = f - 2 * st[a], g1 = f - st[a];
-                m2 = fo[gg] > T(0) && fo[g1] > T(0) && !(lk && (lk[gg] || lk[g1])) ? vel[gg] : m1;
-            }
-            ni = id[a] + 2;
-            if (ni >= dim[a]) p2 = p1;
-            else {
-                int gg = f + 2 * st[a], g1 = f + st[a];
-                p2 = fo[gg] > T(0) && fo[g1] > T(0) && !(lk && (lk[gg] || lk[g1])) ? vel[gg] : p1;
-            }
-        }
-        T fp, fm;
-        if (adv[a] >= T(0)) {
-            fp = v0 + T(0.5) * vanLeer(v0 - m1, p1 - v0);
-            fm = m1 + T(0.5) * vanLeer(m1 - m2, v0 - m1);
-        } else {
-            fp = p1 - T(0.5) * vanLeer(p1 - v0, p2 - p1);
-            fm = v0 - T(0.5) * vanLeer(v0 - m1, p1 - v0);
-        }
+        const T m1 = hm1 && om1 > T(0) && !cm1 ? vm1 : v0;
+        const T p1 = hp1 && op1 > T(0) && !cp1 ? vp1 : v0;
+        const T m2 = hm2 && om2 > T(0) && om1 > T(0) && !(cm2 || cm1) ? vm2 : m1;
+        const T p2 = hp2 && op2 > T(0) && op1 > T(0) && !(cp2 || cp1) ? vp2 : p1;
+        // the upwind-biased face values, the limiter arguments chosen by the
+        // sign of the advecting velocity (two van Leer evaluations, no branch)
+        const bool pos = adv[a] >= T(0);
+        const T vlA = vanLeer(v0 - m1, p1 - v0);
+        const T vlB = vanLeer(pos ? m1 - m2 : p1 - v0, pos ? v0 - m1 : p2 - p1);
+        const T fp = pos ? v0 + T(0.5) * vlA : p1 - T(0.5) * vlB;
+        const T fm = pos ? m1 + T(0.5) * vlB : v0 - T(0.5) * vlA;
         acc -= adv[a] * (fp - fm) * idx;
         lap += (m1 - T(2) * v0 + p1) * idx2;
     }
@@ -833,35 +837,30 @@ __global__ void k_velcorr(const Scn<R>* __restrict__ S, Dom dom, int comp) {
         const R* am = comp == 0 ? g.ax : comp == 1 ? g.ay : g.az;
         const T s = (T)g.sv[SV_DT] / (T)g.dx;
         const R* P = g.p;
+        // every load of the face up front (cell indices clamped into the grid,
+        // used only where the face has that cell)
+        const int ca = comp == 0 ? i : comp == 1 ? j : k;   // index of the face along its axis
+        const int na = comp == 0 ? nx : comp == 1 ? ny : nz;
+        const int stc = comp == 0 ? 1 : comp == 1 ? nx : nx * ny;
+        const int cHi = ca < na ? i + nx * (j + ny * k) : 0;
+        const int cLo = ca > 0 ? i + nx * (j + ny * k) - stc : 0;
         const T fof = fo[f];
+        T un = vel[f];
+        const T amf = am[f];
+        const T pHi = P[cHi], pLo = P[cLo];
         if (comp == 2 && k == 0) {
             // the ground faces are not visited by the reference's loop
             vm = 0;
         } else if (fof <= T(0)) {
             vel[f] = 0;
         } else {
-            T un = vel[f];
-            if (comp == 0) {
-                if (am[f] > T(0) && !((i == 0 || i == nx) && !bndOpen(g, 0, i == 0 ? 0 : 1, g.oz + (k + 0.5) * g.dx))) {
-                    T hi = i < nx ? P[i + nx * (j + ny * k)] : (un < T(0) ? T(-0.5) * un * un : T(0));
-                    T lo = i > 0 ? P[i - 1 + nx * (j + ny * k)] : (un > T(0) ? T(-0.5) * un * un : T(0));
-                    un = clampd(un - s * (hi - lo), -T(K_VMAX), T(K_VMAX));
-                    vel[f] = un;
-                }
-            } else if (comp == 1) {
-                if (am[f] > T(0) && !((j == 0 || j == ny) && !bndOpen(g, 1, j == 0 ? 0 : 1, g.oz + (k + 0.5) * g.dx))) {
-                    T hi = j < ny ? P[i + nx * (j + ny * k)] : (un < T(0) ? T(-0.5) * un * un : T(0));
-                    T lo = j > 0 ? P[i + nx * (j - 1 + ny * k)] : (un > T(0) ? T(-0.5) * un * un : T(0));
-                    un = clampd(un - s * (hi - lo), -T(K_VMAX), T(K_VMAX));
-                    vel[f] = un;
-                }
-            } else {
-                if (am[f] > T(0)) {
-                    T hi = k < nz ? P[i + nx * (j + ny * k)] : (un < T(0) ? T(-0.5) * un * un : T(0));
-                    T lo = P[i + nx * (j + ny * (k - 1))];
-                    un = clampd(un - s * (hi - lo), -T(K_VMAX), T(K_VMAX));
-                    vel[f] = un;
-                }
+            // open boundary faces of x and y take part where the wind profile leaves them open
+            const bool side = comp != 2 && (ca == 0 || ca == na);
+            if (amf > T(0) && !(side && !bndOpen(g, comp, ca == 0 ? 0 : 1, g.oz + (k + 0.5) * g.dx))) {
+                const T hi = ca < na ? pHi : (un < T(0) ? T(-0.5) * un * un : T(0));
+                const T lo = ca > 0 ? pLo : (un > T(0) ? T(-0.5) * un * un : T(0));
+                un = clampd(un - s * (hi - lo), -T(K_VMAX), T(K_VMAX));
+                vel[f] = un;
             }
             vm = fabs(un) * fof;   // in the arithmetic type, as the reference's float build
         }
@@ -1111,12 +1110,150 @@ __device__ __forceinline__ void advectCells(const Scn<R>* __restrict__ S, const 
     }
 }
 
-// The FP32 transport runs fastest with the compiler's own register choice (80
-// registers: 2.0 ms per batch-of-64 step, against 2.9 ms under any launch
-// bound); the FP64 body at 128 registers wants two CTAs per SM guaranteed.
+// superbeeTimes without a branch on the sign of den: with sg = sign(den),
+// superbee(num / den) den = sg superbee(sg num / (sg den)) (sg den), and the
+// sign flips are exact, so the value is superbeeTimes' value.
+__device__ __forceinline__ float superbeeTimesSigned(float num, float den) {
+    const float sg = den > 0.f ? 1.f : -1.f;
+    const float n = sg * num, d = sg * den;
+    return sg * fmaxf(0.f, fmaxf(fminf(2.f * n, d), fminf(n, 2.f * d)));
+}
+
+// FP32 transport of one gas cell (the mixed path) with the cell kernel's
+// expressions, laid out so that a warp's lanes follow one instruction stream:
+// what a face needs from the cell's side (its flux, the upwind density times
+// the flux, the species' diffusion factors, where the upwind cell's upwind
+// neighbour lies) is worked out once per cell, and each scalar's face is then
+// the same straight-line sequence whatever the direction of the flow. The
+// upwind cell is chosen by selects (fu, fd), the Superbee limiter is
+// superbeeTimesSigned, so a warp whose cells see flows of both signs no longer
+// runs both branches ten times. The values are those of the branching form
+// (src/sim/gasphase.cpp:685-784 in its float build, with the division-free
+// limiter).
+__device__ __forceinline__ void advectCellF32(const Scn<float>& g, int c) {
+    using T = float;
+    const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
+    int i, j, k;
+    ijkOf(g, 0, c, i, j, k);
+    const T dx = (T)g.dx;
+    const T invDx = T(1) / dx;
+    const T dt = (T)g.sv[SV_DT];
+    const T s = dt / dx;
+    const int fa0 = i + (nx + 1) * (j + ny * k);
+    const int fb0 = i + nx * (j + (ny + 1) * k);
+    const T fo[6] = {g.fx[fa0], g.fx[fa0 + 1], g.fy[fb0], g.fy[fb0 + nx], g.fz[c], g.fz[c + sxy]};
+    const T un[6] = {-fo[0] * g.u[fa0], fo[1] * g.u[fa0 + 1], -fo[2] * g.v[fb0], fo[3] * g.v[fb0 + nx],
+                     -fo[4] * g.w[c], fo[5] * g.w[c + sxy]};
+    const int id[3] = {i, j, k};
+    const int dim[3] = {nx, ny, nz}, st[3] = {1, nx, sxy};
+    const T* Tf = g.sc[0];
+    const T nuc = g.nu[c];
+    const T rc = rhoOf(g, c);
+    const T tc = Tf[c];
+    // per face d (axis d / 2, side -1 / +1): open (fo > 0, neighbour not solid);
+    // the neighbour's offset from c (0 outside the domain, where the value is
+    // ambient); and the upwind cell's upwind neighbour: behind this cell for an
+    // outflow, beyond the neighbour for an inflow -- its offset from c, with a
+    // solid cell there standing for the upwind cell itself (offset 0 or the
+    // neighbour's offset) and a cell outside the domain for ambient
+    unsigned openM = 0, nbAmbM = 0, uuAmbM = 0;
+    int nbOff[6], uuOff[6];
+    T ruf[6], kd[6], km[6], mden = rc;
+#pragma unroll
+    for (int d = 0; d < 6; ++d) {
+        const int a = d >> 1, sg = (d & 1) ? 1 : -1;
+        const int n1 = id[a] + sg, n2 = id[a] + 2 * sg, o1 = id[a] - sg;
+        const bool in1 = n1 >= 0 && n1 < dim[a], in2 = n2 >= 0 && n2 < dim[a], ino = o1 >= 0 && o1 < dim[a];
+        const int so = sg * st[a];
+        nbOff[d] = 0;
+        uuOff[d] = 0;
+        ruf[d] = T(0);
+        kd[d] = T(0);
+        km[d] = T(0);
+        if (fo[d] <= T(0) || (in1 && g.blocked[c + so])) continue;
+        openM |= 1u << d;
+        if (in1) nbOff[d] = so;
+        else nbAmbM |= 1u << d;
+        const bool up = un[d] > T(0);
+        const bool uuIn = up ? ino : in2;
+        const int uuCell = up ? -so : 2 * so;
+        if (!uuIn) uuAmbM |= 1u << d;
+        else uuOff[d] = g.blocked[c + uuCell] ? (up ? 0 : so) : uuCell;
+        // temperature face, upwind density, species diffusion (as the cell kernel)
+        const T tn = in1 ? Tf[c + so] : tAmbient<T>();
+        const T tuu = uuIn ? Tf[c + uuOff[d]] : tAmbient<T>();
+        const T tu = up ? tc : tn, td = up ? tn : tc;
+        const T tden = td - tu;
+        const T tface = tu + (fabs(tden) > T(1e-6) ? T(0.5) * superbeeTimesSigned(tu - tuu, tden) : T(0));
+        const T pu = up ? g.Pb[c] : (in1 ? g.Pb[c + so] : T(K_P0));
+        const T rUp = pu / (T(K_RS) * mx(tAbs(tface), T(K_T_MIN)));
+        mden -= s * rUp * un[d];
+        ruf[d] = rUp * un[d];
+        const T nun = in1 ? g.nu[c + so] : nuc;
+        const T Dd = T(0.5) * (nuc + nun) / T(K_SC_T) + T(2.0e-5);
+        const T rfd = in1 ? T(0.5) * (rc + rhoOf(g, c + so)) : rc;
+        kd[d] = fo[d] * Dd * invDx;
+        km[d] = fo[d] * rfd * Dd * invDx;
+    }
+    const bool conservative = mden > T(0.25) * rc;
+    const T invMden = T(1) / mden;
+    // Each scalar: per open face, the limited face value of the upwind cell.
+    // A face without flow adds nothing (flux and upwind density times flux
+    // are 0), whatever value the limiter gives it, so the face value needs no
+    // zero-flux case.
+#pragma unroll 1
+    for (int q = 0; q < NSC; ++q) {
+        const T* __restrict__ Fc = g.sc[q] + c;
+        const T fc = Fc[0];
+        const T amb = ambOf<T>(q);
+        T lo = fc, hi = fc, acc = 0, macc = 0;
+#pragma unroll
+        for (int d = 0; d < 6; ++d) {
+            if (!((openM >> d) & 1u)) continue;
+            const T fnv = Fc[nbOff[d]], fuuv = Fc[uuOff[d]];
+            const T fn = ((nbAmbM >> d) & 1u) ? amb : fnv;
+            const T fuu = ((uuAmbM >> d) & 1u) ? amb : fuuv;
+            lo = mn(lo, fn);
+            hi = mx(hi, fn);
+            const T flux = un[d];
+            const bool up = flux > T(0);
+            const T fu = up ? fc : fn, fd = up ? fn : fc;
+            const T den = fd - fu;
+            const T face = fabs(den) > T(1e-12) ? fu + T(0.5) * superbeeTimesSigned(fu - fuu, den) : fu;
+            acc -= flux * (face - fc);
+            macc -= ruf[d] * face;
+            if (q > 0) {
+                acc += kd[d] * (fn - fc);
+                macc += km[d] * (fn - fc);
+            }
+        }
+        const T val = conservative ? (rc * fc + s * macc) * invMden : fc + s * acc;
+        g.sc2[q][c] = clampd(val, lo, hi);
+    }
+}
+
+// The FP32 transport kernel is bounded to three CTAs per SM (80 registers, a
+// few spilled in the per-cell set-up): 1.71 ms per batch-of-64 step against
+// 2.36 ms with the compiler's own 95 registers (two CTAs). The FP64 body at
+// 128 registers wants two CTAs per SM guaranteed.
 template <class R>
-__global__ void k_advect(const Scn<R>* __restrict__ S, Dom dom) {
-    advectCells<R>(S, dom);
+__device__ __forceinline__ void advectBody(const Scn<R>* __restrict__ S, const Dom& dom) {
+    if constexpr (sizeof(R) == 4) {
+        PHX_PROLOGUE(dom);
+        const int c = tile_ * TPB + threadIdx.x;
+        if (c >= g.N) return;
+        if (g.blocked[c]) {
+            for (int q = 0; q < NSC; ++q) g.sc2[q][c] = g.sc[q][c];
+            return;
+        }
+        advectCellF32(g, c);
+    } else {
+        advectCells<R>(S, dom);
+    }
+}
+template <class R>
+__global__ void __launch_bounds__(TPB, 3) k_advect(const Scn<R>* __restrict__ S, Dom dom) {
+    advectBody<R>(S, dom);
 }
 template <class R>
 __global__ void __launch_bounds__(TPB, 2) k_advect_2cta(const Scn<R>* __restrict__ S, Dom dom) {

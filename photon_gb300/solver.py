@@ -287,6 +287,13 @@ class Batch:
         """unknowns of each level of scenario s's pressure multigrid"""
         return _mg_rows(self.L, self.h, s)
 
+    def mg_nnz(self, s: int) -> list:
+        """stored off-diagonal entries of each level's CSR rows (phx_batch_mg_nnz; 0 for level 0)"""
+        n = len(self.mg_levels(s))
+        out = (ctypes.c_int * 16)()
+        self._check(self.L.phx_batch_mg_nnz(self.h, s, ctypes.cast(out, ctypes.c_void_p), 16))
+        return [out[l] for l in range(min(n, 16))]
+
     def tune_vcycle(self, steps: int = 3, dtMax: float = 0.02) -> list:
         """phx_batch_tune_vcycle: the coarsening stop chosen per size bucket"""
         out = (ctypes.c_int * 8)()
