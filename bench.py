@@ -415,7 +415,8 @@ def measure(args, precision, L, world, clocks: bool):
         # the V-cycle schedule per size bucket, tuned on the developed batch (state restored)
         t0 = time.perf_counter()
         stops = g.tune_vcycle(3, dtMax)
-        vcycle = {"coarsening_stop_per_bucket": stops, "tuning_s": round(time.perf_counter() - t0, 2),
+        vcycle = {"coarsening_stop_per_bucket": stops, "coarse_jacobi_sweeps_per_leg": g.coarse_sweeps,
+                  "tuning_s": round(time.perf_counter() - t0, 2),
                   "buckets": "bucket b: [20000 * 2^b, 20000 * 2^(b+1)) cells"}
     g.run(max(3, args.warmup), dtMax)
     # a working set that fits in L2 is flushed before every timed step

@@ -275,16 +275,21 @@ int phx_batch_mg_nnz(struct phx_ctx* ctx, int scenario, int* nnz, int cap);
  * reference, whose schedule is fixed (levels are added while the coarsest has
  * more than 2000 unknowns, src/sim/pressure_mg.cpp:141). Scenarios fall in
  * size buckets: bucket b holds scenarios of [20000 * 2^b, 20000 * 2^(b+1))
- * cells (bucket 0 also the smaller ones, bucket 7 also the larger ones). For
- * each bucket present in the batch, each candidate coarsening stop (2000,
- * 1000, 500 unknowns) is applied to the bucket's scenarios and the batch is
- * stepped `steps` times (1-50, timed with CUDA events, after one untimed step)
- * from the same saved state at dt_max; every candidate solves to the same
- * relative residual, and the fastest is kept. The choice is recorded process-
- * wide, so scenarios created later with a size in that bucket use it; the
- * batch's state is restored when the call returns. stops_out[0..cap) gets the
- * chosen stop of every bucket (2000 where none was tuned). On an FP64 context
- * the call changes nothing (the FP64 path keeps the reference's schedule). */
+ * cells (bucket 0 also the smaller ones, bucket 7 also the larger ones).
+ * First the coarse levels' smoothing is chosen for the whole batch: two
+ * damped Jacobi sweeps per level on each leg of the V-cycle (the reference's,
+ * src/sim/pressure_mg.cpp:281-297) or one (the environment variable
+ * PHX_COARSE_SWEEPS=1 or 2 fixes it instead). Then, for each bucket present in
+ * the batch, each candidate coarsening stop (2000, 1000, 500 unknowns) is
+ * applied to the bucket's scenarios. Each candidate is timed by stepping the
+ * batch `steps` times (1-50, CUDA events, after one untimed step) from the
+ * same saved state at dt_max; every candidate solves to the same relative
+ * residual, and the fastest is kept. The choices are recorded process-wide,
+ * so scenarios and batches created later use them; the batch's state is
+ * restored when the call returns. stops_out[0..min(cap, 8)) gets the chosen
+ * stop of every bucket (2000 where none was tuned), stops_out[8] (cap > 8)
+ * the sweeps per level and leg. On an FP64 context the call changes nothing
+ * (the FP64 path keeps the reference's schedule). */
 int phx_batch_tune_vcycle(struct phx_ctx* ctx, int steps, double dt_max, int* stops_out, int cap);
 
 /* --- radiation trace -------------------------------------------------------

@@ -77,6 +77,10 @@ inline int vcycleBucket(long long cells) {
 }
 inline std::mutex& vcycleMutex() { static std::mutex m; return m; }
 inline int* vcycleTable() { static int t[VC_BUCKETS] = {0}; return t; }
+// the mixed path's smoothing on the coarse levels: Jacobi sweeps per level on
+// each leg of the V-cycle (2, the reference's schedule, until tuned; 1 after a
+// tuning that found it faster at the solve's relative residual)
+inline int& vcycleSweeps() { static int v = 2; return v; }
 inline int vcycleStopFor(long long cells) {
     std::lock_guard<std::mutex> lock(vcycleMutex());
     const int v = vcycleTable()[vcycleBucket(cells)];
@@ -537,6 +541,7 @@ public:
     // PHX_L0_ROWBLOCK=1 runs level 0 on the row-block kernels instead
     const bool l0Requested = std::getenv("PHX_L0_ROWBLOCK") == nullptr;
     bool useL0 = false;
+    bool smoothOne = false;            // mixed path: one Jacobi sweep per coarse level and leg (vcycleSweeps)
     bool l0RedWide = false;            // the red sweep with L0_RED_WIDE blocks per thread
     int l0grid[L0_MODES + 1] = {};     // per pass; [L0_MODES]: the wide red sweep
     ADom adom[2][D_COUNT];
@@ -765,6 +770,7 @@ public:
                 const int v = vcycleTable()[b];
                 out[b] = v > 0 ? v : MG_COARSE_STOP_REF;
             }
+            if (out && cap > VC_BUCKETS) out[VC_BUCKETS] = kMixed ? vcycleSweeps() : 2;
         };
         if (!kMixed || nscn() == 0) { report(); return PHX_OK; }
         PHX_TRY(ensureTables());
@@ -817,6 +823,28 @@ public:
             *ms = t;
             return PHX_OK;
         };
+        // the coarse levels' smoothing first, one schedule for the batch (two Jacobi
+        // sweeps per level and leg, the reference's, or one; PHX_COARSE_SWEEPS=1|2
+        // fixes it), then the coarsening stop per size bucket
+        auto setSweeps = [&](int v) {
+            std::lock_guard<std::mutex> lock(vcycleMutex());
+            vcycleSweeps() = v;
+        };
+        if (r == PHX_OK) {
+            const char* fixed = std::getenv("PHX_COARSE_SWEEPS");
+            if (fixed && (std::atoi(fixed) == 1 || std::atoi(fixed) == 2)) {
+                setSweeps(std::atoi(fixed));
+            } else {
+                double ms2 = 0, ms1 = 0;
+                setSweeps(2);
+                r = trial(&ms2);
+                if (r == PHX_OK) {
+                    setSweeps(1);
+                    r = trial(&ms1);
+                }
+                setSweeps(r == PHX_OK && ms1 < ms2 ? 1 : 2);
+            }
+        }
         for (int b : order) {
             if (r != PHX_OK) break;
             int best = MG_COARSE_STOP_REF;
@@ -988,6 +1016,10 @@ public:
         maxLevels = 0;
         anyClosed = false;
         anyLeak = false;
+        {
+            std::lock_guard<std::mutex> lock(vcycleMutex());
+            smoothOne = kMixed && vcycleSweeps() == 1;
+        }
         RbShapes<R> shp;
         int t[D_COUNT];
         for (int s = 0; s < n; ++s) {
@@ -1004,6 +1036,7 @@ public:
             anyLeak |= !S.leak.empty();
             S.h.dtMaxArg = dDtMax + s;
             S.h.errWord = dErr;
+            S.h.smooth1 = smoothOne ? 1 : 0;
             shp.add(S.geo.nx, S.geo.ny);
         }
         // per domain, the scenario and tile of every CTA (packed 11 + 20 bits)
@@ -1494,18 +1527,24 @@ public:
             launchRB("k_gs_pre", cfgGs[GS_PRE], k_gs_rb<R, GS_PRE>, S, adom[0][D_RB], cfgGs[GS_PRE].shape, phase);
             launchRB("k_res_restrict", cfgRes, k_res_rb<R>, S, adom[0][D_RB], cfgRes.shape);
         }
-        // down: level 1's first Jacobi sweep; then per level its second sweep and
-        // its residual restricted to level l+1 with l+1's first sweep
+        // down: level 1's first Jacobi sweep; then per level its second sweep (not
+        // in the one-sweep schedule) and its residual restricted to level l+1 with
+        // l+1's first sweep; up: per level the prolongating sweep and (two-sweep
+        // schedule) a plain one
         if (!useL0) launchA("k_jacobi", D_LV0 + 1, TPB, k_jacobi<R>, S, adom[0][D_LV0 + 1], 1, 0);
         for (int l = 1; l < maxLevels - 1; ++l) {
-            launchA("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, adom[0][D_LV0 + l], l, 1);
+            if (!smoothOne) launchA("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, adom[0][D_LV0 + l], l, 1);
             launchA("k_res_restrict_jac0", D_RS0 + l, TPB, k_res_restrict_jac0<R>, S, adom[0][D_RS0 + l], l);
         }
         launchA("k_coarse_dense", D_CO_DENSE, TPB, k_coarse_dense<R>, S, adom[0][D_CO_DENSE]);
         launchA("k_coarse_serial", D_CO_SERIAL, 32, k_coarse_serial<R>, S, adom[0][D_CO_SERIAL]);
         for (int l = maxLevels - 2; l >= 1; --l) {
-            launchA("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, adom[0][D_LV0 + l], l, 2);
-            launchA("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, adom[0][D_LV0 + l], l, 1);
+            if (smoothOne) {
+                launchA("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, adom[0][D_LV0 + l], l, 3);
+            } else {
+                launchA("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, adom[0][D_LV0 + l], l, 2);
+                launchA("k_jacobi", D_LV0 + l, TPB, k_jacobi<R>, S, adom[0][D_LV0 + l], l, 1);
+            }
         }
         if (useL0) {
             launchL0<L0_BLACK>("k_gs_black", phase);

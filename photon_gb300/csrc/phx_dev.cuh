@@ -195,6 +195,8 @@ struct Scn {
     int fp16Scratch;             // mixed path: Jacobi scratch rounded to FP16 (an accuracy study; off by default)
     int fp16Z0;                  // mixed path: level-0 smoother output z rounded to FP16 (an accuracy study; off by default)
     int nLevels;
+    int smooth1;                 // mixed path: one damped Jacobi sweep per coarse level on each leg
+                                 // of the V-cycle (the reference: two, src/sim/pressure_mg.cpp:281-297)
     Level<R> lv[MAX_LEVELS];
     // row-block tiles of the level-0 pressure kernels: tj rows x RB_KZ planes, njb blocks along y
     int tj, njb;

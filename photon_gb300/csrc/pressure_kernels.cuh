@@ -64,13 +64,15 @@ __device__ __forceinline__ R scratchRound(const Scn<R>& g, R v) {
 
 // damped Jacobi sweep on a coarse level (jacobi, pressure_mg.cpp:237-247).
 // mode 0: from x = 0, into y; mode 1: y -> x; mode 2: x plus the coarser
-// level's x prolongated (:290-297), into y.
+// level's x prolongated (:290-297), into y; mode 3 (the mixed path's one-sweep
+// schedule): y plus the coarser level's x prolongated, into x.
 template <class R>
 __device__ __forceinline__ void jacobiRow(const Scn<R>& g, int I, int l, int mode) {
     using T = R;
     const Level<R>& L = g.lv[l];
     if (I >= L.n) return;
-    R* out = mode == 1 ? L.x : L.y;
+    const bool toX = mode == 1 || mode == 3, prolong = mode == 2 || mode == 3;
+    R* out = toX ? L.x : L.y;
     const T dg = L.diag[I];
     if (dg <= 0) { out[I] = 0; return; }
     const T om = T(OMEGA);
@@ -79,18 +81,18 @@ __device__ __forceinline__ void jacobiRow(const Scn<R>& g, int I, int l, int mod
         out[I] = scratchRound(g, (T(1) - om) * T(0) + om * s / dg);
         return;
     }
-    const R* in = mode == 1 ? L.y : L.x;
-    const R* xc = mode == 2 ? g.lv[l + 1].x : nullptr;
+    const R* in = toX ? L.y : L.x;
+    const R* xc = prolong ? g.lv[l + 1].x : nullptr;
     const int* agg = L.agg;
     auto X = [&](int n) -> T {
         T v = in[n];
-        if (mode == 2) v = v + xc[agg[n]];
+        if (prolong) v = v + xc[agg[n]];
         return v;
     };
     T s = L.b[I];
     for (int q = L.rowStart[I]; q < L.rowStart[I + 1]; ++q) s += L.val[q] * X(L.col[q]);
     const T v = (T(1) - om) * X(I) + om * s / dg;
-    out[I] = mode == 1 ? v : scratchRound(g, v);
+    out[I] = toX ? v : scratchRound(g, v);
 }
 template <class R>
 __device__ __forceinline__ void jacobiTile(const Scn<R>& g, int tile, int l, int mode) {
@@ -127,8 +129,9 @@ __device__ __forceinline__ void resRestrictJac0Group(const Scn<R>& g, int jBase,
             const int I = L.child[e0 + idx];
             const T dg = L.diag[I];
             if (dg > 0) {
-                T s = L.b[I] - dg * L.x[I];
-                for (int q = L.rowStart[I]; q < L.rowStart[I + 1]; ++q) s += L.val[q] * L.x[L.col[q]];
+                const R* it = g.smooth1 ? L.y : L.x;   // the level's iterate after its down-leg sweeps
+                T s = L.b[I] - dg * it[I];
+                for (int q = L.rowStart[I]; q < L.rowStart[I + 1]; ++q) s += L.val[q] * it[L.col[q]];
                 r = s;
             }
         }

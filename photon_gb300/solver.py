@@ -295,10 +295,12 @@ class Batch:
         return [out[l] for l in range(min(n, 16))]
 
     def tune_vcycle(self, steps: int = 3, dtMax: float = 0.02) -> list:
-        """phx_batch_tune_vcycle: the coarsening stop chosen per size bucket"""
-        out = (ctypes.c_int * 8)()
-        self._check(self.L.phx_batch_tune_vcycle(self.h, steps, dtMax, ctypes.cast(out, ctypes.c_void_p), 8))
-        return list(out)
+        """phx_batch_tune_vcycle: the coarsening stop chosen per size bucket;
+        the coarse levels' Jacobi sweeps per leg it chose go to self.coarse_sweeps"""
+        out = (ctypes.c_int * 9)()
+        self._check(self.L.phx_batch_tune_vcycle(self.h, steps, dtMax, ctypes.cast(out, ctypes.c_void_p), 9))
+        self.coarse_sweeps = out[8]
+        return list(out)[:8]
 
     def scenario_bytes(self, s: int) -> int:
         return int(self.L.phx_batch_scenario_bytes(self.h, s))

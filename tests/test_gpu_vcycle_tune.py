@@ -45,6 +45,7 @@ def test_tuner_keeps_state_and_picks_candidates():
     levels_ref = [B.mg_levels(s) for s in range(len(cases))]
     stops = B.tune_vcycle(2, 0.02)
     assert len(stops) == 8 and all(v in (2000, 1000, 500) for v in stops), stops
+    assert B.coarse_sweeps in (1, 2)
     for s in range(len(cases)):
         for f in FIELDS:
             assert np.array_equal(B.get(s, f), before[s][f]), (s, f)
@@ -66,3 +67,34 @@ def test_tuner_leaves_fp64_schedule():
     assert B.tune_vcycle(2, 0.02) is not None
     assert B.mg_levels(0) == lv
     B.close()
+
+
+def test_one_sweep_schedule_solves_to_the_bar(monkeypatch):
+    """The mixed path's one-sweep coarse smoothing (one damped Jacobi sweep per
+    level on each leg: the V-cycle stays symmetric) is a different
+    preconditioner, not a different answer: forced through the tuner, the
+    batch still meets the relative residual of 1e-8 on every step, and its
+    pressure stays within the mixed path's bar of the two-sweep run's."""
+    def run(sweeps):
+        monkeypatch.setenv("PHX_COARSE_SWEEPS", str(sweeps))
+        cases = [rel_case(casegen.house(40, 32, 24, 0.2, 5)), rel_case(casegen.house_small(1))]
+        B = Batch(cases, _lib.PREC_MIXED)
+        for _ in range(4):
+            B.step(0.02)
+        B.tune_vcycle(1, 0.02)
+        assert B.coarse_sweeps == sweeps
+        iters = []
+        for _ in range(4):
+            B.step(0.02)
+            for s in range(len(cases)):
+                assert B.stats(s)["pressure_rel_residual"] <= 1e-8
+                iters.append(B.stats(s)["pressure_iters"])
+        p = [B.get(s, "p") for s in range(len(cases))]
+        B.close()
+        return p, iters
+
+    p1, it1 = run(1)
+    p2, it2 = run(2)   # leaves the process-wide schedule at the reference's two sweeps
+    for a, b in zip(p1, p2):
+        assert np.linalg.norm(a - b) <= 1e-3 * np.linalg.norm(b)
+    assert max(it1) <= 2 * max(it2)
