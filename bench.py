@@ -510,8 +510,9 @@ def measure_serving(args, precision):
     seeded geometry, 10-500 kW burners) submitted by client threads at their
     arrival times, admitted under a 150 GB HBM budget and stepped together by
     one serving loop (continuous batching). The simulated durations of
-    30-300 s are scaled by args.serve_scale so the run ends in about a minute.
-    Returns throughput and p50/p99 step and completion latency."""
+    30-300 s are scaled by args.serve_scale (0.01 in the default line, so the
+    run ends in about a minute; --serving-only --serve-scale 1 runs them
+    unscaled). Returns throughput and p50/p99 step and completion latency."""
     import threading
     from photon_gb300 import casegen
     from photon_gb300.serve import Server
@@ -742,6 +743,9 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=8.0, help="request arrivals per second (Poisson)")
     ap.add_argument("--serve-scale", type=float, default=0.01, help="scale of the 30-300 s simulated durations")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serving-only", action="store_true",
+                    help="only the serving form, per --precision (one JSON line; e.g. --serve-scale 1 for the "
+                         "unscaled 30-300 s durations)")
     ap.add_argument("--no-radiation", action="store_true", help="skip the radiation trace and volume render")
     ap.add_argument("--extras-only", action="store_true",
                     help="time only the radiation trace and the volume render (one JSON line)")
@@ -770,6 +774,15 @@ def main():
     if args.precision_study:
         if rank == 0:
             print(json.dumps(precision_study(args)))
+        return 0
+    if args.serving_only:
+        if rank == 0:
+            out = {}
+            if args.precision in ("both", "mixed"):
+                out["mixed"] = measure_serving(args, _lib.PREC_MIXED)
+            if args.precision in ("both", "fp64"):
+                out["fp64"] = measure_serving(args, _lib.PREC_FP64)
+            print(json.dumps({"serving": out}))
         return 0
     if args.extras_only:
         if rank == 0:

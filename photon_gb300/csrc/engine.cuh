@@ -147,7 +147,7 @@ struct Scenario {
         Pb0.assign(NN, 101325.0);
         Z = computeZones(geo, Pb0);
         if (kMixed) coarseStop = vcycleStopFor(NN);   // the tuned schedule of the scenario's size, if any
-        MG = buildMultigrid(geo, DENSE_MAX, coarseStop);
+        MG = buildMultigrid(geo, DENSE_MAX, coarseStop, coarseSolveFor());
         buildLeakFaces();
         return PHX_OK;
     }
@@ -264,6 +264,21 @@ struct Scenario {
         return off + 256;
     }
 
+    // the coarsest solve: the reference's 20 Gauss-Seidel sweep pairs on the FP64
+    // path; on the mixed path the exact inverse of the coarsest matrix
+    // (PHX_COARSE_EXACT=0: the reference's sweeps)
+    static CoarseSolve coarseSolveFor() {
+        CoarseSolve cs;
+        if (kMixed) {
+            static const bool exact = [] {
+                const char* e = std::getenv("PHX_COARSE_EXACT");
+                return !(e && std::atoi(e) == 0);
+            }();
+            cs.exact = exact;
+        }
+        return cs;
+    }
+
     // the levels' arrays in their own arena: level 0's aggregation map, and per
     // coarser level its CSR rows, diagonal, iterate and scratch, child lists and,
     // at the coarsest level, the dense operator
@@ -316,7 +331,7 @@ struct Scenario {
     // batch tables (the level domains change).
     int rebuildLevels(cudaStream_t st, int stop) {
         if (stop == coarseStop && mgArena) return PHX_OK;
-        Multigrid M = buildMultigrid(geo, DENSE_MAX, stop);
+        Multigrid M = buildMultigrid(geo, DENSE_MAX, stop, coarseSolveFor());
         PHX_CK(cudaStreamSynchronize(st));
         char* old = mgArena;
         MG = std::move(M);

@@ -144,7 +144,110 @@ void gsSweep(const MgLevel& L, const double* b, double* x, bool forward) {
 }
 }  // namespace
 
-Multigrid buildMultigrid(const GridGeom& g, int denseMax, int coarseStop) {
+namespace {
+// the host's worker threads for a loop over [0, n) in contiguous chunks
+template <class F>
+void parallelFor(int n, long long work, F f) {
+    int nt = (int)std::min<unsigned>(16, std::max(1u, std::thread::hardware_concurrency()));
+    if (work < 200000) nt = 1;
+    nt = std::max(1, std::min(nt, n));
+    if (nt == 1) { f(0, n); return; }
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; ++t) pool.emplace_back(f, (int)((long long)n * t / nt), (int)((long long)n * (t + 1) / nt));
+    for (auto& th : pool) th.join();
+}
+}  // namespace
+
+bool coarseInverse(const MgLevel& L, std::vector<double>& inv) {
+    const int n = L.n;
+    const size_t nn = (size_t)n * n;
+    // the matrix, lower triangle used: diag on the diagonal, minus the couplings off it;
+    // rows without a positive diagonal become identity rows (their output is zeroed below)
+    std::vector<double> A(nn, 0.0);
+    std::vector<char> dead(n, 0);
+    for (int I = 0; I < n; ++I) {
+        if (L.diag[I] <= 0) { dead[I] = 1; A[(size_t)I * n + I] = 1.0; continue; }
+        A[(size_t)I * n + I] = L.diag[I];
+    }
+    for (int I = 0; I < n; ++I) {
+        if (dead[I]) continue;
+        for (int q = L.rowStart[I]; q < L.rowStart[I + 1]; ++q)
+            if (!dead[L.col[q]]) A[(size_t)I * n + L.col[q]] -= L.val[q];
+    }
+    std::vector<double> d0(n);
+    for (int I = 0; I < n; ++I) d0[I] = A[(size_t)I * n + I];
+    // right-looking blocked Cholesky A = L L^T in the lower triangle; the trailing
+    // update of each block step is split over rows
+    constexpr int B = 64;
+    for (int k0 = 0; k0 < n; k0 += B) {
+        const int k1 = std::min(n, k0 + B);
+        for (int j = k0; j < k1; ++j) {   // the diagonal block
+            double* rj = &A[(size_t)j * n];
+            double dj = rj[j];
+            for (int k = k0; k < j; ++k) dj -= rj[k] * rj[k];
+            if (!(dj > 1e-10 * d0[j])) return false;   // not positive definite: a singular (closed) zone
+            dj = std::sqrt(dj);
+            rj[j] = dj;
+            for (int i = j + 1; i < k1; ++i) {
+                double* ri = &A[(size_t)i * n];
+                double v = ri[j];
+                for (int k = k0; k < j; ++k) v -= ri[k] * rj[k];
+                ri[j] = v / dj;
+            }
+        }
+        // the panel below the block (rows independent), then the trailing matrix,
+        // which reads other rows' panel entries: two passes, each split over rows
+        parallelFor(n - k1, (long long)(n - k1) * (k1 - k0) * (k1 - k0), [&](int a, int b) {
+            for (int i = k1 + a; i < k1 + b; ++i) {
+                double* ri = &A[(size_t)i * n];
+                for (int j = k0; j < k1; ++j) {
+                    const double* rj = &A[(size_t)j * n];
+                    double v = ri[j];
+                    for (int k = k0; k < j; ++k) v -= ri[k] * rj[k];
+                    ri[j] = v / rj[j];
+                }
+            }
+        });
+        parallelFor(n - k1, (long long)(n - k1) * (n - k1) * (k1 - k0) / 2, [&](int a, int b) {
+            for (int i = k1 + a; i < k1 + b; ++i) {
+                double* ri = &A[(size_t)i * n];
+                for (int j = k1; j <= i; ++j) {
+                    const double* rj = &A[(size_t)j * n];
+                    double v = 0;
+                    for (int k = k0; k < k1; ++k) v += ri[k] * rj[k];
+                    ri[j] -= v;
+                }
+            }
+        });
+    }
+    // columns of the inverse: L y = e_j, then L^T x = y (L^T read from a transposed copy)
+    std::vector<double> U(nn, 0.0);
+    for (int i = 0; i < n; ++i)
+        for (int k = 0; k <= i; ++k) U[(size_t)k * n + i] = A[(size_t)i * n + k];
+    inv.assign(nn, 0.0);
+    parallelFor(n, (long long)n * n * n / 2, [&](int a, int b) {
+        std::vector<double> y(n);
+        for (int j = a; j < b; ++j) {
+            std::fill(y.begin(), y.end(), 0.0);
+            for (int i = j; i < n; ++i) {
+                const double* ri = &A[(size_t)i * n];
+                double v = i == j ? 1.0 : 0.0;
+                for (int k = j; k < i; ++k) v -= ri[k] * y[k];
+                y[i] = v / ri[i];
+            }
+            for (int i = n - 1; i >= 0; --i) {
+                const double* ui = &U[(size_t)i * n];
+                double v = y[i];
+                for (int k = i + 1; k < n; ++k) v -= ui[k] * y[k];
+                y[i] = v / ui[i];
+            }
+            for (int i = 0; i < n; ++i) inv[(size_t)i * n + j] = (dead[i] || dead[j]) ? 0.0 : y[i];
+        }
+    });
+    return true;
+}
+
+Multigrid buildMultigrid(const GridGeom& g, int denseMax, int coarseStop, const CoarseSolve& cs) {
     Multigrid M;
     const int nx = g.nx, ny = g.ny, nz = g.nz, n0 = g.N(), sxy = nx * ny;
     M.a0x = g.ax;
@@ -270,9 +373,10 @@ Multigrid buildMultigrid(const GridGeom& g, int denseMax, int coarseStop) {
         childrenOf(F, C.n);
         M.lv.push_back(std::move(C));
     }
-    // dense operator of the coarsest solve: column j = the sweeps applied to e_j
+    // dense operator of the coarsest solve: the exact inverse where asked for and
+    // the matrix is definite; else column j = the sweeps applied to e_j
     MgLevel& Lc = M.lv.back();
-    if (Lc.n <= denseMax) {
+    if (Lc.n <= denseMax && !(cs.exact && coarseInverse(Lc, Lc.dense))) {
         const int n = Lc.n;
         Lc.dense.assign((size_t)n * n, 0.0);
         // columns are independent: split them over the host's threads
@@ -282,7 +386,10 @@ Multigrid buildMultigrid(const GridGeom& g, int denseMax, int coarseStop) {
                 std::fill(b.begin(), b.end(), 0.0);
                 std::fill(x.begin(), x.end(), 0.0);
                 b[jcol] = 1.0;
-                for (int it = 0; it < 20; ++it) { gsSweep(Lc, b.data(), x.data(), true); gsSweep(Lc, b.data(), x.data(), false); }
+                for (int it = 0; it < cs.sweeps; ++it) {
+                    gsSweep(Lc, b.data(), x.data(), true);
+                    gsSweep(Lc, b.data(), x.data(), false);
+                }
                 for (int i = 0; i < n; ++i) Lc.dense[(size_t)i * n + jcol] = x[i];
             }
         };

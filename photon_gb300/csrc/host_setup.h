@@ -65,7 +65,23 @@ struct Multigrid {
 // added while the last one has more than coarseStop unknowns: 2000 is the
 // reference's schedule (:141); a smaller stop gives a deeper hierarchy.
 constexpr int MG_COARSE_STOP_REF = 2000;
-Multigrid buildMultigrid(const GridGeom& g, int denseMax, int coarseStop = MG_COARSE_STOP_REF);
+// forward + backward Gauss-Seidel sweep pairs of the coarsest solve (src/sim/pressure_mg.cpp:258-266)
+constexpr int MG_COARSE_SWEEPS_REF = 20;
+// the coarsest solve's dense operator: the reference's sweeps from x = 0, or,
+// with exact, the inverse of the coarsest matrix (dense Cholesky; the sweeps
+// where the matrix is singular, as with closed zones). The FP64 path keeps the
+// reference's.
+struct CoarseSolve {
+    int sweeps = MG_COARSE_SWEEPS_REF;
+    bool exact = false;
+};
+Multigrid buildMultigrid(const GridGeom& g, int denseMax, int coarseStop = MG_COARSE_STOP_REF,
+                         const CoarseSolve& cs = CoarseSolve());
+// inverse of a level's matrix (diag - off-diagonal couplings) by dense
+// Cholesky, row-major into inv; false (inv untouched) if the matrix is not
+// positive definite to working precision. Rows with diag <= 0 (which the
+// sweeps leave at 0) get 0 rows and columns.
+bool coarseInverse(const MgLevel& L, std::vector<double>& inv);
 
 // Solver::addBurner cell selection (src/sim/gasphase.cpp:72-90): the gas cells
 // whose centres lie in the rectangle at height z + dx/2, or the centre cell.

@@ -370,8 +370,14 @@ __global__ void __launch_bounds__(L0_THREADS, (L0MinCtas<R, MODE>::value)) k_l0(
                     *cnt = 0;
                     if constexpr (MODE == L0_APPLY) {
                         g.sv[SV_DQ] = total;
-                        if (total <= 0) g.sv[SV_DONE] = 1;
-                        else g.sv[SV_ALPHA] = g.sv[SV_RZ] / total;
+                        if (g.sv[SV_BREAK] == 1) {   // the iteration after a breakdown: no update, then a restart
+                            g.sv[SV_ALPHA] = 0;
+                            g.sv[SV_BREAK] = 2;
+                        } else if (total <= 0) {
+                            g.sv[SV_DONE] = 1;
+                        } else {
+                            g.sv[SV_ALPHA] = g.sv[SV_RZ] / total;
+                        }
                     } else {
                         closeCgIteration(g, phase, total);
                     }

@@ -224,6 +224,7 @@ __global__ void k_reset(const Scn<R>* __restrict__ S, Dom dom, int which) {
     sv[SV_BMAX] = 0;
     sv[SV_R64MAX] = 0;
     sv[SV_REPL] = 0;
+    sv[SV_BREAK] = 0;
 }
 
 }  // namespace phx

@@ -89,6 +89,7 @@ enum Slot {
     SV_R64MAX, SV_R0MAX, SV_OUTER, SV_ODONE, SV_ITTOT, SV_REPL,
     SV_HAVEPREV,                 // mixed path: p64prev holds the previous step's pressure
     SV_SRC_MF = 32,              // MAX_SRC injection amounts of this step (-1 = inactive)
+    SV_BREAK = SV_SRC_MF + MAX_SRC,   // mixed path: 1 after a CG breakdown (next update skipped), 2 restart pending
     SV_COUNT = 64
 };
 

@@ -267,16 +267,35 @@ __device__ void closeCgIteration(const Scn<R>& g, int phase, double tot) {
             sv[SV_PREL] = rel;
             converged = !(res > g.tol) || (g.relTol > 0 && rel <= g.relTol) || !(r64 > 0);
             sv[SV_R64MAX] = 0;
-            // closed zones: the replaced residual is no longer conjugate to the
-            // search direction of the singular zone operators; restart the
-            // FP32 CG from it (d = z)
-            if (phase != 0 && g.nClosed > 0) sv[SV_BETA] = 0;
+            // restart the FP32 CG from the replaced residual (d = z) where it is no
+            // longer conjugate to the search direction: closed zones (their
+            // operators are singular), and any scenario whose FP32 recursion had
+            // drifted below the true residual (a strong preconditioner takes the
+            // recursion to FP32's rounding floor within a few iterations; the old
+            // direction then carries only rounding noise)
+            const double rrec = sv[SV_RMAX];
+            if (phase != 0 && (g.nClosed > 0 || r64 > 4.0 * rrec)) sv[SV_BETA] = 0;
         }
-        const bool stop = converged || it >= g.maxIters || !(sv[SV_RZ] > 0);
+        // the first iteration after a breakdown's replacement restarts the FP32 CG (d = z)
+        if (phase != 0 && sv[SV_BREAK] == 2) {
+            sv[SV_BETA] = 0;
+            sv[SV_BREAK] = 0;
+        }
+        // a breakdown (r.z <= 0) of the FP32 recursion short of the FP64 bar: the recursive
+        // residual has reached FP32's rounding floor, not the solution. Replace it by the FP64
+        // residual on the next iteration (whose update is skipped: alpha = 0) and restart from it.
+        const bool breakdown = !(sv[SV_RZ] > 0);
+        const bool recover = breakdown && !replaced && phase != 0 && !converged && it < g.maxIters;
+        if (recover) {
+            sv[SV_BREAK] = 1;
+            sv[SV_RZ] = 1.0;   // any positive value: the skipped update does not use it
+            sv[SV_BETA] = 0;
+        }
+        const bool stop = converged || it >= g.maxIters || (breakdown && !recover);
         const double rrec = sv[SV_RMAX];
         const bool claims = phase != 0 && ((g.relTol > 0 && rrec <= 2.0 * g.relTol * sv[SV_BMAX]) ||
                                            rrec / sv[SV_INV] <= 0.5 * g.tol);
-        sv[SV_REPL] = (!stop && phase != 0 && ((it % g.replaceEvery) == 0 || claims)) ? 1.0 : 0.0;
+        sv[SV_REPL] = (!stop && phase != 0 && ((it % g.replaceEvery) == 0 || claims || recover)) ? 1.0 : 0.0;
         sv[SV_RMAX] = 0;
         if (stop) sv[SV_DONE] = 1;
     }

@@ -505,8 +505,14 @@ __global__ void __launch_bounds__(RB_THREADS, 2) k_cg_apply_rb(const Scn<R>* __r
         double total;
         if (lastCtaSumC(g, PS_DQ, tile, sst_[s + 1] - sst_[s], dot, &total, sh, &amLast) && threadIdx.x == 0) {
             g.sv[SV_DQ] = total;
-            if (total <= 0) g.sv[SV_DONE] = 1;
-            else g.sv[SV_ALPHA] = g.sv[SV_RZ] / total;
+            if (g.sv[SV_BREAK] == 1) {   // the iteration after a breakdown: no update, then a restart
+                g.sv[SV_ALPHA] = 0;
+                g.sv[SV_BREAK] = 2;
+            } else if (total <= 0) {
+                g.sv[SV_DONE] = 1;
+            } else {
+                g.sv[SV_ALPHA] = g.sv[SV_RZ] / total;
+            }
         }
     }
 }
