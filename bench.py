@@ -38,6 +38,11 @@ sys.path.insert(0, ROOT)
 
 METRIC = "cell-updates/s, mixed+batched vs FP64 GPU @1e-8 resid; p50/p99 scenario latency"
 REL_TOL = 1e-8
+
+
+def tol_str(x: float) -> str:
+    """1e-08 -> 1e-8"""
+    return ("%g" % x).replace("e-0", "e-")
 SPINUP_STEPS = 100   # untimed steps that develop the plume before warm-up
 
 
@@ -329,8 +334,9 @@ def run_reference(args, rank, world):
             "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded house generator)",
             "config": {"workload": args.workload, "scenarios": len(cases), "cells": cells,
-                       "pressure_stop": "relative 1e-8: the reference's absolute stop set each step to 1e-8 max|b| of its "
-                                        "previous step", "threads": threads, "spinup_steps": args.spinup,
+                       "pressure_stop": "relative %s: the reference's absolute stop set each step to %s max|b| of its "
+                                        "previous step" % (tol_str(REL_TOL), tol_str(REL_TOL)), "threads": threads,
+                       "spinup_steps": args.spinup,
                        "cpu_model": cpu_model(),
                        "hardware": "host CPU cores of rank 0 (the reference has no GPU path)"},
             "impl": "reference",
@@ -576,7 +582,7 @@ def measure_serving(args, precision):
             "config": {"arrivals": "Poisson, %.1f requests/s" % args.serve_rate,
                        "cells": "20k-1.32M log-uniform", "hbm_budget_gb": 150,
                        "duration": "30-300 s simulated x %g" % args.serve_scale,
-                       "pressure_stop": "relative %g" % REL_TOL}}
+                       "pressure_stop": "relative %s" % tol_str(REL_TOL)}}
 
 
 def measure_radiation(args, cpu_baseline: bool):
@@ -721,12 +727,14 @@ def precision_study(args):
                 "samples": len(p_err), "mixed_max": max(p_err), "mixed_median": float(np.median(p_err)),
                 "fp64_at_1e-8_max": max(p_err64), "fp64_at_1e-8_median": float(np.median(p_err64)),
                 "mixed_all": [float("%.3e" % e) for e in p_err]},
-            "mixed_rel_residual": {"max": max(rres), "steps_above_1e-8": int(sum(r > REL_TOL for r in rres))},
+            "pressure_stop": "relative %s (both paths' probe steps and the mixed run)" % tol_str(REL_TOL),
+            "mixed_rel_residual": {"max": max(rres), "steps_above_stop": int(sum(r > REL_TOL for r in rres))},
             "layer_T_rel_err": {"max": float(lerr.max()), "mean": float(lerr.mean())},
             "layer_T_K": {"fp64": [round(float(v), 2) for v in lf[ok]], "mixed": [round(float(v), 2) for v in lm[ok]]}}
 
 
 def main():
+    global REL_TOL
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -743,6 +751,8 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=8.0, help="request arrivals per second (Poisson)")
     ap.add_argument("--serve-scale", type=float, default=0.01, help="scale of the 30-300 s simulated durations")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--rel-tol", type=float, default=REL_TOL,
+                    help="the pressure solve's relative stop max|r| <= rel_tol max|b| for every arm (default 1e-8)")
     ap.add_argument("--serving-only", action="store_true",
                     help="only the serving form, per --precision (one JSON line; e.g. --serve-scale 1 for the "
                          "unscaled 30-300 s durations)")
@@ -758,6 +768,7 @@ def main():
     ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64"],
                     help="which paths to time (the line's value is the mixed path unless only fp64 runs)")
     args = ap.parse_args()
+    REL_TOL = args.rel_tol
     rank, world, local = rank_info()
     if args.impl == "reference":
         return run_reference(args, rank, world)
@@ -834,7 +845,7 @@ def main():
                 "data": "synthetic (seeded house generator; no dataset)",
                 "config": {"workload": args.workload, "scenarios": len(cases), "cells": mixed["cells"],
                            "precision": "mixed: FP32 fields and stencils, FP32 MG-CG inside FP64 refinement",
-                           "pressure_stop": "relative 1e-8 (max|r| <= 1e-8 max|b|, FP64)",
+                           "pressure_stop": "relative %s (max|r| <= %s max|b|, FP64)" % (tol_str(REL_TOL), tol_str(REL_TOL)),
                            "l2": "flushed before each step" if mixed["flush"] else "inputs larger than L2",
                            "spinup_steps": args.spinup,
                            "vcycle_schedule": mixed.get("vcycle"),
