@@ -295,14 +295,23 @@ __device__ __forceinline__ float warpMax(float v) {
     return v;
 }
 
-// CTA-wide max of non-negative values into *dst (one atomic per warp)
-__device__ __forceinline__ void blockMaxTo(double* dst, double v) {
+// CTA-wide max of non-negative values into *dst: warp maxima, then one warp
+// over them and one atomic per CTA (an atomic per warp put thousands of
+// same-address atomics per scenario into each launch). Every thread of the CTA
+// must call it (it has barriers); V is the arithmetic type of the values.
+template <class V>
+__device__ __forceinline__ void blockMaxTo(double* dst, V v) {
+    __shared__ V shMax[32];
     v = warpMax(v);
-    if ((threadIdx.x & 31) == 0) atomicMaxPos(dst, v);
-}
-__device__ __forceinline__ void blockMaxTo(double* dst, float v) {
-    v = warpMax(v);
-    if ((threadIdx.x & 31) == 0) atomicMaxPos(dst, (double)v);
+    const int w = (int)(threadIdx.x >> 5), l = (int)(threadIdx.x & 31), nw = (int)((blockDim.x + 31) >> 5);
+    __syncthreads();   // a previous call's last warp may still read the buffer
+    if (l == 0) shMax[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        V x = l < nw ? shMax[l] : V(0);
+        x = warpMax(x);
+        if (l == 0) atomicMaxPos(dst, (double)x);
+    }
 }
 
 // Sums of the FP32 path: an unevaluated pair hi + lo of floats (about 48
