@@ -390,7 +390,14 @@ struct Scenario {
         s.nZones = (int)Z.zoneP.size();
         s.nClosed = (int)Z.closed.size();
         s.mixed = kMixed ? 1 : 0;
-        s.replaceEvery = REPLACE_EVERY;
+        {   // PHX_REPLACE_EVERY=n: another interval, for measurements
+            static const int every = [] {
+                const char* e = std::getenv("PHX_REPLACE_EVERY");
+                const int v = e ? std::atoi(e) : 0;
+                return v >= 2 && v <= 100 ? v : REPLACE_EVERY;
+            }();
+            s.replaceEvery = every;
+        }
         s.extrap = std::getenv("PHX_NO_EXTRAP") == nullptr;   // mixed path: extrapolated initial guess
         s.fp16Scratch = kMixed && std::getenv("PHX_FP16_SCRATCH") != nullptr;
         s.fp16Z0 = kMixed && std::getenv("PHX_FP16_Z0") != nullptr;
