@@ -6,6 +6,7 @@
 // a CUDA graph whose pressure-solve loops are device-side while nodes.
 // Instantiated per precision by engine_fp64.cu and engine_mixed.cu.
 #pragma once
+#include <array>
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -1128,10 +1129,33 @@ public:
         int dev = 0, sms = 0;
         PHX_CK(cudaGetDevice(&dev));
         PHX_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        // Grid per pass: k times the resident CTAs, or (k = 0) one CTA per tile.
+        // q = A d and the red sweep end every tile with a reduction of d.q or
+        // r.z; one CTA per tile lets the SM overlap those of different tiles,
+        // which a persistent CTA runs one after the other (mixed batch of 64:
+        // 443 to 452 M cell-updates/s). The smoothing passes have no reduction
+        // and run one persistent wave. PHX_L0_WAVES="k0,k1,k2,k3,k4" (in pass
+        // order; one value sets all five) overrides this for measurements.
+        static const std::array<int, L0_MODES> waves = [] {
+            std::array<int, L0_MODES> w = {0, 1, 1, 1, 0};
+            if (const char* e = std::getenv("PHX_L0_WAVES")) {
+                int v[L0_MODES], n = 0;
+                for (const char* c = e; *c && n < L0_MODES;) {
+                    v[n++] = std::max(0, std::atoi(c));
+                    while (*c && *c != ',') ++c;
+                    if (*c == ',') ++c;
+                }
+                if (n > 0) for (int m = 0; m < L0_MODES; ++m) w[m] = v[n == 1 ? 0 : std::min(m, n - 1)];
+            }
+            return w;
+        }();
         auto one = [&](auto kern, int mode) -> int {
             int occ = 0;
             PHX_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, L0_THREADS, 0));
-            l0grid[mode] = std::min(sms * std::max(occ, 1), persistCtas * TPB / L0_THREADS);
+            const int k = waves[std::min(mode, L0_MODES - 1)];
+            const int cap = persistCtas * TPB / L0_THREADS;   // PHX_PERSIST_CTAS caps every shape
+            l0grid[mode] = k == 0 ? (persistCtas < PERSIST_CTAS ? cap : (1 << 30))
+                                  : std::min(sms * std::max(occ, 1) * k, cap * k);
             return PHX_OK;
         };
         PHX_TRY(one(k_l0<R, L0_APPLY, 1>, L0_APPLY));
@@ -1141,8 +1165,12 @@ public:
         PHX_TRY(one(k_l0<R, L0_RED, 1>, L0_RED));
         PHX_TRY(one(k_l0<R, L0_RED, L0_RED_WIDE>, L0_MODES));
         // several blocks per thread only where the batch's wide tiles still fill
-        // every CTA slot of the GPU twice
-        l0RedWide = dom[D_L0R].total >= 2 * l0grid[L0_MODES];
+        // every CTA slot of the GPU twice (PHX_L0_RED_WIDE=0|1 forces it)
+        static const int redWide = [] {
+            const char* e = std::getenv("PHX_L0_RED_WIDE");
+            return e ? std::atoi(e) : -1;
+        }();
+        l0RedWide = redWide >= 0 ? redWide == 1 : dom[D_L0R].total >= 2 * l0grid[L0_MODES];
         useL0 = true;
         return PHX_OK;
     }
