@@ -32,7 +32,7 @@ UNITS = {
     "server.cpp": [],
 }
 HEADERS = ["phx_dev.cuh", "step_kernels.cuh", "pressure_kernels.cuh", "engine.cuh", "engine.h", "host_setup.h",
-           "mixed_kernels.cuh", "rowblock.cuh", "level0.cuh", "radiation.cuh", "volume.cuh"]
+           "mixed_kernels.cuh", "rowblock.cuh", "level0.cuh", "fdiv.cuh", "radiation.cuh", "volume.cuh"]
 
 
 def _newer(target, deps):

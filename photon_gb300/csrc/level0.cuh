@@ -31,6 +31,7 @@
 #pragma once
 #include <type_traits>
 
+#include "fdiv.cuh"
 #include "rowblock.cuh"
 
 namespace phx {
@@ -62,6 +63,17 @@ __host__ __device__ inline int l0Tiles(int nx, int ny, int nz, int bpt) {
 // diagonal of a coded cell
 template <class T>
 __device__ __forceinline__ T codeDiag(unsigned cd) { return (T)(__popc(cd & 63u) + (cd >> 7)); }
+
+// a smoothing sweep's division by the diagonal: for a coded cell of the FP64
+// path by the integer diagonal in three FP64 operations (fdiv.cuh, the same
+// quotient), otherwise as the row-block kernels divide
+template <class T>
+__device__ __forceinline__ T l0Div(T a, unsigned cd, T dg) {
+    if constexpr (sizeof(T) == 8) {
+        if (!(cd & CODE_GENERAL)) return divSmall(a, (int)(__popc(cd & 63u) + (cd >> 7)));
+    }
+    return gsDiv(a, dg);
+}
 
 // the general-cell form of the stencil: coefficients and diagonal from the arrays
 template <class R>
@@ -213,7 +225,7 @@ __global__ void __launch_bounds__(L0_THREADS, (L0MinCtas<R, MODE>::value)) k_l0(
                 if (!red) return rv;                                  // black: its right-hand side
                 const unsigned cd = cf[c];
                 const T dg = (cd & CODE_GENERAL) ? g.diag[c] : codeDiag<T>(cd);
-                return dg <= T(0) ? T(0) : gsDiv(rv, dg);             // red: after the first half sweep
+                return dg <= T(0) ? T(0) : l0Div(rv, cd, dg);         // red: after the first half sweep
             } else if constexpr (MODE == L0_BLACK) {
                 if (!red) return rf[c];
                 const int a = af[c];
@@ -296,17 +308,17 @@ __global__ void __launch_bounds__(L0_THREADS, (L0MinCtas<R, MODE>::value)) k_l0(
             } else if constexpr (MODE == L0_PRE) {
                 if (red) { g.z[c] = z0Store(g, X[u]); continue; }
                 T zc = T(0);
-                if (dg > T(0)) zc = z0Store(g, gsDiv(l0Sum<1>(X[u], code, gen, n, i, j, k, nx, ny, nz), dg));
+                if (dg > T(0)) zc = z0Store(g, l0Div(l0Sum<1>(X[u], code, gen, n, i, j, k, nx, ny, nz), code, dg));
                 g.z[c] = zc;
             } else if constexpr (MODE == L0_BLACK) {
                 if (red) continue;
                 T zc = T(0);
-                if (dg > T(0)) zc = z0Store(g, gsDiv(l0Sum<1>(X[u], code, gen, n, i, j, k, nx, ny, nz), dg));
+                if (dg > T(0)) zc = z0Store(g, l0Div(l0Sum<1>(X[u], code, gen, n, i, j, k, nx, ny, nz), code, dg));
                 g.z[c] = zc;
             } else if constexpr (MODE == L0_RED) {
                 if (red) {
                     T zc = T(0);
-                    if (dg > T(0)) zc = z0Store(g, gsDiv(l0Sum<1>(X[u], code, gen, n, i, j, k, nx, ny, nz), dg));
+                    if (dg > T(0)) zc = z0Store(g, l0Div(l0Sum<1>(X[u], code, gen, n, i, j, k, nx, ny, nz), code, dg));
                     g.z[c] = zc;
                     dot = accAdd(dot, dotTerm(X[u], zc));
                 } else {
