@@ -1149,13 +1149,15 @@ public:
             }
             return w;
         }();
+        int residentWide = 0;   // CTAs of the four-block red sweep resident on the GPU at once
         auto one = [&](auto kern, int mode) -> int {
             int occ = 0;
             PHX_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, L0_THREADS, 0));
             const int k = waves[std::min(mode, L0_MODES - 1)];
             const int cap = persistCtas * TPB / L0_THREADS;   // PHX_PERSIST_CTAS caps every shape
-            l0grid[mode] = k == 0 ? (persistCtas < PERSIST_CTAS ? cap : (1 << 30))
-                                  : std::min(sms * std::max(occ, 1) * k, cap * k);
+            const int resident = std::min(sms * std::max(occ, 1), cap);
+            if (mode == L0_MODES) residentWide = resident;
+            l0grid[mode] = k == 0 ? (persistCtas < PERSIST_CTAS ? cap : (1 << 30)) : resident * k;
             return PHX_OK;
         };
         PHX_TRY(one(k_l0<R, L0_APPLY, 1>, L0_APPLY));
@@ -1170,7 +1172,7 @@ public:
             const char* e = std::getenv("PHX_L0_RED_WIDE");
             return e ? std::atoi(e) : -1;
         }();
-        l0RedWide = redWide >= 0 ? redWide == 1 : dom[D_L0R].total >= 2 * l0grid[L0_MODES];
+        l0RedWide = redWide >= 0 ? redWide == 1 : (long long)dom[D_L0R].total >= 2LL * residentWide;
         useL0 = true;
         return PHX_OK;
     }
